@@ -1,0 +1,210 @@
+/*
+ * soapgb.h -- C ABI of libsoapgb, the GB300 (sm_103a) engine for SOAP-GPU's
+ * per-phase spectral synthesis.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (SOAPGB_OK == 0).  On failure the
+ *    context keeps a message, readable with soapgb_last_error().
+ *  - Buffers are owned by the caller.  `mem` says where ALL the array arguments of
+ *    one call live: SOAPGB_HOST (the library copies in and out through its own
+ *    device workspace, inside the call) or SOAPGB_DEVICE (device pointers on the
+ *    context's device; nothing is copied).  Host-mode calls return after the
+ *    results are in host memory; device-mode calls are asynchronous on the
+ *    context's stream (soapgb_synchronize() waits).
+ *  - Arrays are row-major float64 unless stated; a "cube" is n_mu rows of n
+ *    pixels, row b holding mu bin b.  n is the pixel count of the wavelength grid
+ *    and n_eff = floor(n / 512) * 512 the number of pixels the reference processes
+ *    and writes (it launches n/512 blocks of 512 threads).
+ *  - One context = one device + one CUDA stream; a context must not be used from
+ *    two host threads at once.
+ *
+ * Each function names the reference code it replaces (paths relative to the
+ * reference's SOAP_code/ directory).  The reference exposes these steps as
+ * separate executables driven through argv and float64 .bin files by
+ * run_all_SOAP.py; the drop-in executables built from soap_gpu_gb300/csrc/tools
+ * keep that argv/file contract on top of this ABI.
+ */
+#ifndef SOAPGB_H
+#define SOAPGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SOAPGB_OK 0
+#define SOAPGB_ERR_ARG 1       /* invalid argument / size */
+#define SOAPGB_ERR_CUDA 2      /* CUDA runtime error */
+#define SOAPGB_ERR_ALLOC 3     /* device or host allocation failed */
+#define SOAPGB_ERR_NUMERIC 4   /* fit failed / non-finite result */
+#define SOAPGB_ERR_DEVICE 5    /* a kernel reported an error through its status word */
+
+#define SOAPGB_HOST 0
+#define SOAPGB_DEVICE 1
+
+/* arithmetic forms of the integration kernels */
+#define SOAPGB_PLAIN64 0  /* per-cell FP64, the reference's arithmetic and cell order */
+#define SOAPGB_FAST64 1   /* collapsed shift-FIR in FP64 (same function, re-associated) */
+#define SOAPGB_FAST32 2   /* collapsed shift-FIR in FP32 with compensated (Kahan) sums;
+                             FP64 for Doppler factors, grid positions, tap weights */
+
+typedef struct soapgb_ctx soapgb_ctx;
+
+/* Star / disk parameters, as run_all_SOAP.py forwards them to SOAP_initialize
+ * (run_all_SOAP.py:226-229, SOAP_initialize.cu:513-537). */
+typedef struct {
+    int grid;            /* disk grid side G */
+    double period;       /* rotation period [d] */
+    double omega_ratio;  /* differential rotation W_ratio */
+    double incl;         /* inclination [deg] */
+    double radius_km;    /* stellar radius [km] */
+    double u1, u2;       /* quadratic limb darkening */
+    double lb[4];        /* facula limb-brightening cubic LB0..LB3 */
+} soapgb_star;
+
+/* Per-cell disk maps (G*G each, iy-major: k = iy*G + iz).  Invisible cells hold
+ * -999 (region 0), as written by SOAP_initialize.cu:399-422. */
+typedef struct {
+    double *delta;       /* rotational velocity [km/s] */
+    double *limb;        /* limb darkening */
+    double *mu;          /* mu = cos(theta) */
+    int *region;         /* mu-bin index into the cubes */
+    double *lb;          /* facula limb brightening */
+} soapgb_maps;
+
+/* Seed spectra (run_all_SOAP.py:94-100): n_mu x n each. */
+typedef struct {
+    const double *q_norm;    /* quiet, continuum-normalised  (new_noconti_convec_T_eff_T*) */
+    const double *q_sed;     /* quiet, with continuum        (new_conti_convec_T_eff_T*)   */
+    const double *spot_norm; /* spot, normalised             (new_noconti_convec_T_eff_Ts) */
+    const double *fac_norm;  /* facula, normalised           (new_noconti_convec_T_eff_Tf) */
+    const double *spot_sed;  /* spot continuum, row 0 used   (new_conti_T_eff_Ts)          */
+    const double *fac_sed;   /* facula continuum, row 0 used (new_conti_T_eff_Tf)          */
+    int n_mu;
+} soapgb_cubes;
+
+/* Temperatures forwarded to SOAP_integration (SOAP_integration.cu:469-497). */
+typedef struct {
+    int t_star;
+    int t_diff_spot;
+    int t_diff_fac;
+    int nrho;            /* rim points per region (config [main] nrho) */
+    int solar;           /* 1: facula intensity is a Planck ratio (SOAP_integration_solar.cu:433) */
+} soapgb_activity;
+
+/* ---- context ------------------------------------------------------------ */
+int soapgb_ctx_create(int device, soapgb_ctx **out);
+int soapgb_ctx_destroy(soapgb_ctx *ctx);
+const char *soapgb_last_error(const soapgb_ctx *ctx);
+/* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores the
+ * context's own stream. */
+int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream);
+int soapgb_synchronize(soapgb_ctx *ctx);
+/* Number of kernel launches issued by this context since creation. */
+long long soapgb_launch_count(const soapgb_ctx *ctx);
+/* Library version string. */
+const char *soapgb_version(void);
+
+/* ---- a3: disk maps ------------------------------------------------------
+ * Replaces the grid part of itot, SOAP_initialize.cu:297-395 (and the map files
+ * written at :399-422).  mu_boundary: n_mu-1 descending boundaries; a cell takes
+ * the first bin k with mu > mu_boundary[k], else the last bin. */
+int soapgb_disk_maps(soapgb_ctx *ctx, const soapgb_star *star, int n_mu,
+                     const double *mu_boundary, int mem, soapgb_maps *maps_out);
+
+/* ---- a4-a7: quiet-star disk integration ---------------------------------
+ * Replaces itot's cell loop, SOAP_initialize.cu:339-395 (fast_shift,
+ * fast_interp_new, fast_sum at :117-176): sum over visible cells (iy-major order)
+ * of the cell's Doppler-shifted, linearly interpolated, limb-darkened cube row.
+ * sum_out: n values ([n_eff, n) set to 0).  `step` is the grid step passed as
+ * argv[10] of SOAP_initialize. */
+int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
+                      const double *cube, int n_mu, int grid, const double *delta,
+                      const double *limb, const int *region, double step, int mem,
+                      double *sum_out);
+
+/* ---- a8 / a14: instrumental convolution + normalisation -----------------
+ * Replaces lower_resolution_gpu, SOAP_initialize.cu:446-505 (quiet) and
+ * SOAP_resolution.cu:235-310 (per phase and type).  For each of n_spec spectra
+ * A_s = base - spec_s (base may be NULL: A_s = spec_s), all n long with zero tail:
+ *   C_s[i] = sum_{m=i-w}^{i+w-2} step_mult (1 - A_s[m]) e^{-(m-i)^2 step_exp^2 / (2 s_i^2)} / (s_i sqrt(2 pi))
+ *   for w < i < n-1-w and i < n_eff, with w = rndup(window * dl_f32(sigma_v, wave[0]) / (wave[1]-wave[0]))
+ *   out_s[i] = 1 - C_s[i] (1 - min A_s) / max(sentinel, max_{C != 0} C_s),  i < n_eff.
+ * The reference hard-codes step_mult = step_exp = 0.005 in SOAP_resolution and
+ * step_exp = 0.005 in SOAP_initialize; sentinel is its -60000 start value.
+ * out: n_spec x n_eff.  minmax_out (optional, host or device like the rest):
+ * n_spec x 2 (min A, max C). */
+int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec,
+                            const double *wave, const double *base, const double *spec,
+                            double sigma_v, double window, double step_mult, double step_exp,
+                            double sentinel, int mem, double *out, double *minmax_out);
+
+/* ---- a9-a10: per-phase temperature and type maps -------------------------
+ * Replaces spot_init_gpu / spot_phase_gpu / spot_area / spot_scan and the region
+ * loop, SOAP_integration.cu:21-161,326-390,686-785.  regions: rows of
+ * (lat, long, size, type) -- type 0 spot, 1 facula -- phase p uses rows
+ * [reg_offsets[p], reg_offsets[p+1]) applied in order (later rows overwrite).
+ * temp/bi: n_phase x G*G, -9999 where no region. */
+int soapgb_phase_maps(soapgb_ctx *ctx, int grid, double incl, int n_phase,
+                      const double *phases, const int *reg_offsets, const double *regions,
+                      const soapgb_activity *act, int mem, double *temp, double *bi);
+
+/* ---- a11-a12: per-phase active-region integration ------------------------
+ * Replaces spot_integrate, SOAP_integration.cu:392-447 (+ fast_flux / fast_bconv /
+ * fast_tot / fast_intensity(_fac) at :285-323): for every active cell of every
+ * phase, in iy-major order,
+ *   flux += s - I q,  bconv += q - a,  tot += s - I a
+ * with q, s, a the shifted rows of q_norm, q_sed and spot_norm|fac_norm.
+ * flux/bconv/tot: n_phase x n each ([n_eff, n) set to 0). */
+int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
+                           int grid, int n_phase, const double *temp, const double *bi,
+                           const soapgb_maps *maps, const soapgb_cubes *cubes, double step,
+                           const soapgb_activity *act, int mem,
+                           double *flux, double *bconv, double *tot);
+
+/* ---- a15-a16: mask CCF ---------------------------------------------------
+ * Replaces calculate_CCF_1 / calc_mask / calculate_CCF_2, CCF_func.py:5-91, with
+ * the extended grid of run_all_SOAP.py:292-295.  wave_trim: the n_w trimmed
+ * wavelengths; lines filtered by the caller (run_all_SOAP.py:288).  mask_step and
+ * index_old are the literals 0.005 and 20000 of CCF_func.py:8-9,62-63 (pass the
+ * real step and int(wave_extend/step) for other grids).  spectra: n_spec x n_w;
+ * ccf_out: n_spec x n_v raw sums.  If `normalise` is set each CCF is divided by its
+ * max and apodised as run_all_SOAP.py:306-314.  form: PLAIN64 / FAST64 sum in FP64;
+ * FAST32 multiplies in FP32 and sums with compensation (FP64 assembly). */
+int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel, int n_lines,
+               const double *line_wave, const double *line_weight, int n_w,
+               const double *wave_trim, double step_size, double wave_extend,
+               double mask_step, int index_old, int n_spec, const double *spectra,
+               int normalise, int mem, double *ccf_out);
+
+/* ---- a17-a18: Gaussian fit + bisector -------------------------------------
+ * Replaces BIS_FIT2.cpp:97-317 (GSL trust-region Levenberg-Marquardt fit of
+ * c + k exp(-(x-x0)^2 / 2 sigma^2), then the 91-depth bisector and its span), for
+ * n_spec CCFs at once.  x: n velocities [m/s] shared by all; y, err: n_spec x n
+ * (err may be NULL for unit errors).  Outputs per spectrum: model[n],
+ * par[5] = (c, |k|, span, v0, fwhm), depth[91], bis[91]; iters (optional int per
+ * spectrum, < 0 when the fit did not converge). */
+int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double *x, const double *y,
+                     const double *err, int mem, double *model, double *par, double *depth,
+                     double *bis, int *iters);
+
+/* ---- composite: the per-phase stages in one call --------------------------
+ * Runs a9-a14 for every phase: maps, integration, convolution and normalisation of
+ * the three deficit spectra against the quiet spectra.  quiet_sed / quiet_norm are
+ * the n-long disk sums of a4-a7 (tail zero).  lower: n_phase x 3 x n_eff, types in
+ * the order tot, flux, bconv (SOAP_resolution.cu:414-416); raw (optional):
+ * n_phase x 3 x n_eff deficit spectra in the same order.  conv_step is the step
+ * used in the Gaussian (0.005 in the reference binaries). */
+int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
+                          const soapgb_star *star, const soapgb_maps *maps,
+                          const soapgb_cubes *cubes, double step, const soapgb_activity *act,
+                          int n_phase, const double *phases, const int *reg_offsets,
+                          const double *regions, const double *quiet_sed,
+                          const double *quiet_norm, double sigma_v, double conv_step,
+                          double sentinel, int mem, double *lower, double *raw);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOAPGB_H */

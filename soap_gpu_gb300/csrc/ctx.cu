@@ -1,0 +1,142 @@
+// Context, error reporting and device workspace of libsoapgb.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace soapgb {
+
+int set_error(soapgb_ctx *ctx, int code, const char *fmt, ...) {
+    if (ctx) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+int cuda_check(soapgb_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return SOAPGB_OK;
+    int code = (e == cudaErrorMemoryAllocation) ? SOAPGB_ERR_ALLOC : SOAPGB_ERR_CUDA;
+    return set_error(ctx, code, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+int Workspace::commit() {
+    if (total <= ctx->ws_size) return SOAPGB_OK;
+    // grow: wait for in-flight work that may still read the old buffer
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "workspace sync");
+    if (ctx->ws) cudaFree(ctx->ws);
+    ctx->ws = nullptr;
+    ctx->ws_size = 0;
+    size_t want = total + (total >> 3);  // 12.5% headroom for the next call
+    e = cudaMalloc((void **)&ctx->ws, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaMalloc((void **)&ctx->ws, total);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(ctx, SOAPGB_ERR_ALLOC, "workspace allocation of %zu bytes failed", total);
+        }
+        want = total;
+    }
+    ctx->ws_size = want;
+    return SOAPGB_OK;
+}
+
+const void *stage_in(soapgb_ctx *ctx, int mem, const void *p, size_t bytes, void *dst, int *rc) {
+    *rc = SOAPGB_OK;
+    if (mem == SOAPGB_DEVICE || p == nullptr || bytes == 0) return p;
+    cudaError_t e = cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        *rc = cuda_check(ctx, e, "host to device copy");
+        return nullptr;
+    }
+    return dst;
+}
+
+int check_status(soapgb_ctx *ctx, const char *what) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, what);
+    if (h != 0) {
+        cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+        return set_error(ctx, SOAPGB_ERR_DEVICE, "%s: device status %d", what, h);
+    }
+    return SOAPGB_OK;
+}
+
+int grid_for(soapgb_ctx *ctx, long long work, int block) {
+    long long g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffffLL) g = 0x7fffffffLL;
+    (void)ctx;
+    return (int)g;
+}
+
+}  // namespace soapgb
+
+using namespace soapgb;
+
+extern "C" {
+
+const char *soapgb_version(void) { return "soapgb 0.1 (sm_103a)"; }
+
+int soapgb_ctx_create(int device, soapgb_ctx **out) {
+    if (!out) return SOAPGB_ERR_ARG;
+    *out = nullptr;
+    soapgb_ctx *ctx = new soapgb_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        int rc = cuda_check(ctx, e, "soapgb_ctx_create");
+        // keep the context so the caller can read the message, but mark it unusable
+        ctx->stream = nullptr;
+        *out = ctx;
+        return rc;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return SOAPGB_OK;
+}
+
+int soapgb_ctx_destroy(soapgb_ctx *ctx) {
+    if (!ctx) return SOAPGB_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ws) cudaFree(ctx->ws);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return SOAPGB_OK;
+}
+
+const char *soapgb_last_error(const soapgb_ctx *ctx) {
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    return SOAPGB_OK;
+}
+
+int soapgb_synchronize(soapgb_ctx *ctx) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_status(ctx, "soapgb_synchronize");
+}
+
+long long soapgb_launch_count(const soapgb_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,549 @@
+// Collapsed shift-FIR engine: the FAST64 / FAST32 forms of the disk and phase
+// integration (the same function as SOAP_initialize.cu:339-395 and
+// SOAP_integration.cu:392-447, re-associated).
+//
+// For a uniform wavelength grid the reference's per-cell interpolation at output
+// pixel j reads the source position u_j = (j - off) / r (r = 1 + fbeta,
+// off = fbeta lambda0 / step): owner i = floor(u_j), weight w = u_j - i.  Over a tile
+// of T pixels starting at j0, u_j = i0 + dj + phi + delta dj with i0 = floor(u_{j0}),
+// phi = u_{j0} - i0, delta = 1/r - 1 (|delta| ~ v/c ~ 1e-5).  While phi + delta dj
+// stays in [0, 1) the cell contributes
+//     L (1 - phi - delta dj) S_b[j - k] + L (phi + delta dj) S_b[j - k + 1],   k = j0 - i0,
+// which is linear in dj with coefficients that only depend on (b, k).  Summing the
+// coefficients of all such ("regular") cells per (kind, b, k) group collapses
+// thousands of cells into a few dozen two-tap filters per tile.  Cells whose weight
+// wraps inside the tile, or whose owners leave [0, n_eff-2], are added directly
+// ("exceptions"), exactly as the per-cell form does.
+//
+// Per tile, a block of 256 threads owns 1024 pixels:
+//   setup  -- FP64 position of every cell at j0 (the only FP64 step), warp
+//             segmented reduction of equal keys (cells come in map order, so
+//             keys repeat in runs), FP64 atomics into a shared hash table;
+//   apply  -- every thread walks the group list for its four pixels (coalesced
+//             two-tap loads, compensated sums in FP32 for FAST32).
+#include <algorithm>
+#include <cmath>
+
+#include "fir.cuh"
+
+using namespace soapgb;
+
+constexpr int FIR_THREADS = 256;
+constexpr int FIR_PIX = 4;
+constexpr int FIR_TILE = FIR_THREADS * FIR_PIX;
+constexpr int FIR_HASH = 1024;     // shared hash slots (kind, bin, shift)
+constexpr int FIR_EXC = 512;       // shared exception slots
+
+enum { MODE_QUIET = 0, MODE_PHASE = 1 };
+
+// per grid cell constants (phase independent)
+struct CellGeo {
+    double ir;     // 1 / (1 + fbeta)
+    double offir;  // fbeta lambda0 / step / (1 + fbeta)
+    double dlt;    // ir - 1
+    double L;      // limb darkening
+    double w2;     // (1 + LB) L
+    int row;       // mu bin
+    int zero_v;    // delta == 0: the reference copies the row
+};
+
+__global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const double *__restrict__ limb,
+                           const double *__restrict__ lb, const int *__restrict__ region, int n_mu, double lambda0,
+                           double step, CellGeo *geo, int *status) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= gm) return;
+    double d = delta[k];
+    CellGeo g;
+    double beta = d * 1000. / SOAP_C_LIGHT;
+    double fbeta = sqrt((1 + beta) / (1 - beta)) - 1;
+    double r = 1 + fbeta;
+    double off = fbeta * lambda0 / step;
+    g.ir = 1.0 / r;
+    g.offir = off / r;
+    g.dlt = g.ir - 1.0;
+    g.L = limb[k];
+    g.w2 = lb ? (1.0 + lb[k]) * g.L : g.L;
+    int row = region[k];
+    if ((unsigned)row >= (unsigned)n_mu && g.L > -998.0) {
+        atomicExch(status, 21);
+        row = 0;
+    }
+    g.row = ((unsigned)row < (unsigned)n_mu) ? row : 0;
+    g.zero_v = (d == 0.0);
+    geo[k] = g;
+}
+
+// wavelength grid must be uniform for the collapsed form
+__global__ void k_check_uniform(int n_eff, const double *__restrict__ lam, double step, int *status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    double expect = lam[0] + (double)i * step;
+    if (fabs(lam[i] - expect) > 1e-6 * step) atomicExch(status, 31);
+}
+
+template <typename T>
+__global__ void k_to_type(long long count, const double *__restrict__ a, const double *__restrict__ b, T *out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    double v = b ? a[i] - b[i] : a[i];
+    out[i] = (T)v;
+}
+
+// compensated accumulator
+template <typename T>
+struct Acc {
+    T s, c;
+    __device__ __forceinline__ void zero() { s = (T)0; c = (T)0; }
+    __device__ __forceinline__ void add(T x) {
+        if constexpr (sizeof(T) == 4) {
+            T y = x - c;
+            T t = s + y;
+            c = (t - s) - y;
+            s = t;
+        } else {
+            s += x;
+        }
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
+struct FirCubes {
+    // PHASE: q_sed, q_norm, spot_norm, dq_spot, fac_norm, dq_fac; QUIET: [0] only
+    const void *c[6];
+    const double *spot_sed;
+    const double *fac_sed;
+};
+
+struct Exc {
+    int i0;          // owner at j0
+    int row;
+    int kind;        // 0 spot, 1 facula (phase); 0 (quiet)
+    int parts;       // 1: the L-weighted sums, 2: the (1+LB) L-weighted facula sums
+    double phi, dlt, L, w2, temp;
+    int zero_v;
+};
+
+__device__ __forceinline__ unsigned fir_key(int kind, int row, int k) {
+    // kind < 4, row < 2^12, k in [-2^14, 2^14)
+    return ((unsigned)kind << 28) | ((unsigned)row << 16) | (unsigned)((k + 16384) & 0xffff);
+}
+
+template <typename T>
+__device__ __forceinline__ T lerp_at(const T *__restrict__ row, long long i, T w) {
+    T s0 = row[i], s1 = row[i + 1];
+    return s0 + (s1 - s0) * w;
+}
+
+// loi_Planck ratio B(lambda, t) / B(lambda, tn) (SOAP_integration.cu:205-212)
+__device__ __forceinline__ double fir_planck_ratio(double lambda0, double t, double tn) {
+    double c = 299792458.;
+    double h = 6.62606896e-34;
+    double k_b = 1.380e-23;
+    double scale = 1e-10;
+    double a = (h * c) / (lambda0 * k_b * scale);
+    return (exp(a / tn) - 1) / (exp(a / t) - 1);
+}
+
+struct FirShared {
+    unsigned key[FIR_HASH];
+    double val[FIR_HASH][3];
+    int grp[FIR_HASH];
+    Exc exc[FIR_EXC];
+    int nexc, ngrp;
+};
+
+// One pass of the warp-cooperative insertion: lanes holding a key (active) fold
+// runs of equal keys and the run's last lane adds the sums to the hash table.
+// Returns whether this lane's contribution reached the table.
+__device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned key, double a0, double a1,
+                                           double bb, int lane) {
+    if (!active) key = 0xfffffffeu;
+    unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+    bool seg = (lane == 0) || (prev != key);
+    for (int o = 1; o < 32; o <<= 1) {
+        double v0 = __shfl_up_sync(0xffffffffu, a0, o);
+        double v1 = __shfl_up_sync(0xffffffffu, a1, o);
+        double v2 = __shfl_up_sync(0xffffffffu, bb, o);
+        int sg = __shfl_up_sync(0xffffffffu, (int)seg, o);
+        if (lane >= o && !seg) {
+            a0 += v0;
+            a1 += v1;
+            bb += v2;
+            seg = sg;
+        }
+    }
+    unsigned next = __shfl_down_sync(0xffffffffu, key, 1);
+    bool tail = (lane == 31) || (next != key);
+    bool ok = true;
+    if (active && tail) {
+        ok = false;
+        unsigned h = (key * 2654435761u) & (FIR_HASH - 1);
+        for (int probe = 0; probe < 64 && !ok; ++probe) {
+            unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
+            if (old == 0xffffffffu || old == key) {
+                atomicAdd(&sh.val[h][0], a0);
+                atomicAdd(&sh.val[h][1], a1);
+                atomicAdd(&sh.val[h][2], bb);
+                ok = true;
+            } else {
+                h = (h + 1) & (FIR_HASH - 1);
+            }
+        }
+    }
+    // every lane learns the outcome of its run's tail
+    unsigned tails = __ballot_sync(0xffffffffu, tail);
+    int my_tail = __ffs(tails & (0xffffffffu << lane)) - 1;
+    int tail_ok = __shfl_sync(0xffffffffu, (int)ok, my_tail);
+    return !active || tail_ok;
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const double *__restrict__ lam,
+                                                     FirCubes cubes, const int *__restrict__ cells,
+                                                     const int *__restrict__ counts, int max_cells,
+                                                     const CellGeo *__restrict__ geo,
+                                                     const double *__restrict__ temp, const double *__restrict__ bi,
+                                                     long long gm, int solar, int t_norm_fac,
+                                                     double *__restrict__ out0, double *__restrict__ out1,
+                                                     double *__restrict__ out2, long long out_stride) {
+    extern __shared__ __align__(16) unsigned char fir_smem[];
+    FirShared &sh = *reinterpret_cast<FirShared *>(fir_smem);
+
+    const int p = blockIdx.y;
+    const int j0 = blockIdx.x * FIR_TILE;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int n_cells = counts[p];
+    const int *pc = cells + (long long)p * max_cells;
+    const double *pt = (MODE == MODE_PHASE) ? temp + (long long)p * gm : nullptr;
+    const double *pb = (MODE == MODE_PHASE) ? bi + (long long)p * gm : nullptr;
+    const int t_eff = min(FIR_TILE, n_eff - j0);
+    if (t_eff <= 0) {   // whole tile in the zero tail [n_eff, n)
+        for (int q = 0; q < FIR_PIX; ++q) {
+            int j = j0 + tid + q * FIR_THREADS;
+            if (j >= n) continue;
+            long long o = (long long)p * out_stride + j;
+            out0[o] = 0.0;
+            if constexpr (MODE == MODE_PHASE) { out1[o] = 0.0; out2[o] = 0.0; }
+        }
+        return;
+    }
+
+    for (int q = tid; q < FIR_HASH; q += FIR_THREADS) {
+        sh.key[q] = 0xffffffffu;
+        sh.val[q][0] = sh.val[q][1] = sh.val[q][2] = 0.0;
+    }
+    if (tid == 0) sh.nexc = 0;
+
+    // accumulators: QUIET [0]; PHASE: S, Qs, As, Bs, Qf, Af, Bf
+    constexpr int NACC = (MODE == MODE_QUIET) ? 1 : 7;
+    Acc<T> acc[NACC][FIR_PIX];
+#pragma unroll
+    for (int a = 0; a < NACC; ++a)
+#pragma unroll
+        for (int q = 0; q < FIR_PIX; ++q) acc[a][q].zero();
+    __syncthreads();
+
+    // direct evaluation of the collected exceptions (the per-cell arithmetic)
+    auto flush = [&]() {
+        int ne = sh.nexc;
+        for (int e = 0; e < ne; ++e) {
+            const Exc &x = sh.exc[e];
+            long long off = (long long)x.row * n;
+#pragma unroll
+            for (int q = 0; q < FIR_PIX; ++q) {
+                int dj = tid + q * FIR_THREADS;
+                int j = j0 + dj;
+                if (j >= n_eff) continue;
+                long long i;
+                T w;
+                if (x.zero_v) {
+                    i = j;
+                    w = (T)0;
+                } else {
+                    double wd = x.phi + x.dlt * (double)dj;
+                    i = (long long)x.i0 + dj;
+                    if (wd >= 1.0) { wd -= 1.0; i += 1; }
+                    else if (wd < 0.0) { wd += 1.0; i -= 1; }
+                    if (i < 0 || i > n_eff - 2) continue;
+                    w = (T)wd;
+                }
+                auto val = [&](int ci) -> T {
+                    const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
+                    if (x.zero_v) return rowp[i];
+                    return lerp_at(rowp, i, w);
+                };
+                T L = (T)x.L;
+                if constexpr (MODE == MODE_QUIET) {
+                    acc[0][q].add(L * val(0));
+                } else {
+                    if (x.parts & 1) {
+                        acc[0][q].add(L * val(0));                              // S  (q_sed)
+                        if (x.kind == 0) {
+                            T Lq = L;
+                            if ((double)(int)x.temp != x.temp) {                // spot Planck ratio
+                                double lj = lam[j];
+                                Lq = (T)(x.L * fir_planck_ratio(lj, x.temp, (double)(int)x.temp));
+                            }
+                            acc[1][q].add(Lq * val(1));                         // Qs (q_norm)
+                            acc[2][q].add(Lq * val(2));                         // As (spot_norm)
+                            acc[3][q].add(L * val(3));                          // Bs (q_norm - spot_norm)
+                        } else {
+                            acc[6][q].add(L * val(5));                          // Bf (q_norm - fac_norm)
+                        }
+                    }
+                    if ((x.parts & 2) && x.kind == 1) {
+                        T w2 = (T)x.w2;
+                        if (solar) w2 = (T)(x.L * fir_planck_ratio(lam[j], x.temp, (double)t_norm_fac));
+                        acc[4][q].add(w2 * val(1));                             // Qf
+                        acc[5][q].add(w2 * val(4));                             // Af (fac_norm)
+                    }
+                }
+            }
+        }
+    };
+
+    // --- setup: place every cell at this tile -----------------------------------
+    for (int c0 = 0; c0 < n_cells; c0 += FIR_THREADS) {
+        int ci = c0 + tid;
+        bool have = ci < n_cells;
+        int cell = have ? pc[ci] : 0;
+        CellGeo g = geo[cell];
+        int kind = 0;
+        double tcell = 0.0;
+        bool regular = false;
+        long long i0 = 0;
+        double phi = 0.0;
+        if (have) {
+            if constexpr (MODE == MODE_PHASE) {
+                kind = (pb[cell] == 0.0) ? 0 : 1;
+                tcell = pt[cell];
+            }
+            double u0 = fma((double)j0, g.ir, -g.offir);
+            double fl = floor(u0);
+            i0 = (long long)fl;
+            phi = u0 - fl;
+            double w_end = phi + g.dlt * (double)(t_eff - 1);
+            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= 0.0) && (w_end < 1.0);
+            if (g.zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
+            if constexpr (MODE == MODE_PHASE) {
+                if (kind == 0 && (double)(int)tcell != tcell) regular = false;   // spot Planck ratio != 1
+                if (kind == 1 && solar) regular = false;                        // per-pixel Planck ratio
+            }
+        }
+        int k = j0 - (int)i0;
+        // pass A: weight L (spot: kind 0, facula: kind 1; quiet: kind 0)
+        bool okA = fir_insert(sh, have && regular, fir_key(kind, g.row, k), g.L * (1.0 - phi), g.L * phi,
+                              g.L * g.dlt, lane);
+        bool okB = true;
+        if constexpr (MODE == MODE_PHASE) {
+            // pass B: facula (1 + LB) L weight
+            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, g.row, k), g.w2 * (1.0 - phi),
+                             g.w2 * phi, g.w2 * g.dlt, lane);
+        }
+        int parts = 0;
+        if (have) {
+            if (!regular) parts = 3;
+            else parts = (okA ? 0 : 1) | (okB ? 0 : 2);
+        }
+        if (parts) {
+            int slot = atomicAdd(&sh.nexc, 1);
+            Exc x;
+            x.i0 = (int)i0;
+            x.row = g.row;
+            x.kind = kind;
+            x.parts = parts;
+            x.phi = phi;
+            x.dlt = g.dlt;
+            x.L = g.L;
+            x.w2 = g.w2;
+            x.temp = tcell;
+            x.zero_v = g.zero_v;
+            sh.exc[slot] = x;
+        }
+        __syncthreads();
+        if (sh.nexc > FIR_EXC - FIR_THREADS) {
+            flush();
+            __syncthreads();
+            if (tid == 0) sh.nexc = 0;
+        }
+        __syncthreads();
+    }
+    flush();
+    __syncthreads();
+    if (tid == 0) {
+        int ng = 0;
+        for (int q = 0; q < FIR_HASH; ++q)
+            if (sh.key[q] != 0xffffffffu) sh.grp[ng++] = q;
+        sh.ngrp = ng;
+    }
+    __syncthreads();
+    // --- apply the collapsed groups ---------------------------------------------
+    int ng = sh.ngrp;
+    for (int e = 0; e < ng; ++e) {
+        int h = sh.grp[e];
+        unsigned key = sh.key[h];
+        int kind = (int)(key >> 28);
+        int row = (int)((key >> 16) & 0xfff);
+        int k = (int)(key & 0xffff) - 16384;
+        double A0 = sh.val[h][0], A1 = sh.val[h][1], B = sh.val[h][2];
+        long long off = (long long)row * n;
+#pragma unroll
+        for (int q = 0; q < FIR_PIX; ++q) {
+            int dj = tid + q * FIR_THREADS;
+            int j = j0 + dj;
+            if (j >= n_eff) continue;
+            long long i = (long long)j - k;
+            T c0 = (T)(A0 - B * (double)dj);
+            T c1 = (T)(A1 + B * (double)dj);
+            auto two = [&](int ci) -> T {
+                const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
+                return c0 * rowp[i] + c1 * rowp[i + 1];
+            };
+            if constexpr (MODE == MODE_QUIET) {
+                acc[0][q].add(two(0));
+            } else {
+                if (kind == 0) {              // spot, weight L
+                    acc[0][q].add(two(0));
+                    acc[1][q].add(two(1));
+                    acc[2][q].add(two(2));
+                    acc[3][q].add(two(3));
+                } else if (kind == 1) {       // facula, weight L
+                    acc[0][q].add(two(0));
+                    acc[6][q].add(two(5));
+                } else {                      // facula, weight (1 + LB) L
+                    acc[4][q].add(two(1));
+                    acc[5][q].add(two(4));
+                }
+            }
+        }
+    }
+    // --- outputs ----------------------------------------------------------------
+#pragma unroll
+    for (int q = 0; q < FIR_PIX; ++q) {
+        int j = j0 + tid + q * FIR_THREADS;
+        if (j >= n) continue;
+        long long o = (long long)p * out_stride + j;
+        if (j >= n_eff) {
+            out0[o] = 0.0;
+            if constexpr (MODE == MODE_PHASE) { out1[o] = 0.0; out2[o] = 0.0; }
+            continue;
+        }
+        if constexpr (MODE == MODE_QUIET) {
+            out0[o] = acc[0][q].get();
+        } else {
+            double S = acc[0][q].get(), Qs = acc[1][q].get(), As = acc[2][q].get(), Bs = acc[3][q].get();
+            double Qf = acc[4][q].get(), Af = acc[5][q].get(), Bf = acc[6][q].get();
+            double is = cubes.spot_sed[j], fs = cubes.fac_sed[j];
+            out0[o] = S - is * Qs - fs * Qf;   // flux
+            out1[o] = Bs + Bf;                 // bconv
+            out2[o] = S - is * As - fs * Af;   // tot
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase) {
+    FirPlanSizes p;
+    if (form == SOAPGB_PLAIN64) return p;
+    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    size_t cube = align256(tsz * (size_t)n * n_mu);
+    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + (phase ? 6 : 1) * cube;
+    return p;
+}
+
+template <typename T, int MODE>
+static int launch_fir(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const FirCubes &fc, const int *cells,
+                      const int *counts, int max_cells, const CellGeo *geo, const double *temp, const double *bi,
+                      long long gm, int solar, int t_norm_fac, double *o0, double *o1, double *o2,
+                      long long out_stride, int n_lists) {
+    size_t smem = sizeof(FirShared);
+    SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // tiles cover [0, n): tiles past n_eff only write the zero tail
+    dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
+    k_fir<T, MODE><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, cells, counts, max_cells, geo, temp, bi,
+                                                          gm, solar, t_norm_fac, o0, o1, o2, out_stride);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, const FirPlanSizes &plan) {
+    (void)plan;
+    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    size_t cube_elems = (size_t)a.n * a.n_mu;
+    long long gm = a.max_cells;
+    char *p = scratch;
+    CellGeo *geo = (CellGeo *)p;
+    p += align256(sizeof(CellGeo) * (size_t)gm);
+    void *cube = p;
+    p += align256(tsz * cube_elems);
+    (void)p;
+    double lambda0;
+    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, a.wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    k_check_uniform<<<grid_for(ctx, a.n_eff, 256), 256, 0, ctx->stream>>>(a.n_eff, a.wave, a.step, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, a.delta, a.limb, nullptr, a.region, a.n_mu,
+                                                                lambda0, a.step, geo, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    FirCubes fc{};
+    if (form == SOAPGB_FAST32) {
+        k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube);
+        SOAP_LAUNCHED(ctx);
+        fc.c[0] = cube;
+        return launch_fir<float, MODE_QUIET>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
+                                             nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+    }
+    fc.c[0] = a.cube;
+    return launch_fir<double, MODE_QUIET>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
+                                          nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+}
+
+int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan) {
+    (void)plan;
+    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    int n_mu = a.cubes->n_mu;
+    size_t cube_elems = (size_t)a.n * n_mu;
+    char *p = scratch;
+    CellGeo *geo = (CellGeo *)p;
+    p += align256(sizeof(CellGeo) * (size_t)a.gm);
+    void *cb[6];
+    for (int q = 0; q < 6; ++q) {
+        cb[q] = p;
+        p += align256(tsz * cube_elems);
+    }
+    double lambda0;
+    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, a.wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    k_check_uniform<<<grid_for(ctx, a.n_eff, 256), 256, 0, ctx->stream>>>(a.n_eff, a.wave, a.step, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    k_cell_geo<<<grid_for(ctx, a.gm, 256), 256, 0, ctx->stream>>>(a.gm, a.delta, a.limb, a.lb, a.region, n_mu,
+                                                                  lambda0, a.step, geo, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    const soapgb_cubes &c = *a.cubes;
+    // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
+    const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
+    const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
+    FirCubes fc{};
+    for (int q = 0; q < 6; ++q) {
+        if (form == SOAPGB_FAST32)
+            k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)cb[q]);
+        else
+            k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)cb[q]);
+        SOAP_LAUNCHED(ctx);
+        fc.c[q] = cb[q];
+    }
+    fc.spot_sed = c.spot_sed;
+    fc.fac_sed = c.fac_sed;
+    int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
+    if (form == SOAPGB_FAST32)
+        return launch_fir<float, MODE_PHASE>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
+                                             a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot,
+                                             a.out_stride, a.n_phase);
+    return launch_fir<double, MODE_PHASE>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
+                                          a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot,
+                                          a.out_stride, a.n_phase);
+}

@@ -1,0 +1,47 @@
+// Collapsed shift-FIR engine (FAST64 / FAST32 forms of the disk and phase integration).
+#pragma once
+#include "internal.cuh"
+
+struct FirPlanSizes {
+    size_t bytes = 0;
+};
+
+// workspace of the FAST forms: per-cell geometry for the G*G grid plus typed cube
+// copies (one cube for the quiet disk, six for the phase integration)
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase);
+
+struct FirQuietArgs {
+    int n, n_eff;
+    const double *wave;
+    const double *cube;     // n_mu x n (FP64, device)
+    int n_mu;
+    int max_cells;
+    const int *n_cells;     // device: number of visible cells
+    const int *cells;       // visible cells, map order
+    const double *delta, *limb;
+    const int *region;
+    double step;
+    double *out;            // n (tail set to 0)
+};
+
+int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, const FirPlanSizes &plan);
+
+struct FirPhaseArgs {
+    int n, n_eff;
+    const double *wave;
+    const soapgb_cubes *cubes;  // device pointers, FP64
+    int n_phase;
+    int max_cells;
+    const int *cells;           // n_phase x max_cells active cells, map order
+    const int *counts;          // n_phase
+    const double *temp, *bi;    // n_phase x G*G
+    const double *delta, *limb, *lb;
+    const int *region;
+    long long gm;               // G*G
+    double step;
+    const soapgb_activity *act;
+    double *flux, *bconv, *tot; // n_phase x n
+    long long out_stride;       // distance between phases in the outputs
+};
+
+int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);

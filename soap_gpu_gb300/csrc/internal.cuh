@@ -1,0 +1,129 @@
+// Internal declarations shared by the libsoapgb translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/soapgb.h"
+
+#define SOAP_C_LIGHT 299792458.
+#define SOAP_PI 3.141592653589793238463
+
+struct soapgb_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;      // stream in use
+    cudaStream_t own_stream = nullptr;  // stream created by the context
+    std::string err;
+    // device workspace (grown on demand, reused across calls)
+    char *ws = nullptr;
+    size_t ws_size = 0;
+    // device status word written by kernels (0 = ok)
+    int *d_status = nullptr;
+    long long launches = 0;
+    int num_sms = 0;
+};
+
+namespace soapgb {
+
+int set_error(soapgb_ctx *ctx, int code, const char *fmt, ...);
+int cuda_check(soapgb_ctx *ctx, cudaError_t e, const char *what);
+#define SOAP_CUDA(ctx, call)                                         \
+    do {                                                             \
+        cudaError_t _e = (call);                                     \
+        if (_e != cudaSuccess) return soapgb::cuda_check(ctx, _e, #call); \
+    } while (0)
+#define SOAP_LAUNCHED(ctx)                                                   \
+    do {                                                                     \
+        (ctx)->launches++;                                                   \
+        cudaError_t _e = cudaGetLastError();                                 \
+        if (_e != cudaSuccess) return soapgb::cuda_check(ctx, _e, "kernel launch"); \
+    } while (0)
+
+// Bump allocator over the context workspace.  Usage: plan sizes with add(),
+// then commit() (grows the workspace if needed), then take pointers with get().
+struct Workspace {
+    soapgb_ctx *ctx;
+    std::vector<size_t> sizes;
+    std::vector<size_t> offs;
+    size_t total = 0;
+    explicit Workspace(soapgb_ctx *c) : ctx(c) {}
+    int add(size_t bytes) {
+        size_t off = (total + 255) & ~size_t(255);
+        offs.push_back(off);
+        sizes.push_back(bytes);
+        total = off + bytes;
+        return (int)offs.size() - 1;
+    }
+    int commit();
+    template <class T> T *get(int slot) const { return reinterpret_cast<T *>(ctx->ws + offs[slot]); }
+};
+
+// Copy an input array into the workspace when it is a host array; returns the
+// device pointer to use.  `slot` must have been planned with add(bytes) when mem
+// is host (pass slot -1 for device mode).
+const void *stage_in(soapgb_ctx *ctx, int mem, const void *p, size_t bytes, void *dst, int *rc);
+
+int check_status(soapgb_ctx *ctx, const char *what);
+
+// number of visible cells etc. via ordered compaction helpers (regions.cu)
+int compact_cells(soapgb_ctx *ctx, int n_lists, int cells_per_list, const double *key,
+                  double lo, double hi, int key_stride, int *idx_out, int *count_out);
+
+int grid_for(soapgb_ctx *ctx, long long work, int block);
+
+}  // namespace soapgb
+
+// ---------------------------------------------------------------------------
+// Device helpers: the reference's expressions, written out once.
+// ---------------------------------------------------------------------------
+
+// Delta_lambda, SOAP_initialize.cu:55-66
+__device__ __forceinline__ double soap_delta_lambda(double line_width, double lambda_line0) {
+    double beta = line_width / SOAP_C_LIGHT;
+    return -1 * lambda_line0 * (1 - sqrt((1 + beta) / (1 - beta)));
+}
+
+// Per-cell Doppler constants of fast_shift / fast_interp_new (SOAP_initialize.cu:117-167).
+struct CellShift {
+    double fbeta;     // sqrt((1+b)/(1-b)) - 1
+    double sq;        // sqrt((1+b)/(1-b))
+    double off;       // fbeta * lambda0 / step
+};
+
+__device__ __forceinline__ CellShift soap_cell_shift(double delta, double lambda0, double step) {
+    CellShift c;
+    double beta = delta * 1000. / SOAP_C_LIGHT;
+    c.sq = sqrt((1 + beta) / (1 - beta));
+    c.fbeta = -1 * (1 - c.sq);
+    c.off = __ddiv_rn(__dmul_rn(c.fbeta, lambda0), step);
+    return c;
+}
+
+// ceil of the shifted source position x_i = i (1 + fbeta) + fbeta lambda0 / step,
+// evaluated without contraction (one rounding per operation, as the oracle does).
+__device__ __forceinline__ long long soap_ceil_pos(long long i, const CellShift &c) {
+    double x = __dadd_rn(__dmul_rn((double)i, 1 + c.fbeta), c.off);
+    return (long long)ceil(x);
+}
+
+// shifted wavelength lambda'_i = lambda_i + Delta_lambda(v, lambda_i)
+__device__ __forceinline__ double soap_lshift(double lam, const CellShift &c) {
+    return lam + (-1 * lam * (1 - c.sq));
+}
+
+// Owner of output pixel j: the source i in [0, n_eff-2] with
+// ceil(x_i) <= j < ceil(x_{i+1}); returns -1 if none.
+__device__ __forceinline__ long long soap_owner(long long j, int n_eff, const CellShift &c) {
+    double r = 1 + c.fbeta;
+    long long i = (long long)floor(((double)j - c.off) / r);
+    if (i < -1) i = -1;
+    if (i > n_eff - 1) i = n_eff - 1;
+    // advance while the next source still starts at or before j
+    while (i + 1 <= n_eff - 1 && soap_ceil_pos(i + 1, c) <= j) ++i;
+    // retreat while this source starts after j
+    while (i >= 0 && soap_ceil_pos(i, c) > j) --i;
+    if (i < 0 || i > n_eff - 2) return -1;
+    return i;
+}

@@ -1,0 +1,151 @@
+// Composite per-phase pipeline: maps -> integration -> convolution/normalisation.
+//
+// Reference: the SOAP_integration and SOAP_resolution processes spawned by
+// run_all_SOAP.py:237-250, which hand the raw deficit spectra over through one
+// float64 file per phase and type (SOAP_integration.cu:802-817 ->
+// SOAP_resolution.cu:398-412).  Here the deficits stay in device memory and all
+// phases go through each stage in one launch.
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "fir.cuh"
+#include "resolution.cuh"
+
+using namespace soapgb;
+
+namespace soapgb {
+int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
+                      const int *h_reg_off, const double *h_regions, const soapgb_activity *act, double *d_temp,
+                      double *d_bi, char *scratch, size_t scratch_bytes);
+size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
+int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *d_wave, int grid, int n_phase,
+                     const double *d_temp, const double *d_bi, const soapgb_maps &dm, const soapgb_cubes &dc,
+                     double step, const soapgb_activity *act, double *d_flux, double *d_bconv, double *d_tot,
+                     long long out_stride, int *d_cells, int *d_counts, char *fir_scratch, const FirPlanSizes &fp);
+}  // namespace soapgb
+
+extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
+                                     const soapgb_star *star, const soapgb_maps *maps, const soapgb_cubes *cubes,
+                                     double step, const soapgb_activity *act, int n_phase, const double *phases,
+                                     const int *reg_offsets, const double *regions, const double *quiet_sed,
+                                     const double *quiet_norm, double sigma_v, double conv_step, double sentinel,
+                                     int mem, double *lower, double *raw) {
+    if (!ctx || !star || !maps || !cubes || !act) return SOAPGB_ERR_ARG;
+    if (n < 3 || n_eff < 2 || n_eff > n || n_phase < 0 || !wave || !phases || !reg_offsets || !quiet_sed ||
+        !quiet_norm || !lower || !(step > 0) || !(sigma_v > 0) || !(conv_step > 0) || cubes->n_mu < 1)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: bad arguments");
+    if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: unknown form %d", form);
+    if (n_phase == 0) return SOAPGB_OK;
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    bool host = (mem == SOAPGB_HOST);
+    int grid = star->grid;
+    long long gm = (long long)grid * grid;
+    int n_mu = cubes->n_mu;
+    // small descriptors on the host
+    std::vector<int> h_off(n_phase + 1);
+    std::vector<double> h_ph(n_phase);
+    double w3[3];
+    if (host) {
+        memcpy(h_off.data(), reg_offsets, sizeof(int) * (n_phase + 1));
+        memcpy(h_ph.data(), phases, sizeof(double) * n_phase);
+        w3[0] = wave[0];
+        w3[1] = wave[1];
+        w3[2] = wave[n_eff - 1];
+    } else {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(h_off.data(), reg_offsets, sizeof(int) * (n_phase + 1), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(h_ph.data(), phases, sizeof(double) * n_phase, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(w3, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(w3 + 2, wave + n_eff - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    int n_rows = h_off[n_phase];
+    if (h_off[0] != 0 || n_rows < 0) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: bad reg_offsets");
+    std::vector<double> h_reg(4 * (size_t)(n_rows > 0 ? n_rows : 1));
+    if (n_rows > 0) {
+        if (!regions) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: null regions");
+        if (host) memcpy(h_reg.data(), regions, sizeof(double) * 4 * n_rows);
+        else {
+            SOAP_CUDA(ctx, cudaMemcpyAsync(h_reg.data(), regions, sizeof(double) * 4 * n_rows, cudaMemcpyDeviceToHost, ctx->stream));
+            SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        }
+    }
+    size_t cube_b = sizeof(double) * (size_t)n * n_mu;
+    long long n_spec = 3LL * n_phase;
+    Workspace ws(ctx);
+    int s_wave = ws.add(host ? sizeof(double) * n : 0);
+    int s_c[6];
+    for (int q = 0; q < 4; ++q) s_c[q] = ws.add(host ? cube_b : 0);
+    for (int q = 4; q < 6; ++q) s_c[q] = ws.add(host ? sizeof(double) * n : 0);
+    int s_m[4];
+    for (int q = 0; q < 3; ++q) s_m[q] = ws.add(host ? sizeof(double) * gm : 0);
+    s_m[3] = ws.add(host ? sizeof(int) * gm : 0);
+    int s_qs = ws.add(host ? sizeof(double) * n : 0);
+    int s_qn = ws.add(host ? sizeof(double) * n : 0);
+    int s_lower = ws.add(host ? sizeof(double) * (size_t)n_eff * n_spec : 0);
+    int s_raw = ws.add(sizeof(double) * (size_t)n * n_spec);     // deficits [p][type][n]
+    int s_temp = ws.add(sizeof(double) * gm * n_phase);
+    int s_bi = ws.add(sizeof(double) * gm * n_phase);
+    int s_cells = ws.add(sizeof(int) * gm * n_phase);
+    int s_counts = ws.add(sizeof(int) * n_phase);
+    int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
+    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true);
+    int s_fir = ws.add(fp.bytes);
+    int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
+    int rc = ws.commit();
+    if (rc) return rc;
+#define STAGE(dst, src, bytes, slot)                                               \
+    dst = (decltype(dst))stage_in(ctx, mem, src, bytes, ws.get<void>(slot), &rc); \
+    if (rc) return rc;
+    const double *d_wave;
+    STAGE(d_wave, wave, sizeof(double) * n, s_wave);
+    soapgb_cubes dc;
+    dc.n_mu = n_mu;
+    STAGE(dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
+    STAGE(dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
+    STAGE(dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
+    STAGE(dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
+    STAGE(dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
+    STAGE(dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
+    soapgb_maps dm;
+    const double *cd;
+    STAGE(cd, maps->delta, sizeof(double) * gm, s_m[0]);
+    dm.delta = (double *)cd;
+    STAGE(cd, maps->limb, sizeof(double) * gm, s_m[1]);
+    dm.limb = (double *)cd;
+    STAGE(cd, maps->lb, sizeof(double) * gm, s_m[2]);
+    dm.lb = (double *)cd;
+    const int *ci;
+    STAGE(ci, maps->region, sizeof(int) * gm, s_m[3]);
+    dm.region = (int *)ci;
+    dm.mu = nullptr;
+    const double *d_qs, *d_qn;
+    STAGE(d_qs, quiet_sed, sizeof(double) * n, s_qs);
+    STAGE(d_qn, quiet_norm, sizeof(double) * n, s_qn);
+#undef STAGE
+    double *d_raw = ws.get<double>(s_raw);
+    double *d_temp = ws.get<double>(s_temp), *d_bi = ws.get<double>(s_bi);
+    double *d_lower = host ? ws.get<double>(s_lower) : lower;
+    rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp, d_bi,
+                           ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
+    if (rc) return rc;
+    // deficits in [phase][tot, flux, bconv][n]
+    rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act,
+                          d_raw + n /* flux */, d_raw + 2LL * n /* bconv */, d_raw /* tot */, 3LL * n,
+                          ws.get<int>(s_cells), ws.get<int>(s_counts), ws.get<char>(s_fir), fp);
+    if (rc) return rc;
+    rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, n, d_qs, d_qn, 3,
+                           sigma_v, 50.0, conv_step, conv_step, sentinel, d_lower, n_eff, nullptr, ws.get<char>(s_res));
+    if (rc) return rc;
+    if (raw) {
+        cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n, sizeof(double) * n_eff,
+                                         n_spec, k, ctx->stream));
+    }
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(lower, d_lower, sizeof(double) * (size_t)n_eff * n_spec, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return host ? check_status(ctx, "soapgb_phase_pipeline") : SOAPGB_OK;
+}

@@ -1,0 +1,422 @@
+// a8 / a14: instrumental Gaussian convolution, min/max reductions, normalisation.
+//
+// Reference: SOAP_initialize.cu:69-96,206-294,437-505 and SOAP_resolution.cu:66-310
+// (wav_sigma, conv_inst, reduceMax/MinIdxOptimizedShared, spec_diff, spec_norm:
+// six launches and four blocking copies per spectrum, every reduction block
+// scanning the whole array).  Here:
+//   PLAIN64  -- conv_inst's arithmetic term by term (one thread per pixel, all
+//               2w-1 taps, the reference's operation order), batched over spectra;
+//   FAST64 / FAST32 -- the convolution is linear, so
+//               C = conv(1 - base) + conv(spec);
+//               conv(1 - base) is computed once per base in FP64 and the per-phase
+//               part conv(spec) uses shared tap weights (FP64, or FP32 with FP64
+//               assembly), register-blocked four pixels per thread over staged
+//               spectrum windows.  Taps whose weight is below e^-40 (FAST64) or
+//               e^-30 (FAST32) of the central one are skipped.
+//   min / max -- one pass per spectrum with order-preserving 64-bit integer atomics
+//               (deterministic), then an FP64 normalisation pass.
+#include <algorithm>
+#include <cmath>
+
+#include "internal.cuh"
+#include "resolution.cuh"
+
+using namespace soapgb;
+
+// Delta_lambda_cpu, SOAP_initialize.cu:39-50 (float sqrtf on a double argument)
+static double host_delta_lambda_f32(double line_width, double lambda_line0) {
+    double beta = line_width / SOAP_C_LIGHT;
+    return -1 * lambda_line0 * (1 - (double)sqrtf((float)((1 + beta) / (1 - beta))));
+}
+
+// rndup, SOAP_initialize.cu:19-36
+static double host_rndup(double n, int nb_decimal) {
+    double t = n * pow(10, nb_decimal) - floor(n * pow(10, nb_decimal));
+    if (t >= 0.5) {
+        n *= pow(10, nb_decimal);
+        n = ceil(n);
+        n /= pow(10, nb_decimal);
+    } else {
+        n *= pow(10, nb_decimal);
+        n = floor(n);
+        n /= pow(10, nb_decimal);
+    }
+    return n;
+}
+
+namespace soapgb {
+int conv_halfwidth(double wave0, double wave1, double sigma_v, double window) {
+    double wavelength_step = wave1 - wave0;
+    return (int)host_rndup((window * host_delta_lambda_f32(sigma_v, wave0)) / wavelength_step, 0);
+}
+}  // namespace soapgb
+
+__device__ __forceinline__ unsigned long long soap_ord_enc(double v) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double soap_ord_dec(unsigned long long u) {
+    u = (u & 0x8000000000000000ULL) ? (u & 0x7fffffffffffffffULL) : ~u;
+    return __longlong_as_double((long long)u);
+}
+
+// spectrum s uses base_b when b_every > 0 and s % b_every == b_every - 1
+__device__ __forceinline__ const double *soap_base_for(int s, const double *base_a, const double *base_b, int b_every) {
+    if (b_every > 0 && (s % b_every) == b_every - 1) return base_b;
+    return base_a;
+}
+
+// ---------------------------------------------------------------------------
+// PLAIN64 convolution: conv_inst term by term.  grid (pixel blocks, spectra)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_conv_plain64(int n, int n_eff, const double *__restrict__ lam,
+                                                      const double *__restrict__ spec, long long spec_stride,
+                                                      const double *__restrict__ base_a,
+                                                      const double *__restrict__ base_b, int b_every,
+                                                      double sigma_v, int wid, double step_mult, double step_exp,
+                                                      double *__restrict__ conv, long long conv_stride) {
+    int s = blockIdx.y;
+    int index = blockIdx.x * blockDim.x + threadIdx.x;
+    if (index >= n_eff) return;
+    const double *sp = spec + (long long)s * spec_stride;
+    const double *bp = soap_base_for(s, base_a, base_b, b_every);
+    double acc = 0.0;
+    if ((index > wid) && (index + wid < n - 1)) {
+        double sig = soap_delta_lambda(sigma_v, lam[index]);
+        double norm = __dmul_rn(sig, sqrt(2. * SOAP_PI));
+        double den = __dmul_rn(__dmul_rn(2.0, sig), sig);
+        for (int m = index - wid; m < index + wid - 1; m++) {
+            int d = m - index;
+            double a = bp ? __dsub_rn(bp[m], sp[m]) : sp[m];
+            double e = exp(__ddiv_rn(__dmul_rn(__dmul_rn((double)(-d * d), step_exp), step_exp), den));
+            double t = __dmul_rn(__ddiv_rn(__dmul_rn(__dmul_rn(step_mult, __dsub_rn(1.0, a)), 1.), norm), e);
+            acc = __dadd_rn(acc, t);
+        }
+    }
+    conv[(long long)s * conv_stride + index] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// FAST convolution of x (no "1 -"): out[i] = sum_d w_i(d) x[i+d], d in the
+// reference window [-wid, wid-2] intersected with the significant taps.  Block =
+// 256 threads x 4 pixels = 1024 pixels; SB spectra per block staged in smem.
+// sign: +1 for conv(x), or the base pass computes conv(1 - base) with x = 1 - base.
+// ---------------------------------------------------------------------------
+constexpr int FC_THREADS = 256;
+constexpr int FC_PIX = 4;
+constexpr int FC_TILE = FC_THREADS * FC_PIX;
+
+template <typename T, int SB>
+__global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, const double *__restrict__ lam,
+                                                          const double *__restrict__ spec, long long spec_stride,
+                                                          int n_spec, int one_minus, double sigma_v, int wid,
+                                                          int halo, double step_mult, double step_exp,
+                                                          double cut, double *__restrict__ conv,
+                                                          long long conv_stride) {
+    extern __shared__ unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);
+    int win = FC_TILE + 2 * halo;
+    int i0 = blockIdx.x * FC_TILE;
+    int s0 = blockIdx.y * SB;
+    int nsb = min(SB, n_spec - s0);
+    // stage [i0 - halo, i0 + FC_TILE + halo) of each spectrum (0 outside [0, n))
+    for (int q = 0; q < nsb; ++q) {
+        const double *sp = spec + (long long)(s0 + q) * spec_stride;
+        for (int t = threadIdx.x; t < win; t += FC_THREADS) {
+            int m = i0 - halo + t;
+            double v = (m >= 0 && m < n) ? sp[m] : 0.0;
+            if (one_minus) v = (m >= 0 && m < n) ? 1.0 - v : 0.0;
+            xs[q * win + t] = (T)v;
+        }
+    }
+    __syncthreads();
+    int ib = i0 + threadIdx.x * FC_PIX;   // first pixel of this thread
+    T acc[SB][FC_PIX];
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) acc[q][p] = (T)0;
+    // per-pixel tap parameters
+    double kq[FC_PIX], cq[FC_PIX];
+    int dlo[FC_PIX], dhi[FC_PIX];
+    bool live[FC_PIX];
+    int elo = 1 << 30, ehi = -(1 << 30);
+#pragma unroll
+    for (int p = 0; p < FC_PIX; ++p) {
+        int i = ib + p;
+        live[p] = (i < n_eff) && (i > wid) && (i + wid < n - 1);
+        kq[p] = 0.0;
+        cq[p] = 0.0;
+        dlo[p] = 0;
+        dhi[p] = -1;
+        if (live[p]) {
+            double sig = soap_delta_lambda(sigma_v, lam[i]);
+            kq[p] = step_mult / (sig * sqrt(2. * SOAP_PI));
+            cq[p] = step_exp * step_exp / (2.0 * sig * sig);
+            int r = (int)floor(sqrt(cut / cq[p]));
+            dlo[p] = max(-wid, -r);
+            dhi[p] = min(wid - 2, r);
+            dlo[p] = max(dlo[p], -halo);   // never binds: halo covers the widest reach
+            dhi[p] = min(dhi[p], halo);
+            elo = min(elo, i + dlo[p]);
+            ehi = max(ehi, i + dhi[p]);
+        }
+    }
+    if (elo <= ehi) {
+        for (int e = elo; e <= ehi; ++e) {
+            T w[FC_PIX];
+#pragma unroll
+            for (int p = 0; p < FC_PIX; ++p) {
+                int d = e - (ib + p);
+                if (live[p] && d >= dlo[p] && d <= dhi[p]) {
+                    double arg = -(double)(d * d) * cq[p];
+                    if constexpr (sizeof(T) == 4) w[p] = (T)((float)kq[p] * __expf((float)arg));
+                    else w[p] = (T)(kq[p] * exp(arg));
+                } else {
+                    w[p] = (T)0;
+                }
+            }
+            int li = e - (i0 - halo);
+#pragma unroll
+            for (int q = 0; q < SB; ++q) {
+                if (q < nsb) {
+                    T xv = xs[q * win + li];
+#pragma unroll
+                    for (int p = 0; p < FC_PIX; ++p) acc[q][p] += w[p] * xv;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < SB; ++q) {
+        if (q >= nsb) continue;
+        double *cp = conv + (long long)(s0 + q) * conv_stride;
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            int i = ib + p;
+            if (i < n_eff) cp[i] = live[p] ? (double)acc[q][p] : 0.0;
+        }
+    }
+}
+
+// C_s += Cbase (FP64) where the reference has a C value; fused with min/max.
+// grid (blocks, spectra).  A_s = base - spec over [0, n); C over [0, n_eff).
+__global__ void __launch_bounds__(256) k_minmax(int n, int n_eff, const double *__restrict__ spec,
+                                                long long spec_stride, const double *__restrict__ base_a,
+                                                const double *__restrict__ base_b, int b_every,
+                                                double *__restrict__ conv, long long conv_stride,
+                                                const double *__restrict__ cb_a, const double *__restrict__ cb_b,
+                                                unsigned long long *mm /* n_spec x 2: min A, max C */) {
+    int s = blockIdx.y;
+    const double *sp = spec + (long long)s * spec_stride;
+    const double *bp = soap_base_for(s, base_a, base_b, b_every);
+    const double *cb = soap_base_for(s, cb_a, cb_b, b_every);
+    double *cp = conv + (long long)s * conv_stride;
+    unsigned long long mn = ~0ULL, mx = 0ULL;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double a = bp ? __dsub_rn(bp[i], sp[i]) : sp[i];
+        if (a == a) mn = min(mn, soap_ord_enc(a));
+        if (i < n_eff) {
+            double c = cp[i];
+            if (cb) {   // fast forms: C = conv(1 - base) + conv(spec)
+                c = __dadd_rn(cb[i], c);
+                cp[i] = c;
+            }
+            if (c != 0.0 && c == c) mx = max(mx, soap_ord_enc(c));
+        }
+    }
+    // block reduce
+    __shared__ unsigned long long smn[8], smx[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { smn[w] = mn; smx[w] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) { mn = min(mn, smn[q]); mx = max(mx, smx[q]); }
+        atomicMin(&mm[2 * s], mn);
+        if (mx != 0ULL) atomicMax(&mm[2 * s + 1], mx);
+    }
+}
+
+__global__ void k_minmax_init(int n_spec, double sentinel, unsigned long long *mm) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n_spec) {
+        mm[2 * s] = ~0ULL;
+        mm[2 * s + 1] = soap_ord_enc(sentinel);
+    }
+}
+
+// spec_norm: out = 1 - C (1 - min) / max
+__global__ void __launch_bounds__(256) k_norm(int n_eff, const double *__restrict__ conv, long long conv_stride,
+                                              const unsigned long long *__restrict__ mm, double *__restrict__ out,
+                                              long long out_stride, double *minmax_out) {
+    int s = blockIdx.y;
+    double mn = soap_ord_dec(mm[2 * s]);
+    double mx = soap_ord_dec(mm[2 * s + 1]);
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_eff) {
+        double c = conv[(long long)s * conv_stride + i];
+        out[(long long)s * out_stride + i] = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(c, __dsub_rn(1.0, mn)), mx));
+    }
+    if (minmax_out && blockIdx.x == 0 && threadIdx.x == 0) {
+        minmax_out[2 * s] = mn;
+        minmax_out[2 * s + 1] = mx;
+    }
+}
+
+namespace soapgb {
+
+size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
+    size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
+    b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
+    if (form != SOAPGB_PLAIN64) b += 2 * (sizeof(double) * (size_t)n_eff + 256);  // base convs
+    (void)n;
+    return b;
+}
+
+template <typename T, int SB>
+static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const double *spec,
+                            long long spec_stride, int n_spec, int one_minus, double sigma_v, int wid,
+                            double step_mult, double step_exp, double cut, double *conv, long long conv_stride,
+                            double sig_max) {
+    // halo: the widest significant reach, at the largest sigma (bounded by the window)
+    double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
+    int r = (int)floor(sqrt(cut / cmin)) + 2;
+    int halo = std::min(wid, r);
+    if (halo < 1) halo = 1;
+    size_t smem = sizeof(T) * (size_t)SB * (FC_TILE + 2 * halo);
+    if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
+    if (smem > 48 * 1024)
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv_fast<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
+    k_conv_fast<T, SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, lam, spec, spec_stride, n_spec, one_minus,
+                                                            sigma_v, wid, halo, step_mult, step_exp, cut, conv,
+                                                            conv_stride);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
+                      double wave1, double wave_last, const double *d_spec, long long spec_stride, const double *base_a,
+                      const double *base_b, int b_every, double sigma_v, double window, double step_mult,
+                      double step_exp, double sentinel, double *d_out, long long out_stride, double *d_minmax,
+                      char *scratch) {
+    int wid = conv_halfwidth(wave0, wave1, sigma_v, window);
+    char *p = scratch;
+    double *conv = (double *)p;
+    p += (sizeof(double) * (size_t)n_eff * n_spec + 255) & ~size_t(255);
+    unsigned long long *mm = (unsigned long long *)p;
+    p += (sizeof(unsigned long long) * 2 * n_spec + 255) & ~size_t(255);
+    double *cb_a = nullptr, *cb_b = nullptr;
+    if (form == SOAPGB_PLAIN64) {
+        dim3 g(grid_for(ctx, n_eff, 256), n_spec);
+        k_conv_plain64<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_spec, spec_stride, base_a, base_b, b_every,
+                                                   sigma_v, wid, step_mult, step_exp, conv, n_eff);
+        SOAP_LAUNCHED(ctx);
+    } else {
+        // the largest sigma (sigma grows with wavelength) sets the widest reach
+        double lmax = std::max(std::fabs(wave0), std::fabs(wave_last)) * 1.001;
+        double sig_max = -1 * lmax * (1 - sqrt((1 + sigma_v / SOAP_C_LIGHT) / (1 - sigma_v / SOAP_C_LIGHT)));
+        if (!(sig_max > 0)) return set_error(ctx, SOAPGB_ERR_ARG, "non-positive instrument sigma");
+        double cut = (form == SOAPGB_FAST32) ? 30.0 : 40.0;
+        int rc;
+        if (base_a) {
+            cb_a = (double *)p;
+            p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
+            rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult,
+                                             step_exp, 40.0, cb_a, 0, sig_max);
+            if (rc) return rc;
+        }
+        if (base_b && b_every > 0) {
+            cb_b = (double *)p;
+            p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
+            rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_b, 0, 1, 1, sigma_v, wid, step_mult,
+                                             step_exp, 40.0, cb_b, 0, sig_max);
+            if (rc) return rc;
+        }
+        // without a base the whole (1 - A) is convolved: keep that one-time pass in FP64
+        if (form == SOAPGB_FAST32 && base_a)
+            rc = launch_conv_fast<float, 8>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, 0, sigma_v, wid,
+                                            step_mult, step_exp, cut, conv, n_eff, sig_max);
+        else
+            rc = launch_conv_fast<double, 4>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, base_a ? 0 : 1,
+                                             sigma_v, wid, step_mult, step_exp, base_a ? cut : 40.0, conv, n_eff,
+                                             sig_max);
+        if (rc) return rc;
+    }
+    k_minmax_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm);
+    SOAP_LAUNCHED(ctx);
+    {
+        int bx = std::max(1, std::min(64, (n + 255) / 256));
+        dim3 g(bx, n_spec);
+        k_minmax<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_spec, spec_stride, base_a, base_b, b_every, conv, n_eff,
+                                             cb_a, cb_b, mm);
+        SOAP_LAUNCHED(ctx);
+    }
+    {
+        dim3 g(grid_for(ctx, n_eff, 256), n_spec);
+        k_norm<<<g, 256, 0, ctx->stream>>>(n_eff, conv, n_eff, mm, d_out, out_stride, d_minmax);
+        SOAP_LAUNCHED(ctx);
+    }
+    return SOAPGB_OK;
+}
+
+}  // namespace soapgb
+
+extern "C" int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, const double *wave,
+                                       const double *base, const double *spec, double sigma_v, double window,
+                                       double step_mult, double step_exp, double sentinel, int mem, double *out,
+                                       double *minmax_out) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    if (n < 3 || n_eff < 1 || n_eff > n || n_spec < 0 || !wave || !spec || !out || !(sigma_v > 0) ||
+        !(step_exp > 0))
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution: bad arguments");
+    if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution: unknown form %d", form);
+    if (n_spec == 0) return SOAPGB_OK;
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    bool host = (mem == SOAPGB_HOST);
+    double w01[3];
+    if (host) {
+        w01[0] = wave[0];
+        w01[1] = wave[1];
+        w01[2] = wave[n_eff - 1];
+    } else {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(w01, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(w01 + 2, wave + n_eff - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    int wid = conv_halfwidth(w01[0], w01[1], sigma_v, window);
+    if (wid < 1 || 2 * wid + 2 >= n)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution: convolution half width %d invalid for n=%d", wid, n);
+    Workspace ws(ctx);
+    int s_wave = ws.add(host ? sizeof(double) * n : 0);
+    int s_base = ws.add(host && base ? sizeof(double) * n : 0);
+    int s_spec = ws.add(host ? sizeof(double) * (size_t)n * n_spec : 0);
+    int s_out = ws.add(host ? sizeof(double) * (size_t)n_eff * n_spec : 0);
+    int s_mm = ws.add(host && minmax_out ? sizeof(double) * 2 * n_spec : 0);
+    int s_scr = ws.add(resolution_scratch_bytes(form, n, n_eff, n_spec));
+    int rc = ws.commit();
+    if (rc) return rc;
+    const double *d_wave = (const double *)stage_in(ctx, mem, wave, sizeof(double) * n, ws.get<void>(s_wave), &rc);
+    if (rc) return rc;
+    const double *d_base = (const double *)stage_in(ctx, mem, base, base ? sizeof(double) * n : 0, ws.get<void>(s_base), &rc);
+    if (rc) return rc;
+    const double *d_spec = (const double *)stage_in(ctx, mem, spec, sizeof(double) * (size_t)n * n_spec, ws.get<void>(s_spec), &rc);
+    if (rc) return rc;
+    double *d_out = host ? ws.get<double>(s_out) : out;
+    double *d_mm = minmax_out ? (host ? ws.get<double>(s_mm) : minmax_out) : nullptr;
+    rc = resolution_device(ctx, form, n, n_eff, n_spec, d_wave, w01[0], w01[1], w01[2], d_spec, n, d_base, nullptr, 0,
+                           sigma_v, window, step_mult, step_exp, sentinel, d_out, n_eff, d_mm, ws.get<char>(s_scr));
+    if (rc) return rc;
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)n_eff * n_spec, cudaMemcpyDeviceToHost, ctx->stream));
+        if (minmax_out)
+            SOAP_CUDA(ctx, cudaMemcpyAsync(minmax_out, d_mm, sizeof(double) * 2 * n_spec, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return host ? check_status(ctx, "soapgb_lower_resolution") : SOAPGB_OK;
+}
