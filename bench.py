@@ -1,0 +1,451 @@
+"""Benchmark: phase-spectra/s of the per-phase synthesis path on the 300x300-grid,
+310,000-pixel workload (facula + overlapping spot, 100 phases, R = 115000).
+
+One step = the per-phase stages for all 100 phases: region maps, active-region
+integration of the tot / flux / bconv deficit spectra, instrumental convolution and
+normalisation (SOAP_integration + SOAP_resolution of the reference).  `value` is
+phase-spectra/s with the inputs resident in device memory; `e2e` runs the same call
+through the C ABI with host buffers (pinned), the host-to-device copy of every input
+and the device-to-host copy of the 300 output spectra inside the timed region.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--form fast32|fast64|plain64]
+       python bench.py --impl reference ...   (the reference path's CPU restatement,
+                                               OpenMP on all host cores)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spectra/s at 300² grid, 310k px: FP32-comp vs FP64 at ≤1 cm/s RV error"
+UNIT = "phase-spectra/s"
+C_LIGHT = 299792458.0
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            if ln.startswith("bytes_per_launch"):
+                try:
+                    return float(ln.split("=")[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def rank_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rk = int(os.environ.get("RANK", "0"))
+    lr = int(os.environ.get("LOCAL_RANK", str(rk)))
+    return ws, rk, lr
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(rank=0):
+    from soap_gpu_gb300 import synth
+    case = synth.make_case(1)
+    inp = synth.generate(case)
+    # weak scaling: every rank integrates its own block of phases of the same star
+    phases = case.phases + rank * case.rot_num
+    return case, inp, phases
+
+
+def star_struct(case, lb):
+    import ctypes
+    from soap_gpu_gb300._lib import Star
+    return Star(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                (ctypes.c_double * 4)(*lb))
+
+
+# ---------------------------------------------------------------------------
+# own arm
+# ---------------------------------------------------------------------------
+def run_own(args):
+    import torch
+    from soap_gpu_gb300._lib import Activity
+    from soap_gpu_gb300.api import Context
+    from soap_gpu_gb300 import rv
+
+    ws, rk, lr = rank_info()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(lr)
+    dev = "cuda:%d" % lr
+    case, inp, phases = make_workload(rk)
+    n, n_eff, n_mu = case.n, case.n_eff, case.n_mu
+    lb = inp.lb
+    star = star_struct(case, lb)
+    act = Activity(case.t_star, case.t_diff_spot, case.t_diff_fac, case.nrho, 0)
+    regions = [case.regions for _ in phases]
+    ctx = Context(lr)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    wave_d = T(inp.wave)
+    maps_d = ctx.disk_maps(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                           T(inp.mu_boundary), lb)
+    cubes_np = dict(q_norm=inp.q_norm, q_sed=inp.q_sed, spot_norm=inp.spot_norm, fac_norm=inp.fac_norm,
+                    spot_sed=inp.spot_sed[0], fac_sed=inp.fac_sed[0])
+    cubes_d = {k: T(v) for k, v in cubes_np.items()}
+    form = args.form
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q_norm_d = ctx.quiet_disk(form, wave_d, cubes_d["q_norm"], n_eff, maps_d, case.grid, case.step)
+    q_sed_d = ctx.quiet_disk(form, wave_d, cubes_d["q_sed"], n_eff, maps_d, case.grid, case.step)
+    torch.cuda.synchronize()
+    quiet_ms = (time.perf_counter() - t0) * 1e3
+    phases_d = T(phases)
+    out = torch.empty((len(phases), 3, n_eff), dtype=torch.float64, device=dev)
+
+    def step_dev():
+        ctx.phase_pipeline(form, wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases_d, regions, q_sed_d,
+                           q_norm_d, case.sigma_v, conv_step=case.step, out=out)
+
+    for _ in range(args.warmup):
+        step_dev()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(lr)
+    clocks.start()
+    l0 = ctx.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step_dev()
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        tdist.barrier()
+    clk = clocks.stop()
+    t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    if dist:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    n_units = len(phases) * ws * args.steps
+    value = n_units / (ms_total / 1e3)
+
+    # --- end to end through the C ABI with pinned host buffers ----------------------
+    def pinned(a):
+        t_ = torch.empty(a.shape, dtype=torch.float64 if a.dtype != np.int32 else torch.int32, pin_memory=True)
+        t_.numpy()[...] = a
+        return t_.numpy()
+
+    wave_h = pinned(inp.wave)
+    cubes_h = {k: pinned(np.ascontiguousarray(v)) for k, v in cubes_np.items()}
+    maps_h = {k: pinned(v.cpu().numpy()) for k, v in maps_d.items()}
+    qs_h, qn_h = pinned(q_sed_d.cpu().numpy()), pinned(q_norm_d.cpu().numpy())
+    ph_h = pinned(phases)
+    out_h = pinned(np.zeros((len(phases), 3, n_eff)))
+    h2d = (wave_h.nbytes + sum(v.nbytes for v in cubes_h.values()) + sum(v.nbytes for v in maps_h.values()) -
+           maps_h["mu"].nbytes + qs_h.nbytes + qn_h.nbytes + ph_h.nbytes)
+    d2h = out_h.nbytes
+
+    def step_host():
+        ctx.phase_pipeline(form, wave_h, n_eff, star, maps_h, cubes_h, case.step, act, ph_h, regions, qs_h, qn_h,
+                           case.sigma_v, conv_step=case.step, out=out_h)
+
+    for _ in range(max(1, args.warmup)):
+        step_host()
+    if dist:
+        tdist.barrier()
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    te = (time.perf_counter() - te0) * 1e3
+    te_t = torch.tensor([te], device=dev, dtype=torch.float64)
+    if dist:
+        tdist.all_reduce(te_t, op=tdist.ReduceOp.MAX)
+    e2e_value = n_units / (float(te_t.item()) / 1e3)
+
+    # --- stage timing and roofline of the dominant kernel ----------------------------
+    stage = stage_times(ctx, form, case, inp, wave_d, maps_d, cubes_d, q_sed_d, q_norm_d, phases_d, regions, act)
+    result = None
+    if rk == 0:
+        peak, peak_kind = measured_peaks()
+        dom = max(stage["kernels"], key=lambda k: stage["kernels"][k]["ms"])
+        kd = stage["kernels"][dom]
+        achieved = kd["bytes"] / (kd["ms"] / 1e3) / 1e9
+        traffic = profile_traffic()
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": kd["bytes"], "ms_per_launch": round(kd["ms"], 4)}
+        err = accuracy(ctx, case, inp, form, out, wave_d, maps_d, cubes_d, phases_d, regions, act, star)
+        cpu = cpu_baseline(case, inp, sample_phases=1) if not args.no_cpu else None
+        result = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if form == "fast32" else "f64", "data": "synthetic",
+            "config": {"workload": "300x300 grid, 310,000 px (3800-6900 A at 0.01 A), 20 mu bins, facula 3% + "
+                                   "spot 1% overlapping, 100 phases per GPU, R=115000",
+                       "form": form, "phases_per_step": len(phases), "l2": "inputs (cubes 4x49.6 MB FP64) and "
+                       "outputs (744 MB) exceed the 129 MB L2", "quiet_stage_ms": round(quiet_ms, 2)},
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "accuracy": err,
+            "stages_ms": {k: round(v["ms"], 4) for k, v in stage["kernels"].items()},
+            "clocks": clk,
+        }
+    if dist:
+        tdist.barrier()
+        tdist.destroy_process_group()
+    ctx.close()
+    return result
+
+
+def stage_times(ctx, form, case, inp, wave_d, maps_d, cubes_d, q_sed_d, q_norm_d, phases_d, regions, act):
+    """CUDA-event timing of each stage alone (on the launch stream) + algorithmic bytes."""
+    import torch
+    n, n_eff = case.n, case.n_eff
+    n_phase = len(regions)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    temp, bi = ctx.phase_maps(case.grid, case.incl, phases_d.cpu().numpy(), regions, act)
+    temp_d, bi_d = torch.as_tensor(temp, device=wave_d.device), torch.as_tensor(bi, device=wave_d.device)
+    res = {}
+    res["phase_maps"] = {"ms": timed(lambda: ctx.phase_maps(case.grid, case.incl, phases_d, regions, act)),
+                         "bytes": 2 * 8 * case.grid ** 2 * n_phase}
+    flux = [None]
+
+    def integ():
+        flux[0] = ctx.phase_integrate(form, wave_d, n_eff, case.grid, temp_d, bi_d, maps_d, cubes_d, case.step, act)
+
+    res["integration"] = {"ms": timed(integ)}
+    # algorithmic bytes: the mu rows the active cells touch (6 typed cubes), the
+    # per-cell maps and the three FP64 outputs
+    rows_used = 0
+    for p in range(n_phase):
+        act_cells = bi[p] >= 0
+        rows_used += len(np.unique(maps_d["region"].cpu().numpy()[act_cells]))
+    tsz = 4 if form == "fast32" else 8
+    res["integration"]["bytes"] = rows_used * 6 * n * tsz + 3 * 8 * n * n_phase + 2 * 8 * case.grid ** 2 * n_phase
+    raw = torch.stack([flux[0][2], flux[0][0], flux[0][1]], dim=1).reshape(3 * n_phase, n).contiguous()
+
+    def resol():
+        ctx.lower_resolution(form, wave_d, raw[: 2 * n_phase], n_eff, case.sigma_v, base=q_sed_d,
+                             step_mult=case.step, step_exp=case.step)
+        ctx.lower_resolution(form, wave_d, raw[2 * n_phase:], n_eff, case.sigma_v, base=q_norm_d,
+                             step_mult=case.step, step_exp=case.step)
+
+    res["resolution"] = {"ms": timed(resol), "bytes": 3 * n_phase * (8 * n + 8 * n_eff * 3)}
+    return {"kernels": res}
+
+
+def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, regions, act, star):
+    """Error of the measured form against the plain FP64 form (the reference's
+    arithmetic): max relative flux error of the normalised spectra and the RV / BIS /
+    FWHM differences of the CCF Gaussian fits, in cm/s."""
+    import torch
+    from soap_gpu_gb300 import rv
+    n_eff = case.n_eff
+    q_norm64 = ctx.quiet_disk("plain64", wave_d, cubes_d["q_norm"], n_eff, maps_d, case.grid, case.step)
+    q_sed64 = ctx.quiet_disk("plain64", wave_d, cubes_d["q_sed"], n_eff, maps_d, case.grid, case.step)
+    ref = ctx.phase_pipeline("plain64", wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases_d, regions,
+                             q_sed64, q_norm64, case.sigma_v, conv_step=case.step)
+    torch.cuda.synchronize()
+    o, r = out_d.cpu().numpy(), ref.cpu().numpy()
+    scale = np.max(np.abs(r), axis=2, keepdims=True)
+    flux_err = float(np.max(np.abs(o - r) / scale))
+    wave = inp.wave[:n_eff]
+    series_o = rv.rv_series(ctx, case, wave, o, inp.mask_wave, inp.mask_weight)
+    series_r = rv.rv_series(ctx, case, wave, r, inp.mask_wave, inp.mask_weight)
+    d = {k: float(np.max(np.abs(series_o[k] - series_r[k])) * 100.0) for k in ("rv", "span", "fwhm")}
+    return {"against": "plain64", "flux_rel_max": flux_err, "rv_cms_max": d["rv"], "bis_span_cms_max": d["span"],
+            "fwhm_cms_max": d["fwhm"], "rv_range_ms": float(np.ptp(series_r["rv"]))}
+
+
+def cpu_baseline(case, inp, sample_phases=1):
+    """The reference path's CPU restatement (oracle, OpenMP) on a bounded sample:
+    `sample_phases` phases of the same workload, integration + convolution."""
+    import oracle
+    nth = oracle.num_threads()
+    n_eff = case.n_eff
+    maps = oracle.disk_maps(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                            inp.mu_boundary, inp.lb)
+    # the quiet spectra only scale the normalisation; a coarse-grid disk sum stands in
+    qmaps = oracle.disk_maps(40, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                             inp.mu_boundary, inp.lb)
+    q_norm = oracle.quiet_disk(inp.wave, inp.q_norm, n_eff, qmaps, 40, case.step)
+    q_sed = oracle.quiet_disk(inp.wave, inp.q_sed, n_eff, qmaps, 40, case.step)
+    ph = case.phases[len(case.phases) // 2: len(case.phases) // 2 + sample_phases]
+    t0 = time.perf_counter()
+    for p in ph:
+        temp, bi = oracle.phase_maps(case.grid, case.nrho, case.incl, p, case.regions, case.t_star, case.t_diff_spot,
+                                     case.t_diff_fac)
+        f, b, t = oracle.phase_integrate(inp.wave, n_eff, case.grid, temp, bi, maps, inp.q_norm, inp.q_sed,
+                                         inp.spot_norm, inp.fac_norm, inp.spot_sed[0], inp.fac_sed[0], case.step)
+        for spec, base in ((t, q_sed), (f, q_sed), (b, q_norm)):
+            oracle.lower_resolution(inp.wave, base - spec, n_eff, case.sigma_v, step_mult=case.step,
+                                    step_exp=case.step)
+    dt = time.perf_counter() - t0
+    return {"value": round(len(ph) / dt, 4), "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": "%d phase(s) of the same workload (maps + integration + 3 convolutions), oracle C with "
+                      "OpenMP over pixels" % len(ph), "seconds": round(dt, 3)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    ws, rk, lr = rank_info()
+    if rk != 0:
+        return None
+    from soap_gpu_gb300 import synth
+    import oracle
+    case = synth.make_case(1)
+    inp = synth.generate(case)
+    n_eff = case.n_eff
+    maps = oracle.disk_maps(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                            inp.mu_boundary, inp.lb)
+    qmaps = oracle.disk_maps(40, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                             inp.mu_boundary, inp.lb)
+    q_norm = oracle.quiet_disk(inp.wave, inp.q_norm, n_eff, qmaps, 40, case.step)
+    q_sed = oracle.quiet_disk(inp.wave, inp.q_sed, n_eff, qmaps, 40, case.step)
+
+    def step(p):
+        temp, bi = oracle.phase_maps(case.grid, case.nrho, case.incl, p, case.regions, case.t_star,
+                                     case.t_diff_spot, case.t_diff_fac)
+        f, b, t = oracle.phase_integrate(inp.wave, n_eff, case.grid, temp, bi, maps, inp.q_norm, inp.q_sed,
+                                         inp.spot_norm, inp.fac_norm, inp.spot_sed[0], inp.fac_sed[0], case.step)
+        for spec, base in ((t, q_sed), (f, q_sed), (b, q_norm)):
+            oracle.lower_resolution(inp.wave, base - spec, n_eff, case.sigma_v, step_mult=case.step,
+                                    step_exp=case.step)
+
+    phases = case.phases
+    for w in range(args.warmup):
+        step(phases[w % len(phases)])
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        step(phases[(args.warmup + s) % len(phases)])
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    nth = oracle.num_threads()
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "300x300 grid, 310,000 px, facula + spot, one phase per step (a bounded sample "
+                                   "of the 100-phase job)", "form": "reference CPU restatement"},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": "one phase per step: maps + integration + 3 convolutions"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="own", choices=["own", "reference"])
+    ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "own":
+        args.warmup = 3
+    res = run_reference(args) if args.impl == "reference" else run_own(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

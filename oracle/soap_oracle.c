@@ -159,11 +159,16 @@ static void orc_cell_interp(int sem, int n, int n_eff, const double *lambda,
             for (int j = 0; j < n_eff; j++) out[j] = row[j] * limb;
             return;
         }
+        #pragma omp parallel for schedule(static)
         for (int i = 0; i < n_eff; i++)   /* fast_shift, SOAP_initialize.cu:125 */
             lshift[i] = lambda[i] + orc_delta_lambda(delta * 1000., lambda[i]);
+        #pragma omp parallel for schedule(static)
         for (int j = 0; j < n_eff; j++) out[j] = 0.0;
-        long c_lo = orc_ceil_pos(0, fbeta, lambda0, step);
-        for (int i = 0; i + 1 < n_eff; i++) {
+        /* every source i owns the pixels [ceil(x_i), ceil(x_{i+1})): disjoint ranges,
+         * so the sources can be processed in parallel */
+        #pragma omp parallel for schedule(static)
+        for (int i = 0; i < n_eff - 1; i++) {
+            long c_lo = orc_ceil_pos(i, fbeta, lambda0, step);
             long c_hi = orc_ceil_pos(i + 1, fbeta, lambda0, step);
             long j0 = c_lo < 0 ? 0 : c_lo;
             long j1 = c_hi > n_eff ? n_eff : c_hi;
@@ -173,7 +178,6 @@ static void orc_cell_interp(int sem, int n, int n_eff, const double *lambda,
                 for (long j = j0; j < j1; j++)
                     out[j] = (row[i] + g / d * (lambda[j] - lshift[i])) * limb;
             }
-            c_lo = c_hi;
         }
         return;
     }
@@ -208,6 +212,7 @@ void orc_quiet_disk(int sem, int n, int n_eff, const double *lambda, const doubl
         if (limb_maps[k] == -999.0) continue;   /* invisible cell */
         const double *row = cube + (size_t)region_maps[k] * n;
         orc_cell_interp(sem, n, n_eff, lambda, row, delta_maps[k], limb_maps[k], step, lshift, tmp);
+        #pragma omp parallel for schedule(static)
         for (int j = 0; j < n_eff; j++) sum_out[j] = sum_out[j] + tmp[j];   /* fast_sum */
     }
     free(lshift);
@@ -420,12 +425,14 @@ void orc_phase_integrate(int sem, int n, int n_eff, const double *lambda, int gr
         orc_cell_interp(sem, n, n_eff, lambda, q_sed + off, d, l, step, lshift, sv);
         if (bi == 0.0) {
             int t_norm = (int)temp_maps[k];
+            #pragma omp parallel for schedule(static)
             for (int j = 0; j < n_eff; j++)       /* fast_intensity */
                 inten[j] = orc_planck(lambda[j], temp_maps[k]) / orc_planck(lambda[j], t_norm) * spot_sed[j];
             orc_cell_interp(sem, n, n_eff, lambda, spot_norm + off, d, l, step, lshift, a);
         } else {
             if (solar) {                          /* SOAP_integration_solar.cu:427,433 */
                 int t_norm = (int)(t_star + t_diff_fac + 0.9 - 216.8);
+                #pragma omp parallel for schedule(static)
                 for (int j = 0; j < n_eff; j++)
                     inten[j] = orc_planck(lambda[j], temp_maps[k]) / orc_planck(lambda[j], t_norm) * fac_sed[j];
             } else {                              /* fast_intensity_fac */
@@ -433,6 +440,7 @@ void orc_phase_integrate(int sem, int n, int n_eff, const double *lambda, int gr
             }
             orc_cell_interp(sem, n, n_eff, lambda, fac_norm + off, d, l, step, lshift, a);
         }
+        #pragma omp parallel for schedule(static)
         for (int j = 0; j < n_eff; j++) {         /* fast_flux / fast_bconv / fast_tot */
             flux[j] = flux[j] + sv[j] - inten[j] * q[j];
             bconv[j] = bconv[j] + q[j] - a[j];

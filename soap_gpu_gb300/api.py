@@ -173,7 +173,7 @@ class Context:
         return off, reg
 
     def phase_maps(self, grid, incl, phases, regions_per_phase, act: Activity):
-        a = self._args()
+        a = self._args(phases)
         off, reg = self._regions(regions_per_phase)
         n_phase = len(phases)
         gm = int(grid) ** 2

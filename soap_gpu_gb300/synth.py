@@ -269,14 +269,14 @@ def write_reference_layout(inp: Inputs, root: str, output_prefix: str = "",
     lines = ["[main]", "", "grid     : %d" % case.grid, "nrho     : %d" % case.nrho,
              "instrument_reso : %d" % case.inst_reso, "rot_num: %r" % case.rot_num,
              "rot_step: %r" % case.rot_step, "", "", "[star]", "",
-             "radius_sun : %d" % R_SUN_KM, "radius     : %r" % case.radius, "prot       : %r" % case.period,
+             "radius_sun : %d" % R_SUN_KM, "radius     : %r" % case.radius, "prot       : %r" % float(case.period),
              "W_ratio    : %r" % case.w_ratio, "I          : %r" % case.incl,
              "Tstar      : %d" % case.t_star, "Tdiff_spot : %d" % case.t_diff_spot,
              "Tdiff_faculae : %d" % case.t_diff_fac, "limb1      : %r" % case.u1,
              "limb2      : %r" % case.u2, "N_act: %d" % len(case.regions), ""]
     for i, (lat, lon, size, typ) in enumerate(case.regions):
-        lines += ["[active_regions_%d]" % (i + 1), "longitude: %r" % lon, "latitude: %r" % lat,
-                  "size: %r" % size, "type: %d" % int(typ), ""]
+        lines += ["[active_regions_%d]" % (i + 1), "longitude: %r" % float(lon), "latitude: %r" % float(lat),
+                  "size: %r" % float(size), "type: %d" % int(typ), ""]
     lines += ["[data_io]", "no_thread: 512", "input_prefix: .", "output_prefix: %s" % output_prefix,
               "file_prefix: ", "input_dir: /input_spec/", "maps_dir: /SOAP_density/",
               "raw_dir: /SOAP_raw_spec/", "spec_dir: /SOAP_resolution/",

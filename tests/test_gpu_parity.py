@@ -2,7 +2,9 @@
 
 Tolerances: integer / index outputs (mu bins, visibility, region maps, CCF mask
 entries) bit-exact; PLAIN64 spectra within 1e-12 relative to the spectrum's scale
-(the reference's arithmetic, one rounding per operation); FAST64 within 1e-11;
+(the reference's arithmetic, one rounding per operation);
+FAST64 (the collapsed form re-associates the cell sum and evaluates the shifted
+position analytically instead of through lambda differences) within 5e-11;
 FAST32 within 2e-6 of scale (the precision form's flux budget is 1e-6 on the final
 normalised spectra, checked at full size in test_gpu_fullsize.py).
 """
@@ -35,7 +37,7 @@ def test_quiet_disk_plain64(ctx, grid, n):
     assert rel_err(got, ref) <= 1e-13
 
 
-@pytest.mark.parametrize("form,tol", [("fast64", 1e-12), ("fast32", 1e-6)])
+@pytest.mark.parametrize("form,tol", [("fast64", 5e-11), ("fast32", 1e-6)])
 @pytest.mark.parametrize("grid,n", [(40, 4200), (33, 4096), (17, 2100)])
 def test_quiet_disk_fast(ctx, form, tol, grid, n):
     inp = small_inputs(grid=grid, n=n)
@@ -140,7 +142,7 @@ def test_phase_integrate_plain64(ctx, solar):
         assert rel_err(tot[p], rt) <= tol
 
 
-@pytest.mark.parametrize("form,tol", [("fast64", 1e-12), ("fast32", 1e-6)])
+@pytest.mark.parametrize("form,tol", [("fast64", 5e-11), ("fast32", 1e-6)])
 @pytest.mark.parametrize("solar", [False, True])
 def test_phase_integrate_fast(ctx, form, tol, solar):
     inp = small_inputs()

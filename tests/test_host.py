@@ -1,0 +1,57 @@
+"""Host-side logic: synthetic inputs, the config_hpc.cfg layout, file formats."""
+import os
+
+import numpy as np
+
+from soap_gpu_gb300 import config, synth
+
+
+def test_cases_match_the_workload_definitions():
+    c0, c1 = synth.make_case(0), synth.make_case(1)
+    assert (c0.grid, c0.n, c0.n_eff, c0.n_mu, c0.n_phase, len(c0.velocities)) == (100, 20000, 19968, 10, 25, 81)
+    assert (c1.grid, c1.n, c1.n_eff, c1.n_mu, c1.n_phase, len(c1.velocities)) == (300, 310000, 309760, 20, 100, 161)
+    assert abs(c0.sigma_v - 1107.0446527883928) < 1e-9
+    # vsini 2 km/s at the equator, inclination 90
+    v_eq = 2 * np.pi * c0.radius_km / (c0.period * 86400.0)
+    assert abs(v_eq - 2.0) < 1e-12
+    # 1 % of the hemisphere for s = 0.1, 3 % for s = 0.1732
+    assert abs(c1.regions[1, 2] ** 2 - 0.01) < 1e-12 and abs(c1.regions[0, 2] ** 2 - 0.03) < 1e-4
+
+
+def test_generator_is_deterministic_and_sane():
+    case = synth.small_case(seed=5, grid=20, n=3000, n_phase=2, n_mu=4)
+    a, b = synth.generate(case), synth.generate(case)
+    assert np.array_equal(a.q_norm, b.q_norm) and np.array_equal(a.mask_wave, b.mask_wave)
+    assert a.q_norm.shape == (4, 3000)
+    assert np.all(a.q_norm <= 1.0 + 1e-12) and np.all(a.q_norm >= 0.0)
+    assert np.all(np.diff(a.mu_boundary) < 0)
+    assert np.allclose(np.diff(a.wave), case.step)
+
+
+def test_reference_layout_round_trip(tmp_path):
+    case = synth.small_case(seed=2, grid=24, n=2600, n_phase=3, n_mu=4)
+    inp = synth.generate(case)
+    cfg_path = synth.write_reference_layout(inp, str(tmp_path))
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        rc = config.load_config(cfg_path)
+        assert rc.grid == case.grid and rc.nrho == case.nrho
+        assert abs(rc.inst_sigma - case.sigma_v) < 1e-9
+        assert np.allclose(rc.regions, case.regions)
+        assert len(rc.phases) == case.n_phase
+        assert np.allclose(rc.velocities, case.velocities)
+        for key, path in rc.cube_paths.items():
+            arr = np.fromfile(path, dtype=np.float64).reshape(case.n_mu, case.n)
+            assert np.array_equal(arr, getattr(inp, key)), key
+        wave = np.fromfile(rc.input_dir + rc.wave_array_name)
+        assert np.array_equal(wave, inp.wave)
+        mu = np.fromfile(rc.input_dir + rc.mu_array_name)
+        assert mu.size == case.n_mu - 1
+        lbf = np.load(rc.input_dir + "Limb_brightening_info.npz")
+        lb = config.lb_params(rc.t_star, lbf["LB_G2"], lbf["LB_K0"], lbf["LB_M0"], lbf["Temp_array"])
+        assert np.allclose(lb, inp.lb)
+        mask = np.loadtxt(rc.input_prefix + rc.mask_prefix + config.mask_template_name(rc.t_star))
+        assert mask.shape[1] == 2
+    finally:
+        os.chdir(cwd)
