@@ -247,12 +247,14 @@ def mask_name(t_star: float) -> str:
     return types[int(np.argmin(np.abs(teff - t_star)))] + '_mask.txt'
 
 
-def write_reference_layout(inp: Inputs, root: str, output_prefix: str = "",
+def write_reference_layout(inp: Inputs, root: str, output_prefix: str = "", file_prefix: str = "syn",
                            keyword: str = "nreal") -> str:
     """Write input_spec/, input_mask/ and config_hpc.cfg under ``root``.
 
     The layout is the one ``run_all_SOAP.py`` reads (``config_hpc.cfg`` keys at
-    ``run_all_SOAP.py:56-127``); returns the config path.
+    ``run_all_SOAP.py:56-127``); returns the config path.  ``file_prefix`` must not be
+    empty: the driver joins argv with spaces for ``os.system``, so an empty prefix
+    would vanish from the command line and shift every later argument.
     """
     case = inp.case
     spec_dir = os.path.join(root, "input_spec")
@@ -278,7 +280,7 @@ def write_reference_layout(inp: Inputs, root: str, output_prefix: str = "",
         lines += ["[active_regions_%d]" % (i + 1), "longitude: %r" % float(lon), "latitude: %r" % float(lat),
                   "size: %r" % float(size), "type: %d" % int(typ), ""]
     lines += ["[data_io]", "no_thread: 512", "input_prefix: .", "output_prefix: %s" % output_prefix,
-              "file_prefix: ", "input_dir: /input_spec/", "maps_dir: /SOAP_density/",
+              "file_prefix: %s" % file_prefix, "input_dir: /input_spec/", "maps_dir: /SOAP_density/",
               "raw_dir: /SOAP_raw_spec/", "spec_dir: /SOAP_resolution/",
               "mu_array_name: mu_boundary_array.bin", "wave_array_name: solar_wavelength.bin",
               "CCF_window: %r" % case.ccf_window, "CCF_size: %r" % case.ccf_size,
