@@ -204,6 +204,28 @@ int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const dou
                           const double *quiet_norm, double sigma_v, double conv_step,
                           double sentinel, int mem, double *lower, double *raw);
 
+/* ---- allocation-free convolution + normalisation --------------------------
+ * No counterpart in the reference: an extra entry point of this library.  The
+ * same computation as soapgb_lower_resolution in the PLAIN64 form, for callers
+ * that must not have the library allocate device memory -- an application whose
+ * device memory belongs to another allocator (a framework's caching pool or an
+ * arena reserved at start-up), or a latency-bound loop that cannot absorb the
+ * device-wide synchronisation of cudaMalloc / cudaFree.  Its scratch is a fixed
+ * SOAPGB_NOALLOC_SCRATCH_BYTES array in the library's device image, held by every
+ * GPU that loads the library until the process exits; soapgb_noalloc_capacity(n_eff)
+ * gives how many spectra of n_eff pixels fit in one call, and larger requests are
+ * rejected with SOAPGB_ERR_ARG.  All array arguments are device pointers.  The
+ * first call on a device looks up the array's device address (a
+ * cudaGetSymbolAddress call with that device current); make that first call before
+ * any stream capture.  Calls share the array: two calls whose work overlaps on the
+ * GPU (different streams or contexts on one device) race on it. */
+#define SOAPGB_NOALLOC_SCRATCH_BYTES (8 * 1024 * 1024)
+size_t soapgb_noalloc_capacity(int n_eff);
+int soapgb_lower_resolution_noalloc(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *wave,
+                                    const double *base, const double *spec, double sigma_v,
+                                    double window, double step_mult, double step_exp,
+                                    double sentinel, double *out, double *minmax_out);
+
 #ifdef __cplusplus
 }
 #endif
