@@ -122,12 +122,12 @@ def rank_info():
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
-def make_workload(rank=0):
+def make_workload(rank=0, n_phase=100):
     from soap_gpu_gb300 import synth
     case = synth.make_case(1)
     inp = synth.generate(case)
     # weak scaling: every rank integrates its own block of phases of the same star
-    phases = case.phases + rank * case.rot_num
+    phases = (case.phases + rank * case.rot_num)[:n_phase]
     return case, inp, phases
 
 
@@ -154,7 +154,7 @@ def run_own(args):
         tdist.init_process_group("nccl")
     torch.cuda.set_device(lr)
     dev = "cuda:%d" % lr
-    case, inp, phases = make_workload(rk)
+    case, inp, phases = make_workload(rk, args.phases)
     n, n_eff, n_mu = case.n, case.n_eff, case.n_mu
     lb = inp.lb
     star = star_struct(case, lb)
@@ -201,6 +201,10 @@ def run_own(args):
     torch.cuda.synchronize()
     launches = ctx.launches - l0
     ms = ev0.elapsed_time(ev1)
+    if args.profile_only:
+        clocks.stop()
+        ctx.close()
+        return {"profile_only": True, "ms_per_step": ms / args.steps, "launches_per_step": launches / args.steps}
     if dist:
         tdist.barrier()
     clk = clocks.stop()
@@ -439,6 +443,9 @@ def main():
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only the warm-up and timed device steps (for ncu launch lists)")
+    ap.add_argument("--phases", type=int, default=100, help="phases per step (100 is the benchmarked workload)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "own":
         args.warmup = 3

@@ -43,6 +43,7 @@ struct CellGeo {
     double dlt;    // ir - 1
     double L;      // limb darkening
     double w2;     // (1 + LB) L
+    float Lf, w2f, dltf;   // the same in FP32 (the FP32 form's coefficients)
     int row;       // mu bin
     int zero_v;    // delta == 0: the reference copies the row
 };
@@ -63,6 +64,9 @@ __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const
     g.dlt = g.ir - 1.0;
     g.L = limb[k];
     g.w2 = lb ? (1.0 + lb[k]) * g.L : g.L;
+    g.Lf = (float)g.L;
+    g.w2f = (float)g.w2;
+    g.dltf = (float)g.dlt;
     int row = region[k];
     if ((unsigned)row >= (unsigned)n_mu && g.L > -998.0) {
         atomicExch(status, 21);
@@ -148,27 +152,62 @@ struct FirShared {
     unsigned key[FIR_HASH];
     double val[FIR_HASH][3];
     int grp[FIR_HASH];
+    float gcoef[FIR_HASH][3];   // FP32 form: group coefficients for the apply phase
     Exc exc[FIR_EXC];
     int nexc, ngrp;
 };
 
+// float pair with an error term (TwoSum): the FP32 form reduces runs of up to 32
+// coefficient terms without growing the rounding error
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    float s = a.hi + b.hi;
+    float bp = s - a.hi;
+    float e = (a.hi - (s - bp)) + (b.hi - bp);
+    e += a.lo + b.lo;
+    float hi = s + e;
+    F2 r;
+    r.hi = hi;
+    r.lo = e - (hi - s);
+    return r;
+}
+
+template <typename V>
+__device__ __forceinline__ V shfl_up_v(V v, int o);
+template <>
+__device__ __forceinline__ double shfl_up_v<double>(double v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
+template <>
+__device__ __forceinline__ F2 shfl_up_v<F2>(F2 v, int o) {
+    F2 r;
+    r.hi = __shfl_up_sync(0xffffffffu, v.hi, o);
+    r.lo = __shfl_up_sync(0xffffffffu, v.lo, o);
+    return r;
+}
+__device__ __forceinline__ double v_add(double a, double b) { return a + b; }
+__device__ __forceinline__ F2 v_add(F2 a, F2 b) { return f2_add(a, b); }
+__device__ __forceinline__ double v_get(double a) { return a; }
+__device__ __forceinline__ double v_get(F2 a) { return (double)a.hi + (double)a.lo; }
+
 // One pass of the warp-cooperative insertion: lanes holding a key (active) fold
-// runs of equal keys and the run's last lane adds the sums to the hash table.
-// Returns whether this lane's contribution reached the table.
-__device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned key, double a0, double a1,
-                                           double bb, int lane) {
+// runs of equal keys (segmented scan) and the run's last lane adds the sums to the
+// shared hash table.  Returns whether this lane's contribution reached the table.
+// V = double (FAST64) or F2 (FAST32: compensated FP32 pairs).
+template <typename V>
+__device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned key, V a0, V a1, V bb, int lane) {
     if (!active) key = 0xfffffffeu;
     unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
     bool seg = (lane == 0) || (prev != key);
     for (int o = 1; o < 32; o <<= 1) {
-        double v0 = __shfl_up_sync(0xffffffffu, a0, o);
-        double v1 = __shfl_up_sync(0xffffffffu, a1, o);
-        double v2 = __shfl_up_sync(0xffffffffu, bb, o);
+        V v0 = shfl_up_v(a0, o);
+        V v1 = shfl_up_v(a1, o);
+        V v2 = shfl_up_v(bb, o);
         int sg = __shfl_up_sync(0xffffffffu, (int)seg, o);
         if (lane >= o && !seg) {
-            a0 += v0;
-            a1 += v1;
-            bb += v2;
+            a0 = v_add(a0, v0);
+            a1 = v_add(a1, v1);
+            bb = v_add(bb, v2);
             seg = sg;
         }
     }
@@ -181,9 +220,9 @@ __device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned 
         for (int probe = 0; probe < 64 && !ok; ++probe) {
             unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
             if (old == 0xffffffffu || old == key) {
-                atomicAdd(&sh.val[h][0], a0);
-                atomicAdd(&sh.val[h][1], a1);
-                atomicAdd(&sh.val[h][2], bb);
+                atomicAdd(&sh.val[h][0], v_get(a0));
+                atomicAdd(&sh.val[h][1], v_get(a1));
+                atomicAdd(&sh.val[h][2], v_get(bb));
                 ok = true;
             } else {
                 h = (h + 1) & (FIR_HASH - 1);
@@ -195,6 +234,23 @@ __device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned 
     int my_tail = __ffs(tails & (0xffffffffu << lane)) - 1;
     int tail_ok = __shfl_sync(0xffffffffu, (int)ok, my_tail);
     return !active || tail_ok;
+}
+
+template <typename T>
+__device__ __forceinline__ auto coef3(T w, T phi, T dlt) {
+    if constexpr (sizeof(T) == 4) {
+        struct R { F2 a0, a1, bb; } r;
+        r.a0 = F2{w * (1.0f - phi), 0.0f};
+        r.a1 = F2{w * phi, 0.0f};
+        r.bb = F2{w * dlt, 0.0f};
+        return r;
+    } else {
+        struct R { double a0, a1, bb; } r;
+        r.a0 = w * (1.0 - phi);
+        r.a1 = w * phi;
+        r.bb = w * dlt;
+        return r;
+    }
 }
 
 template <typename T, int MODE>
@@ -260,12 +316,12 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                     i = j;
                     w = (T)0;
                 } else {
-                    double wd = x.phi + x.dlt * (double)dj;
+                    T wd = (T)x.phi + (T)x.dlt * (T)dj;
                     i = (long long)x.i0 + dj;
-                    if (wd >= 1.0) { wd -= 1.0; i += 1; }
-                    else if (wd < 0.0) { wd += 1.0; i -= 1; }
+                    if (wd >= (T)1) { wd -= (T)1; i += 1; }
+                    else if (wd < (T)0) { wd += (T)1; i -= 1; }
                     if (i < 0 || i > n_eff - 2) continue;
-                    w = (T)wd;
+                    w = wd;
                 }
                 auto val = [&](int ci) -> T {
                     const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
@@ -318,12 +374,17 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                 kind = (pb[cell] == 0.0) ? 0 : 1;
                 tcell = pt[cell];
             }
+            // the only FP64 step: the cell's source position at the tile start
             double u0 = fma((double)j0, g.ir, -g.offir);
             double fl = floor(u0);
             i0 = (long long)fl;
             phi = u0 - fl;
-            double w_end = phi + g.dlt * (double)(t_eff - 1);
-            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= 0.0) && (w_end < 1.0);
+            T phi_t = (T)phi;
+            T dlt_t;
+            if constexpr (sizeof(T) == 4) dlt_t = g.dltf;
+            else dlt_t = g.dlt;
+            T w_end = phi_t + dlt_t * (T)(t_eff - 1);
+            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= (T)0) && (w_end < (T)1);
             if (g.zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
             if constexpr (MODE == MODE_PHASE) {
                 if (kind == 0 && (double)(int)tcell != tcell) regular = false;   // spot Planck ratio != 1
@@ -332,13 +393,16 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         }
         int k = j0 - (int)i0;
         // pass A: weight L (spot: kind 0, facula: kind 1; quiet: kind 0)
-        bool okA = fir_insert(sh, have && regular, fir_key(kind, g.row, k), g.L * (1.0 - phi), g.L * phi,
-                              g.L * g.dlt, lane);
+        T Lw, W2w, Dw;
+        if constexpr (sizeof(T) == 4) { Lw = g.Lf; W2w = g.w2f; Dw = g.dltf; }
+        else { Lw = g.L; W2w = g.w2; Dw = g.dlt; }
+        auto ca = coef3<T>(Lw, (T)phi, Dw);
+        bool okA = fir_insert(sh, have && regular, fir_key(kind, g.row, k), ca.a0, ca.a1, ca.bb, lane);
         bool okB = true;
         if constexpr (MODE == MODE_PHASE) {
             // pass B: facula (1 + LB) L weight
-            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, g.row, k), g.w2 * (1.0 - phi),
-                             g.w2 * phi, g.w2 * g.dlt, lane);
+            auto cb = coef3<T>(W2w, (T)phi, Dw);
+            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, g.row, k), cb.a0, cb.a1, cb.bb, lane);
         }
         int parts = 0;
         if (have) {
@@ -377,6 +441,13 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         sh.ngrp = ng;
     }
     __syncthreads();
+    for (int e = tid; e < sh.ngrp; e += FIR_THREADS) {
+        int h = sh.grp[e];
+        sh.gcoef[e][0] = (float)sh.val[h][0];
+        sh.gcoef[e][1] = (float)sh.val[h][1];
+        sh.gcoef[e][2] = (float)sh.val[h][2];
+    }
+    __syncthreads();
     // --- apply the collapsed groups ---------------------------------------------
     int ng = sh.ngrp;
     for (int e = 0; e < ng; ++e) {
@@ -385,7 +456,16 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         int kind = (int)(key >> 28);
         int row = (int)((key >> 16) & 0xfff);
         int k = (int)(key & 0xffff) - 16384;
-        double A0 = sh.val[h][0], A1 = sh.val[h][1], B = sh.val[h][2];
+        T A0, A1, B;
+        if constexpr (sizeof(T) == 4) {
+            A0 = sh.gcoef[e][0];
+            A1 = sh.gcoef[e][1];
+            B = sh.gcoef[e][2];
+        } else {
+            A0 = sh.val[h][0];
+            A1 = sh.val[h][1];
+            B = sh.val[h][2];
+        }
         long long off = (long long)row * n;
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) {
@@ -393,8 +473,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             int j = j0 + dj;
             if (j >= n_eff) continue;
             long long i = (long long)j - k;
-            T c0 = (T)(A0 - B * (double)dj);
-            T c1 = (T)(A1 + B * (double)dj);
+            T c0 = A0 - B * (T)dj;
+            T c1 = A1 + B * (T)dj;
             auto two = [&](int ci) -> T {
                 const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
                 return c0 * rowp[i] + c1 * rowp[i + 1];

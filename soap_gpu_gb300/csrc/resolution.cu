@@ -96,6 +96,30 @@ __global__ void __launch_bounds__(256) k_conv_plain64(int n, int n_eff, const do
     conv[(long long)s * conv_stride + index] = acc;
 }
 
+// per-pixel tap parameters of the fast forms: weight scale kq = step_mult / (s sqrt(2 pi)),
+// exponent coefficient cq = step_exp^2 / (2 s^2), significant tap range [dlo, dhi]
+// (dhi < dlo marks a pixel outside the reference's convolution interior)
+template <typename T>
+__global__ void k_conv_params(int n, int n_eff, const double *__restrict__ lam, double sigma_v, int wid, int halo,
+                              double step_mult, double step_exp, double cut, T *kq, T *cq, int2 *rng) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    bool live = (i > wid) && (i + wid < n - 1);
+    double k = 0.0, c = 0.0;
+    int lo = 0, hi = -1;
+    if (live) {
+        double sig = soap_delta_lambda(sigma_v, lam[i]);
+        k = step_mult / (sig * sqrt(2. * SOAP_PI));
+        c = step_exp * step_exp / (2.0 * sig * sig);
+        int r = (int)floor(sqrt(cut / c));
+        lo = max(max(-wid, -r), -halo);
+        hi = min(min(wid - 2, r), halo);
+    }
+    kq[i] = (T)k;
+    cq[i] = (T)c;
+    rng[i] = make_int2(lo, hi);
+}
+
 // ---------------------------------------------------------------------------
 // FAST convolution of x (no "1 -"): out[i] = sum_d w_i(d) x[i+d], d in the
 // reference window [-wid, wid-2] intersected with the significant taps.  Block =
@@ -107,12 +131,11 @@ constexpr int FC_PIX = 4;
 constexpr int FC_TILE = FC_THREADS * FC_PIX;
 
 template <typename T, int SB>
-__global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, const double *__restrict__ lam,
+__global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, const T *__restrict__ kqa,
+                                                          const T *__restrict__ cqa, const int2 *__restrict__ rnga,
                                                           const double *__restrict__ spec, long long spec_stride,
-                                                          int n_spec, int one_minus, double sigma_v, int wid,
-                                                          int halo, double step_mult, double step_exp,
-                                                          double cut, double *__restrict__ conv,
-                                                          long long conv_stride) {
+                                                          int n_spec, int one_minus, int halo,
+                                                          double *__restrict__ conv, long long conv_stride) {
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);
     int win = FC_TILE + 2 * halo;
@@ -136,30 +159,26 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
     for (int q = 0; q < SB; ++q)
 #pragma unroll
         for (int p = 0; p < FC_PIX; ++p) acc[q][p] = (T)0;
-    // per-pixel tap parameters
-    double kq[FC_PIX], cq[FC_PIX];
+    T kq[FC_PIX], cq[FC_PIX];
     int dlo[FC_PIX], dhi[FC_PIX];
-    bool live[FC_PIX];
     int elo = 1 << 30, ehi = -(1 << 30);
 #pragma unroll
     for (int p = 0; p < FC_PIX; ++p) {
         int i = ib + p;
-        live[p] = (i < n_eff) && (i > wid) && (i + wid < n - 1);
-        kq[p] = 0.0;
-        cq[p] = 0.0;
+        kq[p] = (T)0;
+        cq[p] = (T)0;
         dlo[p] = 0;
         dhi[p] = -1;
-        if (live[p]) {
-            double sig = soap_delta_lambda(sigma_v, lam[i]);
-            kq[p] = step_mult / (sig * sqrt(2. * SOAP_PI));
-            cq[p] = step_exp * step_exp / (2.0 * sig * sig);
-            int r = (int)floor(sqrt(cut / cq[p]));
-            dlo[p] = max(-wid, -r);
-            dhi[p] = min(wid - 2, r);
-            dlo[p] = max(dlo[p], -halo);   // never binds: halo covers the widest reach
-            dhi[p] = min(dhi[p], halo);
-            elo = min(elo, i + dlo[p]);
-            ehi = max(ehi, i + dhi[p]);
+        if (i < n_eff) {
+            kq[p] = kqa[i];
+            cq[p] = cqa[i];
+            int2 r = rnga[i];
+            dlo[p] = r.x;
+            dhi[p] = r.y;
+            if (r.x <= r.y) {
+                elo = min(elo, i + r.x);
+                ehi = max(ehi, i + r.y);
+            }
         }
     }
     if (elo <= ehi) {
@@ -168,10 +187,10 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) {
                 int d = e - (ib + p);
-                if (live[p] && d >= dlo[p] && d <= dhi[p]) {
-                    double arg = -(double)(d * d) * cq[p];
-                    if constexpr (sizeof(T) == 4) w[p] = (T)((float)kq[p] * __expf((float)arg));
-                    else w[p] = (T)(kq[p] * exp(arg));
+                if (d >= dlo[p] && d <= dhi[p]) {
+                    T arg = -(T)(d * d) * cq[p];
+                    if constexpr (sizeof(T) == 4) w[p] = kq[p] * __expf(arg);
+                    else w[p] = kq[p] * exp(arg);
                 } else {
                     w[p] = (T)0;
                 }
@@ -194,7 +213,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
 #pragma unroll
         for (int p = 0; p < FC_PIX; ++p) {
             int i = ib + p;
-            if (i < n_eff) cp[i] = live[p] ? (double)acc[q][p] : 0.0;
+            if (i < n_eff) cp[i] = (dlo[p] <= dhi[p]) ? (double)acc[q][p] : 0.0;
         }
     }
 }
@@ -252,14 +271,17 @@ __global__ void k_minmax_init(int n_spec, double sentinel, unsigned long long *m
 // spec_norm: out = 1 - C (1 - min) / max
 __global__ void __launch_bounds__(256) k_norm(int n_eff, const double *__restrict__ conv, long long conv_stride,
                                               const unsigned long long *__restrict__ mm, double *__restrict__ out,
-                                              long long out_stride, double *minmax_out) {
+                                              long long out_stride, double *minmax_out, int exact) {
     int s = blockIdx.y;
     double mn = soap_ord_dec(mm[2 * s]);
     double mx = soap_ord_dec(mm[2 * s + 1]);
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_eff) {
         double c = conv[(long long)s * conv_stride + i];
-        out[(long long)s * out_stride + i] = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(c, __dsub_rn(1.0, mn)), mx));
+        if (exact)   // spec_norm's operation order (one division per pixel)
+            out[(long long)s * out_stride + i] = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(c, __dsub_rn(1.0, mn)), mx));
+        else         // fast forms: one factor per spectrum
+            out[(long long)s * out_stride + i] = 1.0 - c * ((1.0 - mn) / mx);
     }
     if (minmax_out && blockIdx.x == 0 && threadIdx.x == 0) {
         minmax_out[2 * s] = mn;
@@ -269,10 +291,14 @@ __global__ void __launch_bounds__(256) k_norm(int n_eff, const double *__restric
 
 namespace soapgb {
 
+static size_t conv_param_bytes(int n_eff) {
+    return 2 * ((sizeof(double) * (size_t)n_eff + 255) & ~size_t(255)) + ((sizeof(int2) * (size_t)n_eff + 255) & ~size_t(255));
+}
+
 size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
     size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
     b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
-    if (form != SOAPGB_PLAIN64) b += 2 * (sizeof(double) * (size_t)n_eff + 256);  // base convs
+    if (form != SOAPGB_PLAIN64) b += 2 * (sizeof(double) * (size_t)n_eff + 256) + conv_param_bytes(n_eff) + 256;
     (void)n;
     return b;
 }
@@ -281,7 +307,7 @@ template <typename T, int SB>
 static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const double *spec,
                             long long spec_stride, int n_spec, int one_minus, double sigma_v, int wid,
                             double step_mult, double step_exp, double cut, double *conv, long long conv_stride,
-                            double sig_max) {
+                            double sig_max, char *param_scratch) {
     // halo: the widest significant reach, at the largest sigma (bounded by the window)
     double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
     int r = (int)floor(sqrt(cut / cmin)) + 2;
@@ -291,10 +317,15 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
     if (smem > 48 * 1024)
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv_fast<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    T *kq = (T *)param_scratch;
+    T *cq = (T *)(param_scratch + ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
+    int2 *rng = (int2 *)(param_scratch + 2 * ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
+    k_conv_params<T><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
+                                                                        step_exp, cut, kq, cq, rng);
+    SOAP_LAUNCHED(ctx);
     dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
-    k_conv_fast<T, SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, lam, spec, spec_stride, n_spec, one_minus,
-                                                            sigma_v, wid, halo, step_mult, step_exp, cut, conv,
-                                                            conv_stride);
+    k_conv_fast<T, SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride, n_spec,
+                                                            one_minus, halo, conv, conv_stride);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -323,28 +354,30 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
         if (!(sig_max > 0)) return set_error(ctx, SOAPGB_ERR_ARG, "non-positive instrument sigma");
         double cut = (form == SOAPGB_FAST32) ? 30.0 : 40.0;
         int rc;
+        char *pscr = p;   // per-pixel tap parameters (rewritten by each launch below)
+        p += conv_param_bytes(n_eff) + 256;
         if (base_a) {
             cb_a = (double *)p;
             p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult,
-                                             step_exp, 40.0, cb_a, 0, sig_max);
+                                             step_exp, 40.0, cb_a, 0, sig_max, pscr);
             if (rc) return rc;
         }
         if (base_b && b_every > 0) {
             cb_b = (double *)p;
             p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_b, 0, 1, 1, sigma_v, wid, step_mult,
-                                             step_exp, 40.0, cb_b, 0, sig_max);
+                                             step_exp, 40.0, cb_b, 0, sig_max, pscr);
             if (rc) return rc;
         }
         // without a base the whole (1 - A) is convolved: keep that one-time pass in FP64
         if (form == SOAPGB_FAST32 && base_a)
             rc = launch_conv_fast<float, 8>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, 0, sigma_v, wid,
-                                            step_mult, step_exp, cut, conv, n_eff, sig_max);
+                                            step_mult, step_exp, cut, conv, n_eff, sig_max, pscr);
         else
             rc = launch_conv_fast<double, 4>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, base_a ? 0 : 1,
                                              sigma_v, wid, step_mult, step_exp, base_a ? cut : 40.0, conv, n_eff,
-                                             sig_max);
+                                             sig_max, pscr);
         if (rc) return rc;
     }
     k_minmax_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm);
@@ -358,7 +391,8 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
     }
     {
         dim3 g(grid_for(ctx, n_eff, 256), n_spec);
-        k_norm<<<g, 256, 0, ctx->stream>>>(n_eff, conv, n_eff, mm, d_out, out_stride, d_minmax);
+        k_norm<<<g, 256, 0, ctx->stream>>>(n_eff, conv, n_eff, mm, d_out, out_stride, d_minmax,
+                                           form == SOAPGB_PLAIN64);
         SOAP_LAUNCHED(ctx);
     }
     return SOAPGB_OK;
