@@ -122,12 +122,12 @@ def rank_info():
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
-def make_workload(rank=0, n_phase=100):
+def make_workload(rank=0, n_phase=100, phase0=0):
     from soap_gpu_gb300 import synth
     case = synth.make_case(1)
     inp = synth.generate(case)
     # weak scaling: every rank integrates its own block of phases of the same star
-    phases = (case.phases + rank * case.rot_num)[:n_phase]
+    phases = (case.phases + rank * case.rot_num)[phase0:phase0 + n_phase]
     return case, inp, phases
 
 
@@ -154,7 +154,7 @@ def run_own(args):
         tdist.init_process_group("nccl")
     torch.cuda.set_device(lr)
     dev = "cuda:%d" % lr
-    case, inp, phases = make_workload(rk, args.phases)
+    case, inp, phases = make_workload(rk, args.phases, args.phase0)
     n, n_eff, n_mu = case.n, case.n_eff, case.n_mu
     lb = inp.lb
     star = star_struct(case, lb)
@@ -446,6 +446,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed device steps (for ncu launch lists)")
     ap.add_argument("--phases", type=int, default=100, help="phases per step (100 is the benchmarked workload)")
+    ap.add_argument("--phase0", type=int, default=0, help="index of the first phase (profiling subsets)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "own":
         args.warmup = 3

@@ -70,9 +70,9 @@ __global__ void __launch_bounds__(1024) k_compact(const double *__restrict__ key
     for (int start = 0; start < n; start += blockDim.x) {
         int i = start + threadIdx.x;
         bool p = false;
-        if (i < n) {
-            double v = kk[i];
-            p = (v >= lo) && (v <= hi);
+        if (i < n) {   // lo <= v <= hi by integer compares of the ordered bit patterns
+            unsigned long long v = soap_ord64(kk[i]);
+            p = (v >= soap_ord64(lo)) && (v <= soap_ord64(hi));
         }
         unsigned m = __ballot_sync(0xffffffffu, p);
         int pre = __popc(m & ((1u << lane) - 1u));

@@ -43,7 +43,10 @@ struct CellGeo {
     double dlt;    // ir - 1
     double L;      // limb darkening
     double w2;     // (1 + LB) L
-    float Lf, w2f, dltf;   // the same in FP32 (the FP32 form's coefficients)
+    // FP32 form: the position t(j0) = j0 dlt - offir in float pairs (hi + lo carries
+    // 48 significant bits, the precision of the FP64 position), and FP32 weights
+    float dlt_hi, dlt_lo, off_hi, off_lo;
+    float Lf, w2f, dltf;
     int row;       // mu bin
     int zero_v;    // delta == 0: the reference copies the row
 };
@@ -67,6 +70,10 @@ __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const
     g.Lf = (float)g.L;
     g.w2f = (float)g.w2;
     g.dltf = (float)g.dlt;
+    g.dlt_hi = (float)g.dlt;
+    g.dlt_lo = (float)(g.dlt - (double)g.dlt_hi);
+    g.off_hi = (float)g.offir;
+    g.off_lo = (float)(g.offir - (double)g.off_hi);
     int row = region[k];
     if ((unsigned)row >= (unsigned)n_mu && g.L > -998.0) {
         atomicExch(status, 21);
@@ -111,20 +118,65 @@ struct Acc {
     __device__ __forceinline__ double get() const { return (double)s - (double)c; }
 };
 
+// Source position of a cell at the tile start, on the FP32 pipe: u0 = j0 + t with
+// t = j0 dlt - offir evaluated in float pairs (exact products by fmaf, TwoSum for
+// the sums); returns i0 = floor(u0) and phi = u0 - i0.  |t| < 2^20 and j0 < 2^24.
+__device__ __forceinline__ void fir_pos32(int j0, const float dlt_hi, const float dlt_lo, const float off_hi,
+                                          const float off_lo, int &i0, float &phi) {
+    float j0f = (float)j0;
+    float pr = j0f * dlt_hi;
+    float pe = fmaf(j0f, dlt_hi, -pr);
+    float q = j0f * dlt_lo;
+    float sm = pr - off_hi;
+    float bp = sm - pr;
+    float err = (pr - (sm - bp)) + (-off_hi - bp);
+    float tl = err + (pe + (q - off_lo));
+    float th = sm + tl;
+    tl = tl - (th - sm);
+    float fl = floorf(th);
+    float fr = (th - fl) + tl;
+    if (fr < 0.f) {
+        fr += 1.f;
+        fl -= 1.f;
+    } else if (fr >= 1.f) {
+        fr -= 1.f;
+        fl += 1.f;
+    }
+    i0 = j0 + (int)fl;
+    phi = fr;
+}
+
+// exact tests on FP64 values with integer instructions (no FP64 pipe)
+__device__ __forceinline__ bool bits_is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ bool bits_is_integral(double v) {
+    long long b = __double_as_longlong(v);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e >= 52) return true;
+    if (e < 0) return (b << 1) == 0;
+    long long mant = b & 0xfffffffffffffLL;
+    return (mant & ((1LL << (52 - e)) - 1)) == 0;
+}
+
 struct FirCubes {
     // PHASE: q_sed, q_norm, spot_norm, dq_spot, fac_norm, dq_fac; QUIET: [0] only
     const void *c[6];
     const double *spot_sed;
     const double *fac_sed;
+    // FP32 form: the two continuum rows as float pairs (hi, lo)
+    const float2 *spot_sed2;
+    const float2 *fac_sed2;
 };
 
+template <typename T>
 struct Exc {
     int i0;          // owner at j0
     int row;
     int kind;        // 0 spot, 1 facula (phase); 0 (quiet)
     int parts;       // 1: the L-weighted sums, 2: the (1+LB) L-weighted facula sums
-    double phi, dlt, L, w2, temp;
     int zero_v;
+    int plain_t;     // spot temperature is an integer: Planck ratio exactly 1
+    T phi, dlt, L, w2;
+    double temp;
 };
 
 __device__ __forceinline__ unsigned fir_key(int kind, int row, int k) {
@@ -148,12 +200,13 @@ __device__ __forceinline__ double fir_planck_ratio(double lambda0, double t, dou
     return (exp(a / tn) - 1) / (exp(a / t) - 1);
 }
 
+template <typename T>
 struct FirShared {
     unsigned key[FIR_HASH];
     double val[FIR_HASH][3];
     int grp[FIR_HASH];
     float gcoef[FIR_HASH][3];   // FP32 form: group coefficients for the apply phase
-    Exc exc[FIR_EXC];
+    Exc<T> exc[FIR_EXC];
     int nexc, ngrp;
 };
 
@@ -194,8 +247,8 @@ __device__ __forceinline__ double v_get(F2 a) { return (double)a.hi + (double)a.
 // runs of equal keys (segmented scan) and the run's last lane adds the sums to the
 // shared hash table.  Returns whether this lane's contribution reached the table.
 // V = double (FAST64) or F2 (FAST32: compensated FP32 pairs).
-template <typename V>
-__device__ __forceinline__ bool fir_insert(FirShared &sh, bool active, unsigned key, V a0, V a1, V bb, int lane) {
+template <typename V, typename SH>
+__device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, V a0, V a1, V bb, int lane) {
     if (!active) key = 0xfffffffeu;
     unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
     bool seg = (lane == 0) || (prev != key);
@@ -253,17 +306,36 @@ __device__ __forceinline__ auto coef3(T w, T phi, T dlt) {
     }
 }
 
-template <typename T, int MODE>
+// float-pair arithmetic for the FP32 form's output combination
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    float hi = p + e;
+    F2 r;
+    r.hi = hi;
+    r.lo = e - (hi - p);
+    return r;
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) {
+    a.hi = -a.hi;
+    a.lo = -a.lo;
+    return a;
+}
+
+// QUIET: OutT = double (one spectrum, once per star); PHASE: OutT = T (the FP32 form
+// keeps its deficits in FP32 for the FP32 convolution that consumes them)
+template <typename T, int MODE, typename OutT>
 __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const double *__restrict__ lam,
                                                      FirCubes cubes, const int *__restrict__ cells,
                                                      const int *__restrict__ counts, int max_cells,
                                                      const CellGeo *__restrict__ geo,
                                                      const double *__restrict__ temp, const double *__restrict__ bi,
                                                      long long gm, int solar, int t_norm_fac,
-                                                     double *__restrict__ out0, double *__restrict__ out1,
-                                                     double *__restrict__ out2, long long out_stride) {
+                                                     OutT *__restrict__ out0, OutT *__restrict__ out1,
+                                                     OutT *__restrict__ out2, long long out_stride) {
     extern __shared__ __align__(16) unsigned char fir_smem[];
-    FirShared &sh = *reinterpret_cast<FirShared *>(fir_smem);
+    FirShared<T> &sh = *reinterpret_cast<FirShared<T> *>(fir_smem);
 
     const int p = blockIdx.y;
     const int j0 = blockIdx.x * FIR_TILE;
@@ -278,8 +350,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             int j = j0 + tid + q * FIR_THREADS;
             if (j >= n) continue;
             long long o = (long long)p * out_stride + j;
-            out0[o] = 0.0;
-            if constexpr (MODE == MODE_PHASE) { out1[o] = 0.0; out2[o] = 0.0; }
+            out0[o] = (OutT)0;
+            if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
         }
         return;
     }
@@ -303,7 +375,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     auto flush = [&]() {
         int ne = sh.nexc;
         for (int e = 0; e < ne; ++e) {
-            const Exc &x = sh.exc[e];
+            const Exc<T> &x = sh.exc[e];
             long long off = (long long)x.row * n;
 #pragma unroll
             for (int q = 0; q < FIR_PIX; ++q) {
@@ -316,7 +388,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                     i = j;
                     w = (T)0;
                 } else {
-                    T wd = (T)x.phi + (T)x.dlt * (T)dj;
+                    T wd = x.phi + x.dlt * (T)dj;
                     i = (long long)x.i0 + dj;
                     if (wd >= (T)1) { wd -= (T)1; i += 1; }
                     else if (wd < (T)0) { wd += (T)1; i -= 1; }
@@ -328,7 +400,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                     if (x.zero_v) return rowp[i];
                     return lerp_at(rowp, i, w);
                 };
-                T L = (T)x.L;
+                T L = x.L;
                 if constexpr (MODE == MODE_QUIET) {
                     acc[0][q].add(L * val(0));
                 } else {
@@ -336,10 +408,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                         acc[0][q].add(L * val(0));                              // S  (q_sed)
                         if (x.kind == 0) {
                             T Lq = L;
-                            if ((double)(int)x.temp != x.temp) {                // spot Planck ratio
-                                double lj = lam[j];
-                                Lq = (T)(x.L * fir_planck_ratio(lj, x.temp, (double)(int)x.temp));
-                            }
+                            if (!x.plain_t)                                     // spot Planck ratio
+                                Lq = (T)((double)x.L * fir_planck_ratio(lam[j], x.temp, (double)(int)x.temp));
                             acc[1][q].add(Lq * val(1));                         // Qs (q_norm)
                             acc[2][q].add(Lq * val(2));                         // As (spot_norm)
                             acc[3][q].add(L * val(3));                          // Bs (q_norm - spot_norm)
@@ -348,8 +418,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                         }
                     }
                     if ((x.parts & 2) && x.kind == 1) {
-                        T w2 = (T)x.w2;
-                        if (solar) w2 = (T)(x.L * fir_planck_ratio(lam[j], x.temp, (double)t_norm_fac));
+                        T w2 = x.w2;
+                        if (solar) w2 = (T)((double)x.L * fir_planck_ratio(lam[j], x.temp, (double)t_norm_fac));
                         acc[4][q].add(w2 * val(1));                             // Qf
                         acc[5][q].add(w2 * val(4));                             // Af (fac_norm)
                     }
@@ -363,46 +433,48 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         int ci = c0 + tid;
         bool have = ci < n_cells;
         int cell = have ? pc[ci] : 0;
-        CellGeo g = geo[cell];
-        int kind = 0;
+        const CellGeo &g = geo[cell];
+        int kind = 0, plain_t = 1;
         double tcell = 0.0;
         bool regular = false;
-        long long i0 = 0;
-        double phi = 0.0;
-        if (have) {
-            if constexpr (MODE == MODE_PHASE) {
-                kind = (pb[cell] == 0.0) ? 0 : 1;
-                tcell = pt[cell];
-            }
-            // the only FP64 step: the cell's source position at the tile start
-            double u0 = fma((double)j0, g.ir, -g.offir);
-            double fl = floor(u0);
-            i0 = (long long)fl;
-            phi = u0 - fl;
-            T phi_t = (T)phi;
-            T dlt_t;
-            if constexpr (sizeof(T) == 4) dlt_t = g.dltf;
-            else dlt_t = g.dlt;
-            T w_end = phi_t + dlt_t * (T)(t_eff - 1);
-            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= (T)0) && (w_end < (T)1);
-            if (g.zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
-            if constexpr (MODE == MODE_PHASE) {
-                if (kind == 0 && (double)(int)tcell != tcell) regular = false;   // spot Planck ratio != 1
-                if (kind == 1 && solar) regular = false;                        // per-pixel Planck ratio
-            }
-        }
-        int k = j0 - (int)i0;
-        // pass A: weight L (spot: kind 0, facula: kind 1; quiet: kind 0)
-        T Lw, W2w, Dw;
+        int i0 = 0;
+        T phi = (T)0, Lw, W2w, Dw;
         if constexpr (sizeof(T) == 4) { Lw = g.Lf; W2w = g.w2f; Dw = g.dltf; }
         else { Lw = g.L; W2w = g.w2; Dw = g.dlt; }
-        auto ca = coef3<T>(Lw, (T)phi, Dw);
-        bool okA = fir_insert(sh, have && regular, fir_key(kind, g.row, k), ca.a0, ca.a1, ca.bb, lane);
+        int row = g.row, zero_v = g.zero_v;
+        if (have) {
+            if constexpr (MODE == MODE_PHASE) {
+                kind = bits_is_zero(pb[cell]) ? 0 : 1;
+                tcell = pt[cell];
+                plain_t = bits_is_integral(tcell);
+            }
+            if constexpr (sizeof(T) == 4) {
+                float ph;
+                fir_pos32(j0, g.dlt_hi, g.dlt_lo, g.off_hi, g.off_lo, i0, ph);
+                phi = ph;
+            } else {
+                double u0 = fma((double)j0, g.ir, -g.offir);
+                double fl = floor(u0);
+                i0 = (int)fl;
+                phi = u0 - fl;
+            }
+            T w_end = phi + Dw * (T)(t_eff - 1);
+            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= (T)0) && (w_end < (T)1);
+            if (zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
+            if constexpr (MODE == MODE_PHASE) {
+                if (kind == 0 && !plain_t) regular = false;    // spot Planck ratio != 1
+                if (kind == 1 && solar) regular = false;       // per-pixel Planck ratio
+            }
+        }
+        int k = j0 - i0;
+        // pass A: weight L (spot: kind 0, facula: kind 1; quiet: kind 0)
+        auto ca = coef3<T>(Lw, phi, Dw);
+        bool okA = fir_insert(sh, have && regular, fir_key(kind, row, k), ca.a0, ca.a1, ca.bb, lane);
         bool okB = true;
         if constexpr (MODE == MODE_PHASE) {
             // pass B: facula (1 + LB) L weight
-            auto cb = coef3<T>(W2w, (T)phi, Dw);
-            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, g.row, k), cb.a0, cb.a1, cb.bb, lane);
+            auto cb = coef3<T>(W2w, phi, Dw);
+            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, row, k), cb.a0, cb.a1, cb.bb, lane);
         }
         int parts = 0;
         if (have) {
@@ -411,17 +483,18 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         }
         if (parts) {
             int slot = atomicAdd(&sh.nexc, 1);
-            Exc x;
-            x.i0 = (int)i0;
-            x.row = g.row;
+            Exc<T> x;
+            x.i0 = i0;
+            x.row = row;
             x.kind = kind;
             x.parts = parts;
+            x.zero_v = zero_v;
+            x.plain_t = plain_t;
             x.phi = phi;
-            x.dlt = g.dlt;
-            x.L = g.L;
-            x.w2 = g.w2;
+            x.dlt = Dw;
+            x.L = Lw;
+            x.w2 = W2w;
             x.temp = tcell;
-            x.zero_v = g.zero_v;
             sh.exc[slot] = x;
         }
         __syncthreads();
@@ -434,11 +507,29 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     }
     flush();
     __syncthreads();
-    if (tid == 0) {
-        int ng = 0;
-        for (int q = 0; q < FIR_HASH; ++q)
-            if (sh.key[q] != 0xffffffffu) sh.grp[ng++] = q;
-        sh.ngrp = ng;
+    // compact the occupied hash slots (ballot prefix per warp, warps in order)
+    {
+        constexpr int PER = FIR_HASH / FIR_THREADS;   // slots per thread
+        static_assert(FIR_HASH % FIR_THREADS == 0, "hash size");
+        int base_slot = tid * PER;
+        int cnt = 0;
+#pragma unroll
+        for (int q = 0; q < PER; ++q) cnt += (sh.key[base_slot + q] != 0xffffffffu);
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        __shared__ int wsum[FIR_THREADS / 32];
+        if (lane == 31) wsum[tid >> 5] = incl;
+        __syncthreads();
+        int woff = 0;
+        for (int w = 0; w < (tid >> 5); ++w) woff += wsum[w];
+        int pos = woff + incl - cnt;
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (sh.key[base_slot + q] != 0xffffffffu) sh.grp[pos++] = base_slot + q;
+        if (tid == FIR_THREADS - 1) sh.ngrp = woff + incl;
     }
     __syncthreads();
     for (int e = tid; e < sh.ngrp; e += FIR_THREADS) {
@@ -504,19 +595,32 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         if (j >= n) continue;
         long long o = (long long)p * out_stride + j;
         if (j >= n_eff) {
-            out0[o] = 0.0;
-            if constexpr (MODE == MODE_PHASE) { out1[o] = 0.0; out2[o] = 0.0; }
+            out0[o] = (OutT)0;
+            if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
             continue;
         }
         if constexpr (MODE == MODE_QUIET) {
-            out0[o] = acc[0][q].get();
+            out0[o] = (OutT)acc[0][q].get();
+        } else if constexpr (sizeof(T) == 4) {
+            // flux = S - I_s Qs - I_f Qf, tot = S - I_s As - I_f Af in float pairs: the
+            // facula terms nearly cancel S, so no FP32 rounding before the subtraction
+            F2 S{acc[0][q].s, -acc[0][q].c}, Qs{acc[1][q].s, -acc[1][q].c}, As{acc[2][q].s, -acc[2][q].c};
+            F2 Qf{acc[4][q].s, -acc[4][q].c}, Af{acc[5][q].s, -acc[5][q].c};
+            float2 is2 = cubes.spot_sed2[j], fs2 = cubes.fac_sed2[j];
+            F2 is{is2.x, is2.y}, fs{fs2.x, fs2.y};
+            F2 fl = f2_add(f2_add(S, f2_neg(f2_mul(is, Qs))), f2_neg(f2_mul(fs, Qf)));
+            F2 tt = f2_add(f2_add(S, f2_neg(f2_mul(is, As))), f2_neg(f2_mul(fs, Af)));
+            F2 bc = f2_add(F2{acc[3][q].s, -acc[3][q].c}, F2{acc[6][q].s, -acc[6][q].c});
+            out0[o] = (OutT)(fl.hi + fl.lo);   // flux
+            out1[o] = (OutT)(bc.hi + bc.lo);   // bconv
+            out2[o] = (OutT)(tt.hi + tt.lo);   // tot
         } else {
             double S = acc[0][q].get(), Qs = acc[1][q].get(), As = acc[2][q].get(), Bs = acc[3][q].get();
             double Qf = acc[4][q].get(), Af = acc[5][q].get(), Bf = acc[6][q].get();
             double is = cubes.spot_sed[j], fs = cubes.fac_sed[j];
-            out0[o] = S - is * Qs - fs * Qf;   // flux
-            out1[o] = Bs + Bf;                 // bconv
-            out2[o] = S - is * As - fs * Af;   // tot
+            out0[o] = (OutT)(S - is * Qs - fs * Qf);   // flux
+            out1[o] = (OutT)(Bs + Bf);                 // bconv
+            out2[o] = (OutT)(S - is * As - fs * Af);   // tot
         }
     }
 }
@@ -526,26 +630,48 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
 // ---------------------------------------------------------------------------
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+__global__ void k_pair_rows(int n, const double *__restrict__ a, const double *__restrict__ b, float2 *pa, float2 *pb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float ah = (float)a[i], bh = (float)b[i];
+    pa[i] = make_float2(ah, (float)(a[i] - (double)ah));
+    pb[i] = make_float2(bh, (float)(b[i] - (double)bh));
+}
+
 FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase) {
     FirPlanSizes p;
     if (form == SOAPGB_PLAIN64) return p;
     size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
     size_t cube = align256(tsz * (size_t)n * n_mu);
-    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + (phase ? 6 : 1) * cube;
+    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + (phase ? 6 : 1) * cube + 2 * align256(sizeof(float2) * n);
     return p;
 }
 
-template <typename T, int MODE>
+template <typename T, int MODE, typename OutT>
 static int launch_fir(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const FirCubes &fc, const int *cells,
                       const int *counts, int max_cells, const CellGeo *geo, const double *temp, const double *bi,
-                      long long gm, int solar, int t_norm_fac, double *o0, double *o1, double *o2,
-                      long long out_stride, int n_lists) {
-    size_t smem = sizeof(FirShared);
-    SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                      long long gm, int solar, int t_norm_fac, OutT *o0, OutT *o1, OutT *o2, long long out_stride,
+                      int n_lists) {
+    size_t smem = sizeof(FirShared<T>);
+    SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // tiles cover [0, n): tiles past n_eff only write the zero tail
     dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
-    k_fir<T, MODE><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, cells, counts, max_cells, geo, temp, bi,
-                                                          gm, solar, t_norm_fac, o0, o1, o2, out_stride);
+    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, cells, counts, max_cells, geo,
+                                                                temp, bi, gm, solar, t_norm_fac, o0, o1, o2,
+                                                                out_stride);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
+                       const double *limb, const double *lb, const int *region, int n_mu, CellGeo *geo) {
+    double lambda0;
+    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    k_check_uniform<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, wave, step, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, lambda0, step, geo,
+                                                                ctx->d_status);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -560,26 +686,19 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     p += align256(sizeof(CellGeo) * (size_t)gm);
     void *cube = p;
     p += align256(tsz * cube_elems);
-    (void)p;
-    double lambda0;
-    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, a.wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    k_check_uniform<<<grid_for(ctx, a.n_eff, 256), 256, 0, ctx->stream>>>(a.n_eff, a.wave, a.step, ctx->d_status);
-    SOAP_LAUNCHED(ctx);
-    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, a.delta, a.limb, nullptr, a.region, a.n_mu,
-                                                                lambda0, a.step, geo, ctx->d_status);
-    SOAP_LAUNCHED(ctx);
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo);
+    if (rc) return rc;
     FirCubes fc{};
     if (form == SOAPGB_FAST32) {
         k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube);
         SOAP_LAUNCHED(ctx);
         fc.c[0] = cube;
-        return launch_fir<float, MODE_QUIET>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
-                                             nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+        return launch_fir<float, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells,
+                                                     geo, nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
     }
     fc.c[0] = a.cube;
-    return launch_fir<double, MODE_QUIET>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
-                                          nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+    return launch_fir<double, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
+                                                  nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
 }
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan) {
@@ -595,14 +714,11 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         cb[q] = p;
         p += align256(tsz * cube_elems);
     }
-    double lambda0;
-    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, a.wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    k_check_uniform<<<grid_for(ctx, a.n_eff, 256), 256, 0, ctx->stream>>>(a.n_eff, a.wave, a.step, ctx->d_status);
-    SOAP_LAUNCHED(ctx);
-    k_cell_geo<<<grid_for(ctx, a.gm, 256), 256, 0, ctx->stream>>>(a.gm, a.delta, a.limb, a.lb, a.region, n_mu,
-                                                                  lambda0, a.step, geo, ctx->d_status);
-    SOAP_LAUNCHED(ctx);
+    float2 *sed2a = (float2 *)p;
+    p += align256(sizeof(float2) * a.n);
+    float2 *sed2b = (float2 *)p;
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo);
+    if (rc) return rc;
     const soapgb_cubes &c = *a.cubes;
     // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
     const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
@@ -619,11 +735,19 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     fc.spot_sed = c.spot_sed;
     fc.fac_sed = c.fac_sed;
     int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
-    if (form == SOAPGB_FAST32)
-        return launch_fir<float, MODE_PHASE>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
-                                             a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot,
-                                             a.out_stride, a.n_phase);
-    return launch_fir<double, MODE_PHASE>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
-                                          a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot,
-                                          a.out_stride, a.n_phase);
+    if (form == SOAPGB_FAST32) {
+        k_pair_rows<<<grid_for(ctx, a.n, 256), 256, 0, ctx->stream>>>(a.n, c.spot_sed, c.fac_sed, sed2a, sed2b);
+        SOAP_LAUNCHED(ctx);
+        fc.spot_sed2 = sed2a;
+        fc.fac_sed2 = sed2b;
+        if (!a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP32 form writes FP32 deficits");
+        return launch_fir<float, MODE_PHASE, float>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells,
+                                                    geo, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
+                                                    (float *)a.flux, (float *)a.bconv, (float *)a.tot, a.out_stride,
+                                                    a.n_phase);
+    }
+    if (a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP64 form writes FP64 deficits");
+    return launch_fir<double, MODE_PHASE, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
+                                                  a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, (double *)a.flux,
+                                                  (double *)a.bconv, (double *)a.tot, a.out_stride, a.n_phase);
 }

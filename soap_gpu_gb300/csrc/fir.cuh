@@ -40,7 +40,8 @@ struct FirPhaseArgs {
     long long gm;               // G*G
     double step;
     const soapgb_activity *act;
-    double *flux, *bconv, *tot; // n_phase x n
+    void *flux, *bconv, *tot;   // n_phase x n: float (FAST32) or double (FAST64)
+    int out_f32;
     long long out_stride;       // distance between phases in the outputs
 };
 

@@ -152,15 +152,24 @@ __global__ void __launch_bounds__(256) k_phase_plain64(
     }
 }
 
+// float -> double copy without FP64 instructions
+__global__ void k_f32_widen(long long count, const float *__restrict__ a, double *__restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = soap_f32_to_f64(a[i]);
+}
+
 namespace soapgb {
 
 // Integration on device buffers (all pointers device).  temp/bi: n_phase x gm.
 // out_stride: distance between phases in flux/bconv/tot (>= n).
+// Outputs are float for the FP32 form (out_f32 must be set), double otherwise.
 int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *d_wave, int grid, int n_phase,
                      const double *d_temp, const double *d_bi, const soapgb_maps &dm, const soapgb_cubes &dc,
-                     double step, const soapgb_activity *act, double *d_flux, double *d_bconv, double *d_tot,
+                     double step, const soapgb_activity *act, void *d_flux, void *d_bconv, void *d_tot, int out_f32,
                      long long out_stride, int *d_cells, int *d_counts, char *fir_scratch,
                      const FirPlanSizes &fp) {
+    if ((form == SOAPGB_FAST32) != (out_f32 != 0))
+        return set_error(ctx, SOAPGB_ERR_ARG, "integration: FP32 outputs go with the FP32 form only");
     long long gm = (long long)grid * grid;
     int rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
     if (rc) return rc;
@@ -169,7 +178,8 @@ int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *
         k_phase_plain64<<<g, 256, 0, ctx->stream>>>(
             n, n_eff, d_wave, dc.q_norm, dc.q_sed, dc.spot_norm, dc.fac_norm, dc.spot_sed, dc.fac_sed, (int)gm,
             d_cells, d_counts, d_temp, d_bi, dm.delta, dm.limb, dm.lb, dm.region, gm, step, act->solar,
-            act->t_star, act->t_diff_fac, d_flux, d_bconv, d_tot, out_stride, dc.n_mu, ctx->d_status);
+            act->t_star, act->t_diff_fac, (double *)d_flux, (double *)d_bconv, (double *)d_tot, out_stride, dc.n_mu,
+            ctx->d_status);
         SOAP_LAUNCHED(ctx);
         return SOAPGB_OK;
     }
@@ -194,6 +204,7 @@ int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *
     a.flux = d_flux;
     a.bconv = d_bconv;
     a.tot = d_tot;
+    a.out_f32 = out_f32;
     a.out_stride = out_stride;
     return fir_phase(ctx, form, a, fir_scratch, fp);
 }
@@ -232,6 +243,7 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
     for (int q = 0; q < 3; ++q) s_out[q] = ws.add(host ? sizeof(double) * (size_t)n * n_phase : 0);
     int s_cells = ws.add(sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
+    int s_f32 = ws.add(form == SOAPGB_FAST32 ? sizeof(float) * 3 * (size_t)n * n_phase : 0);
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true);
     int s_fir = ws.add(fp.bytes);
     int rc = ws.commit();
@@ -268,9 +280,24 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
     double *d_flux = host ? ws.get<double>(s_out[0]) : flux;
     double *d_bconv = host ? ws.get<double>(s_out[1]) : bconv;
     double *d_tot = host ? ws.get<double>(s_out[2]) : tot;
-    rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act, d_flux,
-                          d_bconv, d_tot, n, ws.get<int>(s_cells), ws.get<int>(s_counts), ws.get<char>(s_fir), fp);
-    if (rc) return rc;
+    if (form == SOAPGB_FAST32) {
+        float *f32 = ws.get<float>(s_f32);
+        size_t pn = (size_t)n * n_phase;
+        rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act, f32,
+                              f32 + pn, f32 + 2 * pn, 1, n, ws.get<int>(s_cells), ws.get<int>(s_counts),
+                              ws.get<char>(s_fir), fp);
+        if (rc) return rc;
+        double *outs[3] = {d_flux, d_bconv, d_tot};
+        for (int q = 0; q < 3; ++q) {
+            k_f32_widen<<<grid_for(ctx, (long long)pn, 256), 256, 0, ctx->stream>>>((long long)pn, f32 + q * pn, outs[q]);
+            SOAP_LAUNCHED(ctx);
+        }
+    } else {
+        rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act, d_flux,
+                              d_bconv, d_tot, 0, n, ws.get<int>(s_cells), ws.get<int>(s_counts), ws.get<char>(s_fir),
+                              fp);
+        if (rc) return rc;
+    }
     if (host) {
         size_t ob = sizeof(double) * (size_t)n * n_phase;
         SOAP_CUDA(ctx, cudaMemcpyAsync(flux, d_flux, ob, cudaMemcpyDeviceToHost, ctx->stream));

@@ -79,6 +79,30 @@ int grid_for(soapgb_ctx *ctx, long long work, int block);
 // Device helpers: the reference's expressions, written out once.
 // ---------------------------------------------------------------------------
 
+// float -> double by bit manipulation on the integer pipes (GB300's FP64 pipe runs at
+// 1/64 of the FP32 rate; this keeps FP32 results' exact value in FP64 storage)
+__device__ __forceinline__ double soap_f32_to_f64(float f) {
+    unsigned b = __float_as_uint(f);
+    unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    unsigned e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    unsigned long long r;
+    if (e == 0u) {
+        if (m != 0u) return (double)f;   // subnormal: rare, convert on the FP64 pipe
+        r = sign;
+    } else if (e == 255u) {
+        r = sign | 0x7ff0000000000000ULL | ((unsigned long long)m << 29);
+    } else {
+        r = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    }
+    return __longlong_as_double((long long)r);
+}
+
+// order-preserving map of a double onto uint64 (integer compares and atomics)
+__device__ __forceinline__ unsigned long long soap_ord64(double v) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
+}
+
 // Delta_lambda, SOAP_initialize.cu:55-66
 __device__ __forceinline__ double soap_delta_lambda(double line_width, double lambda_line0) {
     double beta = line_width / SOAP_C_LIGHT;

@@ -85,7 +85,7 @@ extern "C" int soapgb_lower_resolution_noalloc(soapgb_ctx *ctx, int n, int n_eff
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution_noalloc: half width %d invalid for n=%d", wid, n);
     // the PLAIN64 kernels write every convolution value and initialise the min/max
     // words themselves, so nothing left in the array by an earlier call is read
-    return resolution_device(ctx, SOAPGB_PLAIN64, n, n_eff, n_spec, wave, w3[0], w3[1], w3[2], spec, n, base,
+    return resolution_device(ctx, SOAPGB_PLAIN64, n, n_eff, n_spec, wave, w3[0], w3[1], w3[2], spec, 0, n, base,
                              nullptr, 0, sigma_v, window, step_mult, step_exp, sentinel, out, n_eff, minmax_out,
                              (char *)scratch);
 }

@@ -21,9 +21,17 @@ int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const
 size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
 int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *d_wave, int grid, int n_phase,
                      const double *d_temp, const double *d_bi, const soapgb_maps &dm, const soapgb_cubes &dc,
-                     double step, const soapgb_activity *act, double *d_flux, double *d_bconv, double *d_tot,
+                     double step, const soapgb_activity *act, void *d_flux, void *d_bconv, void *d_tot, int out_f32,
                      long long out_stride, int *d_cells, int *d_counts, char *fir_scratch, const FirPlanSizes &fp);
 }  // namespace soapgb
+
+// the FP32 form's deficits [spectrum][n] -> the FP64 raw output [spectrum][n_eff]
+__global__ void k_widen_rows(long long n_rows, int n, int n_eff, const float *__restrict__ in, double *__restrict__ out) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_rows * n_eff) return;
+    long long r = t / n_eff, i = t % n_eff;
+    out[t] = soap_f32_to_f64(in[r * n + i]);
+}
 
 extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
                                      const soapgb_star *star, const soapgb_maps *maps, const soapgb_cubes *cubes,
@@ -84,7 +92,9 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_qs = ws.add(host ? sizeof(double) * n : 0);
     int s_qn = ws.add(host ? sizeof(double) * n : 0);
     int s_lower = ws.add(host ? sizeof(double) * (size_t)n_eff * n_spec : 0);
-    int s_raw = ws.add(sizeof(double) * (size_t)n * n_spec);     // deficits [p][type][n]
+    size_t esz = (form == SOAPGB_FAST32) ? sizeof(float) : sizeof(double);
+    int s_raw = ws.add(esz * (size_t)n * n_spec);                // deficits [p][type][n]
+    int s_rawd = ws.add(form == SOAPGB_FAST32 && raw && host ? sizeof(double) * (size_t)n_eff * n_spec : 0);
     int s_temp = ws.add(sizeof(double) * gm * n_phase);
     int s_bi = ws.add(sizeof(double) * gm * n_phase);
     int s_cells = ws.add(sizeof(int) * gm * n_phase);
@@ -124,7 +134,8 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     STAGE(d_qs, quiet_sed, sizeof(double) * n, s_qs);
     STAGE(d_qn, quiet_norm, sizeof(double) * n, s_qn);
 #undef STAGE
-    double *d_raw = ws.get<double>(s_raw);
+    char *d_raw = ws.get<char>(s_raw);
+    int f32 = (form == SOAPGB_FAST32);
     double *d_temp = ws.get<double>(s_temp), *d_bi = ws.get<double>(s_bi);
     double *d_lower = host ? ws.get<double>(s_lower) : lower;
     rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp, d_bi,
@@ -132,16 +143,25 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     if (rc) return rc;
     // deficits in [phase][tot, flux, bconv][n]
     rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act,
-                          d_raw + n /* flux */, d_raw + 2LL * n /* bconv */, d_raw /* tot */, 3LL * n,
+                          d_raw + esz * n /* flux */, d_raw + esz * 2 * n /* bconv */, d_raw /* tot */, f32, 3LL * n,
                           ws.get<int>(s_cells), ws.get<int>(s_counts), ws.get<char>(s_fir), fp);
     if (rc) return rc;
-    rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, n, d_qs, d_qn, 3,
+    rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, f32, n, d_qs, d_qn, 3,
                            sigma_v, 50.0, conv_step, conv_step, sentinel, d_lower, n_eff, nullptr, ws.get<char>(s_res));
     if (rc) return rc;
     if (raw) {
-        cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-        SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n, sizeof(double) * n_eff,
-                                         n_spec, k, ctx->stream));
+        if (f32) {
+            double *dst = host ? ws.get<double>(s_rawd) : raw;
+            long long tot_el = (long long)n_spec * n_eff;
+            k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(n_spec, n, n_eff, (const float *)d_raw, dst);
+            SOAP_LAUNCHED(ctx);
+            if (host)
+                SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+            SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n,
+                                             sizeof(double) * n_eff, n_spec, k, ctx->stream));
+        }
     }
     if (host) {
         SOAP_CUDA(ctx, cudaMemcpyAsync(lower, d_lower, sizeof(double) * (size_t)n_eff * n_spec, cudaMemcpyDeviceToHost, ctx->stream));

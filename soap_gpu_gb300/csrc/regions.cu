@@ -96,13 +96,18 @@ __global__ void k_phase_scan(int grid, double delta_grid, const RegionPhase *__r
     int p = blockIdx.y;
     if (k >= gm) return;
     int iy = (int)(k / grid), iz = (int)(k % grid);
-    double y = __dadd_rn(-1., __dmul_rn((double)iy, delta_grid));
-    double z = __dadd_rn(-1., __dmul_rn((double)iz, delta_grid));
+    double y = 0.0, z = 0.0;
+    bool have_yz = false;   // FP64 only for cells inside a bounding box
     double t = -9999.0, b = -9999.0;
     int r0 = reg_off[p], r1 = reg_off[p + 1];
     for (int r = r0; r < r1; ++r) {
         RegionPhase rp = table[r];
         if (!rp.visible || iy < rp.iy0 || iy >= rp.iy1 || iz < rp.iz0 || iz >= rp.iz1) continue;
+        if (!have_yz) {
+            y = __dadd_rn(-1., __dmul_rn((double)iy, delta_grid));
+            z = __dadd_rn(-1., __dmul_rn((double)iz, delta_grid));
+            have_yz = true;
+        }
         if (!(__dadd_rn(__dmul_rn(z, z), __dmul_rn(y, y)) < 1.)) continue;
         double xa0 = __dsqrt_rn(__dsub_rn(1., __dadd_rn(__dmul_rn(y, y), __dmul_rn(z, z))));
         double xi0 = __dadd_rn(__dadd_rn(__dmul_rn(rp.r0, xa0), __dmul_rn(rp.r1, y)), __dmul_rn(rp.r2, z));

@@ -51,10 +51,7 @@ int conv_halfwidth(double wave0, double wave1, double sigma_v, double window) {
 }
 }  // namespace soapgb
 
-__device__ __forceinline__ unsigned long long soap_ord_enc(double v) {
-    unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
-}
+__device__ __forceinline__ unsigned long long soap_ord_enc(double v) { return soap_ord64(v); }
 __device__ __forceinline__ double soap_ord_dec(unsigned long long u) {
     u = (u & 0x8000000000000000ULL) ? (u & 0x7fffffffffffffffULL) : ~u;
     return __longlong_as_double((long long)u);
@@ -130,12 +127,12 @@ constexpr int FC_THREADS = 256;
 constexpr int FC_PIX = 4;
 constexpr int FC_TILE = FC_THREADS * FC_PIX;
 
-template <typename T, int SB>
+template <typename T, int SB, typename SrcT, typename OutT>
 __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, const T *__restrict__ kqa,
                                                           const T *__restrict__ cqa, const int2 *__restrict__ rnga,
-                                                          const double *__restrict__ spec, long long spec_stride,
+                                                          const SrcT *__restrict__ spec, long long spec_stride,
                                                           int n_spec, int one_minus, int halo,
-                                                          double *__restrict__ conv, long long conv_stride) {
+                                                          OutT *__restrict__ conv, long long conv_stride) {
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);
     int win = FC_TILE + 2 * halo;
@@ -144,12 +141,12 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
     int nsb = min(SB, n_spec - s0);
     // stage [i0 - halo, i0 + FC_TILE + halo) of each spectrum (0 outside [0, n))
     for (int q = 0; q < nsb; ++q) {
-        const double *sp = spec + (long long)(s0 + q) * spec_stride;
+        const SrcT *sp = spec + (long long)(s0 + q) * spec_stride;
         for (int t = threadIdx.x; t < win; t += FC_THREADS) {
             int m = i0 - halo + t;
-            double v = (m >= 0 && m < n) ? sp[m] : 0.0;
-            if (one_minus) v = (m >= 0 && m < n) ? 1.0 - v : 0.0;
-            xs[q * win + t] = (T)v;
+            T v = (m >= 0 && m < n) ? (T)sp[m] : (T)0;
+            if (one_minus) v = (m >= 0 && m < n) ? (T)1 - v : (T)0;
+            xs[q * win + t] = v;
         }
     }
     __syncthreads();
@@ -227,11 +224,11 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
 #pragma unroll
     for (int q = 0; q < SB; ++q) {
         if (q >= nsb) continue;
-        double *cp = conv + (long long)(s0 + q) * conv_stride;
+        OutT *cp = conv + (long long)(s0 + q) * conv_stride;
 #pragma unroll
         for (int p = 0; p < FC_PIX; ++p) {
             int i = ib + p;
-            if (i < n_eff) cp[i] = (dlo[p] <= dhi[p]) ? (double)acc[q][p] : 0.0;
+            if (i < n_eff) cp[i] = (dlo[p] <= dhi[p]) ? (OutT)acc[q][p] : (OutT)0;
         }
     }
 }
@@ -307,6 +304,169 @@ __global__ void __launch_bounds__(256) k_norm(int n_eff, const double *__restric
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// FAST32 reductions and normalisation.  The per-pixel work stays on the FP32
+// pipe; the normalisation constants min A and max C are still exact FP64 values:
+// pass 1 finds the FP32 extrema and, per block, the block's own extrema; pass 2
+// re-evaluates in FP64 only the pixels of the blocks that can hold the exact
+// extremum (FP32 value within 2^-21 of the magnitudes involved).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned soap_ord32(float v) {
+    unsigned u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float soap_dec32(unsigned u) {
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(u);
+}
+
+__global__ void k_base_prep(int n, int n_eff, const double *__restrict__ base, const double *__restrict__ cb,
+                            float *base32, float *cb32) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) base32[i] = (float)base[i];
+    if (i < n_eff) cb32[i] = (float)cb[i];
+}
+
+__global__ void k_mm32_init(int n_spec, double sentinel, unsigned *mm32, unsigned long long *mm64) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n_spec) {
+        mm32[4 * s + 0] = 0xffffffffu;                 // min A (FP32 key)
+        mm32[4 * s + 1] = 0u;                          // max C (FP32 key)
+        mm32[4 * s + 2] = 0u;                          // max(|base| + |spec|)
+        mm32[4 * s + 3] = 0u;                          // max(|cb| + |conv|)
+        mm64[2 * s + 0] = ~0ULL;
+        mm64[2 * s + 1] = soap_ord_enc(sentinel);
+    }
+}
+
+// pass 1: FP32 extrema per spectrum and per block
+__global__ void __launch_bounds__(256) k_minmax32(int n, int n_eff, const float *__restrict__ spec,
+                                                  long long spec_stride, const float *__restrict__ b32a,
+                                                  const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                                  const float *__restrict__ c32b, int b_every,
+                                                  const float *__restrict__ conv, long long conv_stride,
+                                                  unsigned *mm32, float *blk) {
+    int s = blockIdx.y;
+    bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+    const float *sp = spec + (long long)s * spec_stride;
+    const float *bs = use_b ? b32b : b32a;
+    const float *cbs = use_b ? c32b : c32a;
+    const float *cv = conv + (long long)s * conv_stride;
+    float mn = INFINITY, mx = -INFINITY, ma = 0.f, mc = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float b = bs[i], x = sp[i];
+        float a = b - x;
+        mn = fminf(mn, a);
+        ma = fmaxf(ma, fabsf(b) + fabsf(x));
+        if (i < n_eff) {
+            float cb = cbs[i], cd = cv[i];
+            float c = cb + cd;
+            if (c != 0.f) mx = fmaxf(mx, c);
+            mc = fmaxf(mc, fabsf(cb) + fabsf(cd));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+    }
+    __shared__ float sh[4][8];
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { sh[0][w] = mn; sh[1][w] = mx; sh[2][w] = ma; sh[3][w] = mc; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
+            mn = fminf(mn, sh[0][q]); mx = fmaxf(mx, sh[1][q]); ma = fmaxf(ma, sh[2][q]); mc = fmaxf(mc, sh[3][q]);
+        }
+        float *bk = blk + ((long long)s * gridDim.x + blockIdx.x) * 2;
+        bk[0] = mn;
+        bk[1] = mx;
+        atomicMin(&mm32[4 * s + 0], soap_ord32(mn));
+        if (mx > -INFINITY) atomicMax(&mm32[4 * s + 1], soap_ord32(mx));
+        atomicMax(&mm32[4 * s + 2], soap_ord32(ma));
+        atomicMax(&mm32[4 * s + 3], soap_ord32(mc));
+    }
+}
+
+// pass 2: exact FP64 values of the candidates of the blocks that can hold an extremum
+__global__ void __launch_bounds__(256) k_refine64(int n, int n_eff, const float *__restrict__ spec,
+                                                  long long spec_stride, const double *__restrict__ ba,
+                                                  const double *__restrict__ bb, const double *__restrict__ cba,
+                                                  const double *__restrict__ cbb, const float *__restrict__ b32a,
+                                                  const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                                  const float *__restrict__ c32b, int b_every,
+                                                  const float *__restrict__ conv, long long conv_stride,
+                                                  const unsigned *__restrict__ mm32, const float *__restrict__ blk,
+                                                  unsigned long long *mm64) {
+    int s = blockIdx.y;
+    float mnA = soap_dec32(mm32[4 * s + 0]), mxC = soap_dec32(mm32[4 * s + 1]);
+    float tolA = ldexpf(soap_dec32(mm32[4 * s + 2]), -21), tolC = ldexpf(soap_dec32(mm32[4 * s + 3]), -21);
+    const float *bk = blk + ((long long)s * gridDim.x + blockIdx.x) * 2;
+    bool needA = bk[0] <= mnA + tolA;
+    bool needC = (mm32[4 * s + 1] != 0u) && (bk[1] >= mxC - tolC);
+    if (!needA && !needC) return;          // uniform for the whole block
+    bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+    const float *sp = spec + (long long)s * spec_stride;
+    const float *bs = use_b ? b32b : b32a;
+    const float *cbs = use_b ? c32b : c32a;
+    const double *b64 = use_b ? bb : ba;
+    const double *c64 = use_b ? cbb : cba;
+    const float *cv = conv + (long long)s * conv_stride;
+    unsigned long long mn = ~0ULL, mx = 0ULL;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float x = sp[i];
+        if (needA && bs[i] - x <= mnA + tolA) {
+            double a = b64[i] - (double)x;
+            mn = min(mn, soap_ord_enc(a));
+        }
+        if (needC && i < n_eff) {
+            float cd = cv[i];
+            float c = cbs[i] + cd;
+            if (c != 0.f && c >= mxC - tolC) {
+                double cx = c64[i] + (double)cd;
+                if (cx != 0.0) mx = max(mx, soap_ord_enc(cx));
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mn != ~0ULL) atomicMin(&mm64[2 * s], mn);
+        if (mx != 0ULL) atomicMax(&mm64[2 * s + 1], mx);
+    }
+}
+
+// FP64 normalisation constants per spectrum -> FP32 factor
+__global__ void k_factor(int n_spec, const unsigned long long *__restrict__ mm64, float *fac, double *minmax_out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_spec) return;
+    double mn = soap_ord_dec(mm64[2 * s]), mx = soap_ord_dec(mm64[2 * s + 1]);
+    fac[s] = (float)((1.0 - mn) / mx);
+    if (minmax_out) {
+        minmax_out[2 * s] = mn;
+        minmax_out[2 * s + 1] = mx;
+    }
+}
+
+// out = 1 - C f on the FP32 pipe, stored as FP64 bits without an FP64 instruction
+__global__ void __launch_bounds__(256) k_norm32(int n_eff, const float *__restrict__ c32a,
+                                                const float *__restrict__ c32b, int b_every,
+                                                const float *__restrict__ conv, long long conv_stride,
+                                                const float *__restrict__ fac, double *__restrict__ out,
+                                                long long out_stride) {
+    int s = blockIdx.y;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+    const float *cbs = use_b ? c32b : c32a;
+    float c = cbs[i] + conv[(long long)s * conv_stride + i];
+    out[(long long)s * out_stride + i] = soap_f32_to_f64(fmaf(-c, fac[s], 1.0f));
+}
+
 namespace soapgb {
 
 static size_t conv_param_bytes(int n_eff) {
@@ -317,14 +477,20 @@ size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
     size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
     b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
     if (form != SOAPGB_PLAIN64) b += 2 * (sizeof(double) * (size_t)n_eff + 256) + conv_param_bytes(n_eff) + 256;
+    if (form == SOAPGB_FAST32) {
+        b += 2 * (sizeof(float) * (size_t)n + 256) + 2 * (sizeof(float) * (size_t)n_eff + 256);   // base32, cb32
+        b += sizeof(float) * (size_t)n * n_spec + 256;                                        // FP32 spectra
+        b += 16 * (size_t)n_spec + 256 + 4 * (size_t)n_spec + 256;                               // mm32, factor
+        b += sizeof(float) * 2 * 64 * (size_t)n_spec + 256;                                      // block extrema
+    }
     (void)n;
     return b;
 }
 
-template <typename T, int SB>
-static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const double *spec,
+template <typename T, int SB, typename SrcT = double, typename OutT = double>
+static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const SrcT *spec,
                             long long spec_stride, int n_spec, int one_minus, double sigma_v, int wid,
-                            double step_mult, double step_exp, double cut, double *conv, long long conv_stride,
+                            double step_mult, double step_exp, double cut, OutT *conv, long long conv_stride,
                             double sig_max, char *param_scratch) {
     // halo: the widest significant reach, at the largest sigma (bounded by the window)
     double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
@@ -334,7 +500,8 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     size_t smem = sizeof(T) * (size_t)SB * (FC_TILE + 2 * halo);
     if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
     if (smem > 48 * 1024)
-        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv_fast<T, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv_fast<T, SB, SrcT, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
     T *kq = (T *)param_scratch;
     T *cq = (T *)(param_scratch + ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
     int2 *rng = (int2 *)(param_scratch + 2 * ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
@@ -342,24 +509,36 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
                                                                         step_exp, cut, kq, cq, rng);
     SOAP_LAUNCHED(ctx);
     dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
-    k_conv_fast<T, SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride, n_spec,
-                                                            one_minus, halo, conv, conv_stride);
+    k_conv_fast<T, SB, SrcT, OutT><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride,
+                                                                        n_spec, one_minus, halo, conv, conv_stride);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
 
+__global__ void k_f64_to_f32(long long count, const double *__restrict__ a, float *out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = (float)a[i];
+}
+
+static char *carve(char *&p, size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) & ~size_t(255);
+    return r;
+}
+
 int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
-                      double wave1, double wave_last, const double *d_spec, long long spec_stride, const double *base_a,
-                      const double *base_b, int b_every, double sigma_v, double window, double step_mult,
-                      double step_exp, double sentinel, double *d_out, long long out_stride, double *d_minmax,
-                      char *scratch) {
+                      double wave1, double wave_last, const void *d_spec_v, int spec_f32, long long spec_stride,
+                      const double *base_a, const double *base_b, int b_every, double sigma_v, double window,
+                      double step_mult, double step_exp, double sentinel, double *d_out, long long out_stride,
+                      double *d_minmax, char *scratch) {
     int wid = conv_halfwidth(wave0, wave1, sigma_v, window);
     char *p = scratch;
-    double *conv = (double *)p;
-    p += (sizeof(double) * (size_t)n_eff * n_spec + 255) & ~size_t(255);
-    unsigned long long *mm = (unsigned long long *)p;
-    p += (sizeof(unsigned long long) * 2 * n_spec + 255) & ~size_t(255);
+    double *conv = (double *)carve(p, sizeof(double) * (size_t)n_eff * n_spec);
+    unsigned long long *mm = (unsigned long long *)carve(p, sizeof(unsigned long long) * 2 * n_spec);
     double *cb_a = nullptr, *cb_b = nullptr;
+    const double *d_spec = (const double *)d_spec_v;
+    if (spec_f32 && form != SOAPGB_FAST32)
+        return set_error(ctx, SOAPGB_ERR_ARG, "FP32 spectra are accepted by the FP32 form only");
     if (form == SOAPGB_PLAIN64) {
         dim3 g(grid_for(ctx, n_eff, 256), n_spec);
         k_conv_plain64<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_spec, spec_stride, base_a, base_b, b_every,
@@ -372,30 +551,71 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
         if (!(sig_max > 0)) return set_error(ctx, SOAPGB_ERR_ARG, "non-positive instrument sigma");
         double cut = (form == SOAPGB_FAST32) ? 30.0 : 40.0;
         int rc;
-        char *pscr = p;   // per-pixel tap parameters (rewritten by each launch below)
-        p += conv_param_bytes(n_eff) + 256;
+        char *pscr = carve(p, conv_param_bytes(n_eff));   // per-pixel tap parameters (rewritten per launch)
         if (base_a) {
-            cb_a = (double *)p;
-            p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
+            cb_a = (double *)carve(p, sizeof(double) * (size_t)n_eff);
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult,
                                              step_exp, 40.0, cb_a, 0, sig_max, pscr);
             if (rc) return rc;
         }
         if (base_b && b_every > 0) {
-            cb_b = (double *)p;
-            p += (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
+            cb_b = (double *)carve(p, sizeof(double) * (size_t)n_eff);
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_b, 0, 1, 1, sigma_v, wid, step_mult,
                                              step_exp, 40.0, cb_b, 0, sig_max, pscr);
             if (rc) return rc;
         }
-        // without a base the whole (1 - A) is convolved: keep that one-time pass in FP64
-        if (form == SOAPGB_FAST32 && base_a)
-            rc = launch_conv_fast<float, 8>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, 0, sigma_v, wid,
-                                            step_mult, step_exp, cut, conv, n_eff, sig_max, pscr);
-        else
-            rc = launch_conv_fast<double, 4>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, base_a ? 0 : 1,
-                                             sigma_v, wid, step_mult, step_exp, base_a ? cut : 40.0, conv, n_eff,
-                                             sig_max, pscr);
+        if (form == SOAPGB_FAST32 && base_a) {
+            // ---- FP32 pipe throughout, exact FP64 normalisation constants ------------
+            const float *spec32 = (const float *)d_spec_v;
+            if (!spec_f32) {
+                float *tmp = (float *)carve(p, sizeof(float) * (size_t)n * n_spec);
+                for (int q = 0; q < n_spec; ++q) {
+                    k_f64_to_f32<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, d_spec + (long long)q * spec_stride,
+                                                                                tmp + (long long)q * n);
+                    SOAP_LAUNCHED(ctx);
+                }
+                spec32 = tmp;
+                spec_stride = n;
+            }
+            float *b32a = (float *)carve(p, sizeof(float) * (size_t)n);
+            float *b32b = (float *)carve(p, sizeof(float) * (size_t)n);
+            float *c32a = (float *)carve(p, sizeof(float) * (size_t)n_eff);
+            float *c32b = (float *)carve(p, sizeof(float) * (size_t)n_eff);
+            unsigned *mm32 = (unsigned *)carve(p, 16 * (size_t)n_spec);
+            float *fac = (float *)carve(p, 4 * (size_t)n_spec);
+            int bx = std::max(1, std::min(64, (n + 255) / 256));
+            float *blk = (float *)carve(p, sizeof(float) * 2 * (size_t)bx * n_spec);
+            k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_a, cb_a, b32a, c32a);
+            SOAP_LAUNCHED(ctx);
+            if (cb_b) {
+                k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_b, cb_b, b32b, c32b);
+                SOAP_LAUNCHED(ctx);
+            }
+            float *conv32 = (float *)conv;
+            rc = launch_conv_fast<float, 8, float, float>(ctx, n, n_eff, d_wave, spec32, spec_stride, n_spec, 0,
+                                                          sigma_v, wid, step_mult, step_exp, cut, conv32, n_eff,
+                                                          sig_max, pscr);
+            if (rc) return rc;
+            k_mm32_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm32, mm);
+            SOAP_LAUNCHED(ctx);
+            dim3 g2(bx, n_spec);
+            k_minmax32<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, b32a, b32b, c32a, c32b, b_every,
+                                                    conv32, n_eff, mm32, blk);
+            SOAP_LAUNCHED(ctx);
+            k_refine64<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
+                                                    b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm);
+            SOAP_LAUNCHED(ctx);
+            k_factor<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, mm, fac, d_minmax);
+            SOAP_LAUNCHED(ctx);
+            dim3 g3(grid_for(ctx, n_eff, 256), n_spec);
+            k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out, out_stride);
+            SOAP_LAUNCHED(ctx);
+            return SOAPGB_OK;
+        }
+        // FAST64, or no base (the whole (1 - A) is convolved): FP64
+        rc = launch_conv_fast<double, 4>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, base_a ? 0 : 1,
+                                         sigma_v, wid, step_mult, step_exp, base_a ? cut : 40.0, conv, n_eff,
+                                         sig_max, pscr);
         if (rc) return rc;
     }
     k_minmax_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm);
@@ -461,7 +681,7 @@ extern "C" int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_e
     if (rc) return rc;
     double *d_out = host ? ws.get<double>(s_out) : out;
     double *d_mm = minmax_out ? (host ? ws.get<double>(s_mm) : minmax_out) : nullptr;
-    rc = resolution_device(ctx, form, n, n_eff, n_spec, d_wave, w01[0], w01[1], w01[2], d_spec, n, d_base, nullptr, 0,
+    rc = resolution_device(ctx, form, n, n_eff, n_spec, d_wave, w01[0], w01[1], w01[2], d_spec, 0, n, d_base, nullptr, 0,
                            sigma_v, window, step_mult, step_exp, sentinel, d_out, n_eff, d_mm, ws.get<char>(s_scr));
     if (rc) return rc;
     if (host) {

@@ -92,7 +92,10 @@ def test_lower_resolution_with_base(ctx, form, tol):
     for s in range(3):
         ref, _, mm = oracle.lower_resolution(inp.wave, base - spec[s], n_eff, inp.case.sigma_v)
         assert rel_err(got[s], ref) <= tol
-        assert gmm[s, 0] == mm[0]
+        if form == "fast32":   # the FP32 form rounds the spectra to FP32 before the exact FP64 minimum
+            assert abs(gmm[s, 0] - mm[0]) <= 1e-7 * np.max(np.abs(spec[s]))
+        else:
+            assert gmm[s, 0] == mm[0]
 
 
 def test_phase_maps_exact(ctx):
