@@ -274,7 +274,7 @@ extern "C" int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, co
     int s_out = ws.add(host ? sizeof(double) * n : 0);
     int s_cells = ws.add(sizeof(int) * gm);
     int s_count = ws.add(sizeof(int));
-    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, false);
+    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, false, 1);
     int s_fir = ws.add(fp.bytes);
     int rc = ws.commit();
     if (rc) return rc;

@@ -51,9 +51,36 @@ struct CellGeo {
     int zero_v;    // delta == 0: the reference copies the row
 };
 
+// the FP32 form's per-cell constants, two 16-byte loads:
+// a = (dlt_hi, dlt_lo, off_hi, off_lo), b = (L, (1 + LB) L, dlt, bits(row | zero_v << 31))
+struct __align__(16) CellGeo32 {
+    float4 a, b;
+};
+
+// per (list, entry) record: x = grid cell, y = flags (bit 0 facula, bit 1 integral temperature)
+__global__ void k_list_records(int n_lists, int max_cells, const int *__restrict__ cells,
+                               const int *__restrict__ counts, const double *__restrict__ temp,
+                               const double *__restrict__ bi, long long gm, int2 *recs) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int l = blockIdx.y;
+    if (t >= counts[l]) return;
+    int cell = cells[(long long)l * max_cells + t];
+    int flags = 2;
+    if (bi) {
+        double b = bi[(long long)l * gm + cell];
+        double tc = temp[(long long)l * gm + cell];
+        flags = ((__double_as_longlong(b) << 1) == 0 ? 0 : 1);
+        long long tb = __double_as_longlong(tc);
+        int e = (int)((tb >> 52) & 0x7ff) - 1023;
+        bool integral = (e >= 52) || (e < 0 ? (tb << 1) == 0 : ((tb & 0xfffffffffffffLL) & ((1LL << (52 - e)) - 1)) == 0);
+        flags |= integral ? 2 : 0;
+    }
+    recs[(long long)l * max_cells + t] = make_int2(cell, flags);
+}
+
 __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const double *__restrict__ limb,
                            const double *__restrict__ lb, const int *__restrict__ region, int n_mu, double lambda0,
-                           double step, CellGeo *geo, int *status) {
+                           double step, CellGeo *geo, CellGeo32 *geo32, int *status) {
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= gm) return;
     double d = delta[k];
@@ -82,6 +109,10 @@ __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const
     g.row = ((unsigned)row < (unsigned)n_mu) ? row : 0;
     g.zero_v = (d == 0.0);
     geo[k] = g;
+    CellGeo32 h;
+    h.a = make_float4(g.dlt_hi, g.dlt_lo, g.off_hi, g.off_lo);
+    h.b = make_float4(g.Lf, g.w2f, g.dltf, __int_as_float(g.row | (g.zero_v ? (int)0x80000000 : 0)));
+    geo32[k] = h;
 }
 
 // wavelength grid must be uniform for the collapsed form
@@ -203,7 +234,9 @@ __device__ __forceinline__ double fir_planck_ratio(double lambda0, double t, dou
 template <typename T>
 struct FirShared {
     unsigned key[FIR_HASH];
-    double val[FIR_HASH][3];
+    // group coefficients in 64-bit fixed point: integer atomics are native, exact and
+    // order independent (A0, A1 scaled by 2^40, B by 2^56)
+    unsigned long long val[FIR_HASH][3];
     int grp[FIR_HASH];
     float gcoef[FIR_HASH][3];   // FP32 form: group coefficients for the apply phase
     Exc<T> exc[FIR_EXC];
@@ -240,8 +273,15 @@ __device__ __forceinline__ F2 shfl_up_v<F2>(F2 v, int o) {
 }
 __device__ __forceinline__ double v_add(double a, double b) { return a + b; }
 __device__ __forceinline__ F2 v_add(F2 a, F2 b) { return f2_add(a, b); }
-__device__ __forceinline__ double v_get(double a) { return a; }
-__device__ __forceinline__ double v_get(F2 a) { return (double)a.hi + (double)a.lo; }
+constexpr float FIX_A_F = 1099511627776.0f;          // 2^40
+constexpr float FIX_B_F = 72057594037927936.0f;       // 2^56
+__device__ __forceinline__ unsigned long long v_fix(double a, double scale) {
+    return (unsigned long long)__double2ll_rn(a * scale);
+}
+__device__ __forceinline__ unsigned long long v_fix(F2 a, float scale) {
+    // hi * 2^k and lo * 2^k are exact in FP32; each rounds to an integer separately
+    return (unsigned long long)(__float2ll_rn(a.hi * scale) + __float2ll_rn(a.lo * scale));
+}
 
 // One pass of the warp-cooperative insertion: lanes holding a key (active) fold
 // runs of equal keys (segmented scan) and the run's last lane adds the sums to the
@@ -273,9 +313,9 @@ __device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, V 
         for (int probe = 0; probe < 64 && !ok; ++probe) {
             unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
             if (old == 0xffffffffu || old == key) {
-                atomicAdd(&sh.val[h][0], v_get(a0));
-                atomicAdd(&sh.val[h][1], v_get(a1));
-                atomicAdd(&sh.val[h][2], v_get(bb));
+                atomicAdd(&sh.val[h][0], v_fix(a0, FIX_A_F));
+                atomicAdd(&sh.val[h][1], v_fix(a1, FIX_A_F));
+                atomicAdd(&sh.val[h][2], v_fix(bb, FIX_B_F));
                 ok = true;
             } else {
                 h = (h + 1) & (FIR_HASH - 1);
@@ -327,9 +367,10 @@ __device__ __forceinline__ F2 f2_neg(F2 a) {
 // keeps its deficits in FP32 for the FP32 convolution that consumes them)
 template <typename T, int MODE, typename OutT>
 __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const double *__restrict__ lam,
-                                                     FirCubes cubes, const int *__restrict__ cells,
+                                                     FirCubes cubes, const int2 *__restrict__ recs,
                                                      const int *__restrict__ counts, int max_cells,
                                                      const CellGeo *__restrict__ geo,
+                                                     const CellGeo32 *__restrict__ geo32,
                                                      const double *__restrict__ temp, const double *__restrict__ bi,
                                                      long long gm, int solar, int t_norm_fac,
                                                      OutT *__restrict__ out0, OutT *__restrict__ out1,
@@ -341,9 +382,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     const int j0 = blockIdx.x * FIR_TILE;
     const int tid = threadIdx.x, lane = tid & 31;
     const int n_cells = counts[p];
-    const int *pc = cells + (long long)p * max_cells;
+    const int2 *pr = recs + (long long)p * max_cells;
     const double *pt = (MODE == MODE_PHASE) ? temp + (long long)p * gm : nullptr;
-    const double *pb = (MODE == MODE_PHASE) ? bi + (long long)p * gm : nullptr;
     const int t_eff = min(FIR_TILE, n_eff - j0);
     if (t_eff <= 0) {   // whole tile in the zero tail [n_eff, n)
         for (int q = 0; q < FIR_PIX; ++q) {
@@ -358,7 +398,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
 
     for (int q = tid; q < FIR_HASH; q += FIR_THREADS) {
         sh.key[q] = 0xffffffffu;
-        sh.val[q][0] = sh.val[q][1] = sh.val[q][2] = 0.0;
+        sh.val[q][0] = sh.val[q][1] = sh.val[q][2] = 0ULL;
     }
     if (tid == 0) sh.nexc = 0;
 
@@ -432,28 +472,38 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     for (int c0 = 0; c0 < n_cells; c0 += FIR_THREADS) {
         int ci = c0 + tid;
         bool have = ci < n_cells;
-        int cell = have ? pc[ci] : 0;
-        const CellGeo &g = geo[cell];
-        int kind = 0, plain_t = 1;
-        double tcell = 0.0;
+        int2 rec = have ? pr[ci] : make_int2(0, 2);
+        int cell = rec.x;
+        int kind = (MODE == MODE_PHASE) ? (rec.y & 1) : 0;
+        int plain_t = (rec.y >> 1) & 1;
         bool regular = false;
         int i0 = 0;
         T phi = (T)0, Lw, W2w, Dw;
-        if constexpr (sizeof(T) == 4) { Lw = g.Lf; W2w = g.w2f; Dw = g.dltf; }
-        else { Lw = g.L; W2w = g.w2; Dw = g.dlt; }
-        int row = g.row, zero_v = g.zero_v;
+        int row, zero_v;
+        float dh = 0.f, dl = 0.f, oh = 0.f, ol = 0.f;
+        double gir = 0.0, goff = 0.0;
+        if constexpr (sizeof(T) == 4) {
+            CellGeo32 h = geo32[cell];
+            dh = h.a.x; dl = h.a.y; oh = h.a.z; ol = h.a.w;
+            Lw = h.b.x; W2w = h.b.y; Dw = h.b.z;
+            int rz = __float_as_int(h.b.w);
+            row = rz & 0x7fffffff;
+            zero_v = (rz >> 31) & 1;
+        } else {
+            const CellGeo &g = geo[cell];
+            Lw = g.L; W2w = g.w2; Dw = g.dlt;
+            row = g.row;
+            zero_v = g.zero_v;
+            gir = g.ir;
+            goff = g.offir;
+        }
         if (have) {
-            if constexpr (MODE == MODE_PHASE) {
-                kind = bits_is_zero(pb[cell]) ? 0 : 1;
-                tcell = pt[cell];
-                plain_t = bits_is_integral(tcell);
-            }
             if constexpr (sizeof(T) == 4) {
                 float ph;
-                fir_pos32(j0, g.dlt_hi, g.dlt_lo, g.off_hi, g.off_lo, i0, ph);
+                fir_pos32(j0, dh, dl, oh, ol, i0, ph);
                 phi = ph;
             } else {
-                double u0 = fma((double)j0, g.ir, -g.offir);
+                double u0 = fma((double)j0, gir, -goff);
                 double fl = floor(u0);
                 i0 = (int)fl;
                 phi = u0 - fl;
@@ -494,7 +544,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             x.dlt = Dw;
             x.L = Lw;
             x.w2 = W2w;
-            x.temp = tcell;
+            x.temp = (MODE == MODE_PHASE && (!plain_t || solar)) ? pt[cell] : 0.0;
             sh.exc[slot] = x;
         }
         __syncthreads();
@@ -534,9 +584,9 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     __syncthreads();
     for (int e = tid; e < sh.ngrp; e += FIR_THREADS) {
         int h = sh.grp[e];
-        sh.gcoef[e][0] = (float)sh.val[h][0];
-        sh.gcoef[e][1] = (float)sh.val[h][1];
-        sh.gcoef[e][2] = (float)sh.val[h][2];
+        sh.gcoef[e][0] = __ll2float_rn((long long)sh.val[h][0]) * (1.0f / FIX_A_F);
+        sh.gcoef[e][1] = __ll2float_rn((long long)sh.val[h][1]) * (1.0f / FIX_A_F);
+        sh.gcoef[e][2] = __ll2float_rn((long long)sh.val[h][2]) * (1.0f / FIX_B_F);
     }
     __syncthreads();
     // --- apply the collapsed groups ---------------------------------------------
@@ -553,9 +603,9 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             A1 = sh.gcoef[e][1];
             B = sh.gcoef[e][2];
         } else {
-            A0 = sh.val[h][0];
-            A1 = sh.val[h][1];
-            B = sh.val[h][2];
+            A0 = __ll2double_rn((long long)sh.val[h][0]) * (1.0 / (double)FIX_A_F);
+            A1 = __ll2double_rn((long long)sh.val[h][1]) * (1.0 / (double)FIX_A_F);
+            B = __ll2double_rn((long long)sh.val[h][2]) * (1.0 / (double)FIX_B_F);
         }
         long long off = (long long)row * n;
 #pragma unroll
@@ -638,40 +688,50 @@ __global__ void k_pair_rows(int n, const double *__restrict__ a, const double *_
     pb[i] = make_float2(bh, (float)(b[i] - (double)bh));
 }
 
-FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase) {
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists) {
     FirPlanSizes p;
     if (form == SOAPGB_PLAIN64) return p;
     size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
     size_t cube = align256(tsz * (size_t)n * n_mu);
-    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + (phase ? 6 : 1) * cube + 2 * align256(sizeof(float2) * n);
+    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + align256(sizeof(CellGeo32) * (size_t)gm) +
+              (phase ? 6 : 1) * cube + 2 * align256(sizeof(float2) * n) +
+              align256(sizeof(int2) * (size_t)gm * (size_t)(n_lists > 0 ? n_lists : 1));
     return p;
 }
 
 template <typename T, int MODE, typename OutT>
 static int launch_fir(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const FirCubes &fc, const int *cells,
-                      const int *counts, int max_cells, const CellGeo *geo, const double *temp, const double *bi,
-                      long long gm, int solar, int t_norm_fac, OutT *o0, OutT *o1, OutT *o2, long long out_stride,
-                      int n_lists) {
+                      const int *counts, int max_cells, const CellGeo *geo, const CellGeo32 *geo32, int2 *recs,
+                      const double *temp, const double *bi, long long gm, int solar, int t_norm_fac, OutT *o0,
+                      OutT *o1, OutT *o2, long long out_stride, int n_lists) {
+    // records are written over the compacted cell lists, in place (int -> int2
+    // needs its own buffer: recs)
+    {
+        dim3 gr(grid_for(ctx, max_cells, 256), n_lists);
+        k_list_records<<<gr, 256, 0, ctx->stream>>>(n_lists, max_cells, cells, counts, temp, bi, gm, recs);
+        SOAP_LAUNCHED(ctx);
+    }
     size_t smem = sizeof(FirShared<T>);
     SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // tiles cover [0, n): tiles past n_eff only write the zero tail
     dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
-    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, cells, counts, max_cells, geo,
-                                                                temp, bi, gm, solar, t_norm_fac, o0, o1, o2,
+    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, recs, counts, max_cells, geo,
+                                                                geo32, temp, bi, gm, solar, t_norm_fac, o0, o1, o2,
                                                                 out_stride);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
 
 static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
-                       const double *limb, const double *lb, const int *region, int n_mu, CellGeo *geo) {
+                       const double *limb, const double *lb, const int *region, int n_mu, CellGeo *geo,
+                       CellGeo32 *geo32) {
     double lambda0;
     SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     k_check_uniform<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, wave, step, ctx->d_status);
     SOAP_LAUNCHED(ctx);
     k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, lambda0, step, geo,
-                                                                ctx->d_status);
+                                                                geo32, ctx->d_status);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -684,9 +744,13 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     char *p = scratch;
     CellGeo *geo = (CellGeo *)p;
     p += align256(sizeof(CellGeo) * (size_t)gm);
+    CellGeo32 *geo32 = (CellGeo32 *)p;
+    p += align256(sizeof(CellGeo32) * (size_t)gm);
     void *cube = p;
     p += align256(tsz * cube_elems);
-    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo);
+    int2 *recs = (int2 *)p;
+    p += align256(sizeof(int2) * (size_t)gm);
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo, geo32);
     if (rc) return rc;
     FirCubes fc{};
     if (form == SOAPGB_FAST32) {
@@ -694,11 +758,13 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
         SOAP_LAUNCHED(ctx);
         fc.c[0] = cube;
         return launch_fir<float, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells,
-                                                     geo, nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+                                                     geo, geo32, recs, nullptr, nullptr, gm, 0, 0, a.out, nullptr,
+                                                     nullptr, 0, 1);
     }
     fc.c[0] = a.cube;
     return launch_fir<double, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
-                                                  nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+                                                  geo32, recs, nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0,
+                                                  1);
 }
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan) {
@@ -709,6 +775,10 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     char *p = scratch;
     CellGeo *geo = (CellGeo *)p;
     p += align256(sizeof(CellGeo) * (size_t)a.gm);
+    CellGeo32 *geo32 = (CellGeo32 *)p;
+    p += align256(sizeof(CellGeo32) * (size_t)a.gm);
+    int2 *recs = (int2 *)p;
+    p += align256(sizeof(int2) * (size_t)a.gm * (size_t)a.n_phase);
     void *cb[6];
     for (int q = 0; q < 6; ++q) {
         cb[q] = p;
@@ -717,7 +787,7 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     float2 *sed2a = (float2 *)p;
     p += align256(sizeof(float2) * a.n);
     float2 *sed2b = (float2 *)p;
-    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo);
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32);
     if (rc) return rc;
     const soapgb_cubes &c = *a.cubes;
     // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
@@ -742,12 +812,13 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         fc.fac_sed2 = sed2b;
         if (!a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP32 form writes FP32 deficits");
         return launch_fir<float, MODE_PHASE, float>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells,
-                                                    geo, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
+                                                    geo, geo32, recs, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
                                                     (float *)a.flux, (float *)a.bconv, (float *)a.tot, a.out_stride,
                                                     a.n_phase);
     }
     if (a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP64 form writes FP64 deficits");
     return launch_fir<double, MODE_PHASE, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
-                                                  a.temp, a.bi, a.gm, a.act->solar, t_norm_fac, (double *)a.flux,
+                                                  geo32, recs, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
+                                                  (double *)a.flux,
                                                   (double *)a.bconv, (double *)a.tot, a.out_stride, a.n_phase);
 }

@@ -8,7 +8,7 @@ struct FirPlanSizes {
 
 // workspace of the FAST forms: per-cell geometry for the G*G grid plus typed cube
 // copies (one cube for the quiet disk, six for the phase integration)
-FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase);
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists);
 
 struct FirQuietArgs {
     int n, n_eff;

@@ -244,7 +244,7 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
     int s_cells = ws.add(sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
     int s_f32 = ws.add(form == SOAPGB_FAST32 ? sizeof(float) * 3 * (size_t)n * n_phase : 0);
-    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true);
+    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
     int s_fir = ws.add(fp.bytes);
     int rc = ws.commit();
     if (rc) return rc;

@@ -100,7 +100,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_cells = ws.add(sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
     int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
-    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true);
+    FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
     int s_fir = ws.add(fp.bytes);
     int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
     int rc = ws.commit();
