@@ -126,7 +126,13 @@ def compare(a_files, b_files, n_eff):
             out[rel] = "shape %s vs %s" % (a.shape, b.shape)
             continue
         if dt == np.int32 or "map" in rel:
-            out[rel] = {"exact": bool(np.array_equal(a, b)), "n_diff": int(np.count_nonzero(a != b))}
+            nd = int(np.count_nonzero(a != b))
+            d = {"exact": nd == 0, "n_diff": nd}
+            if dt != np.int32 and nd:
+                fin = np.isfinite(a) & np.isfinite(b)
+                sc = max(float(np.max(np.abs(a[fin]))) if fin.any() else 0.0, 1e-300)
+                d["max_rel"] = float(np.max(np.abs(a[fin] - b[fin]))) / sc if fin.any() else float("inf")
+            out[rel] = d
             continue
         scale = max(float(np.max(np.abs(a))), 1e-300)
         full = float(np.max(np.abs(a - b)) / scale)
@@ -139,19 +145,22 @@ def summarise(diffs):
     agg = {}
     for rel, d in diffs.items():
         kind = rel.split("/")[-1]
-        for tag in ("_Spec_", "_lower_spec_", "_temp_map_", "_spot_binary_map_", "quiet_sun_spec", "quiet_sun_lower",
+        for tag in ("_Spec_tot", "_Spec_flux", "_Spec_bconv", "_lower_spec_tot", "_lower_spec_flux",
+                    "_lower_spec_bconv", "_temp_map_", "_spot_binary_map_", "quiet_sun_spec", "quiet_sun_lower",
                     "mu_map", "delta_map", "limb_map", "LB_map", "region_map", "quiet_sun_wave"):
             if tag in kind:
-                a = agg.setdefault(tag, {"files": 0, "max_interior": 0.0, "max_full": 0.0, "exact": True})
+                a = agg.setdefault(tag, {"files": 0})
                 a["files"] += 1
-                if isinstance(d, dict):
-                    if "interior" in d:
-                        a["max_interior"] = max(a["max_interior"], d["interior"])
-                        a["max_full"] = max(a["max_full"], d["full"])
-                    else:
-                        a["exact"] = a["exact"] and d["exact"]
+                if not isinstance(d, dict):
+                    a["error"] = d
+                elif "interior" in d:
+                    a["max_interior"] = max(a.get("max_interior", 0.0), d["interior"])
+                    a["max_full"] = max(a.get("max_full", 0.0), d["full"])
                 else:
-                    a["exact"] = False
+                    a["exact"] = a.get("exact", True) and d["exact"]
+                    a["n_diff"] = a.get("n_diff", 0) + d["n_diff"]
+                    if "max_rel" in d:
+                        a["max_rel"] = max(a.get("max_rel", 0.0), d["max_rel"])
                 break
     return agg
 

@@ -11,14 +11,14 @@
 //     L (1 - phi - delta dj) S_b[j - k] + L (phi + delta dj) S_b[j - k + 1],   k = j0 - i0,
 // which is linear in dj with coefficients that only depend on (b, k).  Summing the
 // coefficients of all such ("regular") cells per (kind, b, k) group collapses
-// thousands of cells into a few dozen two-tap filters per tile.  Cells whose weight
-// wraps inside the tile, or whose owners leave [0, n_eff-2], are added directly
-// ("exceptions"), exactly as the per-cell form does.
+// thousands of cells into a few dozen two-tap filters per tile; pixels whose owner
+// j - k leaves [0, n_eff-2] are clipped per group.  Cells whose weight wraps inside
+// the tile are added directly ("exceptions"), exactly as the per-cell form does.
 //
 // Per tile, a block of 256 threads owns 1024 pixels:
-//   setup  -- FP64 position of every cell at j0 (the only FP64 step), warp
-//             segmented reduction of equal keys (cells come in map order, so
-//             keys repeat in runs), FP64 atomics into a shared hash table;
+//   setup  -- position of every cell at j0 (FP64 in FAST64, float pairs in FAST32),
+//             warp segmented reduction of equal keys (cells come in map order, so
+//             keys repeat in runs), 64-bit fixed-point atomics into a shared hash;
 //   apply  -- every thread walks the group list for its four pixels (coalesced
 //             two-tap loads, compensated sums in FP32 for FAST32).
 #include <algorithm>
@@ -131,13 +131,16 @@ __global__ void k_to_type(long long count, const double *__restrict__ a, const d
     out[i] = (T)v;
 }
 
-// compensated accumulator
+// per-pixel sums of the FP32 form: compensated (Kahan) when set
+constexpr bool FIR_COMPENSATED = true;
+
+// per-pixel accumulator
 template <typename T>
 struct Acc {
     T s, c;
     __device__ __forceinline__ void zero() { s = (T)0; c = (T)0; }
     __device__ __forceinline__ void add(T x) {
-        if constexpr (sizeof(T) == 4) {
+        if constexpr (sizeof(T) == 4 && FIR_COMPENSATED) {
             T y = x - c;
             T t = s + y;
             c = (t - s) - y;
@@ -243,8 +246,7 @@ struct FirShared {
     int nexc, ngrp;
 };
 
-// float pair with an error term (TwoSum): the FP32 form reduces runs of up to 32
-// coefficient terms without growing the rounding error
+// float pair with an error term (TwoSum): the FP32 form's output combinations
 struct F2 {
     float hi, lo;
 };
@@ -260,47 +262,62 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
     return r;
 }
 
-template <typename V>
-__device__ __forceinline__ V shfl_up_v(V v, int o);
-template <>
-__device__ __forceinline__ double shfl_up_v<double>(double v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
-template <>
-__device__ __forceinline__ F2 shfl_up_v<F2>(F2 v, int o) {
-    F2 r;
-    r.hi = __shfl_up_sync(0xffffffffu, v.hi, o);
-    r.lo = __shfl_up_sync(0xffffffffu, v.lo, o);
-    return r;
-}
-__device__ __forceinline__ double v_add(double a, double b) { return a + b; }
-__device__ __forceinline__ F2 v_add(F2 a, F2 b) { return f2_add(a, b); }
-constexpr float FIX_A_F = 1099511627776.0f;          // 2^40
-constexpr float FIX_B_F = 72057594037927936.0f;       // 2^56
-__device__ __forceinline__ unsigned long long v_fix(double a, double scale) {
-    return (unsigned long long)__double2ll_rn(a * scale);
-}
-__device__ __forceinline__ unsigned long long v_fix(F2 a, float scale) {
-    // hi * 2^k and lo * 2^k are exact in FP32; each rounds to an integer separately
-    return (unsigned long long)(__float2ll_rn(a.hi * scale) + __float2ll_rn(a.lo * scale));
+constexpr double FIX_A = 1099511627776.0;            // 2^40: A0, A1 (weights <= 1 per cell)
+constexpr double FIX_B = 72057594037927936.0;        // 2^56: B (weight x delta, |delta| ~ 1e-5)
+constexpr float FIX_A_F = 1099511627776.0f;
+constexpr float FIX_B_F = 72057594037927936.0f;
+__device__ __forceinline__ long long v_fix(double a, double scale) { return __double2ll_rn(a * scale); }
+__device__ __forceinline__ long long v_fix(float a, float scale) {
+    // a * 2^k is exact in FP32; the conversion rounds once
+    return __float2ll_rn(a * scale);
 }
 
 // One pass of the warp-cooperative insertion: lanes holding a key (active) fold
-// runs of equal keys (segmented scan) and the run's last lane adds the sums to the
-// shared hash table.  Returns whether this lane's contribution reached the table.
-// V = double (FAST64) or F2 (FAST32: compensated FP32 pairs).
-template <typename V, typename SH>
-__device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, V a0, V a1, V bb, int lane) {
+// runs of equal keys (segmented scan of 64-bit fixed-point values: integer adds,
+// exact and associative) and the run's last lane adds the sums to the shared hash
+// table.  Returns whether this lane's contribution reached the table.
+template <typename SH>
+__device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, long long a0, long long a1,
+                                           long long bb, int lane) {
     if (!active) key = 0xfffffffeu;
     unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
     bool seg = (lane == 0) || (prev != key);
+    // fast path: the whole warp is one run (cells come in map order, so most warps are)
+    if (__all_sync(0xffffffffu, lane == 0 || !seg)) {
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            bb += __shfl_xor_sync(0xffffffffu, bb, o);
+        }
+        bool ok = true;
+        if (key != 0xfffffffeu && lane == 31) {
+            ok = false;
+            unsigned h = (key * 2654435761u) & (FIR_HASH - 1);
+            for (int probe = 0; probe < 64 && !ok; ++probe) {
+                unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
+                if (old == 0xffffffffu || old == key) {
+                    atomicAdd(&sh.val[h][0], (unsigned long long)a0);
+                    atomicAdd(&sh.val[h][1], (unsigned long long)a1);
+                    atomicAdd(&sh.val[h][2], (unsigned long long)bb);
+                    ok = true;
+                } else {
+                    h = (h + 1) & (FIR_HASH - 1);
+                }
+            }
+        }
+        int all_ok = __shfl_sync(0xffffffffu, (int)ok, 31);
+        return !active || all_ok;
+    }
     for (int o = 1; o < 32; o <<= 1) {
-        V v0 = shfl_up_v(a0, o);
-        V v1 = shfl_up_v(a1, o);
-        V v2 = shfl_up_v(bb, o);
+        long long v0 = __shfl_up_sync(0xffffffffu, a0, o);
+        long long v1 = __shfl_up_sync(0xffffffffu, a1, o);
+        long long v2 = __shfl_up_sync(0xffffffffu, bb, o);
         int sg = __shfl_up_sync(0xffffffffu, (int)seg, o);
         if (lane >= o && !seg) {
-            a0 = v_add(a0, v0);
-            a1 = v_add(a1, v1);
-            bb = v_add(bb, v2);
+            a0 += v0;
+            a1 += v1;
+            bb += v2;
             seg = sg;
         }
     }
@@ -313,9 +330,9 @@ __device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, V 
         for (int probe = 0; probe < 64 && !ok; ++probe) {
             unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
             if (old == 0xffffffffu || old == key) {
-                atomicAdd(&sh.val[h][0], v_fix(a0, FIX_A_F));
-                atomicAdd(&sh.val[h][1], v_fix(a1, FIX_A_F));
-                atomicAdd(&sh.val[h][2], v_fix(bb, FIX_B_F));
+                atomicAdd(&sh.val[h][0], (unsigned long long)a0);
+                atomicAdd(&sh.val[h][1], (unsigned long long)a1);
+                atomicAdd(&sh.val[h][2], (unsigned long long)bb);
                 ok = true;
             } else {
                 h = (h + 1) & (FIR_HASH - 1);
@@ -329,21 +346,24 @@ __device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, V 
     return !active || tail_ok;
 }
 
+// a cell's three group coefficients in fixed point: A0 = w (1 - phi), A1 = w phi,
+// B = w delta (the weight at pixel dj is A0 - B dj on the owner, A1 + B dj on owner + 1)
+struct Coef3 {
+    long long a0, a1, bb;
+};
 template <typename T>
-__device__ __forceinline__ auto coef3(T w, T phi, T dlt) {
+__device__ __forceinline__ Coef3 coef3(T w, T phi, T dlt) {
+    Coef3 r;
     if constexpr (sizeof(T) == 4) {
-        struct R { F2 a0, a1, bb; } r;
-        r.a0 = F2{w * (1.0f - phi), 0.0f};
-        r.a1 = F2{w * phi, 0.0f};
-        r.bb = F2{w * dlt, 0.0f};
-        return r;
+        r.a0 = v_fix(w * (1.0f - phi), FIX_A_F);
+        r.a1 = v_fix(w * phi, FIX_A_F);
+        r.bb = v_fix(w * dlt, FIX_B_F);
     } else {
-        struct R { double a0, a1, bb; } r;
-        r.a0 = w * (1.0 - phi);
-        r.a1 = w * phi;
-        r.bb = w * dlt;
-        return r;
+        r.a0 = v_fix(w * (1.0 - phi), FIX_A);
+        r.a1 = v_fix(w * phi, FIX_A);
+        r.bb = v_fix(w * dlt, FIX_B);
     }
+    return r;
 }
 
 // float-pair arithmetic for the FP32 form's output combination
@@ -508,8 +528,12 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
                 i0 = (int)fl;
                 phi = u0 - fl;
             }
+            // owners leaving [0, n_eff-2] do not break the linear form: the apply loop
+            // clips each group's pixel range (pixels without an owner get nothing)
             T w_end = phi + Dw * (T)(t_eff - 1);
-            regular = (i0 >= 0) && (i0 + t_eff - 1 <= n_eff - 2) && (w_end >= (T)0) && (w_end < (T)1);
+            int kk = j0 - i0;
+            regular = (w_end >= (T)0) && (w_end < (T)1) && (kk >= -16384) && (kk < 16384);
+            // v == 0 copies the row up to n_eff - 1, one pixel further than the clip
             if (zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
             if constexpr (MODE == MODE_PHASE) {
                 if (kind == 0 && !plain_t) regular = false;    // spot Planck ratio != 1
@@ -608,11 +632,14 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             B = __ll2double_rn((long long)sh.val[h][2]) * (1.0 / (double)FIX_B_F);
         }
         long long off = (long long)row * n;
+        // pixels whose owner j - k lies in [0, n_eff - 2]
+        const int jlo = max(j0, k);
+        const int jhi = min(j0 + t_eff - 1, n_eff - 2 + k);
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) {
             int dj = tid + q * FIR_THREADS;
             int j = j0 + dj;
-            if (j >= n_eff) continue;
+            if (j < jlo || j > jhi) continue;
             long long i = (long long)j - k;
             T c0 = A0 - B * (T)dj;
             T c1 = A1 + B * (T)dj;
