@@ -291,10 +291,10 @@ extern "C" int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, co
     double *d_out = host ? ws.get<double>(s_out) : sum_out;
     int *d_cells = ws.get<int>(s_cells);
     int *d_count = ws.get<int>(s_count);
-    // visible cells in map order (limb map is -999 elsewhere)
-    rc = compact_cells(ctx, 1, (int)gm, d_limb, -998.0, 1e300, (int)gm, d_cells, d_count);
-    if (rc) return rc;
     if (form == SOAPGB_PLAIN64) {
+        // visible cells in map order (limb map is -999 elsewhere)
+        rc = compact_cells(ctx, 1, (int)gm, d_limb, -998.0, 1e300, (int)gm, d_cells, d_count);
+        if (rc) return rc;
         k_quiet_plain64<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_cube, d_count, d_cells,
                                                                          d_delta, d_limb, d_region, step, n_mu, d_out,
                                                                          ctx->d_status);
@@ -306,9 +306,7 @@ extern "C" int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, co
         qa.wave = d_wave;
         qa.cube = d_cube;
         qa.n_mu = n_mu;
-        qa.max_cells = (int)gm;
-        qa.n_cells = d_count;
-        qa.cells = d_cells;
+        qa.gm = gm;
         qa.delta = d_delta;
         qa.limb = d_limb;
         qa.region = d_region;

@@ -4,23 +4,27 @@
 //
 // For a uniform wavelength grid the reference's per-cell interpolation at output
 // pixel j reads the source position u_j = (j - off) / r (r = 1 + fbeta,
-// off = fbeta lambda0 / step): owner i = floor(u_j), weight w = u_j - i.  Over a tile
-// of T pixels starting at j0, u_j = i0 + dj + phi + delta dj with i0 = floor(u_{j0}),
-// phi = u_{j0} - i0, delta = 1/r - 1 (|delta| ~ v/c ~ 1e-5).  While phi + delta dj
-// stays in [0, 1) the cell contributes
-//     L (1 - phi - delta dj) S_b[j - k] + L (phi + delta dj) S_b[j - k + 1],   k = j0 - i0,
-// which is linear in dj with coefficients that only depend on (b, k).  Summing the
-// coefficients of all such ("regular") cells per (kind, b, k) group collapses
-// thousands of cells into a few dozen two-tap filters per tile; pixels whose owner
-// j - k leaves [0, n_eff-2] are clipped per group.  Cells whose weight wraps inside
-// the tile are added directly ("exceptions"), exactly as the per-cell form does.
+// off = fbeta lambda0 / step): owner i = floor(u_j), weight w = u_j - i.  Write
+// u_j = j + t_c(j) with t_c(j) = j dlt_c - offir_c = dlt_c (j + lambda0 / step),
+// dlt = 1/r - 1 (|dlt| ~ v/c ~ 1e-5).  Over a tile of T pixels from j0, a cell whose
+// m = floor(t_c) does not change inside the tile contributes
+//     L (1 - phi - dlt dj) S_b[j + m] + L (phi + dlt dj) S_b[j + m + 1],   phi = t_c(j0) - m,
+// which is linear in dj; its coefficients summed over all cells sharing (b, m) are
+//     A1 = sum L phi = j0 sum(L dlt) - sum(L offir) - m sum L,  A0 = sum L - A1,  B = sum L dlt.
+// Cells sorted by (mu bin b, v == 0, dlt) have t_c(j) increasing with dlt at every j,
+// so the cells of one (b, m) group form a contiguous range in that order: a tile
+// finds each range with two binary searches and takes its coefficients from FP64
+// prefix sums -- no per-cell work for the regular cells.  Cells whose m changes
+// inside the tile ("wrap" cells, ~|dlt| T of them) lie between consecutive ranges
+// and are evaluated directly, as are spots of non-integral temperature and the
+// solar variant's faculae (per-pixel Planck ratio).  Pixels whose owner j + m leaves
+// [0, n_eff - 2] get nothing from the group, as in the per-cell form.
 //
-// Per tile, a block of 256 threads owns 1024 pixels:
-//   setup  -- position of every cell at j0 (FP64 in FAST64, float pairs in FAST32),
-//             warp segmented reduction of equal keys (cells come in map order, so
-//             keys repeat in runs), 64-bit fixed-point atomics into a shared hash;
-//   apply  -- every thread walks the group list for its four pixels (coalesced
-//             two-tap loads, compensated sums in FP32 for FAST32).
+// Per tile of 1024 pixels, a block of 256 threads walks its list's (class, mu bin)
+// segments in work units of at most FIR_MCH shift values.  Each unit's source
+// windows -- up to four cube rows, 1024 + (shift span) + 2 values each -- are staged
+// in shared memory by TMA bulk copies (cp.async.bulk, mbarrier completion), double
+// buffered so that the next unit's rows arrive while the current one is applied.
 #include <algorithm>
 #include <cmath>
 
@@ -31,10 +35,19 @@ using namespace soapgb;
 constexpr int FIR_THREADS = 256;
 constexpr int FIR_PIX = 4;
 constexpr int FIR_TILE = FIR_THREADS * FIR_PIX;
-constexpr int FIR_HASH = 1024;     // shared hash slots (kind, bin, shift)
-constexpr int FIR_EXC = 512;       // shared exception slots
+constexpr int FIR_WIN = 1152;                    // staged values per cube row (window capacity)
+constexpr int FIR_MCH = FIR_WIN - FIR_TILE - 8;  // shift values per work unit (window + alignment fit)
+constexpr int FIR_EXC = 256;                     // exceptions per batch
+constexpr int FIR_MAX_MU = 256;
+constexpr long long FIR_WAIT_LIMIT = 1LL << 24;  // bounded mbarrier waits
+
+static_assert(FIR_MCH <= FIR_THREADS, "one shift value per thread in a unit");
 
 enum { MODE_QUIET = 0, MODE_PHASE = 1 };
+enum { CLS_SPOT = 0, CLS_FAC = 1, CLS_DIRECT = 2 };
+
+// status words written by the kernels of this file
+enum { FIR_ST_UNIFORM = 31, FIR_ST_SEGMENTS = 34, FIR_ST_FAST = 35, FIR_ST_WAIT = 41 };
 
 // per grid cell constants (phase independent)
 struct CellGeo {
@@ -43,40 +56,16 @@ struct CellGeo {
     double dlt;    // ir - 1
     double L;      // limb darkening
     double w2;     // (1 + LB) L
-    // FP32 form: the position t(j0) = j0 dlt - offir in float pairs (hi + lo carries
-    // 48 significant bits, the precision of the FP64 position), and FP32 weights
-    float dlt_hi, dlt_lo, off_hi, off_lo;
-    float Lf, w2f, dltf;
     int row;       // mu bin
     int zero_v;    // delta == 0: the reference copies the row
 };
 
 // the FP32 form's per-cell constants, two 16-byte loads:
-// a = (dlt_hi, dlt_lo, off_hi, off_lo), b = (L, (1 + LB) L, dlt, bits(row | zero_v << 31))
+// a = (dlt_hi, dlt_lo, offir_hi, offir_lo) (t(j0) = j0 dlt - offir in float pairs, the
+// 48 significant bits of the FP64 position), b = (L, (1 + LB) L, dlt, bits(row | zero_v << 31))
 struct __align__(16) CellGeo32 {
     float4 a, b;
 };
-
-// per (list, entry) record: x = grid cell, y = flags (bit 0 facula, bit 1 integral temperature)
-__global__ void k_list_records(int n_lists, int max_cells, const int *__restrict__ cells,
-                               const int *__restrict__ counts, const double *__restrict__ temp,
-                               const double *__restrict__ bi, long long gm, int2 *recs) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int l = blockIdx.y;
-    if (t >= counts[l]) return;
-    int cell = cells[(long long)l * max_cells + t];
-    int flags = 2;
-    if (bi) {
-        double b = bi[(long long)l * gm + cell];
-        double tc = temp[(long long)l * gm + cell];
-        flags = ((__double_as_longlong(b) << 1) == 0 ? 0 : 1);
-        long long tb = __double_as_longlong(tc);
-        int e = (int)((tb >> 52) & 0x7ff) - 1023;
-        bool integral = (e >= 52) || (e < 0 ? (tb << 1) == 0 : ((tb & 0xfffffffffffffLL) & ((1LL << (52 - e)) - 1)) == 0);
-        flags |= integral ? 2 : 0;
-    }
-    recs[(long long)l * max_cells + t] = make_int2(cell, flags);
-}
 
 __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const double *__restrict__ limb,
                            const double *__restrict__ lb, const int *__restrict__ region, int n_mu, double lambda0,
@@ -94,15 +83,9 @@ __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const
     g.dlt = g.ir - 1.0;
     g.L = limb[k];
     g.w2 = lb ? (1.0 + lb[k]) * g.L : g.L;
-    g.Lf = (float)g.L;
-    g.w2f = (float)g.w2;
-    g.dltf = (float)g.dlt;
-    g.dlt_hi = (float)g.dlt;
-    g.dlt_lo = (float)(g.dlt - (double)g.dlt_hi);
-    g.off_hi = (float)g.offir;
-    g.off_lo = (float)(g.offir - (double)g.off_hi);
     int row = region[k];
-    if ((unsigned)row >= (unsigned)n_mu && g.L > -998.0) {
+    bool visible = g.L > -998.0;
+    if ((unsigned)row >= (unsigned)n_mu && visible) {
         atomicExch(status, 21);
         row = 0;
     }
@@ -110,8 +93,9 @@ __global__ void k_cell_geo(long long gm, const double *__restrict__ delta, const
     g.zero_v = (d == 0.0);
     geo[k] = g;
     CellGeo32 h;
-    h.a = make_float4(g.dlt_hi, g.dlt_lo, g.off_hi, g.off_lo);
-    h.b = make_float4(g.Lf, g.w2f, g.dltf, __int_as_float(g.row | (g.zero_v ? (int)0x80000000 : 0)));
+    float dh = (float)g.dlt, oh = (float)g.offir;
+    h.a = make_float4(dh, (float)(g.dlt - (double)dh), oh, (float)(g.offir - (double)oh));
+    h.b = make_float4((float)g.L, (float)g.w2, (float)g.dlt, __int_as_float(g.row | (g.zero_v ? (int)0x80000000 : 0)));
     geo32[k] = h;
 }
 
@@ -120,7 +104,7 @@ __global__ void k_check_uniform(int n_eff, const double *__restrict__ lam, doubl
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_eff) return;
     double expect = lam[0] + (double)i * step;
-    if (fabs(lam[i] - expect) > 1e-6 * step) atomicExch(status, 31);
+    if (fabs(lam[i] - expect) > 1e-6 * step) atomicExch(status, FIR_ST_UNIFORM);
 }
 
 template <typename T>
@@ -131,10 +115,240 @@ __global__ void k_to_type(long long count, const double *__restrict__ a, const d
     out[i] = (T)v;
 }
 
+// --- cell order ----------------------------------------------------------------
+// pass 1 keys: the slope dlt (order-preserving 64-bit image); pass 2 (stable): mu bin
+// and v == 0, invisible cells last
+__global__ void k_sort_keys1(long long gm, const CellGeo *__restrict__ geo, unsigned long long *keys, int *vals) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= gm) return;
+    keys[k] = soap_ord64(geo[k].dlt);
+    vals[k] = (int)k;
+}
+
+__global__ void k_sort_keys2(long long gm, const CellGeo *__restrict__ geo, const int *__restrict__ order,
+                             unsigned *keys) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= gm) return;
+    const CellGeo &g = geo[order[k]];
+    keys[k] = (g.L > -998.0) ? (unsigned)(g.row * 2 + g.zero_v) : 0x3fffu;
+}
+
+// exact tests on FP64 values with integer instructions (no FP64 pipe)
+__device__ __forceinline__ bool bits_is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ bool bits_is_integral(double v) {
+    long long b = __double_as_longlong(v);
+    int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e >= 52) return true;
+    if (e < 0) return (b << 1) == 0;
+    long long mant = b & 0xfffffffffffffLL;
+    return (mant & ((1LL << (52 - e)) - 1)) == 0;
+}
+
+// --- per-list cell lists in velocity order ---------------------------------------
+// One block per list (the quiet disk, or one phase): the visible cells in the sorted
+// order, split into classes -- 0: spots (integral temperature, Planck ratio exactly 1),
+// 1: faculae, 2: cells evaluated directly (other spots; faculae of the solar
+// variant).  counts[l] = (n0, n1, n2, 0); class c occupies positions
+// [n0 + .. + n_{c-1}, + n_c) of the list.  Active cells are those whose type map value
+// lies in [-0.5, 1.5] (0 spot, otherwise facula), as in the per-cell form's compaction.
+__device__ __forceinline__ int fir_class(const CellGeo &g, const double *bi, const double *temp, long long idx,
+                                         int solar) {
+    if (!(g.L > -998.0)) return -1;
+    if (!bi) return CLS_SPOT;
+    double b = bi[idx];
+    if (!(b >= -0.5 && b <= 1.5)) return -1;
+    if (bits_is_zero(b)) return bits_is_integral(temp[idx]) ? CLS_SPOT : CLS_DIRECT;
+    return solar ? CLS_DIRECT : CLS_FAC;
+}
+
+__global__ void __launch_bounds__(1024) k_fir_lists(long long gm, const int *__restrict__ order,
+                                                    const CellGeo *__restrict__ geo, const double *__restrict__ temp,
+                                                    const double *__restrict__ bi, int solar, int *list_cell,
+                                                    double *list_dlt, int *counts) {
+    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = blockDim.x >> 5;
+    const long long mbase = (long long)l * gm;
+    __shared__ int cnt[3];
+    __shared__ int wc[32][3];
+    __shared__ int base[3];
+    if (tid < 3) cnt[tid] = 0;
+    __syncthreads();
+    int my[3] = {0, 0, 0};
+    for (long long r = tid; r < gm; r += blockDim.x) {
+        int cell = order[r];
+        int c = fir_class(geo[cell], bi, temp, mbase + cell, solar);
+        if (c >= 0) my[c]++;
+    }
+    for (int c = 0; c < 3; ++c) {
+        int v = my[c];
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) atomicAdd(&cnt[c], v);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        base[0] = 0;
+        base[1] = cnt[0];
+        base[2] = cnt[0] + cnt[1];
+        int *o = counts + 4 * l;
+        o[0] = cnt[0];
+        o[1] = cnt[1];
+        o[2] = cnt[2];
+        o[3] = 0;
+    }
+    __syncthreads();
+    // ordered compaction, blockDim entries per pass
+    for (long long r0 = 0; r0 < gm; r0 += blockDim.x) {
+        long long r = r0 + tid;
+        int c = -1, cell = 0;
+        double d = 0.0;
+        if (r < gm) {
+            cell = order[r];
+            const CellGeo &g = geo[cell];
+            c = fir_class(g, bi, temp, mbase + cell, solar);
+            d = g.dlt;
+        }
+        unsigned m[3];
+        for (int q = 0; q < 3; ++q) m[q] = __ballot_sync(0xffffffffu, c == q);
+        if (lane == 0)
+            for (int q = 0; q < 3; ++q) wc[warp][q] = __popc(m[q]);
+        __syncthreads();
+        if (c >= 0) {
+            int pos = base[c] + __popc(m[c] & ((1u << lane) - 1));
+            for (int w = 0; w < warp; ++w) pos += wc[w][c];
+            list_cell[mbase + pos] = cell;
+            list_dlt[mbase + pos] = d;
+        }
+        __syncthreads();
+        if (tid < 3) {
+            int s = 0;
+            for (int w = 0; w < nw; ++w) s += wc[w][tid];
+            base[tid] += s;
+        }
+        __syncthreads();
+    }
+}
+
+// --- prefix sums and segments -------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_scan_excl(double (&v)[NV], int &vi, double (&tot)[NV], int &toti,
+                                                double (*ws)[NV + 1]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    double inc[NV];
+    int inci = vi;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) inc[q] = v[q];
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double t = __shfl_up_sync(0xffffffffu, inc[q], o);
+            if (lane >= o) inc[q] += t;
+        }
+        int ti = __shfl_up_sync(0xffffffffu, inci, o);
+        if (lane >= o) inci += ti;
+    }
+    if (lane == 31) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) ws[warp][q] = inc[q];
+        ws[warp][NV] = (double)inci;
+    }
+    __syncthreads();
+    double off[NV];
+    int offi = 0;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) off[q] = 0.0, tot[q] = 0.0;
+    toti = 0;
+    for (int w = 0; w < nw; ++w) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            if (w < warp) off[q] += ws[w][q];
+            tot[q] += ws[w][q];
+        }
+        int wi = (int)ws[w][NV];
+        if (w < warp) offi += wi;
+        toti += wi;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = off[q] + inc[q] - v[q];
+    vi = offi + inci - vi;
+}
+
+// Block (l, c) for classes 0 and 1: exclusive FP64 prefix sums over the class list of
+// L, L dlt, L offir and (1 + LB) L, (1 + LB) L dlt, (1 + LB) L offir (the prefix of
+// the entry at list position q is stored at index q + c, the class total after its
+// last entry), and the list of (mu bin, v == 0) segments:
+// segs[(l*2 + c)*cap + s] = (first position, row * 2 + zero_v), nseg[l*2 + c].
+__global__ void __launch_bounds__(256) k_fir_prefix(long long gm, const int *__restrict__ counts,
+                                                    const int *__restrict__ list_cell,
+                                                    const CellGeo *__restrict__ geo, double *pre, long long pre_stride,
+                                                    long long pre_comp, int2 *segs, int *nseg, int seg_cap,
+                                                    int *status) {
+    const int l = blockIdx.x, c = blockIdx.y, tid = threadIdx.x;
+    const int *cn = counts + 4 * l;
+    const int cs = (c == 0) ? 0 : cn[0];
+    const int cnt = cn[c];
+    const long long lbase = (long long)l * gm;
+    const long long pbase = (long long)l * pre_stride + c;
+    __shared__ double ws[256 / 32][7];
+    const int per = (cnt + blockDim.x - 1) / blockDim.x;
+    const int a = cs + min(cnt, tid * per), b = cs + min(cnt, (tid + 1) * per);
+    auto key_at = [&](int q) -> int {
+        const CellGeo &g = geo[list_cell[lbase + q]];
+        return g.row * 2 + g.zero_v;
+    };
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    int ns = 0;
+    int prev = (a > cs && a < b) ? key_at(a - 1) : -1;
+    for (int q = a; q < b; ++q) {
+        const CellGeo &g = geo[list_cell[lbase + q]];
+        s[0] += g.L;
+        s[1] += g.L * g.dlt;
+        s[2] += g.L * g.offir;
+        s[3] += g.w2;
+        s[4] += g.w2 * g.dlt;
+        s[5] += g.w2 * g.offir;
+        int k = g.row * 2 + g.zero_v;
+        if (q == cs || k != prev) ns++;
+        prev = k;
+    }
+    double tot[6];
+    int tns;
+    block_scan_excl<6>(s, ns, tot, tns, ws);
+    prev = (a > cs && a < b) ? key_at(a - 1) : -1;
+    for (int q = a; q < b; ++q) {
+        const CellGeo &g = geo[list_cell[lbase + q]];
+        long long pi = pbase + q;
+        pre[pi] = s[0];
+        pre[pre_comp + pi] = s[1];
+        pre[2 * pre_comp + pi] = s[2];
+        pre[3 * pre_comp + pi] = s[3];
+        pre[4 * pre_comp + pi] = s[4];
+        pre[5 * pre_comp + pi] = s[5];
+        s[0] += g.L;
+        s[1] += g.L * g.dlt;
+        s[2] += g.L * g.offir;
+        s[3] += g.w2;
+        s[4] += g.w2 * g.dlt;
+        s[5] += g.w2 * g.offir;
+        int k = g.row * 2 + g.zero_v;
+        if (q == cs || k != prev) {
+            if (ns < seg_cap) segs[(long long)(l * 2 + c) * seg_cap + ns] = make_int2(q, k);
+            ns++;
+        }
+        prev = k;
+    }
+    if (tid == 0) {
+        long long pi = pbase + cs + cnt;
+        for (int q = 0; q < 6; ++q) pre[q * pre_comp + pi] = tot[q];
+        if (tns > seg_cap) atomicExch(status, FIR_ST_SEGMENTS);
+        nseg[l * 2 + c] = min(tns, seg_cap);
+    }
+}
+
+// --- device helpers of the tile kernel -------------------------------------------------
 // per-pixel sums of the FP32 form: compensated (Kahan) when set
 constexpr bool FIR_COMPENSATED = true;
 
-// per-pixel accumulator
 template <typename T>
 struct Acc {
     T s, c;
@@ -152,9 +366,9 @@ struct Acc {
     __device__ __forceinline__ double get() const { return (double)s - (double)c; }
 };
 
-// Source position of a cell at the tile start, on the FP32 pipe: u0 = j0 + t with
-// t = j0 dlt - offir evaluated in float pairs (exact products by fmaf, TwoSum for
-// the sums); returns i0 = floor(u0) and phi = u0 - i0.  |t| < 2^20 and j0 < 2^24.
+// Source position of a cell at j0 on the FP32 pipe: u0 = j0 + t with t = j0 dlt - offir
+// in float pairs (exact products by fmaf, TwoSum for the sums); i0 = floor(u0),
+// phi = u0 - i0.  |t| < 2^20 and j0 < 2^24.
 __device__ __forceinline__ void fir_pos32(int j0, const float dlt_hi, const float dlt_lo, const float off_hi,
                                           const float off_lo, int &i0, float &phi) {
     float j0f = (float)j0;
@@ -180,48 +394,28 @@ __device__ __forceinline__ void fir_pos32(int j0, const float dlt_hi, const floa
     phi = fr;
 }
 
-// exact tests on FP64 values with integer instructions (no FP64 pipe)
-__device__ __forceinline__ bool bits_is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
-__device__ __forceinline__ bool bits_is_integral(double v) {
-    long long b = __double_as_longlong(v);
-    int e = (int)((b >> 52) & 0x7ff) - 1023;
-    if (e >= 52) return true;
-    if (e < 0) return (b << 1) == 0;
-    long long mant = b & 0xfffffffffffffLL;
-    return (mant & ((1LL << (52 - e)) - 1)) == 0;
-}
-
-struct FirCubes {
-    // PHASE: q_sed, q_norm, spot_norm, dq_spot, fac_norm, dq_fac; QUIET: [0] only
-    const void *c[6];
-    const double *spot_sed;
-    const double *fac_sed;
-    // FP32 form: the two continuum rows as float pairs (hi, lo)
-    const float2 *spot_sed2;
-    const float2 *fac_sed2;
-};
-
+// a cell's owner i0 and weight phi at j0 with its constants
 template <typename T>
-struct Exc {
-    int i0;          // owner at j0
-    int row;
-    int kind;        // 0 spot, 1 facula (phase); 0 (quiet)
-    int parts;       // 1: the L-weighted sums, 2: the (1+LB) L-weighted facula sums
-    int zero_v;
-    int plain_t;     // spot temperature is an integer: Planck ratio exactly 1
-    T phi, dlt, L, w2;
-    double temp;
-};
-
-__device__ __forceinline__ unsigned fir_key(int kind, int row, int k) {
-    // kind < 4, row < 2^12, k in [-2^14, 2^14)
-    return ((unsigned)kind << 28) | ((unsigned)row << 16) | (unsigned)((k + 16384) & 0xffff);
-}
-
-template <typename T>
-__device__ __forceinline__ T lerp_at(const T *__restrict__ row, long long i, T w) {
-    T s0 = row[i], s1 = row[i + 1];
-    return s0 + (s1 - s0) * w;
+__device__ __forceinline__ void cell_pos(int j0, const CellGeo *geo, const CellGeo32 *geo32, int cell, int &i0,
+                                         T &phi, T &dlt, T &L, T &w2) {
+    if constexpr (sizeof(T) == 4) {
+        CellGeo32 h = geo32[cell];
+        float ph;
+        fir_pos32(j0, h.a.x, h.a.y, h.a.z, h.a.w, i0, ph);
+        phi = ph;
+        L = h.b.x;
+        w2 = h.b.y;
+        dlt = h.b.z;
+    } else {
+        const CellGeo &g = geo[cell];
+        double u0 = fma((double)j0, g.ir, -g.offir);
+        double fl = floor(u0);
+        i0 = (int)fl;
+        phi = u0 - fl;
+        L = g.L;
+        w2 = g.w2;
+        dlt = g.dlt;
+    }
 }
 
 // loi_Planck ratio B(lambda, t) / B(lambda, tn) (SOAP_integration.cu:205-212)
@@ -233,18 +427,6 @@ __device__ __forceinline__ double fir_planck_ratio(double lambda0, double t, dou
     double a = (h * c) / (lambda0 * k_b * scale);
     return (exp(a / tn) - 1) / (exp(a / t) - 1);
 }
-
-template <typename T>
-struct FirShared {
-    unsigned key[FIR_HASH];
-    // group coefficients in 64-bit fixed point: integer atomics are native, exact and
-    // order independent (A0, A1 scaled by 2^40, B by 2^56)
-    unsigned long long val[FIR_HASH][3];
-    int grp[FIR_HASH];
-    float gcoef[FIR_HASH][3];   // FP32 form: group coefficients for the apply phase
-    Exc<T> exc[FIR_EXC];
-    int nexc, ngrp;
-};
 
 // float pair with an error term (TwoSum): the FP32 form's output combinations
 struct F2 {
@@ -261,112 +443,6 @@ __device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
     r.lo = e - (hi - s);
     return r;
 }
-
-constexpr double FIX_A = 1099511627776.0;            // 2^40: A0, A1 (weights <= 1 per cell)
-constexpr double FIX_B = 72057594037927936.0;        // 2^56: B (weight x delta, |delta| ~ 1e-5)
-constexpr float FIX_A_F = 1099511627776.0f;
-constexpr float FIX_B_F = 72057594037927936.0f;
-__device__ __forceinline__ long long v_fix(double a, double scale) { return __double2ll_rn(a * scale); }
-__device__ __forceinline__ long long v_fix(float a, float scale) {
-    // a * 2^k is exact in FP32; the conversion rounds once
-    return __float2ll_rn(a * scale);
-}
-
-// One pass of the warp-cooperative insertion: lanes holding a key (active) fold
-// runs of equal keys (segmented scan of 64-bit fixed-point values: integer adds,
-// exact and associative) and the run's last lane adds the sums to the shared hash
-// table.  Returns whether this lane's contribution reached the table.
-template <typename SH>
-__device__ __forceinline__ bool fir_insert(SH &sh, bool active, unsigned key, long long a0, long long a1,
-                                           long long bb, int lane) {
-    if (!active) key = 0xfffffffeu;
-    unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
-    bool seg = (lane == 0) || (prev != key);
-    // fast path: the whole warp is one run (cells come in map order, so most warps are)
-    if (__all_sync(0xffffffffu, lane == 0 || !seg)) {
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) {
-            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-            bb += __shfl_xor_sync(0xffffffffu, bb, o);
-        }
-        bool ok = true;
-        if (key != 0xfffffffeu && lane == 31) {
-            ok = false;
-            unsigned h = (key * 2654435761u) & (FIR_HASH - 1);
-            for (int probe = 0; probe < 64 && !ok; ++probe) {
-                unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
-                if (old == 0xffffffffu || old == key) {
-                    atomicAdd(&sh.val[h][0], (unsigned long long)a0);
-                    atomicAdd(&sh.val[h][1], (unsigned long long)a1);
-                    atomicAdd(&sh.val[h][2], (unsigned long long)bb);
-                    ok = true;
-                } else {
-                    h = (h + 1) & (FIR_HASH - 1);
-                }
-            }
-        }
-        int all_ok = __shfl_sync(0xffffffffu, (int)ok, 31);
-        return !active || all_ok;
-    }
-    for (int o = 1; o < 32; o <<= 1) {
-        long long v0 = __shfl_up_sync(0xffffffffu, a0, o);
-        long long v1 = __shfl_up_sync(0xffffffffu, a1, o);
-        long long v2 = __shfl_up_sync(0xffffffffu, bb, o);
-        int sg = __shfl_up_sync(0xffffffffu, (int)seg, o);
-        if (lane >= o && !seg) {
-            a0 += v0;
-            a1 += v1;
-            bb += v2;
-            seg = sg;
-        }
-    }
-    unsigned next = __shfl_down_sync(0xffffffffu, key, 1);
-    bool tail = (lane == 31) || (next != key);
-    bool ok = true;
-    if (active && tail) {
-        ok = false;
-        unsigned h = (key * 2654435761u) & (FIR_HASH - 1);
-        for (int probe = 0; probe < 64 && !ok; ++probe) {
-            unsigned old = atomicCAS(&sh.key[h], 0xffffffffu, key);
-            if (old == 0xffffffffu || old == key) {
-                atomicAdd(&sh.val[h][0], (unsigned long long)a0);
-                atomicAdd(&sh.val[h][1], (unsigned long long)a1);
-                atomicAdd(&sh.val[h][2], (unsigned long long)bb);
-                ok = true;
-            } else {
-                h = (h + 1) & (FIR_HASH - 1);
-            }
-        }
-    }
-    // every lane learns the outcome of its run's tail
-    unsigned tails = __ballot_sync(0xffffffffu, tail);
-    int my_tail = __ffs(tails & (0xffffffffu << lane)) - 1;
-    int tail_ok = __shfl_sync(0xffffffffu, (int)ok, my_tail);
-    return !active || tail_ok;
-}
-
-// a cell's three group coefficients in fixed point: A0 = w (1 - phi), A1 = w phi,
-// B = w delta (the weight at pixel dj is A0 - B dj on the owner, A1 + B dj on owner + 1)
-struct Coef3 {
-    long long a0, a1, bb;
-};
-template <typename T>
-__device__ __forceinline__ Coef3 coef3(T w, T phi, T dlt) {
-    Coef3 r;
-    if constexpr (sizeof(T) == 4) {
-        r.a0 = v_fix(w * (1.0f - phi), FIX_A_F);
-        r.a1 = v_fix(w * phi, FIX_A_F);
-        r.bb = v_fix(w * dlt, FIX_B_F);
-    } else {
-        r.a0 = v_fix(w * (1.0 - phi), FIX_A);
-        r.a1 = v_fix(w * phi, FIX_A);
-        r.bb = v_fix(w * dlt, FIX_B);
-    }
-    return r;
-}
-
-// float-pair arithmetic for the FP32 form's output combination
 __device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
     float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);
@@ -383,44 +459,251 @@ __device__ __forceinline__ F2 f2_neg(F2 a) {
     return a;
 }
 
+// mbarrier + bulk copy (TMA, non-tensor form)
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+    for (long long it = 0; it < FIR_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+struct FirCubes {
+    // PHASE: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm;
+    // QUIET: [0] only.  Workspace slots: 256-byte aligned, padded to 256 bytes.
+    const void *c[6];
+    const double *spot_sed;
+    const double *fac_sed;
+    // FP32 form: the two continuum rows as float pairs (hi, lo)
+    const float2 *spot_sed2;
+    const float2 *fac_sed2;
+};
+
+// cube rows staged for a segment of class cls (window slot q)
+//   spot:   S (q_sed), Qs (q_norm), As (spot_norm), Bs (q_norm - spot_norm)  -- weight L
+//   facula: S (q_sed), Bf (q_norm - fac_norm) -- weight L; Qf (q_norm), Af (fac_norm) -- weight (1+LB) L
+__device__ __forceinline__ int fir_cube_index(int mode, int cls, int q) {
+    if (mode == MODE_QUIET) return 0;
+    if (cls == CLS_SPOT) return q;
+    return (q == 0) ? 0 : (q == 1) ? 5 : (q == 2) ? 1 : 4;
+}
+
+struct FirSeg {
+    int start, end;     // list positions
+    int key;            // row * 2 + zero_v
+    int cls;
+    int m_lo, m_hi;     // floor of t over the segment and the tile
+    int u0;             // first work unit
+};
+
+struct FirUnit {
+    int seg, ma, mb;    // segment, shift values [ma, mb]
+    int w0, w1, off;    // window [w0, w1) (source pixels), offset of w0 in the staged copy
+};
+
+template <typename T>
+struct FirGrp {
+    T a0, a1, b;        // weight L
+    T a0w, a1w, bw;     // weight (1 + LB) L (faculae)
+    int m, ok;
+};
+
+template <typename T>
+struct FirExcW {        // wrap cell of the current unit (reads the staged window)
+    int i0;
+    T phi, dlt, L, w2;
+};
+
+template <typename T>
+struct FirExcD {        // directly evaluated cell (reads the cubes in global memory)
+    int i0, row, kind, zero_v;
+    T phi, dlt, L, w2;
+    double temp;
+};
+
+// per-batch capacities: shift values (group tasks) and staged wrap cells
+template <typename T>
+struct FirCaps {
+    static constexpr int GRP = (sizeof(T) == 4) ? 512 : 256;
+    static constexpr int EXC = (sizeof(T) == 4) ? 512 : 256;
+};
+constexpr int FIR_BATCH_U = 128;   // work units per batch
+
+template <typename T, int NC>
+struct FirSmem {
+    // staged windows; the direct cells' buffer reuses this space once all copies landed
+    union {
+        T win[2][NC][FIR_WIN];
+        FirExcD<T> excd[FIR_EXC];
+    };
+    unsigned long long bar[2];
+    FirUnit bud[FIR_BATCH_U];              // descriptors of the batch's units
+    int ut[FIR_BATCH_U + 1];               // first task of each unit of the batch
+    FirGrp<T> grp[FirCaps<T>::GRP];        // one group per task (shift value)
+    int wlo[FirCaps<T>::GRP];              // first list position of the task's wrap cells
+    int woff[FirCaps<T>::GRP + 1];         // wrap counts, then their exclusive offsets
+    FirExcW<T> excw[FirCaps<T>::EXC];      // wrap cells of the batch
+    int wsum[FIR_THREADS / 32];
+    int nunit, fail, nb, ntask;
+    // followed by FirSeg seg[] (dynamic, 16-byte aligned)
+};
+
+template <typename T, int NC>
+__host__ __device__ constexpr size_t fir_smem_fixed() { return (sizeof(FirSmem<T, NC>) + 15) & ~size_t(15); }
+
+__device__ __forceinline__ int block_excl_scan_int(int v, int *wsum, int &total) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int w = 0; w < FIR_THREADS / 32; ++w) {
+        if (w < warp) off += wsum[w];
+        tot += wsum[w];
+    }
+    __syncthreads();
+    total = tot;
+    return off + inc - v;
+}
+
+// first position q in [lo, hi) with floor(dlt_q X) >= m (dlt ascending, X > 0: the
+// rounded product is monotone in dlt, so the predicate is monotone in q)
+__device__ __forceinline__ int fir_lower_bound(const double *__restrict__ dl, int lo, int hi, double X, int m) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (floor(dl[mid] * X) >= (double)m)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+struct FirTileArgs {
+    int n, n_eff;
+    const double *lam;
+    double los;                 // lambda0 / step
+    FirCubes cubes;
+    const int *list_cell;       // [l][gm]
+    const double *list_dlt;     // [l][gm]
+    const int *counts;          // [l][4]
+    const double *pre;          // 6 components x [l][pre_stride]
+    long long pre_stride, pre_comp;
+    const int2 *segs;           // [l][2][seg_cap]
+    const int *nseg;            // [l][2]
+    int seg_cap;
+    const CellGeo *geo;
+    const CellGeo32 *geo32;
+    const double *temp, *bi;    // [l][gm] (phase)
+    long long gm;
+    int solar, t_norm_fac;
+    void *out0, *out1, *out2;
+    long long out_stride;
+    int *status;
+};
+
 // QUIET: OutT = double (one spectrum, once per star); PHASE: OutT = T (the FP32 form
 // keeps its deficits in FP32 for the FP32 convolution that consumes them)
 template <typename T, int MODE, typename OutT>
-__global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const double *__restrict__ lam,
-                                                     FirCubes cubes, const int2 *__restrict__ recs,
-                                                     const int *__restrict__ counts, int max_cells,
-                                                     const CellGeo *__restrict__ geo,
-                                                     const CellGeo32 *__restrict__ geo32,
-                                                     const double *__restrict__ temp, const double *__restrict__ bi,
-                                                     long long gm, int solar, int t_norm_fac,
-                                                     OutT *__restrict__ out0, OutT *__restrict__ out1,
-                                                     OutT *__restrict__ out2, long long out_stride) {
-    extern __shared__ __align__(16) unsigned char fir_smem[];
-    FirShared<T> &sh = *reinterpret_cast<FirShared<T> *>(fir_smem);
-
-    const int p = blockIdx.y;
+__global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
+    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
+    extern __shared__ __align__(128) unsigned char fir_smem[];
+    FirSmem<T, NC> &sh = *reinterpret_cast<FirSmem<T, NC> *>(fir_smem);
+    FirSeg *segs = reinterpret_cast<FirSeg *>(fir_smem + fir_smem_fixed<T, NC>());
+    const int l = blockIdx.y;
     const int j0 = blockIdx.x * FIR_TILE;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int n_cells = counts[p];
-    const int2 *pr = recs + (long long)p * max_cells;
-    const double *pt = (MODE == MODE_PHASE) ? temp + (long long)p * gm : nullptr;
+    const int tid = threadIdx.x;
+    const int n = A.n, n_eff = A.n_eff;
+    OutT *out0 = reinterpret_cast<OutT *>(A.out0);
+    OutT *out1 = reinterpret_cast<OutT *>(A.out1);
+    OutT *out2 = reinterpret_cast<OutT *>(A.out2);
     const int t_eff = min(FIR_TILE, n_eff - j0);
     if (t_eff <= 0) {   // whole tile in the zero tail [n_eff, n)
         for (int q = 0; q < FIR_PIX; ++q) {
             int j = j0 + tid + q * FIR_THREADS;
             if (j >= n) continue;
-            long long o = (long long)p * out_stride + j;
+            long long o = (long long)l * A.out_stride + j;
             out0[o] = (OutT)0;
             if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
         }
         return;
     }
+    const long long lbase = (long long)l * A.gm;
+    const double *dl = A.list_dlt + lbase;
+    const int *cn = A.counts + 4 * l;
+    const double Xa = (double)j0 + A.los, Xb = (double)(j0 + t_eff - 1) + A.los;
 
-    for (int q = tid; q < FIR_HASH; q += FIR_THREADS) {
-        sh.key[q] = 0xffffffffu;
-        sh.val[q][0] = sh.val[q][1] = sh.val[q][2] = 0ULL;
+    // --- segments of this list with their shift ranges at this tile ------------------
+    const int ns0 = A.nseg[2 * l], ns1 = (MODE == MODE_PHASE) ? A.nseg[2 * l + 1] : 0;
+    const int nsg = ns0 + ns1;
+    if (tid == 0) {
+        mbar_init(&sh.bar[0], 1);
+        mbar_init(&sh.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sh.fail = 0;
     }
-    if (tid == 0) sh.nexc = 0;
+    for (int s = tid; s < nsg; s += FIR_THREADS) {
+        const int c = (s < ns0) ? 0 : 1;
+        const int si = (c == 0) ? s : s - ns0;
+        const int ns_c = (c == 0) ? ns0 : ns1;
+        const int2 *sp = A.segs + (long long)(2 * l + c) * A.seg_cap;
+        const int2 e = sp[si];
+        const int cend = (c == 0) ? cn[0] : cn[0] + cn[1];
+        FirSeg g;
+        g.start = e.x;
+        g.end = (si + 1 < ns_c) ? sp[si + 1].x : cend;
+        g.key = e.y;
+        g.cls = c;
+        const double d0 = dl[g.start], d1 = dl[g.end - 1];
+        g.m_lo = (int)fmin(floor(d0 * Xa), floor(d0 * Xb));
+        g.m_hi = (int)fmax(floor(d1 * Xa), floor(d1 * Xb));
+        if (fmax(fabs(d0), fabs(d1)) * (double)(FIR_TILE - 1) >= 1.0) {
+            atomicExch(A.status, FIR_ST_FAST);   // a weight could wrap twice in one tile
+            g.m_hi = g.m_lo;
+        }
+        g.u0 = 0;
+        segs[s] = g;
+    }
+    __syncthreads();
+    if (tid == 0) {   // work units: ceil((m_hi - m_lo + 1) / FIR_MCH) per segment
+        int u = 0;
+        for (int s = 0; s < nsg; ++s) {
+            segs[s].u0 = u;
+            u += (segs[s].m_hi - segs[s].m_lo + FIR_MCH) / FIR_MCH;
+        }
+        sh.nunit = u;
+    }
+    __syncthreads();
+    const int nunit = sh.nunit;
 
     // accumulators: QUIET [0]; PHASE: S, Qs, As, Bs, Qf, Af, Bf
     constexpr int NACC = (MODE == MODE_QUIET) ? 1 : 7;
@@ -429,248 +712,378 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
     for (int a = 0; a < NACC; ++a)
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) acc[a][q].zero();
-    __syncthreads();
 
-    // direct evaluation of the collected exceptions (the per-cell arithmetic)
-    auto flush = [&]() {
-        int ne = sh.nexc;
-        for (int e = 0; e < ne; ++e) {
-            const Exc<T> &x = sh.exc[e];
-            long long off = (long long)x.row * n;
+    constexpr int GRP = FirCaps<T>::GRP, EXC = FirCaps<T>::EXC;
+    // descriptor of work unit u: its segment, shift values and source window
+    auto describe = [&](int u) -> FirUnit {
+        int lo = 0, hi = nsg - 1;
+        while (lo < hi) {   // last segment with u0 <= u
+            int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].u0 <= u) lo = mid; else hi = mid - 1;
+        }
+        const FirSeg &g = segs[lo];
+        FirUnit d;
+        d.seg = lo;
+        d.ma = g.m_lo + (u - g.u0) * FIR_MCH;
+        d.mb = min(g.m_hi, d.ma + FIR_MCH - 1);
+        d.w0 = max(0, j0 + d.ma - (d.ma > g.m_lo ? 1 : 0));
+        d.w1 = min(n_eff, j0 + t_eff + d.mb + 1);
+        d.off = (d.w1 > d.w0) ? (int)(((((long long)(g.key >> 1) * n + d.w0) * (long long)sizeof(T)) & 15) /
+                                      (long long)sizeof(T))
+                              : 0;
+        return d;
+    };
+    // staging of unit u's rows into buffer u & 1 (thread 0)
+    auto issue = [&](int u, const FirUnit &d) {
+        const FirSeg &g = segs[d.seg];
+        const int b = u & 1;
+        unsigned bytes = 0;
+        uintptr_t rel = 0;   // 16-byte aligned start, relative to the cube base
+        if (d.w1 > d.w0) {
+            const uintptr_t p0 = (uintptr_t)((long long)(g.key >> 1) * n + d.w0) * sizeof(T);
+            const uintptr_t p1 = (uintptr_t)((long long)(g.key >> 1) * n + d.w1) * sizeof(T);
+            rel = p0 & ~uintptr_t(15);
+            bytes = (unsigned)(((p1 + 15) & ~uintptr_t(15)) - rel);
+        }
+        // the buffer was last read through the generic proxy; order those reads before
+        // the async-proxy writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sh.bar[b], bytes * NC);
+        if (bytes) {
 #pragma unroll
-            for (int q = 0; q < FIR_PIX; ++q) {
-                int dj = tid + q * FIR_THREADS;
-                int j = j0 + dj;
-                if (j >= n_eff) continue;
-                long long i;
-                T w;
-                if (x.zero_v) {
-                    i = j;
-                    w = (T)0;
-                } else {
-                    T wd = x.phi + x.dlt * (T)dj;
-                    i = (long long)x.i0 + dj;
-                    if (wd >= (T)1) { wd -= (T)1; i += 1; }
-                    else if (wd < (T)0) { wd += (T)1; i -= 1; }
-                    if (i < 0 || i > n_eff - 2) continue;
-                    w = wd;
-                }
-                auto val = [&](int ci) -> T {
-                    const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
-                    if (x.zero_v) return rowp[i];
-                    return lerp_at(rowp, i, w);
-                };
-                T L = x.L;
-                if constexpr (MODE == MODE_QUIET) {
-                    acc[0][q].add(L * val(0));
-                } else {
-                    if (x.parts & 1) {
-                        acc[0][q].add(L * val(0));                              // S  (q_sed)
-                        if (x.kind == 0) {
-                            T Lq = L;
-                            if (!x.plain_t)                                     // spot Planck ratio
-                                Lq = (T)((double)x.L * fir_planck_ratio(lam[j], x.temp, (double)(int)x.temp));
-                            acc[1][q].add(Lq * val(1));                         // Qs (q_norm)
-                            acc[2][q].add(Lq * val(2));                         // As (spot_norm)
-                            acc[3][q].add(L * val(3));                          // Bs (q_norm - spot_norm)
-                        } else {
-                            acc[6][q].add(L * val(5));                          // Bf (q_norm - fac_norm)
-                        }
-                    }
-                    if ((x.parts & 2) && x.kind == 1) {
-                        T w2 = x.w2;
-                        if (solar) w2 = (T)((double)x.L * fir_planck_ratio(lam[j], x.temp, (double)t_norm_fac));
-                        acc[4][q].add(w2 * val(1));                             // Qf
-                        acc[5][q].add(w2 * val(4));                             // Af (fac_norm)
-                    }
-                }
+            for (int q = 0; q < NC; ++q) {
+                const char *base = reinterpret_cast<const char *>(A.cubes.c[fir_cube_index(MODE, g.cls, q)]);
+                bulk_g2s(&sh.win[b][q][0], base + rel, bytes, &sh.bar[b]);
             }
         }
     };
+    // wrap cells [lo, hi) of the batch into excw[e - dst0]
+    auto fill_exc = [&](int lo, int hi, int dst0, int ntask) {
+        for (int e = lo + tid; e < hi; e += FIR_THREADS) {
+            int a = 0, b = ntask - 1;
+            while (a < b) {   // last task with woff <= e
+                int mid = (a + b + 1) >> 1;
+                if (sh.woff[mid] <= e) a = mid; else b = mid - 1;
+            }
+            const int cell = A.list_cell[lbase + sh.wlo[a] + (e - sh.woff[a])];
+            FirExcW<T> x;
+            cell_pos<T>(j0, A.geo, A.geo32, cell, x.i0, x.phi, x.dlt, x.L, x.w2);
+            sh.excw[e - dst0] = x;
+        }
+    };
 
-    // --- setup: place every cell at this tile -----------------------------------
-    for (int c0 = 0; c0 < n_cells; c0 += FIR_THREADS) {
-        int ci = c0 + tid;
-        bool have = ci < n_cells;
-        int2 rec = have ? pr[ci] : make_int2(0, 2);
-        int cell = rec.x;
-        int kind = (MODE == MODE_PHASE) ? (rec.y & 1) : 0;
-        int plain_t = (rec.y >> 1) & 1;
-        bool regular = false;
-        int i0 = 0;
-        T phi = (T)0, Lw, W2w, Dw;
-        int row, zero_v;
-        float dh = 0.f, dl = 0.f, oh = 0.f, ol = 0.f;
-        double gir = 0.0, goff = 0.0;
-        if constexpr (sizeof(T) == 4) {
-            CellGeo32 h = geo32[cell];
-            dh = h.a.x; dl = h.a.y; oh = h.a.z; ol = h.a.w;
-            Lw = h.b.x; W2w = h.b.y; Dw = h.b.z;
-            int rz = __float_as_int(h.b.w);
-            row = rz & 0x7fffffff;
-            zero_v = (rz >> 31) & 1;
-        } else {
-            const CellGeo &g = geo[cell];
-            Lw = g.L; W2w = g.w2; Dw = g.dlt;
-            row = g.row;
-            zero_v = g.zero_v;
-            gir = g.ir;
-            goff = g.offir;
-        }
-        if (have) {
-            if constexpr (sizeof(T) == 4) {
-                float ph;
-                fir_pos32(j0, dh, dl, oh, ol, i0, ph);
-                phi = ph;
-            } else {
-                double u0 = fma((double)j0, gir, -goff);
-                double fl = floor(u0);
-                i0 = (int)fl;
-                phi = u0 - fl;
+    int u_fail = -1;
+    int issued = -1;   // last unit whose copy was issued (thread 0)
+    for (int ub = 0; ub < nunit;) {
+        // --- batch: units [ub, ub + nb) with at most GRP shift values in total ---------
+        const int nbu = min(FIR_BATCH_U, nunit - ub);
+        for (int t = tid; t < nbu; t += FIR_THREADS) sh.bud[t] = describe(ub + t);
+        __syncthreads();
+        if (tid == 0) {
+            if (issued < ub) {
+                issue(ub, sh.bud[0]);
+                issued = ub;
             }
-            // owners leaving [0, n_eff-2] do not break the linear form: the apply loop
-            // clips each group's pixel range (pixels without an owner get nothing)
-            T w_end = phi + Dw * (T)(t_eff - 1);
-            int kk = j0 - i0;
-            regular = (w_end >= (T)0) && (w_end < (T)1) && (kk >= -16384) && (kk < 16384);
-            // v == 0 copies the row up to n_eff - 1, one pixel further than the clip
-            if (zero_v) regular = regular && (j0 + t_eff - 1 <= n_eff - 2);
-            if constexpr (MODE == MODE_PHASE) {
-                if (kind == 0 && !plain_t) regular = false;    // spot Planck ratio != 1
-                if (kind == 1 && solar) regular = false;       // per-pixel Planck ratio
+            int nb = 0, nt = 0;
+            sh.ut[0] = 0;
+            while (nb < nbu) {
+                const int k = sh.bud[nb].mb - sh.bud[nb].ma + 1;
+                if (nt + k > GRP) break;
+                nt += k;
+                sh.ut[++nb] = nt;
             }
-        }
-        int k = j0 - i0;
-        // pass A: weight L (spot: kind 0, facula: kind 1; quiet: kind 0)
-        auto ca = coef3<T>(Lw, phi, Dw);
-        bool okA = fir_insert(sh, have && regular, fir_key(kind, row, k), ca.a0, ca.a1, ca.bb, lane);
-        bool okB = true;
-        if constexpr (MODE == MODE_PHASE) {
-            // pass B: facula (1 + LB) L weight
-            auto cb = coef3<T>(W2w, phi, Dw);
-            okB = fir_insert(sh, have && regular && kind == 1, fir_key(2, row, k), cb.a0, cb.a1, cb.bb, lane);
-        }
-        int parts = 0;
-        if (have) {
-            if (!regular) parts = 3;
-            else parts = (okA ? 0 : 1) | (okB ? 0 : 2);
-        }
-        if (parts) {
-            int slot = atomicAdd(&sh.nexc, 1);
-            Exc<T> x;
-            x.i0 = i0;
-            x.row = row;
-            x.kind = kind;
-            x.parts = parts;
-            x.zero_v = zero_v;
-            x.plain_t = plain_t;
-            x.phi = phi;
-            x.dlt = Dw;
-            x.L = Lw;
-            x.w2 = W2w;
-            x.temp = (MODE == MODE_PHASE && (!plain_t || solar)) ? pt[cell] : 0.0;
-            sh.exc[slot] = x;
+            sh.nb = nb;
+            sh.ntask = nt;
         }
         __syncthreads();
-        if (sh.nexc > FIR_EXC - FIR_THREADS) {
-            flush();
-            __syncthreads();
-            if (tid == 0) sh.nexc = 0;
-        }
-        __syncthreads();
-    }
-    flush();
-    __syncthreads();
-    // compact the occupied hash slots (ballot prefix per warp, warps in order)
-    {
-        constexpr int PER = FIR_HASH / FIR_THREADS;   // slots per thread
-        static_assert(FIR_HASH % FIR_THREADS == 0, "hash size");
-        int base_slot = tid * PER;
-        int cnt = 0;
-#pragma unroll
-        for (int q = 0; q < PER; ++q) cnt += (sh.key[base_slot + q] != 0xffffffffu);
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        __shared__ int wsum[FIR_THREADS / 32];
-        if (lane == 31) wsum[tid >> 5] = incl;
-        __syncthreads();
-        int woff = 0;
-        for (int w = 0; w < (tid >> 5); ++w) woff += wsum[w];
-        int pos = woff + incl - cnt;
-#pragma unroll
-        for (int q = 0; q < PER; ++q)
-            if (sh.key[base_slot + q] != 0xffffffffu) sh.grp[pos++] = base_slot + q;
-        if (tid == FIR_THREADS - 1) sh.ngrp = woff + incl;
-    }
-    __syncthreads();
-    for (int e = tid; e < sh.ngrp; e += FIR_THREADS) {
-        int h = sh.grp[e];
-        sh.gcoef[e][0] = __ll2float_rn((long long)sh.val[h][0]) * (1.0f / FIX_A_F);
-        sh.gcoef[e][1] = __ll2float_rn((long long)sh.val[h][1]) * (1.0f / FIX_A_F);
-        sh.gcoef[e][2] = __ll2float_rn((long long)sh.val[h][2]) * (1.0f / FIX_B_F);
-    }
-    __syncthreads();
-    // --- apply the collapsed groups ---------------------------------------------
-    int ng = sh.ngrp;
-    for (int e = 0; e < ng; ++e) {
-        int h = sh.grp[e];
-        unsigned key = sh.key[h];
-        int kind = (int)(key >> 28);
-        int row = (int)((key >> 16) & 0xfff);
-        int k = (int)(key & 0xffff) - 16384;
-        T A0, A1, B;
-        if constexpr (sizeof(T) == 4) {
-            A0 = sh.gcoef[e][0];
-            A1 = sh.gcoef[e][1];
-            B = sh.gcoef[e][2];
-        } else {
-            A0 = __ll2double_rn((long long)sh.val[h][0]) * (1.0 / (double)FIX_A_F);
-            A1 = __ll2double_rn((long long)sh.val[h][1]) * (1.0 / (double)FIX_A_F);
-            B = __ll2double_rn((long long)sh.val[h][2]) * (1.0 / (double)FIX_B_F);
-        }
-        long long off = (long long)row * n;
-        // pixels whose owner j - k lies in [0, n_eff - 2]
-        const int jlo = max(j0, k);
-        const int jhi = min(j0 + t_eff - 1, n_eff - 2 + k);
-#pragma unroll
-        for (int q = 0; q < FIR_PIX; ++q) {
-            int dj = tid + q * FIR_THREADS;
-            int j = j0 + dj;
-            if (j < jlo || j > jhi) continue;
-            long long i = (long long)j - k;
-            T c0 = A0 - B * (T)dj;
-            T c1 = A1 + B * (T)dj;
-            auto two = [&](int ci) -> T {
-                const T *rowp = reinterpret_cast<const T *>(cubes.c[ci]) + off;
-                return c0 * rowp[i] + c1 * rowp[i + 1];
-            };
-            if constexpr (MODE == MODE_QUIET) {
-                acc[0][q].add(two(0));
+        const int nb = sh.nb, ntask = sh.ntask;
+        // --- groups and wrap ranges of every shift value of the batch -----------------
+        for (int k = tid; k < ntask; k += FIR_THREADS) {
+            int ui = 0, hi = nb - 1;
+            while (ui < hi) {   // unit of task k
+                int mid = (ui + hi + 1) >> 1;
+                if (sh.ut[mid] <= k) ui = mid; else hi = mid - 1;
+            }
+            const FirUnit d = sh.bud[ui];
+            const FirSeg g = segs[d.seg];
+            const int m = d.ma + (k - sh.ut[ui]);
+            int lowA, lowB, highA, highB;
+            if (m == g.m_lo) {
+                lowA = lowB = g.start;
             } else {
-                if (kind == 0) {              // spot, weight L
-                    acc[0][q].add(two(0));
-                    acc[1][q].add(two(1));
-                    acc[2][q].add(two(2));
-                    acc[3][q].add(two(3));
-                } else if (kind == 1) {       // facula, weight L
-                    acc[0][q].add(two(0));
-                    acc[6][q].add(two(5));
-                } else {                      // facula, weight (1 + LB) L
-                    acc[4][q].add(two(1));
-                    acc[5][q].add(two(4));
+                lowA = fir_lower_bound(dl, g.start, g.end, Xa, m);
+                lowB = fir_lower_bound(dl, g.start, g.end, Xb, m);
+            }
+            if (m == g.m_hi) {
+                highA = highB = g.end;
+            } else {
+                highA = fir_lower_bound(dl, g.start, g.end, Xa, m + 1);
+                highB = fir_lower_bound(dl, g.start, g.end, Xb, m + 1);
+            }
+            const int rlo = max(lowA, lowB), rhi = min(highA, highB);
+            FirGrp<T> gr;
+            gr.m = m;
+            gr.ok = rhi > rlo;
+            gr.a0 = gr.a1 = gr.b = gr.a0w = gr.a1w = gr.bw = (T)0;
+            if (gr.ok) {
+                const double *P = A.pre + (long long)l * A.pre_stride + g.cls;
+                const long long pc = A.pre_comp;
+                const double SL = P[rhi] - P[rlo];
+                const double SLd = P[pc + rhi] - P[pc + rlo];
+                const double SLo = P[2 * pc + rhi] - P[2 * pc + rlo];
+                const double A1 = (double)j0 * SLd - SLo - (double)m * SL;
+                gr.a1 = (T)A1;
+                gr.a0 = (T)(SL - A1);
+                gr.b = (T)SLd;
+                if (MODE == MODE_PHASE && g.cls == CLS_FAC) {
+                    const double Wt = P[3 * pc + rhi] - P[3 * pc + rlo];
+                    const double Wd = P[4 * pc + rhi] - P[4 * pc + rlo];
+                    const double Wo = P[5 * pc + rhi] - P[5 * pc + rlo];
+                    const double W1 = (double)j0 * Wd - Wo - (double)m * Wt;
+                    gr.a1w = (T)W1;
+                    gr.a0w = (T)(Wt - W1);
+                    gr.bw = (T)Wd;
                 }
             }
+            sh.grp[k] = gr;
+            int wl = 0, wc = 0;
+            if (m > g.m_lo) {   // cells whose floor changes across boundary m inside the tile
+                wl = min(lowA, lowB);
+                wc = max(lowA, lowB) - wl;
+            }
+            sh.wlo[k] = wl;
+            sh.woff[k] = wc;
+        }
+        __syncthreads();
+        int etot;
+        {   // exclusive offsets of the wrap counts (GRP / FIR_THREADS entries per thread)
+            constexpr int PER = GRP / FIR_THREADS;
+            const int a = tid * PER;
+            int loc = 0;
+#pragma unroll
+            for (int q = 0; q < PER; ++q)
+                if (a + q < ntask) loc += sh.woff[a + q];
+            int ex = block_excl_scan_int(loc, sh.wsum, etot);
+#pragma unroll
+            for (int q = 0; q < PER; ++q)
+                if (a + q < ntask) {
+                    int v = sh.woff[a + q];
+                    sh.woff[a + q] = ex;
+                    ex += v;
+                }
+            if (tid == 0) sh.woff[ntask] = etot;
+        }
+        __syncthreads();
+        fill_exc(0, min(etot, EXC), 0, ntask);
+        __syncthreads();
+        // --- units of the batch: wait for the rows, apply groups and wrap cells --------
+        for (int ui = 0; ui < nb; ++ui) {
+            const int u = ub + ui;
+            if (tid == 0 && ui + 1 < nb) {
+                issue(u + 1, sh.bud[ui + 1]);
+                issued = u + 1;
+            }
+            const FirUnit d = sh.bud[ui];
+            const FirSeg g = segs[d.seg];
+            const int cls = g.cls, zv = g.key & 1;
+            if (!mbar_wait_bounded(&sh.bar[u & 1], (unsigned)((u >> 1) & 1))) atomicExch(&sh.fail, 1);
+            __syncthreads();
+            if (sh.fail) {
+                u_fail = u;
+                break;
+            }
+            const T(*W)[FIR_WIN] = sh.win[u & 1];
+            const int wo = d.off - d.w0;   // staged index of source pixel i: i + wo
+            const int t_lo = sh.ut[ui], t_hi = sh.ut[ui + 1];
+            for (int t = t_lo; t < t_hi; ++t) {
+                const FirGrp<T> gr = sh.grp[t];
+                if (!gr.ok) continue;
+                const int m = gr.m;
+                // pixels whose owner j + m lies in [0, n_eff - 2] (v == 0: [0, n_eff - 1])
+                const int jlo = max(j0, -m);
+                const int jhi = zv ? j0 + t_eff - 1 : min(j0 + t_eff - 1, n_eff - 2 - m);
+#pragma unroll
+                for (int q = 0; q < FIR_PIX; ++q) {
+                    const int dj = tid + q * FIR_THREADS;
+                    const int j = j0 + dj;
+                    if (j < jlo || j > jhi) continue;
+                    const int x = j + m + wo;
+                    if (zv) {   // single tap: w == 0
+                        if constexpr (MODE == MODE_QUIET) {
+                            acc[0][q].add(gr.a0 * W[0][x]);
+                        } else if (cls == CLS_SPOT) {
+                            acc[0][q].add(gr.a0 * W[0][x]);
+                            acc[1][q].add(gr.a0 * W[1][x]);
+                            acc[2][q].add(gr.a0 * W[2][x]);
+                            acc[3][q].add(gr.a0 * W[3][x]);
+                        } else {
+                            acc[0][q].add(gr.a0 * W[0][x]);
+                            acc[6][q].add(gr.a0 * W[1][x]);
+                            acc[4][q].add(gr.a0w * W[2][x]);
+                            acc[5][q].add(gr.a0w * W[3][x]);
+                        }
+                        continue;
+                    }
+                    const T fdj = (T)dj;
+                    const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
+                    if constexpr (MODE == MODE_QUIET) {
+                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                    } else if (cls == CLS_SPOT) {
+                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                        acc[1][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
+                        acc[2][q].add(c0 * W[2][x] + c1 * W[2][x + 1]);
+                        acc[3][q].add(c0 * W[3][x] + c1 * W[3][x + 1]);
+                    } else {
+                        const T e0 = gr.a0w - gr.bw * fdj, e1 = gr.a1w + gr.bw * fdj;
+                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                        acc[6][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
+                        acc[4][q].add(e0 * W[2][x] + e1 * W[2][x + 1]);
+                        acc[5][q].add(e0 * W[3][x] + e1 * W[3][x + 1]);
+                    }
+                }
+            }
+            // --- wrap cells of the unit (per-cell lerp from the staged rows) ------------
+            const int e_lo = sh.woff[t_lo], e_hi = sh.woff[t_hi];
+            for (int cb = e_lo; cb < e_hi; cb += EXC) {
+                const int ce = min(e_hi, cb + EXC);
+                int x0 = cb;   // excw index of entry cb
+                if (e_hi > EXC) {   // not all staged: refill this chunk
+                    __syncthreads();
+                    fill_exc(cb, ce, cb, ntask);
+                    __syncthreads();
+                    x0 = 0;
+                }
+                for (int e = cb; e < ce; ++e) {
+                    const FirExcW<T> xc = sh.excw[x0 + (e - cb)];
+#pragma unroll
+                    for (int q = 0; q < FIR_PIX; ++q) {
+                        const int dj = tid + q * FIR_THREADS;
+                        const int j = j0 + dj;
+                        if (j >= n_eff) continue;
+                        T wd = xc.phi + xc.dlt * (T)dj;
+                        int i = xc.i0 + dj;
+                        if (wd >= (T)1) { wd -= (T)1; i += 1; }
+                        else if (wd < (T)0) { wd += (T)1; i -= 1; }
+                        if (i < 0 || i > n_eff - 2) continue;
+                        const int x = i + wo;
+                        // the per-cell owner can differ by one from the segment's
+                        // classification when t lies within rounding of an integer: such
+                        // pixels read the row in global memory instead of the window
+                        const bool staged = (i >= d.w0) && (i + 1 < d.w1);
+                        auto lv = [&](int c) -> T {
+                            T s0, s1;
+                            if (staged) {
+                                s0 = W[c][x];
+                                s1 = W[c][x + 1];
+                            } else {
+                                const T *rowp = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE, cls, c)]) +
+                                                (long long)(g.key >> 1) * n;
+                                s0 = rowp[i];
+                                s1 = rowp[i + 1];
+                            }
+                            return s0 + (s1 - s0) * wd;
+                        };
+                        if constexpr (MODE == MODE_QUIET) {
+                            acc[0][q].add(xc.L * lv(0));
+                        } else if (cls == CLS_SPOT) {
+                            acc[0][q].add(xc.L * lv(0));
+                            acc[1][q].add(xc.L * lv(1));
+                            acc[2][q].add(xc.L * lv(2));
+                            acc[3][q].add(xc.L * lv(3));
+                        } else {
+                            acc[0][q].add(xc.L * lv(0));
+                            acc[6][q].add(xc.L * lv(1));
+                            acc[4][q].add(xc.w2 * lv(2));
+                            acc[5][q].add(xc.w2 * lv(3));
+                        }
+                    }
+                }
+            }
+            __syncthreads();   // unit's buffer free
+        }
+        if (u_fail >= 0) break;
+        ub += nb;
+    }
+    if (u_fail >= 0) {
+        // a copy did not land in time: record it, give the copies still in flight (units
+        // u_fail and u_fail + 1) a bounded wait, and leave without writing
+        if (tid == 0) {
+            atomicExch(A.status, FIR_ST_WAIT);
+            mbar_wait_bounded(&sh.bar[u_fail & 1], (unsigned)((u_fail >> 1) & 1));
+            if (u_fail + 1 < nunit)
+                mbar_wait_bounded(&sh.bar[(u_fail + 1) & 1], (unsigned)(((u_fail + 1) >> 1) & 1));
+        }
+        return;
+    }
+
+    // --- directly evaluated cells (class 2: spots of non-integral temperature, solar faculae)
+    if constexpr (MODE == MODE_PHASE) {
+        const int c_start = cn[0] + cn[1], c_cnt = cn[2];
+        for (int b0 = 0; b0 < c_cnt; b0 += FIR_EXC) {
+            const int nb = min(FIR_EXC, c_cnt - b0);
+            if (tid < nb) {
+                const int cell = A.list_cell[lbase + c_start + b0 + tid];
+                FirExcD<T> x;
+                cell_pos<T>(j0, A.geo, A.geo32, cell, x.i0, x.phi, x.dlt, x.L, x.w2);
+                const CellGeo &gg = A.geo[cell];
+                x.row = gg.row;
+                x.zero_v = gg.zero_v;
+                x.temp = A.temp[lbase + cell];
+                x.kind = bits_is_zero(A.bi[lbase + cell]) ? 0 : 1;
+                sh.excd[tid] = x;
+            }
+            __syncthreads();
+            for (int e = 0; e < nb; ++e) {
+                const FirExcD<T> xc = sh.excd[e];
+                const long long off = (long long)xc.row * n;
+#pragma unroll
+                for (int q = 0; q < FIR_PIX; ++q) {
+                    const int dj = tid + q * FIR_THREADS;
+                    const int j = j0 + dj;
+                    if (j >= n_eff) continue;
+                    long long i;
+                    T w;
+                    if (xc.zero_v) {
+                        i = j;
+                        w = (T)0;
+                    } else {
+                        T wd = xc.phi + xc.dlt * (T)dj;
+                        i = (long long)xc.i0 + dj;
+                        if (wd >= (T)1) { wd -= (T)1; i += 1; }
+                        else if (wd < (T)0) { wd += (T)1; i -= 1; }
+                        if (i < 0 || i > n_eff - 2) continue;
+                        w = wd;
+                    }
+                    auto val = [&](int ci) -> T {
+                        const T *rowp = reinterpret_cast<const T *>(A.cubes.c[ci]) + off;
+                        if (xc.zero_v) return rowp[i];
+                        return rowp[i] + (rowp[i + 1] - rowp[i]) * w;
+                    };
+                    const T L = xc.L;
+                    acc[0][q].add(L * val(0));                 // S (q_sed)
+                    if (xc.kind == 0) {                        // spot of non-integral temperature
+                        T Lq = (T)((double)L * fir_planck_ratio(A.lam[j], xc.temp, (double)(int)xc.temp));
+                        acc[1][q].add(Lq * val(1));            // Qs (q_norm)
+                        acc[2][q].add(Lq * val(2));            // As (spot_norm)
+                        acc[3][q].add(L * val(3));             // Bs (q_norm - spot_norm)
+                    } else {                                   // facula of the solar variant
+                        acc[6][q].add(L * val(5));             // Bf (q_norm - fac_norm)
+                        T w2 = (T)((double)L * fir_planck_ratio(A.lam[j], xc.temp, (double)A.t_norm_fac));
+                        acc[4][q].add(w2 * val(1));            // Qf (q_norm)
+                        acc[5][q].add(w2 * val(4));            // Af (fac_norm)
+                    }
+                }
+            }
+            __syncthreads();
         }
     }
-    // --- outputs ----------------------------------------------------------------
+
+    // --- outputs ----------------------------------------------------------------------
 #pragma unroll
     for (int q = 0; q < FIR_PIX; ++q) {
-        int j = j0 + tid + q * FIR_THREADS;
+        const int j = j0 + tid + q * FIR_THREADS;
         if (j >= n) continue;
-        long long o = (long long)p * out_stride + j;
+        const long long o = (long long)l * A.out_stride + j;
         if (j >= n_eff) {
             out0[o] = (OutT)0;
             if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
@@ -683,7 +1096,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
             // facula terms nearly cancel S, so no FP32 rounding before the subtraction
             F2 S{acc[0][q].s, -acc[0][q].c}, Qs{acc[1][q].s, -acc[1][q].c}, As{acc[2][q].s, -acc[2][q].c};
             F2 Qf{acc[4][q].s, -acc[4][q].c}, Af{acc[5][q].s, -acc[5][q].c};
-            float2 is2 = cubes.spot_sed2[j], fs2 = cubes.fac_sed2[j];
+            float2 is2 = A.cubes.spot_sed2[j], fs2 = A.cubes.fac_sed2[j];
             F2 is{is2.x, is2.y}, fs{fs2.x, fs2.y};
             F2 fl = f2_add(f2_add(S, f2_neg(f2_mul(is, Qs))), f2_neg(f2_mul(fs, Qf)));
             F2 tt = f2_add(f2_add(S, f2_neg(f2_mul(is, As))), f2_neg(f2_mul(fs, Af)));
@@ -694,7 +1107,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(int n, int n_eff, const dou
         } else {
             double S = acc[0][q].get(), Qs = acc[1][q].get(), As = acc[2][q].get(), Bs = acc[3][q].get();
             double Qf = acc[4][q].get(), Af = acc[5][q].get(), Bf = acc[6][q].get();
-            double is = cubes.spot_sed[j], fs = cubes.fac_sed[j];
+            double is = A.cubes.spot_sed[j], fs = A.cubes.fac_sed[j];
             out0[o] = (OutT)(S - is * Qs - fs * Qf);   // flux
             out1[o] = (OutT)(Bs + Bf);                 // bconv
             out2[o] = (OutT)(S - is * As - fs * Af);   // tot
@@ -715,106 +1128,198 @@ __global__ void k_pair_rows(int n, const double *__restrict__ a, const double *_
     pb[i] = make_float2(bh, (float)(b[i] - (double)bh));
 }
 
+namespace {
+
+// workspace layout of the FAST forms
+struct FirLayout {
+    enum {
+        GEO, GEO32, CUBE0, SED2A = CUBE0 + 6, SED2B, K1A, K1B, K2A, K2B, VA, VB, SORT_TMP, LCELL, LDLT, COUNTS,
+        PRE, SEGS, NSEG, NSLOT
+    };
+    size_t off[NSLOT] = {0};
+    size_t total = 0;
+    int seg_cap = 0;
+    long long pre_stride = 0, pre_comp = 0;
+};
+
+FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_lists) {
+    FirLayout L;
+    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    size_t sz[FirLayout::NSLOT] = {0};
+    sz[FirLayout::GEO] = sizeof(CellGeo) * (size_t)gm;
+    sz[FirLayout::GEO32] = sizeof(CellGeo32) * (size_t)gm;
+    for (int q = 0; q < 6; ++q) sz[FirLayout::CUBE0 + q] = (q < ncube) ? tsz * (size_t)n * n_mu : 0;
+    sz[FirLayout::SED2A] = sz[FirLayout::SED2B] = sizeof(float2) * (size_t)n;
+    sz[FirLayout::K1A] = sz[FirLayout::K1B] = sizeof(unsigned long long) * (size_t)gm;
+    sz[FirLayout::K2A] = sz[FirLayout::K2B] = sizeof(unsigned) * (size_t)gm;
+    sz[FirLayout::VA] = sz[FirLayout::VB] = sizeof(int) * (size_t)gm;
+    sz[FirLayout::SORT_TMP] = soapgb::fir_sort_temp_bytes(gm);
+    sz[FirLayout::LCELL] = sizeof(int) * (size_t)gm * n_lists;
+    sz[FirLayout::LDLT] = sizeof(double) * (size_t)gm * n_lists;
+    sz[FirLayout::COUNTS] = sizeof(int) * 4 * (size_t)n_lists;
+    L.pre_stride = gm + 2;
+    L.pre_comp = L.pre_stride * n_lists;
+    sz[FirLayout::PRE] = sizeof(double) * 6 * (size_t)L.pre_comp;
+    L.seg_cap = 2 * n_mu;
+    sz[FirLayout::SEGS] = sizeof(int2) * 2 * (size_t)L.seg_cap * n_lists;
+    sz[FirLayout::NSEG] = sizeof(int) * 2 * (size_t)n_lists;
+    size_t t = 0;
+    for (int s = 0; s < FirLayout::NSLOT; ++s) {
+        L.off[s] = t;
+        t += align256(sz[s]);
+    }
+    L.total = t;
+    return L;
+}
+
+}  // namespace
+
 FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists) {
     FirPlanSizes p;
     if (form == SOAPGB_PLAIN64) return p;
-    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    size_t cube = align256(tsz * (size_t)n * n_mu);
-    p.bytes = align256(sizeof(CellGeo) * (size_t)gm) + align256(sizeof(CellGeo32) * (size_t)gm) +
-              (phase ? 6 : 1) * cube + 2 * align256(sizeof(float2) * n) +
-              align256(sizeof(int2) * (size_t)gm * (size_t)(n_lists > 0 ? n_lists : 1));
+    p.bytes = fir_layout(form, n, n_mu, gm, phase ? 6 : 1, n_lists > 0 ? n_lists : 1).total;
     return p;
-}
-
-template <typename T, int MODE, typename OutT>
-static int launch_fir(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const FirCubes &fc, const int *cells,
-                      const int *counts, int max_cells, const CellGeo *geo, const CellGeo32 *geo32, int2 *recs,
-                      const double *temp, const double *bi, long long gm, int solar, int t_norm_fac, OutT *o0,
-                      OutT *o1, OutT *o2, long long out_stride, int n_lists) {
-    // records are written over the compacted cell lists, in place (int -> int2
-    // needs its own buffer: recs)
-    {
-        dim3 gr(grid_for(ctx, max_cells, 256), n_lists);
-        k_list_records<<<gr, 256, 0, ctx->stream>>>(n_lists, max_cells, cells, counts, temp, bi, gm, recs);
-        SOAP_LAUNCHED(ctx);
-    }
-    size_t smem = sizeof(FirShared<T>);
-    SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    // tiles cover [0, n): tiles past n_eff only write the zero tail
-    dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
-    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(n, n_eff, lam, fc, recs, counts, max_cells, geo,
-                                                                geo32, temp, bi, gm, solar, t_norm_fac, o0, o1, o2,
-                                                                out_stride);
-    SOAP_LAUNCHED(ctx);
-    return SOAPGB_OK;
 }
 
 static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
                        const double *limb, const double *lb, const int *region, int n_mu, CellGeo *geo,
-                       CellGeo32 *geo32) {
-    double lambda0;
-    SOAP_CUDA(ctx, cudaMemcpyAsync(&lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+                       CellGeo32 *geo32, double *lambda0) {
+    SOAP_CUDA(ctx, cudaMemcpyAsync(lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     k_check_uniform<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, wave, step, ctx->d_status);
     SOAP_LAUNCHED(ctx);
-    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, lambda0, step, geo,
+    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, *lambda0, step, geo,
                                                                 geo32, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+// velocity-ordered cell lists, prefix sums and segments for n_lists lists
+static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm, int n_lists, const double *temp,
+                     const double *bi, int solar) {
+    const CellGeo *geo = (const CellGeo *)(ws + L.off[FirLayout::GEO]);
+    auto *k1a = (unsigned long long *)(ws + L.off[FirLayout::K1A]);
+    auto *k1b = (unsigned long long *)(ws + L.off[FirLayout::K1B]);
+    auto *k2a = (unsigned *)(ws + L.off[FirLayout::K2A]);
+    auto *k2b = (unsigned *)(ws + L.off[FirLayout::K2B]);
+    int *va = (int *)(ws + L.off[FirLayout::VA]);
+    int *vb = (int *)(ws + L.off[FirLayout::VB]);
+    void *tmp = ws + L.off[FirLayout::SORT_TMP];
+    size_t tmp_bytes = soapgb::fir_sort_temp_bytes(gm);
+    int g = grid_for(ctx, gm, 256);
+    k_sort_keys1<<<g, 256, 0, ctx->stream>>>(gm, geo, k1a, va);
+    SOAP_LAUNCHED(ctx);
+    int rc = soapgb::fir_sort_u64(ctx, gm, k1a, k1b, va, vb, tmp, tmp_bytes);
+    if (rc) return rc;
+    k_sort_keys2<<<g, 256, 0, ctx->stream>>>(gm, geo, vb, k2a);
+    SOAP_LAUNCHED(ctx);
+    rc = soapgb::fir_sort_u32(ctx, gm, k2a, k2b, vb, va, 14, tmp, tmp_bytes);   // stable: dlt order kept per bin
+    if (rc) return rc;
+    int *lcell = (int *)(ws + L.off[FirLayout::LCELL]);
+    double *ldlt = (double *)(ws + L.off[FirLayout::LDLT]);
+    int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
+    k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts);
+    SOAP_LAUNCHED(ctx);
+    double *pre = (double *)(ws + L.off[FirLayout::PRE]);
+    int2 *segs = (int2 *)(ws + L.off[FirLayout::SEGS]);
+    int *nseg = (int *)(ws + L.off[FirLayout::NSEG]);
+    k_fir_prefix<<<dim3(n_lists, 2), 256, 0, ctx->stream>>>(gm, counts, lcell, geo, pre, L.pre_stride, L.pre_comp,
+                                                            segs, nseg, L.seg_cap, ctx->d_status);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+template <typename T, int MODE, typename OutT>
+static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
+                        double los, const FirCubes &fc, const double *temp, const double *bi, long long gm, int solar,
+                        int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists) {
+    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
+    FirTileArgs A;
+    A.n = n;
+    A.n_eff = n_eff;
+    A.lam = lam;
+    A.los = los;
+    A.cubes = fc;
+    A.list_cell = (const int *)(ws + L.off[FirLayout::LCELL]);
+    A.list_dlt = (const double *)(ws + L.off[FirLayout::LDLT]);
+    A.counts = (const int *)(ws + L.off[FirLayout::COUNTS]);
+    A.pre = (const double *)(ws + L.off[FirLayout::PRE]);
+    A.pre_stride = L.pre_stride;
+    A.pre_comp = L.pre_comp;
+    A.segs = (const int2 *)(ws + L.off[FirLayout::SEGS]);
+    A.nseg = (const int *)(ws + L.off[FirLayout::NSEG]);
+    A.seg_cap = L.seg_cap;
+    A.geo = (const CellGeo *)(ws + L.off[FirLayout::GEO]);
+    A.geo32 = (const CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
+    A.temp = temp;
+    A.bi = bi;
+    A.gm = gm;
+    A.solar = solar;
+    A.t_norm_fac = t_norm_fac;
+    A.out0 = o0;
+    A.out1 = o1;
+    A.out2 = o2;
+    A.out_stride = out_stride;
+    A.status = ctx->d_status;
+    size_t smem = fir_smem_fixed<T, NC>() + sizeof(FirSeg) * (size_t)(MODE == MODE_PHASE ? 2 : 1) * L.seg_cap;
+    SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // tiles cover [0, n): tiles past n_eff only write the zero tail
+    dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
+    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(A);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
 
 int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, const FirPlanSizes &plan) {
     (void)plan;
-    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    size_t cube_elems = (size_t)a.n * a.n_mu;
-    long long gm = a.max_cells;
-    char *p = scratch;
-    CellGeo *geo = (CellGeo *)p;
-    p += align256(sizeof(CellGeo) * (size_t)gm);
-    CellGeo32 *geo32 = (CellGeo32 *)p;
-    p += align256(sizeof(CellGeo32) * (size_t)gm);
-    void *cube = p;
-    p += align256(tsz * cube_elems);
-    int2 *recs = (int2 *)p;
-    p += align256(sizeof(int2) * (size_t)gm);
-    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo, geo32);
+    if (a.n_mu > FIR_MAX_MU)
+        return set_error(ctx, SOAPGB_ERR_ARG, "collapsed forms support at most %d mu bins (got %d)", FIR_MAX_MU, a.n_mu);
+    const long long gm = a.gm;
+    FirLayout L = fir_layout(form, a.n, a.n_mu, gm, 1, 1);
+    char *ws = scratch;
+    CellGeo *geo = (CellGeo *)(ws + L.off[FirLayout::GEO]);
+    CellGeo32 *geo32 = (CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
+    double lambda0 = 0.0;
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo, geo32,
+                         &lambda0);
     if (rc) return rc;
+    rc = fir_lists(ctx, L, ws, gm, 1, nullptr, nullptr, 0);
+    if (rc) return rc;
+    size_t cube_elems = (size_t)a.n * a.n_mu;
+    void *cube = ws + L.off[FirLayout::CUBE0];
     FirCubes fc{};
+    fc.c[0] = cube;
+    const double los = lambda0 / a.step;
     if (form == SOAPGB_FAST32) {
         k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube);
         SOAP_LAUNCHED(ctx);
-        fc.c[0] = cube;
-        return launch_fir<float, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells,
-                                                     geo, geo32, recs, nullptr, nullptr, gm, 0, 0, a.out, nullptr,
-                                                     nullptr, 0, 1);
+        return launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr,
+                                                       gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
     }
-    fc.c[0] = a.cube;
-    return launch_fir<double, MODE_QUIET, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.n_cells, a.max_cells, geo,
-                                                  geo32, recs, nullptr, nullptr, gm, 0, 0, a.out, nullptr, nullptr, 0,
-                                                  1);
+    k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (double *)cube);
+    SOAP_LAUNCHED(ctx);
+    return launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr, gm,
+                                                    0, 0, a.out, nullptr, nullptr, 0, 1);
 }
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan) {
     (void)plan;
-    size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    int n_mu = a.cubes->n_mu;
-    size_t cube_elems = (size_t)a.n * n_mu;
-    char *p = scratch;
-    CellGeo *geo = (CellGeo *)p;
-    p += align256(sizeof(CellGeo) * (size_t)a.gm);
-    CellGeo32 *geo32 = (CellGeo32 *)p;
-    p += align256(sizeof(CellGeo32) * (size_t)a.gm);
-    int2 *recs = (int2 *)p;
-    p += align256(sizeof(int2) * (size_t)a.gm * (size_t)a.n_phase);
-    void *cb[6];
-    for (int q = 0; q < 6; ++q) {
-        cb[q] = p;
-        p += align256(tsz * cube_elems);
-    }
-    float2 *sed2a = (float2 *)p;
-    p += align256(sizeof(float2) * a.n);
-    float2 *sed2b = (float2 *)p;
-    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32);
+    const int n_mu = a.cubes->n_mu;
+    if (n_mu > FIR_MAX_MU)
+        return set_error(ctx, SOAPGB_ERR_ARG, "collapsed forms support at most %d mu bins (got %d)", FIR_MAX_MU, n_mu);
+    if ((form == SOAPGB_FAST32) != (a.out_f32 != 0))
+        return set_error(ctx, SOAPGB_ERR_ARG, "FP32 deficits go with the FP32 form only");
+    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    const size_t cube_elems = (size_t)a.n * n_mu;
+    FirLayout L = fir_layout(form, a.n, n_mu, a.gm, 6, a.n_phase);
+    char *ws = scratch;
+    CellGeo *geo = (CellGeo *)(ws + L.off[FirLayout::GEO]);
+    CellGeo32 *geo32 = (CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
+    double lambda0 = 0.0;
+    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32,
+                         &lambda0);
+    if (rc) return rc;
+    rc = fir_lists(ctx, L, ws, a.gm, a.n_phase, a.temp, a.bi, a.act->solar);
     if (rc) return rc;
     const soapgb_cubes &c = *a.cubes;
     // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
@@ -822,30 +1327,30 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
     FirCubes fc{};
     for (int q = 0; q < 6; ++q) {
-        if (form == SOAPGB_FAST32)
-            k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)cb[q]);
+        void *dst = ws + L.off[FirLayout::CUBE0 + q];
+        if (tsz == 4)
+            k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst);
         else
-            k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)cb[q]);
+            k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst);
         SOAP_LAUNCHED(ctx);
-        fc.c[q] = cb[q];
+        fc.c[q] = dst;
     }
     fc.spot_sed = c.spot_sed;
     fc.fac_sed = c.fac_sed;
-    int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
+    const int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
+    const double los = lambda0 / a.step;
     if (form == SOAPGB_FAST32) {
+        float2 *sed2a = (float2 *)(ws + L.off[FirLayout::SED2A]);
+        float2 *sed2b = (float2 *)(ws + L.off[FirLayout::SED2B]);
         k_pair_rows<<<grid_for(ctx, a.n, 256), 256, 0, ctx->stream>>>(a.n, c.spot_sed, c.fac_sed, sed2a, sed2b);
         SOAP_LAUNCHED(ctx);
         fc.spot_sed2 = sed2a;
         fc.fac_sed2 = sed2b;
-        if (!a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP32 form writes FP32 deficits");
-        return launch_fir<float, MODE_PHASE, float>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells,
-                                                    geo, geo32, recs, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
-                                                    (float *)a.flux, (float *)a.bconv, (float *)a.tot, a.out_stride,
-                                                    a.n_phase);
+        return launch_tiles<float, MODE_PHASE, float>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
+                                                      a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
+                                                      a.n_phase);
     }
-    if (a.out_f32) return set_error(ctx, SOAPGB_ERR_ARG, "FP64 form writes FP64 deficits");
-    return launch_fir<double, MODE_PHASE, double>(ctx, a.n, a.n_eff, a.wave, fc, a.cells, a.counts, a.max_cells, geo,
-                                                  geo32, recs, a.temp, a.bi, a.gm, a.act->solar, t_norm_fac,
-                                                  (double *)a.flux,
-                                                  (double *)a.bconv, (double *)a.tot, a.out_stride, a.n_phase);
+    return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
+                                                    a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
+                                                    a.n_phase);
 }

@@ -6,8 +6,9 @@ struct FirPlanSizes {
     size_t bytes = 0;
 };
 
-// workspace of the FAST forms: per-cell geometry for the G*G grid plus typed cube
-// copies (one cube for the quiet disk, six for the phase integration)
+// workspace of the FAST forms: per-cell geometry for the G*G grid, the velocity order
+// of the cells, per-list cell lists / prefix sums / segments and typed cube copies
+// (one cube for the quiet disk, six for the phase integration)
 FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists);
 
 struct FirQuietArgs {
@@ -15,9 +16,7 @@ struct FirQuietArgs {
     const double *wave;
     const double *cube;     // n_mu x n (FP64, device)
     int n_mu;
-    int max_cells;
-    const int *n_cells;     // device: number of visible cells
-    const int *cells;       // visible cells, map order
+    long long gm;           // G*G
     const double *delta, *limb;
     const int *region;
     double step;
@@ -31,9 +30,6 @@ struct FirPhaseArgs {
     const double *wave;
     const soapgb_cubes *cubes;  // device pointers, FP64
     int n_phase;
-    int max_cells;
-    const int *cells;           // n_phase x max_cells active cells, map order
-    const int *counts;          // n_phase
     const double *temp, *bi;    // n_phase x G*G
     const double *delta, *limb, *lb;
     const int *region;
@@ -46,3 +42,12 @@ struct FirPhaseArgs {
 };
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);
+
+namespace soapgb {
+// radix sorts of (key, cell) pairs on the context's stream (fir_sort.cu)
+size_t fir_sort_temp_bytes(long long gm);
+int fir_sort_u64(soapgb_ctx *ctx, long long gm, const unsigned long long *keys_in, unsigned long long *keys_out,
+                 const int *vals_in, int *vals_out, void *temp, size_t temp_bytes);
+int fir_sort_u32(soapgb_ctx *ctx, long long gm, const unsigned *keys_in, unsigned *keys_out, const int *vals_in,
+                 int *vals_out, int end_bit, void *temp, size_t temp_bytes);
+}  // namespace soapgb

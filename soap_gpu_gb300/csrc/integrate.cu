@@ -171,9 +171,9 @@ int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *
     if ((form == SOAPGB_FAST32) != (out_f32 != 0))
         return set_error(ctx, SOAPGB_ERR_ARG, "integration: FP32 outputs go with the FP32 form only");
     long long gm = (long long)grid * grid;
-    int rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
-    if (rc) return rc;
     if (form == SOAPGB_PLAIN64) {
+        int rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
+        if (rc) return rc;
         dim3 g(grid_for(ctx, n, 256), n_phase);
         k_phase_plain64<<<g, 256, 0, ctx->stream>>>(
             n, n_eff, d_wave, dc.q_norm, dc.q_sed, dc.spot_norm, dc.fac_norm, dc.spot_sed, dc.fac_sed, (int)gm,
@@ -189,9 +189,6 @@ int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *
     a.wave = d_wave;
     a.cubes = &dc;
     a.n_phase = n_phase;
-    a.max_cells = (int)gm;
-    a.cells = d_cells;
-    a.counts = d_counts;
     a.temp = d_temp;
     a.bi = d_bi;
     a.delta = dm.delta;
