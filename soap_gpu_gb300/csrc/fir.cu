@@ -164,8 +164,9 @@ __device__ __forceinline__ int fir_class(const CellGeo &g, const double *bi, con
 __global__ void __launch_bounds__(1024) k_fir_lists(long long gm, const int *__restrict__ order,
                                                     const CellGeo *__restrict__ geo, const double *__restrict__ temp,
                                                     const double *__restrict__ bi, int solar, int *list_cell,
-                                                    double *list_dlt, int *counts) {
+                                                    double *list_dlt, int *counts, int only_flagged) {
     const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (only_flagged && counts[4 * l + 3] == 0) return;   // list already built by k_fir_plists
     const int nw = blockDim.x >> 5;
     const long long mbase = (long long)l * gm;
     __shared__ int cnt[3];
@@ -225,6 +226,78 @@ __global__ void __launch_bounds__(1024) k_fir_lists(long long gm, const int *__r
             base[tid] += s;
         }
         __syncthreads();
+    }
+}
+
+// inverse of the cell order: rank[order[r]] = r
+__global__ void k_fir_rank(long long gm, const int *__restrict__ order, int *rank) {
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < gm) rank[order[r]] = (int)r;
+}
+
+// Phase lists of at most FIR_PLIST_CAP active cells (the usual case): one block per
+// phase scans the type map (coalesced), collects (class, rank) keys of the active cells
+// in shared memory and sorts them (bitonic), which gives the same lists as k_fir_lists
+// without visiting every visible cell per phase.  Longer lists are flagged
+// (counts[4l + 3] = 1) and built by k_fir_lists.
+constexpr int FIR_PLIST_CAP = 4096;
+
+__global__ void __launch_bounds__(512) k_fir_plists(long long gm, const int *__restrict__ order,
+                                                   const int *__restrict__ rank, const CellGeo *__restrict__ geo,
+                                                   const double *__restrict__ temp, const double *__restrict__ bi,
+                                                   int solar, int *list_cell, double *list_dlt, int *counts) {
+    __shared__ unsigned keys[FIR_PLIST_CAP];
+    __shared__ int cnt[4];
+    const int l = blockIdx.x, tid = threadIdx.x;
+    const long long mbase = (long long)l * gm;
+    if (tid < 4) cnt[tid] = 0;
+    __syncthreads();
+    for (long long k = tid; k < gm; k += blockDim.x) {
+        const double b = bi[mbase + k];
+        if (!(b >= -0.5 && b <= 1.5)) continue;
+        const int c = fir_class(geo[k], bi, temp, mbase + k, solar);
+        if (c < 0) continue;
+        atomicAdd(&cnt[c + 1], 1);
+        const int pos = atomicAdd(&cnt[0], 1);
+        if (pos < FIR_PLIST_CAP) keys[pos] = ((unsigned)c << 24) | (unsigned)rank[k];
+    }
+    __syncthreads();
+    const int n = cnt[0];
+    if (n > FIR_PLIST_CAP) {
+        if (tid == 0) counts[4 * l + 3] = 1;
+        return;
+    }
+    int np = 1;
+    while (np < n) np <<= 1;
+    for (int i = n + tid; i < np; i += blockDim.x) keys[i] = 0xffffffffu;
+    __syncthreads();
+    for (int k = 2; k <= np; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < np; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned a = keys[i], b2 = keys[ixj];
+                    const bool up = ((i & k) == 0);
+                    if ((a > b2) == up) {
+                        keys[i] = b2;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < n; i += blockDim.x) {
+        const int cell = order[keys[i] & 0xffffffu];
+        list_cell[mbase + i] = cell;
+        list_dlt[mbase + i] = geo[cell].dlt;
+    }
+    if (tid == 0) {
+        int *o = counts + 4 * l;
+        o[0] = cnt[1];
+        o[1] = cnt[2];
+        o[2] = cnt[3];
+        o[3] = 0;
     }
 }
 
@@ -554,6 +627,13 @@ struct FirCaps {
 };
 constexpr int FIR_BATCH_U = 128;   // work units per batch
 
+// lists of at most this many (class 0 + 1) entries have their slopes staged in shared
+// memory for the binary searches
+template <typename T>
+struct FirListCap {
+    static constexpr int N = (sizeof(T) == 4) ? 4096 : 1024;
+};
+
 template <typename T, int NC>
 struct FirSmem {
     // staged windows; the direct cells' buffer reuses this space once all copies landed
@@ -570,6 +650,7 @@ struct FirSmem {
     FirExcW<T> excw[FirCaps<T>::EXC];      // wrap cells of the batch
     int wsum[FIR_THREADS / 32];
     int nunit, fail, nb, ntask;
+    double sdl[FirListCap<T>::N];          // the list's slopes (short lists)
     // followed by FirSeg seg[] (dynamic, 16-byte aligned)
 };
 
@@ -704,6 +785,14 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
     }
     __syncthreads();
     const int nunit = sh.nunit;
+    // slopes of a short list in shared memory: the searches then cost no global latency
+    const int n01 = cn[0] + ((MODE == MODE_PHASE) ? cn[1] : 0);
+    const double *sl = dl;
+    if (n01 <= FirListCap<T>::N) {
+        for (int q = tid; q < n01; q += FIR_THREADS) sh.sdl[q] = dl[q];
+        sl = sh.sdl;
+        __syncthreads();
+    }
 
     // accumulators: QUIET [0]; PHASE: S, Qs, As, Bs, Qf, Af, Bf
     constexpr int NACC = (MODE == MODE_QUIET) ? 1 : 7;
@@ -811,14 +900,14 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
             if (m == g.m_lo) {
                 lowA = lowB = g.start;
             } else {
-                lowA = fir_lower_bound(dl, g.start, g.end, Xa, m);
-                lowB = fir_lower_bound(dl, g.start, g.end, Xb, m);
+                lowA = fir_lower_bound(sl, g.start, g.end, Xa, m);
+                lowB = fir_lower_bound(sl, g.start, g.end, Xb, m);
             }
             if (m == g.m_hi) {
                 highA = highB = g.end;
             } else {
-                highA = fir_lower_bound(dl, g.start, g.end, Xa, m + 1);
-                highB = fir_lower_bound(dl, g.start, g.end, Xb, m + 1);
+                highA = fir_lower_bound(sl, g.start, g.end, Xa, m + 1);
+                highB = fir_lower_bound(sl, g.start, g.end, Xb, m + 1);
             }
             const int rlo = max(lowA, lowB), rhi = min(highA, highB);
             FirGrp<T> gr;
@@ -1218,8 +1307,19 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
     int *lcell = (int *)(ws + L.off[FirLayout::LCELL]);
     double *ldlt = (double *)(ws + L.off[FirLayout::LDLT]);
     int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
-    k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts);
-    SOAP_LAUNCHED(ctx);
+    if (bi && gm < (1LL << 24)) {
+        // phases: short lists by a per-phase sort of the active cells, the rest by a scan
+        int *rank = vb;   // free after the second sort
+        k_fir_rank<<<g, 256, 0, ctx->stream>>>(gm, va, rank);
+        SOAP_LAUNCHED(ctx);
+        k_fir_plists<<<n_lists, 512, 0, ctx->stream>>>(gm, va, rank, geo, temp, bi, solar, lcell, ldlt, counts);
+        SOAP_LAUNCHED(ctx);
+        k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 1);
+        SOAP_LAUNCHED(ctx);
+    } else {
+        k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 0);
+        SOAP_LAUNCHED(ctx);
+    }
     double *pre = (double *)(ws + L.off[FirLayout::PRE]);
     int2 *segs = (int2 *)(ws + L.off[FirLayout::SEGS]);
     int *nseg = (int *)(ws + L.off[FirLayout::NSEG]);

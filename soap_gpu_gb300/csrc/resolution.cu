@@ -340,74 +340,366 @@ __global__ void k_mm32_init(int n_spec, double sentinel, unsigned *mm32, unsigne
     }
 }
 
-// pass 1: FP32 extrema per spectrum and per block
-__global__ void __launch_bounds__(256) k_minmax32(int n, int n_eff, const float *__restrict__ spec,
-                                                  long long spec_stride, const float *__restrict__ b32a,
-                                                  const float *__restrict__ b32b, const float *__restrict__ c32a,
-                                                  const float *__restrict__ c32b, int b_every,
-                                                  const float *__restrict__ conv, long long conv_stride,
-                                                  unsigned *mm32, float *blk) {
-    int s = blockIdx.y;
-    bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
-    const float *sp = spec + (long long)s * spec_stride;
-    const float *bs = use_b ? b32b : b32a;
-    const float *cbs = use_b ? c32b : c32a;
-    const float *cv = conv + (long long)s * conv_stride;
-    float mn = INFINITY, mx = -INFINITY, ma = 0.f, mc = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float b = bs[i], x = sp[i];
-        float a = b - x;
-        mn = fminf(mn, a);
-        ma = fmaxf(ma, fabsf(b) + fabsf(x));
-        if (i < n_eff) {
-            float cb = cbs[i], cd = cv[i];
-            float c = cb + cd;
-            if (c != 0.f) mx = fmaxf(mx, c);
-            mc = fmaxf(mc, fabsf(cb) + fabsf(cd));
+// per-pixel tap constants of the FP32 convolution: weight(d) = 2^(d^2 c2 + lk) with
+// c2 = -step_exp^2 / (2 s^2) log2(e), lk = log2(step_mult / (s sqrt(2 pi))) (FP64, then
+// rounded once); live = inside the reference's convolution interior; rblk[b] = largest
+// significant reach (weight >= e^-cut of the central one) over block b's pixels
+__global__ void k_conv32_params(int n, int n_eff, const double *__restrict__ lam, double sigma_v, int wid, int halo,
+                                double step_mult, double step_exp, double cut, float *c2, float *lk, int *live,
+                                int *rblk) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    bool lv = (i > wid) && (i + wid < n - 1);
+    double a = 0.0, l = -200.0;
+    if (lv) {
+        double sig = soap_delta_lambda(sigma_v, lam[i]);
+        double cq = step_exp * step_exp / (2.0 * sig * sig);
+        a = -cq * 1.4426950408889634;   // log2(e)
+        l = log2(step_mult / (sig * sqrt(2. * SOAP_PI)));
+        int r = min((int)floor(sqrt(cut / cq)) + 1, halo);
+        atomicMax(&rblk[i / FC_TILE], r);
+    }
+    c2[i] = (float)a;
+    lk[i] = (float)l;
+    live[i] = lv ? 1 : 0;
+}
+
+__device__ __forceinline__ float soap_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// --- FAST32 convolution, shared pieces -------------------------------------------------
+// taps of 4 consecutive pixels ib .. ib+3 over SB staged spectra: xrow(q) + x0 is the
+// staged value of source pixel ib - R - sh (x0 + 4 k is 16-byte aligned), R the block's
+// reach, sh in [0, 3] the alignment shift; every weight one FFMA + one ex2
+template <int SB>
+__device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, int R, int sh, int wid,
+                                            const float (&c2)[FC_PIX], const float (&lk)[FC_PIX],
+                                            float (&acc)[SB][FC_PIX]) {
+    // |d| <= R + 6 over the thread's taps: mask only if that can leave [-wid, wid - 2]
+    const bool mask = (R + 8 > wid);
+    const int nch = (3 + 2 * R + sh) / 4 + 1;
+    float dd[FC_PIX];
+#pragma unroll
+    for (int p = 0; p < FC_PIX; ++p) dd[p] = (float)(-R - sh - p);
+    for (int ch = 0; ch < nch; ++ch) {
+        float w[4][FC_PIX];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int p = 0; p < FC_PIX; ++p) {
+                const float d = dd[p] + (float)k;
+                float wv = soap_ex2(fmaf(d * d, c2[p], lk[p]));
+                if (mask && (d < (float)-wid || d > (float)(wid - 2))) wv = 0.f;
+                w[k][p] = wv;
+            }
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) dd[p] += 4.f;
+        const int li = x0 + 4 * ch;
+#pragma unroll
+        for (int q = 0; q < SB; ++q) {
+            const float4 x4 = *reinterpret_cast<const float4 *>(&xs[q * win + li]);
+#pragma unroll
+            for (int p = 0; p < FC_PIX; ++p) {
+                float a = acc[q][p];
+                a = fmaf(w[0][p], x4.x, a);
+                a = fmaf(w[1][p], x4.y, a);
+                a = fmaf(w[2][p], x4.z, a);
+                a = fmaf(w[3][p], x4.w, a);
+                acc[q][p] = a;
+            }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
-        mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+}
+
+// conv outputs of the SB spectra and their extrema: per block of 1024 pixels and
+// spectrum, the FP32 extrema of A = base - spec (over [0, n)) and C = conv(1 - base) +
+// conv(spec) (over [0, n_eff), C != 0) and the magnitudes that bound their rounding
+// (blk, order-preserving atomics into mm32).  xs + xi(i) is the staged spectrum value
+// of pixel i.  Ends with a block barrier.
+template <int SB>
+__device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff, int i0, int ib, int n, int n_eff,
+                                              int s0, int nsb, const bool (&lv)[FC_PIX],
+                                              const float (&acc)[SB][FC_PIX], const float *__restrict__ b32a,
+                                              const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                              const float *__restrict__ c32b, int b_every, float *__restrict__ conv,
+                                              long long conv_stride, unsigned *mm32, float *blk, int nbx,
+                                              float (*red)[4][FC_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < SB; ++q) {
+        float mn = INFINITY, mx = -INFINITY, ma = 0.f, mc = 0.f;
+        if (q < nsb) {
+            const int s = s0 + q;
+            const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+            const float *bs = use_b ? b32b : b32a;
+            const float *cbs = use_b ? c32b : c32a;
+            float *cp = conv + (long long)s * conv_stride;
+#pragma unroll
+            for (int p = 0; p < FC_PIX; ++p) {
+                const int i = ib + p;
+                if (i < n) {
+                    const float b = bs[i], x = xs[q * win + (i - i0) + xoff];
+                    mn = fminf(mn, b - x);
+                    ma = fmaxf(ma, fabsf(b) + fabsf(x));
+                }
+                if (i < n_eff) {
+                    const float cd = lv[p] ? acc[q][p] : 0.f;
+                    cp[i] = cd;
+                    const float cb = cbs[i];
+                    const float c = cb + cd;
+                    if (c != 0.f) mx = fmaxf(mx, c);
+                    mc = fmaxf(mc, fabsf(cb) + fabsf(cd));
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+            mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+        }
+        if (lane == 0) {
+            red[q][0][warp] = mn;
+            red[q][1][warp] = mx;
+            red[q][2][warp] = ma;
+            red[q][3][warp] = mc;
+        }
     }
-    __shared__ float sh[4][8];
-    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { sh[0][w] = mn; sh[1][w] = mx; sh[2][w] = ma; sh[3][w] = mc; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
-            mn = fminf(mn, sh[0][q]); mx = fmaxf(mx, sh[1][q]); ma = fmaxf(ma, sh[2][q]); mc = fmaxf(mc, sh[3][q]);
+    if (threadIdx.x < nsb) {
+        const int q = threadIdx.x, s = s0 + q;
+        float mn = red[q][0][0], mx = red[q][1][0], ma = red[q][2][0], mc = red[q][3][0];
+        for (int w = 1; w < FC_THREADS / 32; ++w) {
+            mn = fminf(mn, red[q][0][w]);
+            mx = fmaxf(mx, red[q][1][w]);
+            ma = fmaxf(ma, red[q][2][w]);
+            mc = fmaxf(mc, red[q][3][w]);
         }
-        float *bk = blk + ((long long)s * gridDim.x + blockIdx.x) * 2;
+        float *bk = blk + ((long long)s * nbx + blockIdx.x) * 2;
         bk[0] = mn;
         bk[1] = mx;
-        atomicMin(&mm32[4 * s + 0], soap_ord32(mn));
+        if (mn < INFINITY) atomicMin(&mm32[4 * s + 0], soap_ord32(mn));
         if (mx > -INFINITY) atomicMax(&mm32[4 * s + 1], soap_ord32(mx));
         atomicMax(&mm32[4 * s + 2], soap_ord32(ma));
         atomicMax(&mm32[4 * s + 3], soap_ord32(mc));
     }
+    __syncthreads();
 }
 
-// pass 2: exact FP64 values of the candidates of the blocks that can hold an extremum
-__global__ void __launch_bounds__(256) k_refine64(int n, int n_eff, const float *__restrict__ spec,
-                                                  long long spec_stride, const double *__restrict__ ba,
-                                                  const double *__restrict__ bb, const double *__restrict__ cba,
-                                                  const double *__restrict__ cbb, const float *__restrict__ b32a,
-                                                  const float *__restrict__ b32b, const float *__restrict__ c32a,
-                                                  const float *__restrict__ c32b, int b_every,
-                                                  const float *__restrict__ conv, long long conv_stride,
-                                                  const unsigned *__restrict__ mm32, const float *__restrict__ blk,
-                                                  unsigned long long *mm64) {
-    int s = blockIdx.y;
-    float mnA = soap_dec32(mm32[4 * s + 0]), mxC = soap_dec32(mm32[4 * s + 1]);
-    float tolA = ldexpf(soap_dec32(mm32[4 * s + 2]), -21), tolC = ldexpf(soap_dec32(mm32[4 * s + 3]), -21);
+// FAST32 convolution of the spectra, fused with the first min/max pass (plain loads:
+// spectra rows that are not 16-byte aligned).  Block = 256 threads x 4 consecutive
+// pixels, SB spectra staged in shared memory; every thread walks the taps e in
+// [ib - R, ib + 3 + R] (R = the block's reach; the start moved down by up to 3 to a
+// 16-byte boundary) four at a time with 16-byte shared loads (conflict-free), one FFMA
+// + one ex2 per weight.  Taps beyond a pixel's own reach carry weights below e^-cut of
+// its central one; where the thread's taps could leave the reference's window
+// [-wid, wid - 2], weights are masked.  Grid (ceil(n / 1024), spectra / SB): blocks
+// past n_eff only scan A.
+template <int SB>
+__global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const float *__restrict__ c2a,
+                                                        const float *__restrict__ lka, const int *__restrict__ livea,
+                                                        const int *__restrict__ rblk, int wid,
+                                                        const float *__restrict__ spec, long long spec_stride,
+                                                        int n_spec, int halo, const float *__restrict__ b32a,
+                                                        const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                                        const float *__restrict__ c32b, int b_every,
+                                                        float *__restrict__ conv, long long conv_stride,
+                                                        unsigned *mm32, float *blk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *xs = reinterpret_cast<float *>(smem_raw);
+    __shared__ float red[SB][4][FC_THREADS / 32];
+    const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
+    const int i0 = blockIdx.x * FC_TILE;
+    const int s0 = blockIdx.y * SB;
+    const int nsb = min(SB, n_spec - s0);
+    for (int q = 0; q < SB; ++q) {
+        const float *sp = spec + (long long)(s0 + q) * spec_stride;
+        for (int t = threadIdx.x; t < win; t += FC_THREADS) {
+            const int m = i0 - halo + t;
+            xs[q * win + t] = (q < nsb && m >= 0 && m < n) ? sp[m] : 0.f;
+        }
+    }
+    __syncthreads();
+    const int ib = i0 + threadIdx.x * FC_PIX;
+    float acc[SB][FC_PIX];
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) acc[q][p] = 0.f;
+    float c2[FC_PIX], lk[FC_PIX];
+    bool lv[FC_PIX];
+#pragma unroll
+    for (int p = 0; p < FC_PIX; ++p) {
+        const int i = ib + p;
+        lv[p] = (i < n_eff) && livea[i];
+        c2[p] = lv[p] ? c2a[i] : 0.f;
+        lk[p] = lv[p] ? lka[i] : -200.f;
+    }
+    const int R = (i0 < n_eff) ? rblk[blockIdx.x] : 0;
+    if (R > 0) {
+        const int sh = (halo - R) & 3;
+        conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh, R, sh, wid, c2, lk, acc);
+    }
+    conv32_finish<SB>(xs, win, halo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every, conv,
+                      conv_stride, mm32, blk, gridDim.x, red);
+}
+
+// The same with TMA staging (spectra rows 16-byte aligned, stride a multiple of 4): a
+// block keeps its pixel tile and walks spectrum batches blockIdx.y, + gridDim.y, ...;
+// the next batch's rows are copied by cp.async.bulk into the other buffer while the
+// current one is convolved.  Staged row r of a batch starts at source pixel
+// mb = floor4(i0 - halo); pixels outside [0, n) are zeroed by the threads once the
+// copy has landed.
+template <int SB>
+__global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
+                                                        const float *__restrict__ lka, const int *__restrict__ livea,
+                                                        const int *__restrict__ rblk, int wid,
+                                                        const float *__restrict__ spec, long long spec_stride,
+                                                        int n_spec, int halo, const float *__restrict__ b32a,
+                                                        const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                                        const float *__restrict__ c32b, int b_every,
+                                                        float *__restrict__ conv, long long conv_stride,
+                                                        unsigned *mm32, float *blk, int nbx, int *status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float red[SB][4][FC_THREADS / 32];
+    __shared__ unsigned long long bar[2];
+    __shared__ int fail;
+    const int win = (FC_TILE + 2 * halo + 12 + 3) & ~3;
+    float *xbuf = reinterpret_cast<float *>(smem_raw);   // [2][SB][win]
+    const int i0 = blockIdx.x * FC_TILE;
+    const int wm0 = i0 - halo;                          // source pixel of window index 0
+    const int mb = (wm0 >= 0) ? (wm0 & ~3) : -((-wm0 + 3) & ~3);
+    const int xo = wm0 - mb;                            // staged index of wm0, in [0, 3]
+    // in-range part [ca, cb) of the staged row, 16-byte aligned at both ends (the row's
+    // allocation is padded beyond n to a multiple of 16 bytes)
+    const int ca = max(mb, 0);
+    const int cb = min(mb + win, (n + 3) & ~3);
+    const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
+    const int nbatch = (n_spec + SB - 1) / SB;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[1])));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fail = 0;
+    }
+    __syncthreads();
+    auto issue = [&](int bt, int buf) {   // thread 0
+        const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
+                     "r"(bytes * (unsigned)nsb)
+                     : "memory");
+        if (bytes) {
+            for (int q = 0; q < nsb; ++q) {
+                const float *src = spec + (long long)(s0 + q) * spec_stride + ca;
+                float *dst = xbuf + ((size_t)buf * SB + q) * win + (ca - mb);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        (unsigned)__cvta_generic_to_shared(dst)),
+                    "l"(src), "r"(bytes), "r"(bar_a)
+                    : "memory");
+            }
+        }
+    };
+    const int ib = i0 + threadIdx.x * FC_PIX;
+    float c2[FC_PIX], lk[FC_PIX];
+    bool lv[FC_PIX];
+#pragma unroll
+    for (int p = 0; p < FC_PIX; ++p) {
+        const int i = ib + p;
+        lv[p] = (i < n_eff) && livea[i];
+        c2[p] = lv[p] ? c2a[i] : 0.f;
+        lk[p] = lv[p] ? lka[i] : -200.f;
+    }
+    const int R = (i0 < n_eff) ? rblk[blockIdx.x] : 0;
+    const int sh = (halo - R + xo) & 3;
+    int k = 0, k_fail = -1;
+    if (threadIdx.x == 0 && blockIdx.y < nbatch) issue(blockIdx.y, 0);
+    for (int bt = blockIdx.y; bt < nbatch; bt += gridDim.y, ++k) {
+        const int buf = k & 1;
+        if (threadIdx.x == 0 && bt + (int)gridDim.y < nbatch) issue(bt + gridDim.y, buf ^ 1);
+        const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        float *xs = xbuf + (size_t)buf * SB * win;
+        bool ok = false;
+        const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
+        for (long long it = 0; it < (1LL << 24) && !ok; ++it) {
+            unsigned r;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(r)
+                : "r"(bar_a), "r"((unsigned)((k >> 1) & 1))
+                : "memory");
+            ok = (r != 0);
+        }
+        if (!ok) atomicExch(&fail, 1);
+        // zero the staged pixels outside [0, n) (and the rows of absent spectra)
+        if (ca > mb || cb < mb + win || nsb < SB) {
+            for (int q = 0; q < SB; ++q)
+                for (int t = threadIdx.x; t < win; t += FC_THREADS) {
+                    const int m = mb + t;
+                    if (q >= nsb || m < 0 || m >= n) xs[q * win + t] = 0.f;
+                }
+        }
+        __syncthreads();
+        if (fail) {
+            k_fail = k;
+            break;
+        }
+        float acc[SB][FC_PIX];
+#pragma unroll
+        for (int q = 0; q < SB; ++q)
+#pragma unroll
+            for (int p = 0; p < FC_PIX; ++p) acc[q][p] = 0.f;
+        if (R > 0)
+            conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
+        conv32_finish<SB>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every,
+                          conv, conv_stride, mm32, blk, nbx, red);
+    }
+    if (k_fail >= 0 && threadIdx.x == 0) {
+        // a staged copy did not land in time: record it and give the next batch's copy,
+        // if one was issued, a bounded wait before leaving
+        atomicExch(status, 42);
+        if (blockIdx.y + (k_fail + 1) * (int)gridDim.y < nbatch) {
+            const int kb = k_fail + 1;
+            const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[kb & 1]);
+            for (long long it = 0; it < (1LL << 24); ++it) {
+                unsigned r;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                    "selp.u32 %0, 1, 0, p;\n\t}"
+                    : "=r"(r)
+                    : "r"(bar_a), "r"((unsigned)((kb >> 1) & 1))
+                    : "memory");
+                if (r) break;
+            }
+        }
+    }
+}
+
+// pass 2 of the fused form: exact FP64 extrema of the candidate pixels of the blocks
+// (1024 pixels each) that can hold one.  grid (blocks, spectra)
+__global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, const float *__restrict__ spec,
+                                                   long long spec_stride, const double *__restrict__ ba,
+                                                   const double *__restrict__ bb, const double *__restrict__ cba,
+                                                   const double *__restrict__ cbb, const float *__restrict__ b32a,
+                                                   const float *__restrict__ b32b, const float *__restrict__ c32a,
+                                                   const float *__restrict__ c32b, int b_every,
+                                                   const float *__restrict__ conv, long long conv_stride,
+                                                   const unsigned *__restrict__ mm32, const float *__restrict__ blk,
+                                                   unsigned long long *mm64) {
+    const int s = blockIdx.y;
+    const float mnA = soap_dec32(mm32[4 * s + 0]), mxC = soap_dec32(mm32[4 * s + 1]);
+    const float tolA = ldexpf(soap_dec32(mm32[4 * s + 2]), -21), tolC = ldexpf(soap_dec32(mm32[4 * s + 3]), -21);
     const float *bk = blk + ((long long)s * gridDim.x + blockIdx.x) * 2;
-    bool needA = bk[0] <= mnA + tolA;
-    bool needC = (mm32[4 * s + 1] != 0u) && (bk[1] >= mxC - tolC);
+    const bool needA = bk[0] <= mnA + tolA;
+    const bool needC = (mm32[4 * s + 1] != 0u) && (bk[1] >= mxC - tolC);
     if (!needA && !needC) return;          // uniform for the whole block
-    bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+    const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
     const float *sp = spec + (long long)s * spec_stride;
     const float *bs = use_b ? b32b : b32a;
     const float *cbs = use_b ? c32b : c32a;
@@ -415,17 +707,18 @@ __global__ void __launch_bounds__(256) k_refine64(int n, int n_eff, const float 
     const double *c64 = use_b ? cbb : cba;
     const float *cv = conv + (long long)s * conv_stride;
     unsigned long long mn = ~0ULL, mx = 0ULL;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float x = sp[i];
+    const int i_end = min(n, (int)(blockIdx.x + 1) * FC_TILE);
+    for (int i = blockIdx.x * FC_TILE + threadIdx.x; i < i_end; i += blockDim.x) {
+        const float x = sp[i];
         if (needA && bs[i] - x <= mnA + tolA) {
-            double a = b64[i] - (double)x;
+            const double a = b64[i] - (double)x;
             mn = min(mn, soap_ord_enc(a));
         }
         if (needC && i < n_eff) {
-            float cd = cv[i];
-            float c = cbs[i] + cd;
+            const float cd = cv[i];
+            const float c = cbs[i] + cd;
             if (c != 0.f && c >= mxC - tolC) {
-                double cx = c64[i] + (double)cd;
+                const double cx = c64[i] + (double)cd;
                 if (cx != 0.0) mx = max(mx, soap_ord_enc(cx));
             }
         }
@@ -467,10 +760,31 @@ __global__ void __launch_bounds__(256) k_norm32(int n_eff, const float *__restri
     out[(long long)s * out_stride + i] = soap_f32_to_f64(fmaf(-c, fac[s], 1.0f));
 }
 
+// k_norm32 four pixels per thread: 16-byte loads and stores (n_eff % 4 == 0, strides
+// multiples of 4, 16-byte aligned rows)
+__global__ void __launch_bounds__(256) k_norm32v(int n_eff, const float *__restrict__ c32a,
+                                                 const float *__restrict__ c32b, int b_every,
+                                                 const float *__restrict__ conv, long long conv_stride,
+                                                 const float *__restrict__ fac, double *__restrict__ out,
+                                                 long long out_stride) {
+    const int s = blockIdx.y;
+    const int i = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n_eff) return;
+    const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
+    const float4 cb = *reinterpret_cast<const float4 *>((use_b ? c32b : c32a) + i);
+    const float4 cd = *reinterpret_cast<const float4 *>(conv + (long long)s * conv_stride + i);
+    const float f = fac[s];
+    double2 *o = reinterpret_cast<double2 *>(out + (long long)s * out_stride + i);
+    o[0] = make_double2(soap_f32_to_f64(fmaf(-(cb.x + cd.x), f, 1.0f)), soap_f32_to_f64(fmaf(-(cb.y + cd.y), f, 1.0f)));
+    o[1] = make_double2(soap_f32_to_f64(fmaf(-(cb.z + cd.z), f, 1.0f)), soap_f32_to_f64(fmaf(-(cb.w + cd.w), f, 1.0f)));
+}
+
 namespace soapgb {
 
 static size_t conv_param_bytes(int n_eff) {
-    return 2 * ((sizeof(double) * (size_t)n_eff + 255) & ~size_t(255)) + ((sizeof(int2) * (size_t)n_eff + 255) & ~size_t(255));
+    // FAST64: kq, cq (double) + ranges (int2); FAST32: c2, lk, live (4 bytes each) + per-block reach
+    return 2 * ((sizeof(double) * (size_t)n_eff + 255) & ~size_t(255)) + ((sizeof(int2) * (size_t)n_eff + 255) & ~size_t(255)) +
+           ((sizeof(int) * (size_t)(n_eff / FC_TILE + 2) + 255) & ~size_t(255));
 }
 
 size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
@@ -481,7 +795,7 @@ size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
         b += 2 * (sizeof(float) * (size_t)n + 256) + 2 * (sizeof(float) * (size_t)n_eff + 256);   // base32, cb32
         b += sizeof(float) * (size_t)n * n_spec + 256;                                        // FP32 spectra
         b += 16 * (size_t)n_spec + 256 + 4 * (size_t)n_spec + 256;                               // mm32, factor
-        b += sizeof(float) * 2 * 64 * (size_t)n_spec + 256;                                      // block extrema
+        b += sizeof(float) * 2 * (size_t)((n + FC_TILE - 1) / FC_TILE) * n_spec + 256;          // block extrema
     }
     (void)n;
     return b;
@@ -511,6 +825,54 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
     k_conv_fast<T, SB, SrcT, OutT><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride,
                                                                         n_spec, one_minus, halo, conv, conv_stride);
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+// FAST32 convolution of the spectra fused with the first extrema pass (k_conv32x)
+static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const float *spec,
+                          long long spec_stride, int n_spec, double sigma_v, int wid, double step_mult,
+                          double step_exp, double cut, double sig_max, char *param_scratch, const float *b32a,
+                          const float *b32b, const float *c32a, const float *c32b, int b_every, float *conv,
+                          unsigned *mm32, float *blk) {
+    constexpr int SB = 8;
+    double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
+    int r = (int)floor(sqrt(cut / cmin)) + 2;
+    int halo = std::min(wid, r);
+    if (halo < 1) halo = 1;
+    const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
+    size_t smem = sizeof(float) * (size_t)SB * win;
+    if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
+    if (smem > 48 * 1024)
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32x<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
+    float *c2 = (float *)param_scratch;
+    float *lk = (float *)(param_scratch + pb);
+    int *live = (int *)(param_scratch + 2 * pb);
+    int *rblk = (int *)(param_scratch + 3 * pb);
+    const int nbx = (n + FC_TILE - 1) / FC_TILE;
+    SOAP_CUDA(ctx, cudaMemsetAsync(rblk, 0, sizeof(int) * (size_t)nbx, ctx->stream));
+    k_conv32_params<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
+                                                                      step_exp, cut, c2, lk, live, rblk);
+    SOAP_LAUNCHED(ctx);
+    const int nbatch = (n_spec + SB - 1) / SB;
+    if (spec_stride % 4 == 0 && ((uintptr_t)spec & 15) == 0) {
+        // TMA staging, double buffered: a block keeps its tile over several spectrum batches
+        const int win_t = (FC_TILE + 2 * halo + 12 + 3) & ~3;
+        size_t smem_t = sizeof(float) * 2 * (size_t)SB * win_t;
+        if (smem_t > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32t<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+        int gy = std::max(1, std::min(nbatch, (2 * std::max(ctx->num_sms, 1) + nbx - 1) / nbx));
+        dim3 g(nbx, gy);
+        k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
+                                                              n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
+                                                              n_eff, mm32, blk, nbx, ctx->d_status);
+    } else {
+        dim3 g(nbx, nbatch);
+        k_conv32x<SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
+                                                           n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv, n_eff,
+                                                           mm32, blk);
+    }
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -583,7 +945,7 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
             float *c32b = (float *)carve(p, sizeof(float) * (size_t)n_eff);
             unsigned *mm32 = (unsigned *)carve(p, 16 * (size_t)n_spec);
             float *fac = (float *)carve(p, 4 * (size_t)n_spec);
-            int bx = std::max(1, std::min(64, (n + 255) / 256));
+            const int bx = (n + FC_TILE - 1) / FC_TILE;   // extrema blocks of 1024 pixels
             float *blk = (float *)carve(p, sizeof(float) * 2 * (size_t)bx * n_spec);
             k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_a, cb_a, b32a, c32a);
             SOAP_LAUNCHED(ctx);
@@ -592,23 +954,27 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
                 SOAP_LAUNCHED(ctx);
             }
             float *conv32 = (float *)conv;
-            rc = launch_conv_fast<float, 8, float, float>(ctx, n, n_eff, d_wave, spec32, spec_stride, n_spec, 0,
-                                                          sigma_v, wid, step_mult, step_exp, cut, conv32, n_eff,
-                                                          sig_max, pscr);
-            if (rc) return rc;
             k_mm32_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm32, mm);
             SOAP_LAUNCHED(ctx);
+            rc = launch_conv32x(ctx, n, n_eff, d_wave, spec32, spec_stride, n_spec, sigma_v, wid, step_mult, step_exp,
+                                cut, sig_max, pscr, b32a, cb_b ? b32b : b32a, c32a, cb_b ? c32b : c32a, b_every,
+                                conv32, mm32, blk);
+            if (rc) return rc;
             dim3 g2(bx, n_spec);
-            k_minmax32<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, b32a, b32b, c32a, c32b, b_every,
-                                                    conv32, n_eff, mm32, blk);
-            SOAP_LAUNCHED(ctx);
-            k_refine64<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
-                                                    b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm);
+            k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
+                                                     b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm);
             SOAP_LAUNCHED(ctx);
             k_factor<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, mm, fac, d_minmax);
             SOAP_LAUNCHED(ctx);
-            dim3 g3(grid_for(ctx, n_eff, 256), n_spec);
-            k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out, out_stride);
+            if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)d_out & 15) == 0) {
+                dim3 g3(grid_for(ctx, n_eff / 4, 256), n_spec);
+                k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
+                                                       out_stride);
+            } else {
+                dim3 g3(grid_for(ctx, n_eff, 256), n_spec);
+                k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
+                                                      out_stride);
+            }
             SOAP_LAUNCHED(ctx);
             return SOAPGB_OK;
         }
