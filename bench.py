@@ -97,16 +97,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary."""
+def profile_traffic(kernel):
+    """Per-launch DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum) of
+    `kernel` from the committed summary profiles/traffic.txt (lines "kernel bytes")."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for ln in f:
-            if ln.startswith("bytes_per_launch"):
+            parts = ln.split()
+            if len(parts) == 2 and parts[0] == kernel:
                 try:
-                    return float(ln.split("=")[1])
+                    return float(parts[1])
                 except ValueError:
                     return None
     return None
@@ -182,15 +184,22 @@ def run_own(args):
         ctx.phase_pipeline(form, wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases_d, regions, q_sed_d,
                            q_norm_d, case.sigma_v, conv_step=case.step, out=out)
 
-    for _ in range(args.warmup):
+    # clocks are sampled from the warm-up on (nvidia-smi needs a moment to start); the
+    # warm-up runs at least W steps and at least half a second so the GPU is under load
+    clocks = ClockSampler(lr)
+    clocks.start()
+    tw = time.perf_counter()
+    nw = 0
+    while nw < args.warmup or time.perf_counter() - tw < 0.5:
         step_dev()
+        nw += 1
+        if nw % 20 == 0:
+            torch.cuda.synchronize()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     if dist:
         tdist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(lr)
-    clocks.start()
     l0 = ctx.launches
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
@@ -249,18 +258,25 @@ def run_own(args):
         tdist.all_reduce(te_t, op=tdist.ReduceOp.MAX)
     e2e_value = n_units / (float(te_t.item()) / 1e3)
 
-    # --- stage timing and roofline of the dominant kernel ----------------------------
-    stage = stage_times(ctx, form, case, inp, wave_d, maps_d, cubes_d, q_sed_d, q_norm_d, phases_d, regions, act)
+    # --- per-kernel CUDA-event times of one step, roofline of the dominant kernel -------
+    ctx.trace(True)
+    for _ in range(2):
+        step_dev()
+    ktab = {k: (c / 2.0, ms / 2.0) for k, (c, ms) in ctx.trace_report().items()}
+    ctx.trace(False)
     result = None
     if rk == 0:
         peak, peak_kind = measured_peaks()
-        dom = max(stage["kernels"], key=lambda k: stage["kernels"][k]["ms"])
-        kd = stage["kernels"][dom]
-        achieved = kd["bytes"] / (kd["ms"] / 1e3) / 1e9
-        traffic = profile_traffic()
+        dom = max(ktab, key=lambda k: ktab[k][1])
+        launches_dom, ms_dom = ktab[dom]
+        ms_launch = ms_dom / max(launches_dom, 1.0)
+        alg = algorithmic_bytes(dom, case, phases_d.cpu().numpy(), regions, act, ctx, maps_d, form)
+        achieved = alg["bytes"] / (ms_launch / 1e3) / 1e9
+        traffic = profile_traffic(dom)
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": kd["bytes"], "ms_per_launch": round(kd["ms"], 4)}
+                "algorithmic_bytes_per_launch": int(alg["bytes"]), "bytes_formula": alg["formula"],
+                "ms_per_launch": round(ms_launch, 4)}
         err = accuracy(ctx, case, inp, form, out, wave_d, maps_d, cubes_d, phases_d, regions, act, star)
         cpu = cpu_baseline(case, inp, sample_phases=1) if not args.no_cpu else None
         result = {
@@ -277,7 +293,7 @@ def run_own(args):
             "roofline": roof,
             "cpu_baseline": cpu,
             "accuracy": err,
-            "stages_ms": {k: round(v["ms"], 4) for k, v in stage["kernels"].items()},
+            "kernels_ms_per_step": {k: round(v[1], 4) for k, v in sorted(ktab.items(), key=lambda x: -x[1][1])},
             "clocks": clk,
         }
     if dist:
@@ -287,53 +303,26 @@ def run_own(args):
     return result
 
 
-def stage_times(ctx, form, case, inp, wave_d, maps_d, cubes_d, q_sed_d, q_norm_d, phases_d, regions, act):
-    """CUDA-event timing of each stage alone (on the launch stream) + algorithmic bytes."""
-    import torch
-    n, n_eff = case.n, case.n_eff
-    n_phase = len(regions)
-    stream = torch.cuda.current_stream()
+def algorithmic_bytes(kernel, case, phases, regions, act, ctx, maps_d, form):
+    """Algorithmic HBM bytes of one launch of `kernel` in one step.
 
-    def timed(fn, reps=3):
-        fn()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / reps
-
-    temp, bi = ctx.phase_maps(case.grid, case.incl, phases_d.cpu().numpy(), regions, act)
-    temp_d, bi_d = torch.as_tensor(temp, device=wave_d.device), torch.as_tensor(bi, device=wave_d.device)
-    res = {}
-    res["phase_maps"] = {"ms": timed(lambda: ctx.phase_maps(case.grid, case.incl, phases_d, regions, act)),
-                         "bytes": 2 * 8 * case.grid ** 2 * n_phase}
-    flux = [None]
-
-    def integ():
-        flux[0] = ctx.phase_integrate(form, wave_d, n_eff, case.grid, temp_d, bi_d, maps_d, cubes_d, case.step, act)
-
-    res["integration"] = {"ms": timed(integ)}
-    # algorithmic bytes: the mu rows the active cells touch (6 typed cubes), the
-    # per-cell maps and the three FP64 outputs
-    rows_used = 0
-    for p in range(n_phase):
-        act_cells = bi[p] >= 0
-        rows_used += len(np.unique(maps_d["region"].cpu().numpy()[act_cells]))
+    fir_tile_phase (active-region integration, all phases in one launch): per phase,
+    (distinct mu rows of its active cells x N_eff x 3 cubes + 2 continua + 3 outputs)
+    x sizeof(element); conv32 / norm32: spectra in + convolution out, convolution in +
+    FP64 spectra out."""
+    n_eff, n_phase = case.n_eff, len(phases)
     tsz = 4 if form == "fast32" else 8
-    res["integration"]["bytes"] = rows_used * 6 * n * tsz + 3 * 8 * n * n_phase + 2 * 8 * case.grid ** 2 * n_phase
-    raw = torch.stack([flux[0][2], flux[0][0], flux[0][1]], dim=1).reshape(3 * n_phase, n).contiguous()
-
-    def resol():
-        ctx.lower_resolution(form, wave_d, raw[: 2 * n_phase], n_eff, case.sigma_v, base=q_sed_d,
-                             step_mult=case.step, step_exp=case.step)
-        ctx.lower_resolution(form, wave_d, raw[2 * n_phase:], n_eff, case.sigma_v, base=q_norm_d,
-                             step_mult=case.step, step_exp=case.step)
-
-    res["resolution"] = {"ms": timed(resol), "bytes": 3 * n_phase * (8 * n + 8 * n_eff * 3)}
-    return {"kernels": res}
+    if kernel == "fir_tile_phase":
+        temp, bi = ctx.phase_maps(case.grid, case.incl, phases, regions, act)
+        region = maps_d["region"].cpu().numpy()
+        rows = sum(len(np.unique(region[(bi[p] >= -0.5) & (bi[p] <= 1.5)])) for p in range(n_phase))
+        return {"bytes": (rows * 3 + (2 + 3) * n_phase) * n_eff * tsz,
+                "formula": "sum_p (mu rows touched x 3 cubes + 2 continua + 3 outputs) x N_eff x %d B" % tsz}
+    if kernel == "conv32":
+        return {"bytes": 3 * n_phase * (case.n + n_eff) * 4, "formula": "3 n_phase x (N + N_eff) x 4 B"}
+    if kernel == "norm32":
+        return {"bytes": 3 * n_phase * n_eff * (4 + 8), "formula": "3 n_phase x N_eff x (4 + 8) B"}
+    return {"bytes": 0, "formula": "not modelled"}
 
 
 def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, regions, act, star):
@@ -416,12 +405,15 @@ def run_reference(args):
             oracle.lower_resolution(inp.wave, base - spec, n_eff, case.sigma_v, step_mult=case.step,
                                     step_exp=case.step)
 
+    # steps walk the 100 phases with stride 37, so that a short run samples phases with
+    # and without visible regions in proportion
     phases = case.phases
+    pick = lambda k: phases[(37 * k) % len(phases)]
     for w in range(args.warmup):
-        step(phases[w % len(phases)])
+        step(pick(w))
     t0 = time.perf_counter()
     for s in range(args.steps):
-        step(phases[(args.warmup + s) % len(phases)])
+        step(pick(args.warmup + s))
     dt = time.perf_counter() - t0
     value = args.steps / dt
     nth = oracle.num_threads()
@@ -438,8 +430,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")

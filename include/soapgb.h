@@ -106,6 +106,16 @@ long long soapgb_launch_count(const soapgb_ctx *ctx);
 /* Library version string. */
 const char *soapgb_version(void);
 
+/* Per-kernel tracing.  The reference times each process with std::chrono and prints
+ * the wall time (SOAP_initialize.cu:603-604, SOAP_integration.cu:852-853,
+ * SOAP_resolution.cu:433-434); here CUDA events bracket the library's kernel launches
+ * on the context's stream while tracing is on.  soapgb_trace_enable(ctx, on) starts or
+ * stops recording (and drops what was recorded); soapgb_trace_report synchronizes the
+ * stream and writes one line per kernel, "name launches total_ms\n", in first-launch
+ * order, then clears the record. */
+int soapgb_trace_enable(soapgb_ctx *ctx, int on);
+int soapgb_trace_report(soapgb_ctx *ctx, char *buf, size_t len);
+
 /* ---- a3: disk maps ------------------------------------------------------
  * Replaces the grid part of itot, SOAP_initialize.cu:297-395 (and the map files
  * written at :399-422).  mu_boundary: n_mu-1 descending boundaries; a cell takes

@@ -52,6 +52,8 @@ SIGNATURES = [
     ("soapgb_synchronize", ctypes.c_int, [_vp]),
     ("soapgb_launch_count", ctypes.c_longlong, [_vp]),
     ("soapgb_version", ctypes.c_char_p, []),
+    ("soapgb_trace_enable", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("soapgb_trace_report", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
     ("soapgb_disk_maps", ctypes.c_int, [_vp, ctypes.POINTER(Star), ctypes.c_int, _vp, ctypes.c_int,
                                         ctypes.POINTER(Maps)]),
     ("soapgb_quiet_disk", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int,

@@ -115,6 +115,20 @@ class Context:
     def launches(self) -> int:
         return int(self.L.soapgb_launch_count(self.h))
 
+    def trace(self, on: bool = True):
+        """Start (or stop) recording CUDA-event times of the library's kernels."""
+        self._check(self.L.soapgb_trace_enable(self.h, 1 if on else 0))
+
+    def trace_report(self) -> dict:
+        """{kernel: (launches, total ms)} recorded since tracing started or the last report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self.L.soapgb_trace_report(self.h, buf, len(buf)))
+        out = {}
+        for ln in buf.value.decode().splitlines():
+            name, cnt, ms = ln.rsplit(" ", 2)
+            out[name] = (int(cnt), float(ms))
+        return out
+
     # -- a3 ---------------------------------------------------------------------
     def disk_maps(self, grid, period, omega_ratio, incl, radius_km, u1, u2, mu_boundary, lb):
         a = self._args(mu_boundary)

@@ -331,24 +331,24 @@ extern "C" int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel,
     SOAP_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int) * (size_t)n_w * n_v, ctx->stream));   // -1
     if (nt > 0) {
         int gb = grid_for(ctx, nt, 256);
-        k_ccf_owner<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, ctx->d_status);
+        SOAP_TRACED(ctx, "ccf_mask", k_ccf_owner<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, ctx->d_status));
         SOAP_LAUNCHED(ctx);
-        k_ccf_count<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, cnt);
+        SOAP_TRACED(ctx, "ccf_mask", k_ccf_count<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, cnt));
         SOAP_LAUNCHED(ctx);
-        k_ccf_scan<<<n_v, 1024, 0, ctx->stream>>>(n_lines, cnt, off, tot);
+        SOAP_TRACED(ctx, "ccf_mask", k_ccf_scan<<<n_v, 1024, 0, ctx->stream>>>(n_lines, cnt, off, tot));
         SOAP_LAUNCHED(ctx);
-        k_ccf_fill<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, off, row_cap,
-                                                col, val);
+        SOAP_TRACED(ctx, "ccf_mask", k_ccf_fill<<<gb, 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner, off, row_cap,
+                                                col, val));
         SOAP_LAUNCHED(ctx);
     } else {
         SOAP_CUDA(ctx, cudaMemsetAsync(tot, 0, sizeof(int) * n_v, ctx->stream));
     }
     if (form == SOAPGB_FAST32) {
         dim3 gd(n_v, (n_spec + 7) / 8);
-        k_ccf_dot<true, 8><<<gd, 256, 0, ctx->stream>>>(n_w, col, val, tot, row_cap, n_spec, d_spec, n_w, d_out, n_v);
+        SOAP_TRACED(ctx, "ccf_dot", k_ccf_dot<true, 8><<<gd, 256, 0, ctx->stream>>>(n_w, col, val, tot, row_cap, n_spec, d_spec, n_w, d_out, n_v));
     } else {
         dim3 gd(n_v, (n_spec + 7) / 8);
-        k_ccf_dot<false, 8><<<gd, 256, 0, ctx->stream>>>(n_w, col, val, tot, row_cap, n_spec, d_spec, n_w, d_out, n_v);
+        SOAP_TRACED(ctx, "ccf_dot", k_ccf_dot<false, 8><<<gd, 256, 0, ctx->stream>>>(n_w, col, val, tot, row_cap, n_spec, d_spec, n_w, d_out, n_v));
     }
     SOAP_LAUNCHED(ctx);
     if (normalise) {

@@ -71,6 +71,37 @@ int check_status(soapgb_ctx *ctx, const char *what) {
     return SOAPGB_OK;
 }
 
+static cudaEvent_t trace_event(soapgb_ctx *ctx) {
+    if (!ctx->ev_free.empty()) {
+        cudaEvent_t e = ctx->ev_free.back();
+        ctx->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+TraceScope::TraceScope(soapgb_ctx *c, const char *n) : ctx(c), name(n) {
+    if (!ctx || !ctx->trace) return;
+    a = trace_event(ctx);
+    if (a) cudaEventRecord(a, ctx->stream);
+}
+
+TraceScope::~TraceScope() {
+    if (!a) return;
+    cudaEvent_t b = trace_event(ctx);
+    if (!b) {
+        ctx->ev_free.push_back(a);
+        return;
+    }
+    cudaEventRecord(b, ctx->stream);
+    ctx->spans.push_back(SoapTraceSpan{name, a, b});
+}
+
 int grid_for(soapgb_ctx *ctx, long long work, int block) {
     long long g = (work + block - 1) / block;
     if (g < 1) g = 1;
@@ -109,10 +140,64 @@ int soapgb_ctx_create(int device, soapgb_ctx **out) {
     return SOAPGB_OK;
 }
 
+int soapgb_trace_enable(soapgb_ctx *ctx, int on) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    for (auto &sp : ctx->spans) {
+        ctx->ev_free.push_back(sp.a);
+        ctx->ev_free.push_back(sp.b);
+    }
+    ctx->spans.clear();
+    ctx->trace = (on != 0);
+    return SOAPGB_OK;
+}
+
+int soapgb_trace_report(soapgb_ctx *ctx, char *buf, size_t len) {
+    if (!ctx || !buf || len == 0) return SOAPGB_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "soapgb_trace_report");
+    // aggregate by name, in first-seen order
+    std::vector<const char *> names;
+    std::vector<int> counts;
+    std::vector<double> ms;
+    for (auto &sp : ctx->spans) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, sp.a, sp.b) != cudaSuccess) {
+            cudaGetLastError();
+            t = 0.f;
+        }
+        size_t k = 0;
+        while (k < names.size() && strcmp(names[k], sp.name) != 0) ++k;
+        if (k == names.size()) {
+            names.push_back(sp.name);
+            counts.push_back(0);
+            ms.push_back(0.0);
+        }
+        counts[k] += 1;
+        ms[k] += t;
+        ctx->ev_free.push_back(sp.a);
+        ctx->ev_free.push_back(sp.b);
+    }
+    ctx->spans.clear();
+    size_t used = 0;
+    buf[0] = '\0';
+    for (size_t k = 0; k < names.size(); ++k) {
+        int w = snprintf(buf + used, len - used, "%s %d %.6f\n", names[k], counts[k], ms[k]);
+        if (w < 0 || (size_t)w >= len - used) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_trace_report: buffer too small");
+        used += (size_t)w;
+    }
+    return SOAPGB_OK;
+}
+
 int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     if (!ctx) return SOAPGB_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &sp : ctx->spans) {
+        cudaEventDestroy(sp.a);
+        cudaEventDestroy(sp.b);
+    }
+    for (auto e : ctx->ev_free) cudaEventDestroy(e);
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

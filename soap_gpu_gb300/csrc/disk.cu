@@ -99,8 +99,8 @@ __global__ void __launch_bounds__(1024) k_compact(const double *__restrict__ key
 namespace soapgb {
 int compact_cells(soapgb_ctx *ctx, int n_lists, int cells_per_list, const double *key, double lo,
                   double hi, int key_stride, int *idx_out, int *count_out) {
-    k_compact<<<n_lists, 1024, 0, ctx->stream>>>(key, key_stride, cells_per_list, lo, hi, idx_out,
-                                                  count_out);
+    SOAP_TRACED(ctx, "compact", k_compact<<<n_lists, 1024, 0, ctx->stream>>>(key, key_stride, cells_per_list, lo, hi, idx_out,
+                                                  count_out));
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -237,9 +237,9 @@ extern "C" int soapgb_disk_maps(soapgb_ctx *ctx, const soapgb_star *star, int n_
     if (!o_delta || !o_limb || !o_mu || !o_lb || !o_reg)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_disk_maps: null map pointer");
     const double *lb = star->lb;
-    k_disk_maps<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(
+    SOAP_TRACED(ctx, "disk_maps", k_disk_maps<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(
         G, d_ov, sin_incl, 2. / G, star->u1, star->u2, n_mu, d_mu, lb[0], lb[1], lb[2], lb[3], o_delta, o_limb,
-        o_mu, o_reg, o_lb);
+        o_mu, o_reg, o_lb));
     SOAP_LAUNCHED(ctx);
     if (mem == SOAPGB_HOST) {
         SOAP_CUDA(ctx, cudaMemcpyAsync(maps_out->delta, o_delta, sizeof(double) * gm, cudaMemcpyDeviceToHost, ctx->stream));
@@ -295,9 +295,9 @@ extern "C" int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, co
         // visible cells in map order (limb map is -999 elsewhere)
         rc = compact_cells(ctx, 1, (int)gm, d_limb, -998.0, 1e300, (int)gm, d_cells, d_count);
         if (rc) return rc;
-        k_quiet_plain64<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_cube, d_count, d_cells,
+        SOAP_TRACED(ctx, "quiet_plain64", k_quiet_plain64<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_cube, d_count, d_cells,
                                                                          d_delta, d_limb, d_region, step, n_mu, d_out,
-                                                                         ctx->d_status);
+                                                                         ctx->d_status));
         SOAP_LAUNCHED(ctx);
     } else {
         FirQuietArgs qa;

@@ -594,8 +594,12 @@ struct FirSeg {
     int u0;             // first work unit
 };
 
+// one work unit: a segment's shift values [ma, mb] with the source window they read
 struct FirUnit {
-    int seg, ma, mb;    // segment, shift values [ma, mb]
+    int cls, key;       // class, row * 2 + zero_v
+    int start, end;     // the segment's list positions
+    int m_lo, m_hi;     // the segment's shift range at this tile
+    int ma, mb;         // this unit's shift values
     int w0, w1, off;    // window [w0, w1) (source pixels), offset of w0 in the staged copy
 };
 
@@ -607,7 +611,7 @@ struct FirGrp {
 };
 
 template <typename T>
-struct FirExcW {        // wrap cell of the current unit (reads the staged window)
+struct FirExcW {        // wrap cell of a unit (reads the staged window)
     int i0;
     T phi, dlt, L, w2;
 };
@@ -619,16 +623,29 @@ struct FirExcD {        // directly evaluated cell (reads the cubes in global me
     double temp;
 };
 
-// per-batch capacities: shift values (group tasks) and staged wrap cells
-template <typename T>
-struct FirCaps {
-    static constexpr int GRP = (sizeof(T) == 4) ? 512 : 256;
-    static constexpr int EXC = (sizeof(T) == 4) ? 512 : 256;
+// Plan of (a batch of) a tile's work units: units, one group per shift value (task),
+// and the wrap cells.  U units, G tasks, E wrap cells at most.
+template <typename T, int U, int G, int E>
+struct FirPlanSt {
+    static constexpr int NU = U, NG = G, NE = E;
+    FirUnit unit[U];
+    int ut[U + 1];          // first task of each unit; ut[nb] = ntask
+    FirGrp<T> grp[G];
+    int wlo[G];             // first list position of each task's wrap cells
+    int woff[G + 1];        // exclusive offsets of the tasks' wrap cells; woff[ntask] = etot
+    FirExcW<T> excw[E];
+    int nunit, nb, ntask, etot, ok;
 };
-constexpr int FIR_BATCH_U = 128;   // work units per batch
+
+// the tile kernel's batches, and the plans precomputed per tile by k_fir_plan
+template <typename T>
+using FirTileSt = FirPlanSt<T, 128, (sizeof(T) == 4) ? 512 : 256, (sizeof(T) == 4) ? 512 : 256>;
+template <typename T>
+using FirPrePlan = FirPlanSt<T, 32, 128, 128>;
+constexpr int FIR_PLAN_THREADS = 64;
 
 // lists of at most this many (class 0 + 1) entries have their slopes staged in shared
-// memory for the binary searches
+// memory for the tile kernel's own searches
 template <typename T>
 struct FirListCap {
     static constexpr int N = (sizeof(T) == 4) ? 4096 : 1024;
@@ -642,14 +659,9 @@ struct FirSmem {
         FirExcD<T> excd[FIR_EXC];
     };
     unsigned long long bar[2];
-    FirUnit bud[FIR_BATCH_U];              // descriptors of the batch's units
-    int ut[FIR_BATCH_U + 1];               // first task of each unit of the batch
-    FirGrp<T> grp[FirCaps<T>::GRP];        // one group per task (shift value)
-    int wlo[FirCaps<T>::GRP];              // first list position of the task's wrap cells
-    int woff[FirCaps<T>::GRP + 1];         // wrap counts, then their exclusive offsets
-    FirExcW<T> excw[FirCaps<T>::EXC];      // wrap cells of the batch
+    FirTileSt<T> st;
     int wsum[FIR_THREADS / 32];
-    int nunit, fail, nb, ntask;
+    int fail;
     double sdl[FirListCap<T>::N];          // the list's slopes (short lists)
     // followed by FirSeg seg[] (dynamic, 16-byte aligned)
 };
@@ -657,6 +669,7 @@ struct FirSmem {
 template <typename T, int NC>
 __host__ __device__ constexpr size_t fir_smem_fixed() { return (sizeof(FirSmem<T, NC>) + 15) & ~size_t(15); }
 
+template <int NT>
 __device__ __forceinline__ int block_excl_scan_int(int v, int *wsum, int &total) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int inc = v;
@@ -667,7 +680,7 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int *wsum, int &total)
     if (lane == 31) wsum[warp] = inc;
     __syncthreads();
     int off = 0, tot = 0;
-    for (int w = 0; w < FIR_THREADS / 32; ++w) {
+    for (int w = 0; w < NT / 32; ++w) {
         if (w < warp) off += wsum[w];
         tot += wsum[w];
     }
@@ -710,49 +723,20 @@ struct FirTileArgs {
     void *out0, *out1, *out2;
     long long out_stride;
     int *status;
+    const void *plan;           // FirPrePlan<T> per (list, tile), or null
 };
 
-// QUIET: OutT = double (one spectrum, once per star); PHASE: OutT = T (the FP32 form
-// keeps its deficits in FP32 for the FP32 convolution that consumes them)
-template <typename T, int MODE, typename OutT>
-__global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
-    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
-    extern __shared__ __align__(128) unsigned char fir_smem[];
-    FirSmem<T, NC> &sh = *reinterpret_cast<FirSmem<T, NC> *>(fir_smem);
-    FirSeg *segs = reinterpret_cast<FirSeg *>(fir_smem + fir_smem_fixed<T, NC>());
-    const int l = blockIdx.y;
-    const int j0 = blockIdx.x * FIR_TILE;
+// The list's (class, mu bin, v == 0) segments with their shift ranges at the tile
+// [j0, j0 + t_eff) and first work units; returns the number of units.  Block-wide.
+template <int MODE, int NT>
+__device__ int fir_segments(const FirTileArgs &A, int l, int j0, int t_eff, FirSeg *segs, int nsg, int *nunit_sh) {
     const int tid = threadIdx.x;
-    const int n = A.n, n_eff = A.n_eff;
-    OutT *out0 = reinterpret_cast<OutT *>(A.out0);
-    OutT *out1 = reinterpret_cast<OutT *>(A.out1);
-    OutT *out2 = reinterpret_cast<OutT *>(A.out2);
-    const int t_eff = min(FIR_TILE, n_eff - j0);
-    if (t_eff <= 0) {   // whole tile in the zero tail [n_eff, n)
-        for (int q = 0; q < FIR_PIX; ++q) {
-            int j = j0 + tid + q * FIR_THREADS;
-            if (j >= n) continue;
-            long long o = (long long)l * A.out_stride + j;
-            out0[o] = (OutT)0;
-            if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
-        }
-        return;
-    }
-    const long long lbase = (long long)l * A.gm;
-    const double *dl = A.list_dlt + lbase;
+    const double *dl = A.list_dlt + (long long)l * A.gm;
     const int *cn = A.counts + 4 * l;
+    const int ns0 = A.nseg[2 * l];
+    const int ns1 = nsg - ns0;
     const double Xa = (double)j0 + A.los, Xb = (double)(j0 + t_eff - 1) + A.los;
-
-    // --- segments of this list with their shift ranges at this tile ------------------
-    const int ns0 = A.nseg[2 * l], ns1 = (MODE == MODE_PHASE) ? A.nseg[2 * l + 1] : 0;
-    const int nsg = ns0 + ns1;
-    if (tid == 0) {
-        mbar_init(&sh.bar[0], 1);
-        mbar_init(&sh.bar[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        sh.fail = 0;
-    }
-    for (int s = tid; s < nsg; s += FIR_THREADS) {
+    for (int s = tid; s < nsg; s += NT) {
         const int c = (s < ns0) ? 0 : 1;
         const int si = (c == 0) ? s : s - ns0;
         const int ns_c = (c == 0) ? ns0 : ns1;
@@ -781,17 +765,256 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
             segs[s].u0 = u;
             u += (segs[s].m_hi - segs[s].m_lo + FIR_MCH) / FIR_MCH;
         }
-        sh.nunit = u;
+        *nunit_sh = u;
     }
     __syncthreads();
-    const int nunit = sh.nunit;
-    // slopes of a short list in shared memory: the searches then cost no global latency
-    const int n01 = cn[0] + ((MODE == MODE_PHASE) ? cn[1] : 0);
-    const double *sl = dl;
-    if (n01 <= FirListCap<T>::N) {
-        for (int q = tid; q < n01; q += FIR_THREADS) sh.sdl[q] = dl[q];
-        sl = sh.sdl;
-        __syncthreads();
+    return *nunit_sh;
+}
+
+// descriptor of work unit u: its segment, shift values and source window
+template <typename T>
+__device__ __forceinline__ FirUnit fir_describe(int u, const FirSeg *segs, int nsg, int j0, int t_eff, int n,
+                                                int n_eff) {
+    int lo = 0, hi = nsg - 1;
+    while (lo < hi) {   // last segment with u0 <= u
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].u0 <= u) lo = mid; else hi = mid - 1;
+    }
+    const FirSeg &g = segs[lo];
+    FirUnit d;
+    d.cls = g.cls;
+    d.key = g.key;
+    d.start = g.start;
+    d.end = g.end;
+    d.m_lo = g.m_lo;
+    d.m_hi = g.m_hi;
+    d.ma = g.m_lo + (u - g.u0) * FIR_MCH;
+    d.mb = min(g.m_hi, d.ma + FIR_MCH - 1);
+    d.w0 = max(0, j0 + d.ma - (d.ma > g.m_lo ? 1 : 0));
+    d.w1 = min(n_eff, j0 + t_eff + d.mb + 1);
+    d.off = (d.w1 > d.w0) ? (int)(((((long long)(g.key >> 1) * n + d.w0) * (long long)sizeof(T)) & 15) /
+                                  (long long)sizeof(T))
+                          : 0;
+    return d;
+}
+
+// wrap cells [lo, hi) of a plan into st.excw[e - dst0]
+template <typename T, int NT, typename ST>
+__device__ __forceinline__ void fir_fill_exc(const FirTileArgs &A, int l, int j0, ST &st, int lo, int hi, int dst0) {
+    const long long lbase = (long long)l * A.gm;
+    for (int e = lo + (int)threadIdx.x; e < hi; e += NT) {
+        int a = 0, b = st.ntask - 1;
+        while (a < b) {   // last task with woff <= e
+            int mid = (a + b + 1) >> 1;
+            if (st.woff[mid] <= e) a = mid; else b = mid - 1;
+        }
+        const int cell = A.list_cell[lbase + st.wlo[a] + (e - st.woff[a])];
+        FirExcW<T> x;
+        cell_pos<T>(j0, A.geo, A.geo32, cell, x.i0, x.phi, x.dlt, x.L, x.w2);
+        st.excw[e - dst0] = x;
+    }
+}
+
+// Plan of the units [ub, ub + nb): as many as fit ST's capacities, their groups (binary
+// searches on the slopes sl, coefficients from the prefix sums) and wrap ranges, and
+// the first ST::NE wrap cells.  Block-wide; sets st.nb, st.ntask, st.etot.
+template <typename T, int MODE, int NT, typename ST>
+__device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, const FirSeg *segs, int nsg,
+                               int nunit, const double *sl, ST &st, int ub, int *wsum) {
+    const int tid = threadIdx.x;
+    const int n = A.n, n_eff = A.n_eff;
+    const double Xa = (double)j0 + A.los, Xb = (double)(j0 + t_eff - 1) + A.los;
+    const int nbu = min(ST::NU, nunit - ub);
+    for (int t = tid; t < nbu; t += NT) st.unit[t] = fir_describe<T>(ub + t, segs, nsg, j0, t_eff, n, n_eff);
+    __syncthreads();
+    if (tid == 0) {
+        int nb = 0, nt = 0;
+        st.ut[0] = 0;
+        while (nb < nbu) {
+            const int k = st.unit[nb].mb - st.unit[nb].ma + 1;
+            if (nt + k > ST::NG) break;
+            nt += k;
+            st.ut[++nb] = nt;
+        }
+        st.nb = nb;
+        st.ntask = nt;
+    }
+    __syncthreads();
+    const int nb = st.nb, ntask = st.ntask;
+    for (int k = tid; k < ntask; k += NT) {
+        int ui = 0, hi = nb - 1;
+        while (ui < hi) {   // unit of task k
+            int mid = (ui + hi + 1) >> 1;
+            if (st.ut[mid] <= k) ui = mid; else hi = mid - 1;
+        }
+        const FirUnit d = st.unit[ui];
+        const int m = d.ma + (k - st.ut[ui]);
+        int lowA, lowB, highA, highB;
+        if (m == d.m_lo) {
+            lowA = lowB = d.start;
+        } else {
+            lowA = fir_lower_bound(sl, d.start, d.end, Xa, m);
+            lowB = fir_lower_bound(sl, d.start, d.end, Xb, m);
+        }
+        if (m == d.m_hi) {
+            highA = highB = d.end;
+        } else {
+            highA = fir_lower_bound(sl, d.start, d.end, Xa, m + 1);
+            highB = fir_lower_bound(sl, d.start, d.end, Xb, m + 1);
+        }
+        const int rlo = max(lowA, lowB), rhi = min(highA, highB);
+        FirGrp<T> gr;
+        gr.m = m;
+        gr.ok = rhi > rlo;
+        gr.a0 = gr.a1 = gr.b = gr.a0w = gr.a1w = gr.bw = (T)0;
+        if (gr.ok) {
+            const double *P = A.pre + (long long)l * A.pre_stride + d.cls;
+            const long long pc = A.pre_comp;
+            const double SL = P[rhi] - P[rlo];
+            const double SLd = P[pc + rhi] - P[pc + rlo];
+            const double SLo = P[2 * pc + rhi] - P[2 * pc + rlo];
+            const double A1 = (double)j0 * SLd - SLo - (double)m * SL;
+            gr.a1 = (T)A1;
+            gr.a0 = (T)(SL - A1);
+            gr.b = (T)SLd;
+            if (MODE == MODE_PHASE && d.cls == CLS_FAC) {
+                const double Wt = P[3 * pc + rhi] - P[3 * pc + rlo];
+                const double Wd = P[4 * pc + rhi] - P[4 * pc + rlo];
+                const double Wo = P[5 * pc + rhi] - P[5 * pc + rlo];
+                const double W1 = (double)j0 * Wd - Wo - (double)m * Wt;
+                gr.a1w = (T)W1;
+                gr.a0w = (T)(Wt - W1);
+                gr.bw = (T)Wd;
+            }
+        }
+        st.grp[k] = gr;
+        int wl = 0, wc = 0;
+        if (m > d.m_lo) {   // cells whose floor changes across boundary m inside the tile
+            wl = min(lowA, lowB);
+            wc = max(lowA, lowB) - wl;
+        }
+        st.wlo[k] = wl;
+        st.woff[k] = wc;
+    }
+    __syncthreads();
+    {   // exclusive offsets of the wrap counts (NG / NT entries per thread)
+        constexpr int PER = ST::NG / NT;
+        static_assert(ST::NG % NT == 0, "task capacity per thread");
+        const int a = tid * PER;
+        int loc = 0;
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (a + q < ntask) loc += st.woff[a + q];
+        int etot;
+        int ex = block_excl_scan_int<NT>(loc, wsum, etot);
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (a + q < ntask) {
+                int v = st.woff[a + q];
+                st.woff[a + q] = ex;
+                ex += v;
+            }
+        if (tid == 0) {
+            st.woff[ntask] = etot;
+            st.etot = etot;
+        }
+    }
+    __syncthreads();
+    fir_fill_exc<T, NT>(A, l, j0, st, 0, min(st.etot, ST::NE), 0);
+    __syncthreads();
+}
+
+// Plans of every (list, tile) of the phase integration, computed ahead of the tile
+// kernel by small blocks (many per SM, so that the searches' load latencies overlap
+// across tiles).  A tile whose units, groups or wrap cells exceed FirPrePlan's
+// capacities gets ok = 0 and plans itself in the tile kernel.
+template <typename T>
+__global__ void __launch_bounds__(FIR_PLAN_THREADS) k_fir_plan(const FirTileArgs A) {
+    extern __shared__ __align__(16) unsigned char plan_smem[];
+    FirPrePlan<T> &st = *reinterpret_cast<FirPrePlan<T> *>(plan_smem);
+    __shared__ int wsum[FIR_PLAN_THREADS / 32];
+    __shared__ int nunit_sh;
+    FirSeg *segs = reinterpret_cast<FirSeg *>(plan_smem + ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)));
+    const int l = blockIdx.y, j0 = blockIdx.x * FIR_TILE, tid = threadIdx.x;
+    FirPrePlan<T> *out = reinterpret_cast<FirPrePlan<T> *>(const_cast<void *>(A.plan)) +
+                         ((long long)l * gridDim.x + blockIdx.x);
+    const int t_eff = min(FIR_TILE, A.n_eff - j0);
+    if (t_eff <= 0) {
+        if (tid == 0) {
+            out->ok = 1;
+            out->nunit = out->nb = out->ntask = out->etot = 0;
+        }
+        return;
+    }
+    const int nsg = A.nseg[2 * l] + A.nseg[2 * l + 1];
+    const int nunit = fir_segments<MODE_PHASE, FIR_PLAN_THREADS>(A, l, j0, t_eff, segs, nsg, &nunit_sh);
+    int ok = 1;
+    if (nunit > FirPrePlan<T>::NU) {
+        ok = 0;
+    } else if (nunit > 0) {
+        fir_plan_batch<T, MODE_PHASE, FIR_PLAN_THREADS>(A, l, j0, t_eff, segs, nsg, nunit,
+                                                        A.list_dlt + (long long)l * A.gm, st, 0, wsum);
+        ok = (st.nb == nunit) && (st.etot <= FirPrePlan<T>::NE);
+    } else if (tid == 0) {
+        st.nb = st.ntask = st.etot = 0;
+        st.ut[0] = 0;
+        st.woff[0] = 0;
+    }
+    __syncthreads();
+    if (ok) {   // copy the used parts
+        const int nb = st.nb, ntask = st.ntask, etot = st.etot;
+        for (int i = tid; i < nb; i += FIR_PLAN_THREADS) out->unit[i] = st.unit[i];
+        for (int i = tid; i <= nb; i += FIR_PLAN_THREADS) out->ut[i] = st.ut[i];
+        for (int i = tid; i < ntask; i += FIR_PLAN_THREADS) {
+            out->grp[i] = st.grp[i];
+            out->wlo[i] = st.wlo[i];
+        }
+        for (int i = tid; i <= ntask; i += FIR_PLAN_THREADS) out->woff[i] = st.woff[i];
+        for (int i = tid; i < etot; i += FIR_PLAN_THREADS) out->excw[i] = st.excw[i];
+    }
+    if (tid == 0) {
+        out->ok = ok;
+        out->nunit = ok ? nunit : 0;
+        out->nb = ok ? st.nb : 0;
+        out->ntask = ok ? st.ntask : 0;
+        out->etot = ok ? st.etot : 0;
+    }
+}
+
+// QUIET: OutT = double (one spectrum, once per star); PHASE: OutT = T (the FP32 form
+// keeps its deficits in FP32 for the FP32 convolution that consumes them)
+template <typename T, int MODE, typename OutT>
+__global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
+    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
+    extern __shared__ __align__(128) unsigned char fir_smem[];
+    FirSmem<T, NC> &sh = *reinterpret_cast<FirSmem<T, NC> *>(fir_smem);
+    FirSeg *segs = reinterpret_cast<FirSeg *>(fir_smem + fir_smem_fixed<T, NC>());
+    FirTileSt<T> &st = sh.st;
+    const int l = blockIdx.y;
+    const int j0 = blockIdx.x * FIR_TILE;
+    const int tid = threadIdx.x;
+    const int n = A.n, n_eff = A.n_eff;
+    OutT *out0 = reinterpret_cast<OutT *>(A.out0);
+    OutT *out1 = reinterpret_cast<OutT *>(A.out1);
+    OutT *out2 = reinterpret_cast<OutT *>(A.out2);
+    const int t_eff = min(FIR_TILE, n_eff - j0);
+    if (t_eff <= 0) {   // whole tile in the zero tail [n_eff, n)
+        for (int q = 0; q < FIR_PIX; ++q) {
+            int j = j0 + tid + q * FIR_THREADS;
+            if (j >= n) continue;
+            long long o = (long long)l * A.out_stride + j;
+            out0[o] = (OutT)0;
+            if constexpr (MODE == MODE_PHASE) { out1[o] = (OutT)0; out2[o] = (OutT)0; }
+        }
+        return;
+    }
+    const long long lbase = (long long)l * A.gm;
+    const int *cn = A.counts + 4 * l;
+    if (tid == 0) {
+        mbar_init(&sh.bar[0], 1);
+        mbar_init(&sh.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sh.fail = 0;
     }
 
     // accumulators: QUIET [0]; PHASE: S, Qs, As, Bs, Qf, Af, Bf
@@ -802,35 +1025,15 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) acc[a][q].zero();
 
-    constexpr int GRP = FirCaps<T>::GRP, EXC = FirCaps<T>::EXC;
-    // descriptor of work unit u: its segment, shift values and source window
-    auto describe = [&](int u) -> FirUnit {
-        int lo = 0, hi = nsg - 1;
-        while (lo < hi) {   // last segment with u0 <= u
-            int mid = (lo + hi + 1) >> 1;
-            if (segs[mid].u0 <= u) lo = mid; else hi = mid - 1;
-        }
-        const FirSeg &g = segs[lo];
-        FirUnit d;
-        d.seg = lo;
-        d.ma = g.m_lo + (u - g.u0) * FIR_MCH;
-        d.mb = min(g.m_hi, d.ma + FIR_MCH - 1);
-        d.w0 = max(0, j0 + d.ma - (d.ma > g.m_lo ? 1 : 0));
-        d.w1 = min(n_eff, j0 + t_eff + d.mb + 1);
-        d.off = (d.w1 > d.w0) ? (int)(((((long long)(g.key >> 1) * n + d.w0) * (long long)sizeof(T)) & 15) /
-                                      (long long)sizeof(T))
-                              : 0;
-        return d;
-    };
+    constexpr int EXC = FirTileSt<T>::NE;
     // staging of unit u's rows into buffer u & 1 (thread 0)
     auto issue = [&](int u, const FirUnit &d) {
-        const FirSeg &g = segs[d.seg];
         const int b = u & 1;
         unsigned bytes = 0;
         uintptr_t rel = 0;   // 16-byte aligned start, relative to the cube base
         if (d.w1 > d.w0) {
-            const uintptr_t p0 = (uintptr_t)((long long)(g.key >> 1) * n + d.w0) * sizeof(T);
-            const uintptr_t p1 = (uintptr_t)((long long)(g.key >> 1) * n + d.w1) * sizeof(T);
+            const uintptr_t p0 = (uintptr_t)((long long)(d.key >> 1) * n + d.w0) * sizeof(T);
+            const uintptr_t p1 = (uintptr_t)((long long)(d.key >> 1) * n + d.w1) * sizeof(T);
             rel = p0 & ~uintptr_t(15);
             bytes = (unsigned)(((p1 + 15) & ~uintptr_t(15)) - rel);
         }
@@ -841,151 +1044,40 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
         if (bytes) {
 #pragma unroll
             for (int q = 0; q < NC; ++q) {
-                const char *base = reinterpret_cast<const char *>(A.cubes.c[fir_cube_index(MODE, g.cls, q)]);
+                const char *base = reinterpret_cast<const char *>(A.cubes.c[fir_cube_index(MODE, d.cls, q)]);
                 bulk_g2s(&sh.win[b][q][0], base + rel, bytes, &sh.bar[b]);
             }
-        }
-    };
-    // wrap cells [lo, hi) of the batch into excw[e - dst0]
-    auto fill_exc = [&](int lo, int hi, int dst0, int ntask) {
-        for (int e = lo + tid; e < hi; e += FIR_THREADS) {
-            int a = 0, b = ntask - 1;
-            while (a < b) {   // last task with woff <= e
-                int mid = (a + b + 1) >> 1;
-                if (sh.woff[mid] <= e) a = mid; else b = mid - 1;
-            }
-            const int cell = A.list_cell[lbase + sh.wlo[a] + (e - sh.woff[a])];
-            FirExcW<T> x;
-            cell_pos<T>(j0, A.geo, A.geo32, cell, x.i0, x.phi, x.dlt, x.L, x.w2);
-            sh.excw[e - dst0] = x;
         }
     };
 
     int u_fail = -1;
     int issued = -1;   // last unit whose copy was issued (thread 0)
-    for (int ub = 0; ub < nunit;) {
-        // --- batch: units [ub, ub + nb) with at most GRP shift values in total ---------
-        const int nbu = min(FIR_BATCH_U, nunit - ub);
-        for (int t = tid; t < nbu; t += FIR_THREADS) sh.bud[t] = describe(ub + t);
-        __syncthreads();
-        if (tid == 0) {
-            if (issued < ub) {
-                issue(ub, sh.bud[0]);
-                issued = ub;
-            }
-            int nb = 0, nt = 0;
-            sh.ut[0] = 0;
-            while (nb < nbu) {
-                const int k = sh.bud[nb].mb - sh.bud[nb].ma + 1;
-                if (nt + k > GRP) break;
-                nt += k;
-                sh.ut[++nb] = nt;
-            }
-            sh.nb = nb;
-            sh.ntask = nt;
+    // apply the planned units st.unit[0, nb) (global unit numbers ub + ui)
+    auto run_units = [&](int ub) {
+        const int nb = st.nb, ntask = st.ntask;
+        if (tid == 0 && nb > 0 && issued < ub) {
+            issue(ub, st.unit[0]);
+            issued = ub;
         }
-        __syncthreads();
-        const int nb = sh.nb, ntask = sh.ntask;
-        // --- groups and wrap ranges of every shift value of the batch -----------------
-        for (int k = tid; k < ntask; k += FIR_THREADS) {
-            int ui = 0, hi = nb - 1;
-            while (ui < hi) {   // unit of task k
-                int mid = (ui + hi + 1) >> 1;
-                if (sh.ut[mid] <= k) ui = mid; else hi = mid - 1;
-            }
-            const FirUnit d = sh.bud[ui];
-            const FirSeg g = segs[d.seg];
-            const int m = d.ma + (k - sh.ut[ui]);
-            int lowA, lowB, highA, highB;
-            if (m == g.m_lo) {
-                lowA = lowB = g.start;
-            } else {
-                lowA = fir_lower_bound(sl, g.start, g.end, Xa, m);
-                lowB = fir_lower_bound(sl, g.start, g.end, Xb, m);
-            }
-            if (m == g.m_hi) {
-                highA = highB = g.end;
-            } else {
-                highA = fir_lower_bound(sl, g.start, g.end, Xa, m + 1);
-                highB = fir_lower_bound(sl, g.start, g.end, Xb, m + 1);
-            }
-            const int rlo = max(lowA, lowB), rhi = min(highA, highB);
-            FirGrp<T> gr;
-            gr.m = m;
-            gr.ok = rhi > rlo;
-            gr.a0 = gr.a1 = gr.b = gr.a0w = gr.a1w = gr.bw = (T)0;
-            if (gr.ok) {
-                const double *P = A.pre + (long long)l * A.pre_stride + g.cls;
-                const long long pc = A.pre_comp;
-                const double SL = P[rhi] - P[rlo];
-                const double SLd = P[pc + rhi] - P[pc + rlo];
-                const double SLo = P[2 * pc + rhi] - P[2 * pc + rlo];
-                const double A1 = (double)j0 * SLd - SLo - (double)m * SL;
-                gr.a1 = (T)A1;
-                gr.a0 = (T)(SL - A1);
-                gr.b = (T)SLd;
-                if (MODE == MODE_PHASE && g.cls == CLS_FAC) {
-                    const double Wt = P[3 * pc + rhi] - P[3 * pc + rlo];
-                    const double Wd = P[4 * pc + rhi] - P[4 * pc + rlo];
-                    const double Wo = P[5 * pc + rhi] - P[5 * pc + rlo];
-                    const double W1 = (double)j0 * Wd - Wo - (double)m * Wt;
-                    gr.a1w = (T)W1;
-                    gr.a0w = (T)(Wt - W1);
-                    gr.bw = (T)Wd;
-                }
-            }
-            sh.grp[k] = gr;
-            int wl = 0, wc = 0;
-            if (m > g.m_lo) {   // cells whose floor changes across boundary m inside the tile
-                wl = min(lowA, lowB);
-                wc = max(lowA, lowB) - wl;
-            }
-            sh.wlo[k] = wl;
-            sh.woff[k] = wc;
-        }
-        __syncthreads();
-        int etot;
-        {   // exclusive offsets of the wrap counts (GRP / FIR_THREADS entries per thread)
-            constexpr int PER = GRP / FIR_THREADS;
-            const int a = tid * PER;
-            int loc = 0;
-#pragma unroll
-            for (int q = 0; q < PER; ++q)
-                if (a + q < ntask) loc += sh.woff[a + q];
-            int ex = block_excl_scan_int(loc, sh.wsum, etot);
-#pragma unroll
-            for (int q = 0; q < PER; ++q)
-                if (a + q < ntask) {
-                    int v = sh.woff[a + q];
-                    sh.woff[a + q] = ex;
-                    ex += v;
-                }
-            if (tid == 0) sh.woff[ntask] = etot;
-        }
-        __syncthreads();
-        fill_exc(0, min(etot, EXC), 0, ntask);
-        __syncthreads();
-        // --- units of the batch: wait for the rows, apply groups and wrap cells --------
         for (int ui = 0; ui < nb; ++ui) {
             const int u = ub + ui;
             if (tid == 0 && ui + 1 < nb) {
-                issue(u + 1, sh.bud[ui + 1]);
+                issue(u + 1, st.unit[ui + 1]);
                 issued = u + 1;
             }
-            const FirUnit d = sh.bud[ui];
-            const FirSeg g = segs[d.seg];
-            const int cls = g.cls, zv = g.key & 1;
+            const FirUnit d = st.unit[ui];
+            const int cls = d.cls, zv = d.key & 1;
             if (!mbar_wait_bounded(&sh.bar[u & 1], (unsigned)((u >> 1) & 1))) atomicExch(&sh.fail, 1);
             __syncthreads();
             if (sh.fail) {
                 u_fail = u;
-                break;
+                return;
             }
             const T(*W)[FIR_WIN] = sh.win[u & 1];
             const int wo = d.off - d.w0;   // staged index of source pixel i: i + wo
-            const int t_lo = sh.ut[ui], t_hi = sh.ut[ui + 1];
+            const int t_lo = st.ut[ui], t_hi = st.ut[ui + 1];
             for (int t = t_lo; t < t_hi; ++t) {
-                const FirGrp<T> gr = sh.grp[t];
+                const FirGrp<T> gr = st.grp[t];
                 if (!gr.ok) continue;
                 const int m = gr.m;
                 // pixels whose owner j + m lies in [0, n_eff - 2] (v == 0: [0, n_eff - 1])
@@ -1032,18 +1124,18 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
                 }
             }
             // --- wrap cells of the unit (per-cell lerp from the staged rows) ------------
-            const int e_lo = sh.woff[t_lo], e_hi = sh.woff[t_hi];
+            const int e_lo = st.woff[t_lo], e_hi = st.woff[t_hi];
             for (int cb = e_lo; cb < e_hi; cb += EXC) {
                 const int ce = min(e_hi, cb + EXC);
                 int x0 = cb;   // excw index of entry cb
                 if (e_hi > EXC) {   // not all staged: refill this chunk
                     __syncthreads();
-                    fill_exc(cb, ce, cb, ntask);
+                    fir_fill_exc<T, FIR_THREADS>(A, l, j0, st, cb, ce, cb);
                     __syncthreads();
                     x0 = 0;
                 }
                 for (int e = cb; e < ce; ++e) {
-                    const FirExcW<T> xc = sh.excw[x0 + (e - cb)];
+                    const FirExcW<T> xc = st.excw[x0 + (e - cb)];
 #pragma unroll
                     for (int q = 0; q < FIR_PIX; ++q) {
                         const int dj = tid + q * FIR_THREADS;
@@ -1066,7 +1158,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
                                 s1 = W[c][x + 1];
                             } else {
                                 const T *rowp = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE, cls, c)]) +
-                                                (long long)(g.key >> 1) * n;
+                                                (long long)(d.key >> 1) * n;
                                 s0 = rowp[i];
                                 s1 = rowp[i + 1];
                             }
@@ -1090,8 +1182,47 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
             }
             __syncthreads();   // unit's buffer free
         }
-        if (u_fail >= 0) break;
-        ub += nb;
+    };
+
+    const FirPrePlan<T> *pl = (MODE == MODE_PHASE && A.plan)
+                                  ? reinterpret_cast<const FirPrePlan<T> *>(A.plan) + ((long long)l * gridDim.x + blockIdx.x)
+                                  : nullptr;
+    if (pl && pl->ok) {
+        // --- precomputed plan: copy it in, then apply ----------------------------------
+        const int nb = pl->nb, ntask = pl->ntask, etot = pl->etot;
+        for (int i = tid; i < nb; i += FIR_THREADS) st.unit[i] = pl->unit[i];
+        for (int i = tid; i <= nb; i += FIR_THREADS) st.ut[i] = pl->ut[i];
+        for (int i = tid; i < ntask; i += FIR_THREADS) {
+            st.grp[i] = pl->grp[i];
+            st.wlo[i] = pl->wlo[i];
+        }
+        for (int i = tid; i <= ntask; i += FIR_THREADS) st.woff[i] = pl->woff[i];
+        for (int i = tid; i < etot; i += FIR_THREADS) st.excw[i] = pl->excw[i];
+        if (tid == 0) {
+            st.nb = nb;
+            st.ntask = ntask;
+            st.etot = etot;
+        }
+        __syncthreads();
+        run_units(0);
+    } else {
+        // --- plan the tile here, batch by batch ------------------------------------------
+        const int nsg = A.nseg[2 * l] + ((MODE == MODE_PHASE) ? A.nseg[2 * l + 1] : 0);
+        const int nunit = fir_segments<MODE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, &st.nunit);
+        // slopes of a short list in shared memory: the searches then cost no global latency
+        const int n01 = cn[0] + ((MODE == MODE_PHASE) ? cn[1] : 0);
+        const double *sl = A.list_dlt + lbase;
+        if (n01 <= FirListCap<T>::N) {
+            for (int q = tid; q < n01; q += FIR_THREADS) sh.sdl[q] = sl[q];
+            sl = sh.sdl;
+            __syncthreads();
+        }
+        for (int ub = 0; ub < nunit;) {
+            fir_plan_batch<T, MODE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, nunit, sl, st, ub, sh.wsum);
+            run_units(ub);
+            if (u_fail >= 0) break;
+            ub += st.nb;
+        }
     }
     if (u_fail >= 0) {
         // a copy did not land in time: record it, give the copies still in flight (units
@@ -1099,7 +1230,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
         if (tid == 0) {
             atomicExch(A.status, FIR_ST_WAIT);
             mbar_wait_bounded(&sh.bar[u_fail & 1], (unsigned)((u_fail >> 1) & 1));
-            if (u_fail + 1 < nunit)
+            if (issued > u_fail)
                 mbar_wait_bounded(&sh.bar[(u_fail + 1) & 1], (unsigned)(((u_fail + 1) >> 1) & 1));
         }
         return;
@@ -1223,7 +1354,7 @@ namespace {
 struct FirLayout {
     enum {
         GEO, GEO32, CUBE0, SED2A = CUBE0 + 6, SED2B, K1A, K1B, K2A, K2B, VA, VB, SORT_TMP, LCELL, LDLT, COUNTS,
-        PRE, SEGS, NSEG, NSLOT
+        PRE, SEGS, NSEG, PLAN, NSLOT
     };
     size_t off[NSLOT] = {0};
     size_t total = 0;
@@ -1252,6 +1383,11 @@ FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_l
     L.seg_cap = 2 * n_mu;
     sz[FirLayout::SEGS] = sizeof(int2) * 2 * (size_t)L.seg_cap * n_lists;
     sz[FirLayout::NSEG] = sizeof(int) * 2 * (size_t)n_lists;
+    // precomputed tile plans of the phase integration
+    const size_t ntile = ((size_t)n + FIR_TILE - 1) / FIR_TILE;
+    if (ncube == 6)
+        sz[FirLayout::PLAN] = ntile * n_lists *
+                              ((form == SOAPGB_FAST32) ? sizeof(FirPrePlan<float>) : sizeof(FirPrePlan<double>));
     size_t t = 0;
     for (int s = 0; s < FirLayout::NSLOT; ++s) {
         L.off[s] = t;
@@ -1277,8 +1413,8 @@ static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double st
     SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     k_check_uniform<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, wave, step, ctx->d_status);
     SOAP_LAUNCHED(ctx);
-    k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, *lambda0, step, geo,
-                                                                geo32, ctx->d_status);
+    SOAP_TRACED(ctx, "cell_geo", k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, *lambda0, step, geo,
+                                                                geo32, ctx->d_status));
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -1298,11 +1434,18 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
     int g = grid_for(ctx, gm, 256);
     k_sort_keys1<<<g, 256, 0, ctx->stream>>>(gm, geo, k1a, va);
     SOAP_LAUNCHED(ctx);
-    int rc = soapgb::fir_sort_u64(ctx, gm, k1a, k1b, va, vb, tmp, tmp_bytes);
+    int rc;
+    {
+        soapgb::TraceScope ts(ctx, "cell_sort");
+        rc = soapgb::fir_sort_u64(ctx, gm, k1a, k1b, va, vb, tmp, tmp_bytes);
+    }
     if (rc) return rc;
     k_sort_keys2<<<g, 256, 0, ctx->stream>>>(gm, geo, vb, k2a);
     SOAP_LAUNCHED(ctx);
-    rc = soapgb::fir_sort_u32(ctx, gm, k2a, k2b, vb, va, 14, tmp, tmp_bytes);   // stable: dlt order kept per bin
+    {
+        soapgb::TraceScope ts(ctx, "cell_sort");
+        rc = soapgb::fir_sort_u32(ctx, gm, k2a, k2b, vb, va, 14, tmp, tmp_bytes);   // stable: dlt order kept per bin
+    }
     if (rc) return rc;
     int *lcell = (int *)(ws + L.off[FirLayout::LCELL]);
     double *ldlt = (double *)(ws + L.off[FirLayout::LDLT]);
@@ -1310,21 +1453,21 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
     if (bi && gm < (1LL << 24)) {
         // phases: short lists by a per-phase sort of the active cells, the rest by a scan
         int *rank = vb;   // free after the second sort
-        k_fir_rank<<<g, 256, 0, ctx->stream>>>(gm, va, rank);
+        SOAP_TRACED(ctx, "fir_rank", k_fir_rank<<<g, 256, 0, ctx->stream>>>(gm, va, rank));
         SOAP_LAUNCHED(ctx);
-        k_fir_plists<<<n_lists, 512, 0, ctx->stream>>>(gm, va, rank, geo, temp, bi, solar, lcell, ldlt, counts);
+        SOAP_TRACED(ctx, "fir_lists", k_fir_plists<<<n_lists, 512, 0, ctx->stream>>>(gm, va, rank, geo, temp, bi, solar, lcell, ldlt, counts));
         SOAP_LAUNCHED(ctx);
-        k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 1);
+        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 1));
         SOAP_LAUNCHED(ctx);
     } else {
-        k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 0);
+        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 0));
         SOAP_LAUNCHED(ctx);
     }
     double *pre = (double *)(ws + L.off[FirLayout::PRE]);
     int2 *segs = (int2 *)(ws + L.off[FirLayout::SEGS]);
     int *nseg = (int *)(ws + L.off[FirLayout::NSEG]);
-    k_fir_prefix<<<dim3(n_lists, 2), 256, 0, ctx->stream>>>(gm, counts, lcell, geo, pre, L.pre_stride, L.pre_comp,
-                                                            segs, nseg, L.seg_cap, ctx->d_status);
+    SOAP_TRACED(ctx, "fir_prefix", k_fir_prefix<<<dim3(n_lists, 2), 256, 0, ctx->stream>>>(gm, counts, lcell, geo, pre, L.pre_stride, L.pre_comp,
+                                                            segs, nseg, L.seg_cap, ctx->d_status));
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -1361,11 +1504,20 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.out2 = o2;
     A.out_stride = out_stride;
     A.status = ctx->d_status;
+    A.plan = nullptr;
+    const int ntile = (n + FIR_TILE - 1) / FIR_TILE;
+    if constexpr (MODE == MODE_PHASE) {
+        A.plan = ws + L.off[FirLayout::PLAN];
+        size_t smem_p = ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)) + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_plan<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+        SOAP_TRACED(ctx, "fir_plan", k_fir_plan<T><<<dim3(ntile, n_lists), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
+        SOAP_LAUNCHED(ctx);
+    }
     size_t smem = fir_smem_fixed<T, NC>() + sizeof(FirSeg) * (size_t)(MODE == MODE_PHASE ? 2 : 1) * L.seg_cap;
     SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // tiles cover [0, n): tiles past n_eff only write the zero tail
     dim3 g((n + FIR_TILE - 1) / FIR_TILE, n_lists);
-    k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(A);
+    SOAP_TRACED(ctx, MODE == MODE_QUIET ? "fir_tile_quiet" : "fir_tile_phase", k_fir<T, MODE, OutT><<<g, FIR_THREADS, smem, ctx->stream>>>(A));
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -1391,12 +1543,12 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     fc.c[0] = cube;
     const double los = lambda0 / a.step;
     if (form == SOAPGB_FAST32) {
-        k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube);
+        SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube));
         SOAP_LAUNCHED(ctx);
         return launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr,
                                                        gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
     }
-    k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (double *)cube);
+    SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (double *)cube));
     SOAP_LAUNCHED(ctx);
     return launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr, gm,
                                                     0, 0, a.out, nullptr, nullptr, 0, 1);
@@ -1429,9 +1581,9 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     for (int q = 0; q < 6; ++q) {
         void *dst = ws + L.off[FirLayout::CUBE0 + q];
         if (tsz == 4)
-            k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst);
+            SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst));
         else
-            k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst);
+            SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst));
         SOAP_LAUNCHED(ctx);
         fc.c[q] = dst;
     }

@@ -300,8 +300,8 @@ extern "C" int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double
     double *xr = ws.get<double>(s_xr);
     k_rebase<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, d_x, xr);
     SOAP_LAUNCHED(ctx);
-    k_gauss_bis<<<(n_spec + FIT_WARPS - 1) / FIT_WARPS, 32 * FIT_WARPS, 0, ctx->stream>>>(
-        n_spec, n, d_x, d_y, d_e, xr, d_model, d_par, d_dep, d_bis, d_it, ws.get<double>(s_scr));
+    SOAP_TRACED(ctx, "gauss_bis", k_gauss_bis<<<(n_spec + FIT_WARPS - 1) / FIT_WARPS, 32 * FIT_WARPS, 0, ctx->stream>>>(
+        n_spec, n, d_x, d_y, d_e, xr, d_model, d_par, d_dep, d_bis, d_it, ws.get<double>(s_scr)));
     SOAP_LAUNCHED(ctx);
     if (host) {
         SOAP_CUDA(ctx, cudaMemcpyAsync(model, d_model, sizeof(double) * (size_t)n * n_spec, cudaMemcpyDeviceToHost, ctx->stream));

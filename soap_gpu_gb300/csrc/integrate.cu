@@ -175,11 +175,11 @@ int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *
         int rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
         if (rc) return rc;
         dim3 g(grid_for(ctx, n, 256), n_phase);
-        k_phase_plain64<<<g, 256, 0, ctx->stream>>>(
+        SOAP_TRACED(ctx, "integrate_plain64", k_phase_plain64<<<g, 256, 0, ctx->stream>>>(
             n, n_eff, d_wave, dc.q_norm, dc.q_sed, dc.spot_norm, dc.fac_norm, dc.spot_sed, dc.fac_sed, (int)gm,
             d_cells, d_counts, d_temp, d_bi, dm.delta, dm.limb, dm.lb, dm.region, gm, step, act->solar,
             act->t_star, act->t_diff_fac, (double *)d_flux, (double *)d_bconv, (double *)d_tot, out_stride, dc.n_mu,
-            ctx->d_status);
+            ctx->d_status));
         SOAP_LAUNCHED(ctx);
         return SOAPGB_OK;
     }
@@ -286,7 +286,7 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
         if (rc) return rc;
         double *outs[3] = {d_flux, d_bconv, d_tot};
         for (int q = 0; q < 3; ++q) {
-            k_f32_widen<<<grid_for(ctx, (long long)pn, 256), 256, 0, ctx->stream>>>((long long)pn, f32 + q * pn, outs[q]);
+            SOAP_TRACED(ctx, "widen", k_f32_widen<<<grid_for(ctx, (long long)pn, 256), 256, 0, ctx->stream>>>((long long)pn, f32 + q * pn, outs[q]));
             SOAP_LAUNCHED(ctx);
         }
     } else {

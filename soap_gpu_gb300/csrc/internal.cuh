@@ -11,6 +11,12 @@
 #define SOAP_C_LIGHT 299792458.
 #define SOAP_PI 3.141592653589793238463
 
+// one traced launch: events recorded around it on the context's stream
+struct SoapTraceSpan {
+    const char *name;
+    cudaEvent_t a, b;
+};
+
 struct soapgb_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;      // stream in use
@@ -23,6 +29,10 @@ struct soapgb_ctx {
     int *d_status = nullptr;
     long long launches = 0;
     int num_sms = 0;
+    // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report
+    bool trace = false;
+    std::vector<SoapTraceSpan> spans;
+    std::vector<cudaEvent_t> ev_free;
 };
 
 namespace soapgb {
@@ -73,7 +83,24 @@ int compact_cells(soapgb_ctx *ctx, int n_lists, int cells_per_list, const double
 
 int grid_for(soapgb_ctx *ctx, long long work, int block);
 
+// Scope around a kernel launch: with tracing on, CUDA events on the context's stream
+// bracket the launch (records nothing otherwise).
+struct TraceScope {
+    soapgb_ctx *ctx;
+    const char *name;
+    cudaEvent_t a = nullptr;
+    TraceScope(soapgb_ctx *c, const char *n);
+    ~TraceScope();
+};
+
 }  // namespace soapgb
+
+// a kernel launch bracketed by trace events (the launch statement may contain commas)
+#define SOAP_TRACED(ctx, name, ...)                  \
+    do {                                             \
+        soapgb::TraceScope _soap_ts((ctx), (name)); \
+        __VA_ARGS__;                                 \
+    } while (0)
 
 // ---------------------------------------------------------------------------
 // Device helpers: the reference's expressions, written out once.

@@ -153,7 +153,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         if (f32) {
             double *dst = host ? ws.get<double>(s_rawd) : raw;
             long long tot_el = (long long)n_spec * n_eff;
-            k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(n_spec, n, n_eff, (const float *)d_raw, dst);
+            SOAP_TRACED(ctx, "widen", k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(n_spec, n, n_eff, (const float *)d_raw, dst));
             SOAP_LAUNCHED(ctx);
             if (host)
                 SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, cudaMemcpyDeviceToHost, ctx->stream));

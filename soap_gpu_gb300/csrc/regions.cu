@@ -179,8 +179,8 @@ int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const
     SOAP_CUDA(ctx, cudaMemcpyAsync(d_off, h_reg_off, ob, cudaMemcpyHostToDevice, ctx->stream));
     long long gm = (long long)grid * grid;
     dim3 g(grid_for(ctx, gm, 256), n_phase);
-    k_phase_scan<<<g, 256, 0, ctx->stream>>>(grid, 2. / grid, d_table, d_off, act->t_star, act->t_diff_spot,
-                                             act->t_diff_fac, d_temp, d_bi);
+    SOAP_TRACED(ctx, "phase_scan", k_phase_scan<<<g, 256, 0, ctx->stream>>>(grid, 2. / grid, d_table, d_off, act->t_star, act->t_diff_spot,
+                                             act->t_diff_fac, d_temp, d_bi));
     SOAP_LAUNCHED(ctx);
     // `table` lives in pageable memory: cudaMemcpyAsync has staged it before returning
     return SOAPGB_OK;

@@ -364,6 +364,29 @@ __global__ void k_conv32_params(int n, int n_eff, const double *__restrict__ lam
     live[i] = lv ? 1 : 0;
 }
 
+// the FP32 tap constants from the FP64 ones of the base convolution (same pixels,
+// same sigma): c2 = -cq log2(e), lk = log2(kq) (FP32 log2 of the rounded scale: one
+// more rounding of the weights' scale), reach from the FP32 cut
+__global__ void k_conv32_derive(int n_eff, const double *__restrict__ kq, const double *__restrict__ cq,
+                                const int2 *__restrict__ rng, int halo, float cut, float *c2, float *lk, int *live,
+                                int *rblk) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    const int2 r = rng[i];
+    const bool lv = r.x <= r.y;
+    float a = 0.f, l = -200.f;
+    if (lv) {
+        const double c = cq[i];
+        a = (float)(-c * 1.4426950408889634);
+        l = log2f((float)kq[i]);
+        const int reach = min((int)floorf(sqrtf(cut / (float)c)) + 2, halo);
+        atomicMax(&rblk[i / FC_TILE], reach);
+    }
+    c2[i] = a;
+    lk[i] = l;
+    live[i] = lv ? 1 : 0;
+}
+
 __device__ __forceinline__ float soap_ex2(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -790,7 +813,9 @@ static size_t conv_param_bytes(int n_eff) {
 size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
     size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
     b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
-    if (form != SOAPGB_PLAIN64) b += 2 * (sizeof(double) * (size_t)n_eff + 256) + conv_param_bytes(n_eff) + 256;
+    if (form != SOAPGB_PLAIN64)
+        b += 2 * (sizeof(double) * (size_t)n_eff + 256) + 2 * (conv_param_bytes(n_eff) + 256) +
+             2 * sizeof(double) * (size_t)n + 256;   // base convolutions, tap constants, staged bases
     if (form == SOAPGB_FAST32) {
         b += 2 * (sizeof(float) * (size_t)n + 256) + 2 * (sizeof(float) * (size_t)n_eff + 256);   // base32, cb32
         b += sizeof(float) * (size_t)n * n_spec + 256;                                        // FP32 spectra
@@ -819,12 +844,12 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     T *kq = (T *)param_scratch;
     T *cq = (T *)(param_scratch + ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
     int2 *rng = (int2 *)(param_scratch + 2 * ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
-    k_conv_params<T><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
-                                                                        step_exp, cut, kq, cq, rng);
+    SOAP_TRACED(ctx, "conv_params", k_conv_params<T><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
+                                                                        step_exp, cut, kq, cq, rng));
     SOAP_LAUNCHED(ctx);
     dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
-    k_conv_fast<T, SB, SrcT, OutT><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride,
-                                                                        n_spec, one_minus, halo, conv, conv_stride);
+    SOAP_TRACED(ctx, "conv64", k_conv_fast<T, SB, SrcT, OutT><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride,
+                                                                        n_spec, one_minus, halo, conv, conv_stride));
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }
@@ -834,7 +859,7 @@ static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, 
                           long long spec_stride, int n_spec, double sigma_v, int wid, double step_mult,
                           double step_exp, double cut, double sig_max, char *param_scratch, const float *b32a,
                           const float *b32b, const float *c32a, const float *c32b, int b_every, float *conv,
-                          unsigned *mm32, float *blk) {
+                          unsigned *mm32, float *blk, const char *params64) {
     constexpr int SB = 8;
     double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
     int r = (int)floor(sqrt(cut / cmin)) + 2;
@@ -852,8 +877,17 @@ static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, 
     int *rblk = (int *)(param_scratch + 3 * pb);
     const int nbx = (n + FC_TILE - 1) / FC_TILE;
     SOAP_CUDA(ctx, cudaMemsetAsync(rblk, 0, sizeof(int) * (size_t)nbx, ctx->stream));
-    k_conv32_params<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
-                                                                      step_exp, cut, c2, lk, live, rblk);
+    if (params64) {   // from the FP64 constants of the base convolution (kq, cq, ranges)
+        const size_t pb64 = (sizeof(double) * (size_t)n_eff + 255) & ~size_t(255);
+        SOAP_TRACED(ctx, "conv_params",
+                    k_conv32_derive<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(
+                        n_eff, (const double *)params64, (const double *)(params64 + pb64),
+                        (const int2 *)(params64 + 2 * pb64), halo, (float)cut, c2, lk, live, rblk));
+    } else {
+        SOAP_TRACED(ctx, "conv_params",
+                    k_conv32_params<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(
+                        n, n_eff, lam, sigma_v, wid, halo, step_mult, step_exp, cut, c2, lk, live, rblk));
+    }
     SOAP_LAUNCHED(ctx);
     const int nbatch = (n_spec + SB - 1) / SB;
     if (spec_stride % 4 == 0 && ((uintptr_t)spec & 15) == 0) {
@@ -864,14 +898,14 @@ static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, 
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32t<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
         int gy = std::max(1, std::min(nbatch, (2 * std::max(ctx->num_sms, 1) + nbx - 1) / nbx));
         dim3 g(nbx, gy);
-        k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
+        SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
-                                                              n_eff, mm32, blk, nbx, ctx->d_status);
+                                                              n_eff, mm32, blk, nbx, ctx->d_status));
     } else {
         dim3 g(nbx, nbatch);
-        k_conv32x<SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
+        SOAP_TRACED(ctx, "conv32", k_conv32x<SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                            n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv, n_eff,
-                                                           mm32, blk);
+                                                           mm32, blk));
     }
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
@@ -903,8 +937,8 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
         return set_error(ctx, SOAPGB_ERR_ARG, "FP32 spectra are accepted by the FP32 form only");
     if (form == SOAPGB_PLAIN64) {
         dim3 g(grid_for(ctx, n_eff, 256), n_spec);
-        k_conv_plain64<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_spec, spec_stride, base_a, base_b, b_every,
-                                                   sigma_v, wid, step_mult, step_exp, conv, n_eff);
+        SOAP_TRACED(ctx, "conv_plain64", k_conv_plain64<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_wave, d_spec, spec_stride, base_a, base_b, b_every,
+                                                   sigma_v, wid, step_mult, step_exp, conv, n_eff));
         SOAP_LAUNCHED(ctx);
     } else {
         // the largest sigma (sigma grows with wavelength) sets the widest reach
@@ -913,17 +947,23 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
         if (!(sig_max > 0)) return set_error(ctx, SOAPGB_ERR_ARG, "non-positive instrument sigma");
         double cut = (form == SOAPGB_FAST32) ? 30.0 : 40.0;
         int rc;
-        char *pscr = carve(p, conv_param_bytes(n_eff));   // per-pixel tap parameters (rewritten per launch)
-        if (base_a) {
+        char *pscr = carve(p, conv_param_bytes(n_eff));     // FP64 tap constants of the base convolution
+        char *pscr32 = carve(p, conv_param_bytes(n_eff));   // FP32 tap constants of the spectra's
+        if (base_a && base_b && b_every > 0) {
+            // both bases in one launch (the FP64 weights are shared): staged as rows of one array
+            double *bb = (double *)carve(p, sizeof(double) * 2 * (size_t)n);
+            double *cb = (double *)carve(p, sizeof(double) * 2 * (size_t)n_eff);
+            SOAP_CUDA(ctx, cudaMemcpyAsync(bb, base_a, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+            SOAP_CUDA(ctx, cudaMemcpyAsync(bb + n, base_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+            rc = launch_conv_fast<double, 2>(ctx, n, n_eff, d_wave, bb, n, 2, 1, sigma_v, wid, step_mult, step_exp,
+                                             40.0, cb, n_eff, sig_max, pscr);
+            if (rc) return rc;
+            cb_a = cb;
+            cb_b = cb + n_eff;
+        } else if (base_a) {
             cb_a = (double *)carve(p, sizeof(double) * (size_t)n_eff);
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult,
                                              step_exp, 40.0, cb_a, 0, sig_max, pscr);
-            if (rc) return rc;
-        }
-        if (base_b && b_every > 0) {
-            cb_b = (double *)carve(p, sizeof(double) * (size_t)n_eff);
-            rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_b, 0, 1, 1, sigma_v, wid, step_mult,
-                                             step_exp, 40.0, cb_b, 0, sig_max, pscr);
             if (rc) return rc;
         }
         if (form == SOAPGB_FAST32 && base_a) {
@@ -957,23 +997,23 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
             k_mm32_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm32, mm);
             SOAP_LAUNCHED(ctx);
             rc = launch_conv32x(ctx, n, n_eff, d_wave, spec32, spec_stride, n_spec, sigma_v, wid, step_mult, step_exp,
-                                cut, sig_max, pscr, b32a, cb_b ? b32b : b32a, c32a, cb_b ? c32b : c32a, b_every,
-                                conv32, mm32, blk);
+                                cut, sig_max, pscr32, b32a, cb_b ? b32b : b32a, c32a, cb_b ? c32b : c32a, b_every,
+                                conv32, mm32, blk, pscr);
             if (rc) return rc;
             dim3 g2(bx, n_spec);
-            k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
-                                                     b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm);
+            SOAP_TRACED(ctx, "refine64", k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
+                                                     b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm));
             SOAP_LAUNCHED(ctx);
             k_factor<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, mm, fac, d_minmax);
             SOAP_LAUNCHED(ctx);
             if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)d_out & 15) == 0) {
                 dim3 g3(grid_for(ctx, n_eff / 4, 256), n_spec);
-                k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
-                                                       out_stride);
+                SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
+                                                       out_stride));
             } else {
                 dim3 g3(grid_for(ctx, n_eff, 256), n_spec);
-                k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
-                                                      out_stride);
+                SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
+                                                      out_stride));
             }
             SOAP_LAUNCHED(ctx);
             return SOAPGB_OK;
@@ -989,14 +1029,14 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
     {
         int bx = std::max(1, std::min(64, (n + 255) / 256));
         dim3 g(bx, n_spec);
-        k_minmax<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_spec, spec_stride, base_a, base_b, b_every, conv, n_eff,
-                                             cb_a, cb_b, mm);
+        SOAP_TRACED(ctx, "minmax64", k_minmax<<<g, 256, 0, ctx->stream>>>(n, n_eff, d_spec, spec_stride, base_a, base_b, b_every, conv, n_eff,
+                                             cb_a, cb_b, mm));
         SOAP_LAUNCHED(ctx);
     }
     {
         dim3 g(grid_for(ctx, n_eff, 256), n_spec);
-        k_norm<<<g, 256, 0, ctx->stream>>>(n_eff, conv, n_eff, mm, d_out, out_stride, d_minmax,
-                                           form == SOAPGB_PLAIN64);
+        SOAP_TRACED(ctx, "norm64", k_norm<<<g, 256, 0, ctx->stream>>>(n_eff, conv, n_eff, mm, d_out, out_stride, d_minmax,
+                                           form == SOAPGB_PLAIN64));
         SOAP_LAUNCHED(ctx);
     }
     return SOAPGB_OK;
