@@ -644,6 +644,29 @@ template <typename T>
 using FirPrePlan = FirPlanSt<T, 32, 128, 128>;
 constexpr int FIR_PLAN_THREADS = 64;
 
+// Compact plan record of one (list, tile) as the plan kernel writes it: int4 header
+// (units, tasks, wrap cells, ok) at 0, then units, ut[nb + 1], woff[ntask + 1], groups and
+// wrap cells, each 8-byte aligned; records sit in slots of FirPlanSlot<T>::BYTES and are
+// copied whole (bytes = the record's size, a multiple of 16) into shared memory.
+template <typename T>
+struct FirPlanLayout {
+    int o_unit, o_ut, o_woff, o_grp, o_exc, bytes;
+    __host__ __device__ constexpr FirPlanLayout(int nb, int ntask, int etot)
+        : o_unit(16),
+          o_ut((16 + (int)sizeof(FirUnit) * nb + 7) & ~7),
+          o_woff((((16 + (int)sizeof(FirUnit) * nb + 7) & ~7) + 4 * (nb + 1) + 7) & ~7),
+          o_grp((((((16 + (int)sizeof(FirUnit) * nb + 7) & ~7) + 4 * (nb + 1) + 7) & ~7) + 4 * (ntask + 1) + 7) & ~7),
+          o_exc(0),
+          bytes(0) {
+        o_exc = (o_grp + (int)sizeof(FirGrp<T>) * ntask + 7) & ~7;
+        bytes = (o_exc + (int)sizeof(FirExcW<T>) * etot + 15) & ~15;
+    }
+};
+template <typename T>
+struct FirPlanSlot {
+    static constexpr int BYTES = FirPlanLayout<T>(FirPrePlan<T>::NU, FirPrePlan<T>::NG, FirPrePlan<T>::NE).bytes;
+};
+
 // lists of at most this many (class 0 + 1) entries have their slopes staged in shared
 // memory for the tile kernel's own searches
 template <typename T>
@@ -689,12 +712,17 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int *wsum, int &total)
     return off + inc - v;
 }
 
-// first position q in [lo, hi) with floor(dlt_q X) >= m (dlt ascending, X > 0: the
-// rounded product is monotone in dlt, so the predicate is monotone in q)
-__device__ __forceinline__ int fir_lower_bound(const double *__restrict__ dl, int lo, int hi, double X, int m) {
+// First position q in [lo, hi) with dlt_q >= theta_m, theta_m = m (1 / X) rounded: the
+// cells whose t = dlt X reaches m.  theta_m is monotone in m and the slopes ascend, so
+// the ranges of consecutive m partition the segment exactly; the comparisons run on the
+// order-preserving integer images of the doubles (no FP64 instruction per step).  A cell
+// within rounding of a boundary may be classified one group away from floor(t); its
+// weight is then within rounding of 0 or 1 and its contribution unchanged.
+__device__ __forceinline__ int fir_lower_bound(const double *__restrict__ dl, int lo, int hi, double invX, int m) {
+    const unsigned long long th = soap_ord64((double)m * invX);
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (floor(dl[mid] * X) >= (double)m)
+        if (soap_ord64(dl[mid]) >= th)
             hi = mid;
         else
             lo = mid + 1;
@@ -749,8 +777,10 @@ __device__ int fir_segments(const FirTileArgs &A, int l, int j0, int t_eff, FirS
         g.key = e.y;
         g.cls = c;
         const double d0 = dl[g.start], d1 = dl[g.end - 1];
-        g.m_lo = (int)fmin(floor(d0 * Xa), floor(d0 * Xb));
-        g.m_hi = (int)fmax(floor(d1 * Xa), floor(d1 * Xb));
+        // one more shift value on either side covers the cells the searches' thresholds
+        // classify one group away from floor(t)
+        g.m_lo = (int)fmin(floor(d0 * Xa), floor(d0 * Xb)) - 1;
+        g.m_hi = (int)fmax(floor(d1 * Xa), floor(d1 * Xb)) + 1;
         if (fmax(fabs(d0), fabs(d1)) * (double)(FIR_TILE - 1) >= 1.0) {
             atomicExch(A.status, FIR_ST_FAST);   // a weight could wrap twice in one tile
             g.m_hi = g.m_lo;
@@ -823,7 +853,7 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
                                int nunit, const double *sl, ST &st, int ub, int *wsum) {
     const int tid = threadIdx.x;
     const int n = A.n, n_eff = A.n_eff;
-    const double Xa = (double)j0 + A.los, Xb = (double)(j0 + t_eff - 1) + A.los;
+    const double iXa = 1.0 / ((double)j0 + A.los), iXb = 1.0 / ((double)(j0 + t_eff - 1) + A.los);
     const int nbu = min(ST::NU, nunit - ub);
     for (int t = tid; t < nbu; t += NT) st.unit[t] = fir_describe<T>(ub + t, segs, nsg, j0, t_eff, n, n_eff);
     __syncthreads();
@@ -853,14 +883,14 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
         if (m == d.m_lo) {
             lowA = lowB = d.start;
         } else {
-            lowA = fir_lower_bound(sl, d.start, d.end, Xa, m);
-            lowB = fir_lower_bound(sl, d.start, d.end, Xb, m);
+            lowA = fir_lower_bound(sl, d.start, d.end, iXa, m);
+            lowB = fir_lower_bound(sl, d.start, d.end, iXb, m);
         }
         if (m == d.m_hi) {
             highA = highB = d.end;
         } else {
-            highA = fir_lower_bound(sl, d.start, d.end, Xa, m + 1);
-            highB = fir_lower_bound(sl, d.start, d.end, Xb, m + 1);
+            highA = fir_lower_bound(sl, d.start, d.end, iXa, m + 1);
+            highB = fir_lower_bound(sl, d.start, d.end, iXb, m + 1);
         }
         const int rlo = max(lowA, lowB), rhi = min(highA, highB);
         FirGrp<T> gr;
@@ -936,13 +966,16 @@ __global__ void __launch_bounds__(FIR_PLAN_THREADS) k_fir_plan(const FirTileArgs
     __shared__ int nunit_sh;
     FirSeg *segs = reinterpret_cast<FirSeg *>(plan_smem + ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)));
     const int l = blockIdx.y, j0 = blockIdx.x * FIR_TILE, tid = threadIdx.x;
-    FirPrePlan<T> *out = reinterpret_cast<FirPrePlan<T> *>(const_cast<void *>(A.plan)) +
-                         ((long long)l * gridDim.x + blockIdx.x);
+    const long long tau = (long long)l * gridDim.x + blockIdx.x;
+    const long long ntot = (long long)gridDim.x * gridDim.y;
+    char *rec = reinterpret_cast<char *>(const_cast<void *>(A.plan)) + tau * FirPlanSlot<T>::BYTES;
+    int *psize = reinterpret_cast<int *>(reinterpret_cast<char *>(const_cast<void *>(A.plan)) +
+                                         ntot * FirPlanSlot<T>::BYTES);
     const int t_eff = min(FIR_TILE, A.n_eff - j0);
     if (t_eff <= 0) {
         if (tid == 0) {
-            out->ok = 1;
-            out->nunit = out->nb = out->ntask = out->etot = 0;
+            *reinterpret_cast<int4 *>(rec) = make_int4(0, 0, 0, 1);
+            psize[tau] = 16;
         }
         return;
     }
@@ -961,23 +994,23 @@ __global__ void __launch_bounds__(FIR_PLAN_THREADS) k_fir_plan(const FirTileArgs
         st.woff[0] = 0;
     }
     __syncthreads();
-    if (ok) {   // copy the used parts
-        const int nb = st.nb, ntask = st.ntask, etot = st.etot;
-        for (int i = tid; i < nb; i += FIR_PLAN_THREADS) out->unit[i] = st.unit[i];
-        for (int i = tid; i <= nb; i += FIR_PLAN_THREADS) out->ut[i] = st.ut[i];
-        for (int i = tid; i < ntask; i += FIR_PLAN_THREADS) {
-            out->grp[i] = st.grp[i];
-            out->wlo[i] = st.wlo[i];
-        }
-        for (int i = tid; i <= ntask; i += FIR_PLAN_THREADS) out->woff[i] = st.woff[i];
-        for (int i = tid; i < etot; i += FIR_PLAN_THREADS) out->excw[i] = st.excw[i];
+    const int nb = ok ? st.nb : 0, ntask = ok ? st.ntask : 0, etot = ok ? st.etot : 0;
+    const FirPlanLayout<T> L(nb, ntask, etot);
+    if (ok) {   // the used parts, compact
+        FirUnit *u = reinterpret_cast<FirUnit *>(rec + L.o_unit);
+        int *ut = reinterpret_cast<int *>(rec + L.o_ut);
+        int *wo = reinterpret_cast<int *>(rec + L.o_woff);
+        FirGrp<T> *gr = reinterpret_cast<FirGrp<T> *>(rec + L.o_grp);
+        FirExcW<T> *ex = reinterpret_cast<FirExcW<T> *>(rec + L.o_exc);
+        for (int i = tid; i < nb; i += FIR_PLAN_THREADS) u[i] = st.unit[i];
+        for (int i = tid; i <= nb; i += FIR_PLAN_THREADS) ut[i] = st.ut[i];
+        for (int i = tid; i <= ntask; i += FIR_PLAN_THREADS) wo[i] = st.woff[i];
+        for (int i = tid; i < ntask; i += FIR_PLAN_THREADS) gr[i] = st.grp[i];
+        for (int i = tid; i < etot; i += FIR_PLAN_THREADS) ex[i] = st.excw[i];
     }
     if (tid == 0) {
-        out->ok = ok;
-        out->nunit = ok ? nunit : 0;
-        out->nb = ok ? st.nb : 0;
-        out->ntask = ok ? st.ntask : 0;
-        out->etot = ok ? st.etot : 0;
+        *reinterpret_cast<int4 *>(rec) = make_int4(nb, ntask, etot, ok);
+        psize[tau] = ok ? L.bytes : 16;
     }
 }
 
@@ -1184,28 +1217,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
         }
     };
 
-    const FirPrePlan<T> *pl = (MODE == MODE_PHASE && A.plan)
-                                  ? reinterpret_cast<const FirPrePlan<T> *>(A.plan) + ((long long)l * gridDim.x + blockIdx.x)
-                                  : nullptr;
-    if (pl && pl->ok) {
-        // --- precomputed plan: copy it in, then apply ----------------------------------
-        const int nb = pl->nb, ntask = pl->ntask, etot = pl->etot;
-        for (int i = tid; i < nb; i += FIR_THREADS) st.unit[i] = pl->unit[i];
-        for (int i = tid; i <= nb; i += FIR_THREADS) st.ut[i] = pl->ut[i];
-        for (int i = tid; i < ntask; i += FIR_THREADS) {
-            st.grp[i] = pl->grp[i];
-            st.wlo[i] = pl->wlo[i];
-        }
-        for (int i = tid; i <= ntask; i += FIR_THREADS) st.woff[i] = pl->woff[i];
-        for (int i = tid; i < etot; i += FIR_THREADS) st.excw[i] = pl->excw[i];
-        if (tid == 0) {
-            st.nb = nb;
-            st.ntask = ntask;
-            st.etot = etot;
-        }
-        __syncthreads();
-        run_units(0);
-    } else {
+    {
         // --- plan the tile here, batch by batch ------------------------------------------
         const int nsg = A.nseg[2 * l] + ((MODE == MODE_PHASE) ? A.nseg[2 * l + 1] : 0);
         const int nunit = fir_segments<MODE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, &st.nunit);
@@ -1335,6 +1347,461 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
     }
 }
 
+// --- phase integration: persistent, pipelined tile kernel -------------------------------
+// true: a work unit's cube rows are staged in shared memory by TMA before it is applied;
+// false: the apply loops read them from global memory (L1-cached), with no per-unit barrier
+constexpr bool FIR_PP_STAGED = true;
+// Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
+// tiles that plan themselves, the direct cells' batch.
+template <typename T>
+struct FirPPSmem {
+    T win[2][4][FIR_WIN];
+    __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
+    unsigned long long wbar[2], pbar[2];
+    FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
+    FirExcD<T> excd[64];
+    int wsum[FIR_THREADS / 32];
+    int fail, nunit_sh;
+    // followed by FirSeg seg[2 * seg_cap] (dynamic, 16-byte aligned)
+};
+
+template <typename T>
+__host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPSmem<T>) + 15) & ~size_t(15); }
+
+// Block b walks the (phase, tile) pairs tau = b, b + G, ... (tau = phase * ntile + tile).
+// A tile's compact plan (k_fir_plan) is copied by TMA one tile ahead into the other plan
+// buffer; the cube windows of its work units stream through two buffers, and the first
+// unit of the next tile is issued while the current tile's last unit is applied, so the
+// copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
+template <typename T>
+__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int ntot) {
+    constexpr int NC = 4;
+    constexpr int SLOT = FirPlanSlot<T>::BYTES;
+    extern __shared__ __align__(128) unsigned char pp_smem[];
+    FirPPSmem<T> &sh = *reinterpret_cast<FirPPSmem<T> *>(pp_smem);
+    FirSeg *segs = reinterpret_cast<FirSeg *>(pp_smem + fir_pp_smem_fixed<T>());
+    const int tid = threadIdx.x;
+    const int G = gridDim.x;
+    const int n = A.n, n_eff = A.n_eff;
+    T *out0 = reinterpret_cast<T *>(A.out0);
+    T *out1 = reinterpret_cast<T *>(A.out1);
+    T *out2 = reinterpret_cast<T *>(A.out2);
+    const char *plans = reinterpret_cast<const char *>(A.plan);
+    const int *psize = reinterpret_cast<const int *>(plans + (size_t)ntot * SLOT);
+    if (tid == 0) {
+        mbar_init(&sh.wbar[0], 1);
+        mbar_init(&sh.wbar[1], 1);
+        mbar_init(&sh.pbar[0], 1);
+        mbar_init(&sh.pbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sh.fail = 0;
+    }
+    __syncthreads();
+
+    // (thread 0) copy the plan of tile tau (bytes long) into plan buffer b
+    auto issue_plan = [&](int tau, int b, unsigned bytes) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sh.pbar[b], bytes);
+        bulk_g2s(&sh.pb[b][0], plans + (size_t)tau * SLOT, bytes, &sh.pbar[b]);
+    };
+    // (thread 0) stage the rows of unit number u (buffer u & 1)
+    auto issue_unit = [&](int u, const FirUnit &d) {
+        const int b = u & 1;
+        unsigned bytes = 0;
+        uintptr_t rel = 0;
+        if (d.w1 > d.w0) {
+            const uintptr_t p0 = (uintptr_t)((long long)(d.key >> 1) * n + d.w0) * sizeof(T);
+            const uintptr_t p1 = (uintptr_t)((long long)(d.key >> 1) * n + d.w1) * sizeof(T);
+            rel = p0 & ~uintptr_t(15);
+            bytes = (unsigned)(((p1 + 15) & ~uintptr_t(15)) - rel);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sh.wbar[b], bytes * NC);
+        if (bytes) {
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                const char *base = reinterpret_cast<const char *>(A.cubes.c[fir_cube_index(MODE_PHASE, d.cls, q)]);
+                bulk_g2s(&sh.win[b][q][0], base + rel, bytes, &sh.wbar[b]);
+            }
+        }
+    };
+
+    Acc<T> acc[7][FIR_PIX];
+#pragma unroll
+    for (int a = 0; a < 7; ++a)
+#pragma unroll
+        for (int q = 0; q < FIR_PIX; ++q) acc[a][q].zero();
+
+    // A unit's terms are summed in plain registers (part[slot][pixel]; slots per class:
+    // spot S, Qs, As, Bs; facula S, Bf, Qf, Af) and folded into the compensated
+    // accumulators once per unit: a unit holds a few percent of a pixel's sum, so its
+    // FP32 partial carries rounding well below the compensated total's.
+    T part[4][FIR_PIX];
+    auto part_zero = [&]() {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int q = 0; q < FIR_PIX; ++q) part[a][q] = (T)0;
+    };
+    auto part_fold = [&](int cls) {
+#pragma unroll
+        for (int q = 0; q < FIR_PIX; ++q) {
+            acc[0][q].add(part[0][q]);
+            if (cls == CLS_SPOT) {
+                acc[1][q].add(part[1][q]);
+                acc[2][q].add(part[2][q]);
+                acc[3][q].add(part[3][q]);
+            } else {
+                acc[6][q].add(part[1][q]);
+                acc[4][q].add(part[2][q]);
+                acc[5][q].add(part[3][q]);
+            }
+        }
+    };
+    // source rows of a unit: staged windows (value of source pixel i at p[c][i + off]) or
+    // the cube rows in global memory (off = 0)
+    struct Src {
+        const T *p[4];
+        int off;
+        bool staged;
+    };
+    auto src_of = [&](const T (*W)[FIR_WIN], const FirUnit &d) {
+        Src sr;
+        if (FIR_PP_STAGED) {
+            for (int c = 0; c < 4; ++c) sr.p[c] = W[c];
+            sr.off = d.off - d.w0;
+            sr.staged = true;
+        } else {
+            for (int c = 0; c < 4; ++c)
+                sr.p[c] = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE_PHASE, d.cls, c)]) +
+                          (long long)(d.key >> 1) * n;
+            sr.off = 0;
+            sr.staged = false;
+        }
+        return sr;
+    };
+    // groups [t_lo, t_hi) of unit d
+    auto apply_groups = [&](const Src &sr, const FirUnit &d, const FirGrp<T> *grp, int t_lo, int t_hi, int j0,
+                            int t_eff) {
+        const int zv = d.key & 1;
+        const bool fac = (d.cls != CLS_SPOT);
+        const T *__restrict__ r0 = sr.p[0] + sr.off;
+        const T *__restrict__ r1 = sr.p[1] + sr.off;
+        const T *__restrict__ r2 = sr.p[2] + sr.off;
+        const T *__restrict__ r3 = sr.p[3] + sr.off;
+        for (int t = t_lo; t < t_hi; ++t) {
+            const FirGrp<T> gr = grp[t];
+            if (!gr.ok) continue;
+            const int m = gr.m;
+            const int jlo = max(j0, -m);
+            const int jhi = zv ? j0 + t_eff - 1 : min(j0 + t_eff - 1, n_eff - 2 - m);
+            // facula slots 2, 3 carry the (1 + LB) L weights, spot slots 2, 3 the L weights
+            const T b0 = fac ? gr.a0w : gr.a0, b1 = fac ? gr.a1w : gr.a1, bb = fac ? gr.bw : gr.b;
+#pragma unroll
+            for (int q = 0; q < FIR_PIX; ++q) {
+                const int dj = tid + q * FIR_THREADS;
+                const int j = j0 + dj;
+                if (j < jlo || j > jhi) continue;
+                const int x = j + m;
+                if (zv) {   // single tap: w == 0
+                    part[0][q] += gr.a0 * r0[x];
+                    part[1][q] += gr.a0 * r1[x];
+                    part[2][q] += b0 * r2[x];
+                    part[3][q] += b0 * r3[x];
+                    continue;
+                }
+                const T fdj = (T)dj;
+                const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
+                const T e0 = b0 - bb * fdj, e1 = b1 + bb * fdj;
+                part[0][q] += c0 * r0[x] + c1 * r0[x + 1];
+                part[1][q] += c0 * r1[x] + c1 * r1[x + 1];
+                part[2][q] += e0 * r2[x] + e1 * r2[x + 1];
+                part[3][q] += e0 * r3[x] + e1 * r3[x + 1];
+            }
+        }
+    };
+    // wrap cells exc[0, ne) of unit d (per-cell lerp; with staged rows, pixels whose owner
+    // falls outside the window read the row in global memory)
+    auto apply_exc = [&](const Src &sr, const FirUnit &d, const FirExcW<T> *exc, int ne, int j0) {
+        const int cls = d.cls;
+        const bool fac = (cls != CLS_SPOT);
+        for (int e = 0; e < ne; ++e) {
+            const FirExcW<T> xc = exc[e];
+            const T w23 = fac ? xc.w2 : xc.L;
+#pragma unroll
+            for (int q = 0; q < FIR_PIX; ++q) {
+                const int dj = tid + q * FIR_THREADS;
+                const int j = j0 + dj;
+                if (j >= n_eff) continue;
+                T wd = xc.phi + xc.dlt * (T)dj;
+                int i = xc.i0 + dj;
+                if (wd >= (T)1) { wd -= (T)1; i += 1; }
+                else if (wd < (T)0) { wd += (T)1; i -= 1; }
+                if (i < 0 || i > n_eff - 2) continue;
+                const bool inwin = !sr.staged || ((i >= d.w0) && (i + 1 < d.w1));
+                auto lv = [&](int c) -> T {
+                    T s0, s1;
+                    if (inwin) {
+                        s0 = sr.p[c][i + sr.off];
+                        s1 = sr.p[c][i + 1 + sr.off];
+                    } else {
+                        const T *rowp = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE_PHASE, cls, c)]) +
+                                        (long long)(d.key >> 1) * n;
+                        s0 = rowp[i];
+                        s1 = rowp[i + 1];
+                    }
+                    return s0 + (s1 - s0) * wd;
+                };
+                part[0][q] += xc.L * lv(0);
+                part[1][q] += xc.L * lv(1);
+                part[2][q] += w23 * lv(2);
+                part[3][q] += w23 * lv(3);
+            }
+        }
+    };
+    // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
+    auto wait_unit = [&](int u) {
+        if (!mbar_wait_bounded(&sh.wbar[u & 1], (unsigned)((u >> 1) & 1))) atomicExch(&sh.fail, 1);
+        __syncthreads();
+        return sh.fail == 0;
+    };
+
+    if (tid == 0) {
+        if (blockIdx.x < ntot) issue_plan(blockIdx.x, 0, (unsigned)psize[blockIdx.x]);
+        if (blockIdx.x + G < ntot) issue_plan(blockIdx.x + G, 1, (unsigned)psize[blockIdx.x + G]);
+    }
+    int ucount = 0;        // units staged and applied so far (window buffer ucount & 1)
+    bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
+    int k = 0;
+    int bad = 0;
+    for (int tau = blockIdx.x; tau < ntot && !bad; tau += G, ++k) {
+        const int pbuf = k & 1;
+        // size of the plan issued at the end of this tile, read early (its latency hides
+        // behind the tile's work)
+        const unsigned next_bytes = (tid == 0 && tau + 2 * G < ntot) ? (unsigned)psize[tau + 2 * G] : 0u;
+        if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1))) atomicExch(&sh.fail, 1);
+        __syncthreads();
+        if (sh.fail) {
+            bad = 1;
+            break;
+        }
+        const int l = tau / ntile, j0 = (tau - l * ntile) * FIR_TILE;
+        const int t_eff = min(FIR_TILE, n_eff - j0);
+        const long long lbase = (long long)l * A.gm;
+        const int *cn = A.counts + 4 * l;
+        const unsigned char *rec = sh.pb[pbuf];
+        const int4 hdr = *reinterpret_cast<const int4 *>(rec);
+        if (t_eff > 0 && hdr.w) {
+            // --- planned tile ------------------------------------------------------------
+            const int nb = hdr.x;
+            const FirPlanLayout<T> L(hdr.x, hdr.y, hdr.z);
+            const FirUnit *units = reinterpret_cast<const FirUnit *>(rec + L.o_unit);
+            const int *ut = reinterpret_cast<const int *>(rec + L.o_ut);
+            const int *woff = reinterpret_cast<const int *>(rec + L.o_woff);
+            const FirGrp<T> *grp = reinterpret_cast<const FirGrp<T> *>(rec + L.o_grp);
+            const FirExcW<T> *exc = reinterpret_cast<const FirExcW<T> *>(rec + L.o_exc);
+            for (int ui = 0; ui < nb; ++ui) {
+                const int u = ucount;
+                if (!FIR_PP_STAGED) {   // rows read from global memory: no staging, no barrier
+                    const FirUnit d = units[ui];
+                    const Src sr = src_of(nullptr, d);
+                    part_zero();
+                    apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
+                    const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
+                    apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
+                    part_fold(d.cls);
+                    continue;
+                }
+                if (tid == 0) {
+                    if (ui == 0 && !pre) issue_unit(u, units[0]);
+                    if (ui + 1 < nb) {
+                        issue_unit(u + 1, units[1 + ui]);
+                    } else {
+                        // last unit: issue the next tile's first unit, from its plan
+                        pre = false;
+                        const int tn = tau + G;
+                        if (tn < ntot && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
+                            const unsigned char *rn = sh.pb[pbuf ^ 1];
+                            const int4 hn = *reinterpret_cast<const int4 *>(rn);
+                            const int ln = tn / ntile, jn = (tn - ln * ntile) * FIR_TILE;
+                            if (hn.w && hn.x > 0 && jn < n_eff) {
+                                const FirPlanLayout<T> Ln(hn.x, hn.y, hn.z);
+                                issue_unit(u + 1, *reinterpret_cast<const FirUnit *>(rn + Ln.o_unit));
+                                pre = true;
+                            }
+                        }
+                    }
+                }
+                if (!wait_unit(u)) {
+                    bad = 1;
+                    break;
+                }
+                const FirUnit d = units[ui];
+                const Src sr = src_of(sh.win[u & 1], d);
+                part_zero();
+                apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
+                const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
+                apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
+                part_fold(d.cls);
+                __syncthreads();
+                ++ucount;
+            }
+        } else if (t_eff > 0) {
+            // --- tile that plans itself, batch by batch ----------------------------------
+            if (tid == 0) pre = false;
+            const int nsg = A.nseg[2 * l] + A.nseg[2 * l + 1];
+            const int nunit = fir_segments<MODE_PHASE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, &sh.nunit_sh);
+            auto &st = sh.st;
+            const double *sl = A.list_dlt + lbase;
+            for (int ub = 0; ub < nunit && !bad;) {
+                fir_plan_batch<T, MODE_PHASE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, nunit, sl, st, ub, sh.wsum);
+                const int nb = st.nb;
+                for (int ui = 0; ui < nb; ++ui) {
+                    const int u = ucount;
+                    if (tid == 0) {
+                        if (ui == 0) issue_unit(u, st.unit[0]);
+                        if (ui + 1 < nb) issue_unit(u + 1, st.unit[ui + 1]);
+                    }
+                    if (!wait_unit(u)) {
+                        bad = 1;
+                        break;
+                    }
+                    const FirUnit d = st.unit[ui];
+                    Src sr;
+                    for (int c = 0; c < 4; ++c) sr.p[c] = sh.win[u & 1][c];
+                    sr.off = d.off - d.w0;
+                    sr.staged = true;
+                    part_zero();
+                    apply_groups(sr, d, st.grp, st.ut[ui], st.ut[ui + 1], j0, t_eff);
+                    const int e_lo = st.woff[st.ut[ui]], e_hi = st.woff[st.ut[ui + 1]];
+                    for (int cb = e_lo; cb < e_hi; cb += FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS>::NE) {
+                        const int ce = min(e_hi, cb + FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS>::NE);
+                        const FirExcW<T> *ex = st.excw + cb;
+                        if (e_hi > FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS>::NE) {   // refill this chunk
+                            __syncthreads();
+                            fir_fill_exc<T, FIR_THREADS>(A, l, j0, st, cb, ce, cb);
+                            __syncthreads();
+                            ex = st.excw;
+                        }
+                        apply_exc(sr, d, ex, ce - cb, j0);
+                    }
+                    part_fold(d.cls);
+                    __syncthreads();
+                    ++ucount;
+                }
+                ub += nb;
+            }
+            if (bad) break;
+        }
+        if (bad) break;
+        // --- directly evaluated cells (spots of non-integral temperature, solar faculae)
+        if (t_eff > 0 && cn[2] > 0) {
+            const int c_start = cn[0] + cn[1], c_cnt = cn[2];
+            for (int b0 = 0; b0 < c_cnt; b0 += 64) {
+                const int nbd = min(64, c_cnt - b0);
+                if (tid < nbd) {
+                    const int cell = A.list_cell[lbase + c_start + b0 + tid];
+                    FirExcD<T> x;
+                    cell_pos<T>(j0, A.geo, A.geo32, cell, x.i0, x.phi, x.dlt, x.L, x.w2);
+                    const CellGeo &gg = A.geo[cell];
+                    x.row = gg.row;
+                    x.zero_v = gg.zero_v;
+                    x.temp = A.temp[lbase + cell];
+                    x.kind = bits_is_zero(A.bi[lbase + cell]) ? 0 : 1;
+                    sh.excd[tid] = x;
+                }
+                __syncthreads();
+                for (int e = 0; e < nbd; ++e) {
+                    const FirExcD<T> xc = sh.excd[e];
+                    const long long off = (long long)xc.row * n;
+#pragma unroll
+                    for (int q = 0; q < FIR_PIX; ++q) {
+                        const int dj = tid + q * FIR_THREADS;
+                        const int j = j0 + dj;
+                        if (j >= n_eff) continue;
+                        long long i;
+                        T w;
+                        if (xc.zero_v) {
+                            i = j;
+                            w = (T)0;
+                        } else {
+                            T wd = xc.phi + xc.dlt * (T)dj;
+                            i = (long long)xc.i0 + dj;
+                            if (wd >= (T)1) { wd -= (T)1; i += 1; }
+                            else if (wd < (T)0) { wd += (T)1; i -= 1; }
+                            if (i < 0 || i > n_eff - 2) continue;
+                            w = wd;
+                        }
+                        auto val = [&](int ci) -> T {
+                            const T *rowp = reinterpret_cast<const T *>(A.cubes.c[ci]) + off;
+                            if (xc.zero_v) return rowp[i];
+                            return rowp[i] + (rowp[i + 1] - rowp[i]) * w;
+                        };
+                        const T Lc = xc.L;
+                        acc[0][q].add(Lc * val(0));
+                        if (xc.kind == 0) {
+                            T Lq = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)(int)xc.temp));
+                            acc[1][q].add(Lq * val(1));
+                            acc[2][q].add(Lq * val(2));
+                            acc[3][q].add(Lc * val(3));
+                        } else {
+                            acc[6][q].add(Lc * val(5));
+                            T w2 = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)A.t_norm_fac));
+                            acc[4][q].add(w2 * val(1));
+                            acc[5][q].add(w2 * val(4));
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // --- outputs; accumulators reset for the next tile ---------------------------------
+#pragma unroll
+        for (int q = 0; q < FIR_PIX; ++q) {
+            const int j = j0 + tid + q * FIR_THREADS;
+            if (j < n) {
+                const long long o = (long long)l * A.out_stride + j;
+                if (j >= n_eff) {
+                    out0[o] = (T)0;
+                    out1[o] = (T)0;
+                    out2[o] = (T)0;
+                } else if constexpr (sizeof(T) == 4) {
+                    F2 S{acc[0][q].s, -acc[0][q].c}, Qs{acc[1][q].s, -acc[1][q].c}, As{acc[2][q].s, -acc[2][q].c};
+                    F2 Qf{acc[4][q].s, -acc[4][q].c}, Af{acc[5][q].s, -acc[5][q].c};
+                    float2 is2 = A.cubes.spot_sed2[j], fs2 = A.cubes.fac_sed2[j];
+                    F2 is{is2.x, is2.y}, fs{fs2.x, fs2.y};
+                    F2 fl = f2_add(f2_add(S, f2_neg(f2_mul(is, Qs))), f2_neg(f2_mul(fs, Qf)));
+                    F2 tt = f2_add(f2_add(S, f2_neg(f2_mul(is, As))), f2_neg(f2_mul(fs, Af)));
+                    F2 bc = f2_add(F2{acc[3][q].s, -acc[3][q].c}, F2{acc[6][q].s, -acc[6][q].c});
+                    out0[o] = (T)(fl.hi + fl.lo);   // flux
+                    out1[o] = (T)(bc.hi + bc.lo);   // bconv
+                    out2[o] = (T)(tt.hi + tt.lo);   // tot
+                } else {
+                    double S = acc[0][q].get(), Qs = acc[1][q].get(), As = acc[2][q].get(), Bs = acc[3][q].get();
+                    double Qf = acc[4][q].get(), Af = acc[5][q].get(), Bf = acc[6][q].get();
+                    double is = A.cubes.spot_sed[j], fs = A.cubes.fac_sed[j];
+                    out0[o] = (T)(S - is * Qs - fs * Qf);
+                    out1[o] = (T)(Bs + Bf);
+                    out2[o] = (T)(S - is * As - fs * Af);
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 7; ++a) acc[a][q].zero();
+        }
+        __syncthreads();   // plan buffer pbuf free
+        if (tid == 0 && tau + 2 * G < ntot) issue_plan(tau + 2 * G, pbuf, next_bytes);
+    }
+    if (bad && tid == 0) {
+        // a copy did not land in time: record it and give the copies possibly in flight a
+        // bounded wait before leaving
+        atomicExch(A.status, FIR_ST_WAIT);
+        mbar_wait_bounded(&sh.wbar[ucount & 1], (unsigned)((ucount >> 1) & 1));
+        mbar_wait_bounded(&sh.wbar[(ucount + 1) & 1], (unsigned)(((ucount + 1) >> 1) & 1));
+        mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1));
+        mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1387,7 +1854,8 @@ FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_l
     const size_t ntile = ((size_t)n + FIR_TILE - 1) / FIR_TILE;
     if (ncube == 6)
         sz[FirLayout::PLAN] = ntile * n_lists *
-                              ((form == SOAPGB_FAST32) ? sizeof(FirPrePlan<float>) : sizeof(FirPrePlan<double>));
+                              ((form == SOAPGB_FAST32) ? (size_t)FirPlanSlot<float>::BYTES + sizeof(int)
+                                                       : (size_t)FirPlanSlot<double>::BYTES + sizeof(int));
     size_t t = 0;
     for (int s = 0; s < FirLayout::NSLOT; ++s) {
         L.off[s] = t;
@@ -1507,11 +1975,22 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.plan = nullptr;
     const int ntile = (n + FIR_TILE - 1) / FIR_TILE;
     if constexpr (MODE == MODE_PHASE) {
+        // plans of every (phase, tile), then the persistent tile kernel
         A.plan = ws + L.off[FirLayout::PLAN];
         size_t smem_p = ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)) + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_plan<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
         SOAP_TRACED(ctx, "fir_plan", k_fir_plan<T><<<dim3(ntile, n_lists), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
         SOAP_LAUNCHED(ctx);
+        const int ntot = ntile * n_lists;
+        size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+        int per_sm = 0;
+        SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fir_pp<T>, FIR_THREADS, smem_t));
+        const int nblk = std::max(1, std::min(ntot, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
+        SOAP_TRACED(ctx, "fir_tile_phase",
+                    k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, ntot));
+        SOAP_LAUNCHED(ctx);
+        return SOAPGB_OK;
     }
     size_t smem = fir_smem_fixed<T, NC>() + sizeof(FirSeg) * (size_t)(MODE == MODE_PHASE ? 2 : 1) * L.seg_cap;
     SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir<T, MODE, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

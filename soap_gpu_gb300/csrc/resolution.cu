@@ -44,6 +44,12 @@ static double host_rndup(double n, int nb_decimal) {
     return n;
 }
 
+// Delta_lambda(sigma_v, lambda) / lambda (SOAP_initialize.cu:55-66 without the factor lambda)
+static double soap_sigma_per_lambda(double sigma_v) {
+    double beta = sigma_v / SOAP_C_LIGHT;
+    return -1 * (1 - sqrt((1 + beta) / (1 - beta)));
+}
+
 namespace soapgb {
 int conv_halfwidth(double wave0, double wave1, double sigma_v, double window) {
     double wavelength_step = wave1 - wave0;
@@ -97,18 +103,22 @@ __global__ void __launch_bounds__(256) k_conv_plain64(int n, int n_eff, const do
 // exponent coefficient cq = step_exp^2 / (2 s^2), significant tap range [dlo, dhi]
 // (dhi < dlo marks a pixel outside the reference's convolution interior)
 template <typename T>
-__global__ void k_conv_params(int n, int n_eff, const double *__restrict__ lam, double sigma_v, int wid, int halo,
-                              double step_mult, double step_exp, double cut, T *kq, T *cq, int2 *rng) {
+__global__ void k_conv_params(int n, int n_eff, const double *__restrict__ lam, double ka, double kb, double kr,
+                              int wid, int halo, T *kq, T *cq, int2 *rng) {
+    // sigma_i = lambda_i (sqrt((1 + b)/(1 - b)) - 1) is proportional to lambda_i, so with
+    // ka = step_mult / (s1 sqrt(2 pi)), kb = step_exp^2 / (2 s1^2), kr = sqrt(cut / kb)
+    // (s1 = sigma at lambda = 1): kq = ka / lambda, cq = kb / lambda^2, reach = kr lambda
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_eff) return;
     bool live = (i > wid) && (i + wid < n - 1);
     double k = 0.0, c = 0.0;
     int lo = 0, hi = -1;
     if (live) {
-        double sig = soap_delta_lambda(sigma_v, lam[i]);
-        k = step_mult / (sig * sqrt(2. * SOAP_PI));
-        c = step_exp * step_exp / (2.0 * sig * sig);
-        int r = (int)floor(sqrt(cut / c));
+        const double l = lam[i];
+        const double inv = 1.0 / l;
+        k = ka * inv;
+        c = kb * inv * inv;
+        int r = (int)floor(kr * l);
         lo = max(max(-wid, -r), -halo);
         hi = min(min(wid - 2, r), halo);
     }
@@ -347,21 +357,25 @@ __global__ void k_mm32_init(int n_spec, double sentinel, unsigned *mm32, unsigne
 __global__ void k_conv32_params(int n, int n_eff, const double *__restrict__ lam, double sigma_v, int wid, int halo,
                                 double step_mult, double step_exp, double cut, float *c2, float *lk, int *live,
                                 int *rblk) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_eff) return;
-    bool lv = (i > wid) && (i + wid < n - 1);
-    double a = 0.0, l = -200.0;
-    if (lv) {
-        double sig = soap_delta_lambda(sigma_v, lam[i]);
-        double cq = step_exp * step_exp / (2.0 * sig * sig);
-        a = -cq * 1.4426950408889634;   // log2(e)
-        l = log2(step_mult / (sig * sqrt(2. * SOAP_PI)));
-        int r = min((int)floor(sqrt(cut / cq)) + 1, halo);
-        atomicMax(&rblk[i / FC_TILE], r);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int reach = 0;
+    if (i < n_eff) {
+        bool lv = (i > wid) && (i + wid < n - 1);
+        double a = 0.0, l = -200.0;
+        if (lv) {
+            double sig = soap_delta_lambda(sigma_v, lam[i]);
+            double cq = step_exp * step_exp / (2.0 * sig * sig);
+            a = -cq * 1.4426950408889634;   // log2(e)
+            l = log2(step_mult / (sig * sqrt(2. * SOAP_PI)));
+            reach = min((int)floor(sqrt(cut / cq)) + 1, halo);
+        }
+        c2[i] = (float)a;
+        lk[i] = (float)l;
+        live[i] = lv ? 1 : 0;
     }
-    c2[i] = (float)a;
-    lk[i] = (float)l;
-    live[i] = lv ? 1 : 0;
+    // a warp's pixels share one block of 1024: one atomic per warp
+    reach = __reduce_max_sync(0xffffffffu, reach);
+    if ((threadIdx.x & 31) == 0 && reach > 0) atomicMax(&rblk[(blockIdx.x * blockDim.x) / FC_TILE], reach);
 }
 
 // the FP32 tap constants from the FP64 ones of the base convolution (same pixels,
@@ -370,21 +384,25 @@ __global__ void k_conv32_params(int n, int n_eff, const double *__restrict__ lam
 __global__ void k_conv32_derive(int n_eff, const double *__restrict__ kq, const double *__restrict__ cq,
                                 const int2 *__restrict__ rng, int halo, float cut, float *c2, float *lk, int *live,
                                 int *rblk) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_eff) return;
-    const int2 r = rng[i];
-    const bool lv = r.x <= r.y;
-    float a = 0.f, l = -200.f;
-    if (lv) {
-        const double c = cq[i];
-        a = (float)(-c * 1.4426950408889634);
-        l = log2f((float)kq[i]);
-        const int reach = min((int)floorf(sqrtf(cut / (float)c)) + 2, halo);
-        atomicMax(&rblk[i / FC_TILE], reach);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int reach = 0;
+    if (i < n_eff) {
+        const int2 r = rng[i];
+        const bool lv = r.x <= r.y;
+        float a = 0.f, l = -200.f;
+        if (lv) {
+            const double c = cq[i];
+            a = (float)(-c * 1.4426950408889634);
+            l = log2f((float)kq[i]);
+            reach = min((int)floorf(sqrtf(cut / (float)c)) + 1, halo);
+        }
+        c2[i] = a;
+        lk[i] = l;
+        live[i] = lv ? 1 : 0;
     }
-    c2[i] = a;
-    lk[i] = l;
-    live[i] = lv ? 1 : 0;
+    // a warp's pixels share one block of 1024: one atomic per warp
+    reach = __reduce_max_sync(0xffffffffu, reach);
+    if ((threadIdx.x & 31) == 0 && reach > 0) atomicMax(&rblk[(blockIdx.x * blockDim.x) / FC_TILE], reach);
 }
 
 __device__ __forceinline__ float soap_ex2(float x) {
@@ -844,8 +862,12 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     T *kq = (T *)param_scratch;
     T *cq = (T *)(param_scratch + ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
     int2 *rng = (int2 *)(param_scratch + 2 * ((sizeof(T) * (size_t)n_eff + 255) & ~size_t(255)));
-    SOAP_TRACED(ctx, "conv_params", k_conv_params<T><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, sigma_v, wid, halo, step_mult,
-                                                                        step_exp, cut, kq, cq, rng));
+    const double s1 = soap_sigma_per_lambda(sigma_v);
+    const double ka = step_mult / (s1 * sqrt(2. * SOAP_PI)), kb = step_exp * step_exp / (2.0 * s1 * s1);
+    const double kr = sqrt(cut / kb);
+    SOAP_TRACED(ctx, "conv_params",
+                k_conv_params<T><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, ka, kb, kr, wid,
+                                                                                    halo, kq, cq, rng));
     SOAP_LAUNCHED(ctx);
     dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
     SOAP_TRACED(ctx, "conv64", k_conv_fast<T, SB, SrcT, OutT><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, kq, cq, rng, spec, spec_stride,
