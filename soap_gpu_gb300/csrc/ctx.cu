@@ -102,6 +102,16 @@ TraceScope::~TraceScope() {
     ctx->spans.push_back(SoapTraceSpan{name, a, b});
 }
 
+int copy_resources(soapgb_ctx *ctx, int count) {
+    if (!ctx->copy_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while ((int)ctx->sync_events.size() < count) {
+        cudaEvent_t e = nullptr;
+        SOAP_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->sync_events.push_back(e);
+    }
+    return SOAPGB_OK;
+}
+
 int grid_for(soapgb_ctx *ctx, long long work, int block) {
     long long g = (work + block - 1) / block;
     if (g < 1) g = 1;
@@ -198,6 +208,11 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
         cudaEventDestroy(sp.b);
     }
     for (auto e : ctx->ev_free) cudaEventDestroy(e);
+    for (auto e : ctx->sync_events) cudaEventDestroy(e);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

@@ -1374,7 +1374,8 @@ __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPS
 // unit of the next tile is issued while the current tile's last unit is applied, so the
 // copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
 template <typename T>
-__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int ntot) {
+__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int tau0, int ntot,
+                                                        int ntot_all) {
     constexpr int NC = 4;
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
     extern __shared__ __align__(128) unsigned char pp_smem[];
@@ -1387,7 +1388,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     T *out1 = reinterpret_cast<T *>(A.out1);
     T *out2 = reinterpret_cast<T *>(A.out2);
     const char *plans = reinterpret_cast<const char *>(A.plan);
-    const int *psize = reinterpret_cast<const int *>(plans + (size_t)ntot * SLOT);
+    const int *psize = reinterpret_cast<const int *>(plans + (size_t)ntot_all * SLOT);
     if (tid == 0) {
         mbar_init(&sh.wbar[0], 1);
         mbar_init(&sh.wbar[1], 1);
@@ -1566,15 +1567,17 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         return sh.fail == 0;
     };
 
+    // tiles tau in [tau0, ntot)
     if (tid == 0) {
-        if (blockIdx.x < ntot) issue_plan(blockIdx.x, 0, (unsigned)psize[blockIdx.x]);
-        if (blockIdx.x + G < ntot) issue_plan(blockIdx.x + G, 1, (unsigned)psize[blockIdx.x + G]);
+        const int t0 = tau0 + (int)blockIdx.x;
+        if (t0 < ntot) issue_plan(t0, 0, (unsigned)psize[t0]);
+        if (t0 + G < ntot) issue_plan(t0 + G, 1, (unsigned)psize[t0 + G]);
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount & 1)
     bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
     int k = 0;
     int bad = 0;
-    for (int tau = blockIdx.x; tau < ntot && !bad; tau += G, ++k) {
+    for (int tau = tau0 + (int)blockIdx.x; tau < ntot && !bad; tau += G, ++k) {
         const int pbuf = k & 1;
         // size of the plan issued at the end of this tile, read early (its latency hides
         // behind the tile's work)
@@ -1877,8 +1880,10 @@ FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase,
 static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
                        const double *limb, const double *lb, const int *region, int n_mu, CellGeo *geo,
                        CellGeo32 *geo32, double *lambda0) {
-    SOAP_CUDA(ctx, cudaMemcpyAsync(lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!(*lambda0 > 0.0)) {   // not given by the caller: read it from the device
+        SOAP_CUDA(ctx, cudaMemcpyAsync(lambda0, wave, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     k_check_uniform<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, wave, step, ctx->d_status);
     SOAP_LAUNCHED(ctx);
     SOAP_TRACED(ctx, "cell_geo", k_cell_geo<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(gm, delta, limb, lb, region, n_mu, *lambda0, step, geo,
@@ -1943,8 +1948,10 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
 template <typename T, int MODE, typename OutT>
 static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
                         double los, const FirCubes &fc, const double *temp, const double *bi, long long gm, int solar,
-                        int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists) {
+                        int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists,
+                        int stage = 7, int l0 = 0, int l1 = -1) {
     constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
+    if (l1 < 0) l1 = n_lists;
     FirTileArgs A;
     A.n = n;
     A.n_eff = n_eff;
@@ -1975,21 +1982,28 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.plan = nullptr;
     const int ntile = (n + FIR_TILE - 1) / FIR_TILE;
     if constexpr (MODE == MODE_PHASE) {
-        // plans of every (phase, tile), then the persistent tile kernel
+        // plans of every (phase, tile) (stage 1), then the persistent tile kernel over the
+        // phases [l0, l1) (stage 4)
         A.plan = ws + L.off[FirLayout::PLAN];
-        size_t smem_p = ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)) + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
-        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_plan<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
-        SOAP_TRACED(ctx, "fir_plan", k_fir_plan<T><<<dim3(ntile, n_lists), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
-        SOAP_LAUNCHED(ctx);
-        const int ntot = ntile * n_lists;
-        size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
-        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
-        int per_sm = 0;
-        SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fir_pp<T>, FIR_THREADS, smem_t));
-        const int nblk = std::max(1, std::min(ntot, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
-        SOAP_TRACED(ctx, "fir_tile_phase",
-                    k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, ntot));
-        SOAP_LAUNCHED(ctx);
+        if (stage & 1) {
+            size_t smem_p = ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)) + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
+            SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_plan<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+            SOAP_TRACED(ctx, "fir_plan",
+                        k_fir_plan<T><<<dim3(ntile, n_lists), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
+            SOAP_LAUNCHED(ctx);
+        }
+        if ((stage & 4) && l1 > l0) {
+            const int tau0 = ntile * l0, ntot = ntile * l1, nrun = ntot - tau0;
+            size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
+            SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+            int per_sm = 0;
+            SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fir_pp<T>, FIR_THREADS, smem_t));
+            const int nblk = std::max(1, std::min(nrun, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
+            SOAP_TRACED(ctx, "fir_tile_phase",
+                        k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, tau0, ntot,
+                                                                                ntile * n_lists));
+            SOAP_LAUNCHED(ctx);
+        }
         return SOAPGB_OK;
     }
     size_t smem = fir_smem_fixed<T, NC>() + sizeof(FirSeg) * (size_t)(MODE == MODE_PHASE ? 2 : 1) * L.seg_cap;
@@ -2046,42 +2060,50 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     char *ws = scratch;
     CellGeo *geo = (CellGeo *)(ws + L.off[FirLayout::GEO]);
     CellGeo32 *geo32 = (CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
-    double lambda0 = 0.0;
-    int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32,
-                         &lambda0);
-    if (rc) return rc;
-    rc = fir_lists(ctx, L, ws, a.gm, a.n_phase, a.temp, a.bi, a.act->solar);
-    if (rc) return rc;
-    const soapgb_cubes &c = *a.cubes;
-    // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
-    const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
-    const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
-    FirCubes fc{};
-    for (int q = 0; q < 6; ++q) {
-        void *dst = ws + L.off[FirLayout::CUBE0 + q];
-        if (tsz == 4)
-            SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst));
-        else
-            SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst));
-        SOAP_LAUNCHED(ctx);
-        fc.c[q] = dst;
+    double lambda0 = a.lambda0;
+    if (a.stage & FIR_STAGE_GEOMETRY) {
+        int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32,
+                             &lambda0);
+        if (rc) return rc;
+        rc = fir_lists(ctx, L, ws, a.gm, a.n_phase, a.temp, a.bi, a.act->solar);
+        if (rc) return rc;
+    } else if (!(lambda0 > 0.0)) {
+        return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: the run stage alone needs lambda0");
     }
+    const soapgb_cubes &c = *a.cubes;
+    FirCubes fc{};
+    for (int q = 0; q < 6; ++q) fc.c[q] = ws + L.off[FirLayout::CUBE0 + q];
     fc.spot_sed = c.spot_sed;
     fc.fac_sed = c.fac_sed;
+    fc.spot_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2A]);
+    fc.fac_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2B]);
+    if (a.stage & FIR_STAGE_CUBES) {
+        // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
+        const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
+        const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
+        for (int q = 0; q < 6; ++q) {
+            void *dst = const_cast<void *>(fc.c[q]);
+            if (tsz == 4)
+                SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst));
+            else
+                SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst));
+            SOAP_LAUNCHED(ctx);
+        }
+        if (form == SOAPGB_FAST32) {
+            k_pair_rows<<<grid_for(ctx, a.n, 256), 256, 0, ctx->stream>>>(a.n, c.spot_sed, c.fac_sed,
+                                                                          (float2 *)fc.spot_sed2, (float2 *)fc.fac_sed2);
+            SOAP_LAUNCHED(ctx);
+        }
+    }
     const int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
     const double los = lambda0 / a.step;
-    if (form == SOAPGB_FAST32) {
-        float2 *sed2a = (float2 *)(ws + L.off[FirLayout::SED2A]);
-        float2 *sed2b = (float2 *)(ws + L.off[FirLayout::SED2B]);
-        k_pair_rows<<<grid_for(ctx, a.n, 256), 256, 0, ctx->stream>>>(a.n, c.spot_sed, c.fac_sed, sed2a, sed2b);
-        SOAP_LAUNCHED(ctx);
-        fc.spot_sed2 = sed2a;
-        fc.fac_sed2 = sed2b;
+    const int st = (a.stage & FIR_STAGE_GEOMETRY ? 1 : 0) | (a.stage & FIR_STAGE_RUN ? 4 : 0);
+    const int l1 = (a.l1 < 0) ? a.n_phase : a.l1;
+    if (form == SOAPGB_FAST32)
         return launch_tiles<float, MODE_PHASE, float>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
                                                       a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
-                                                      a.n_phase);
-    }
+                                                      a.n_phase, st, a.l0, l1);
     return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
                                                     a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
-                                                    a.n_phase);
+                                                    a.n_phase, st, a.l0, l1);
 }

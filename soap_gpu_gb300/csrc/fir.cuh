@@ -39,7 +39,14 @@ struct FirPhaseArgs {
     void *flux, *bconv, *tot;   // n_phase x n: float (FAST32) or double (FAST64)
     int out_f32;
     long long out_stride;       // distance between phases in the outputs
+    // staged use (a pipeline that overlaps chunks of phases with their copies):
+    // FIR_STAGE_GEOMETRY builds the cell order, lists and tile plans of all phases,
+    // FIR_STAGE_CUBES the typed cube copies, FIR_STAGE_RUN integrates phases [l0, l1)
+    int stage = 7;
+    int l0 = 0, l1 = -1;        // l1 < 0: all phases
+    double lambda0 = 0.0;       // wave[0] when known on the host (0: read from the device)
 };
+enum { FIR_STAGE_GEOMETRY = 1, FIR_STAGE_CUBES = 2, FIR_STAGE_RUN = 4 };
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);
 

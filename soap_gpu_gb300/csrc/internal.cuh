@@ -29,6 +29,9 @@ struct soapgb_ctx {
     int *d_status = nullptr;
     long long launches = 0;
     int num_sms = 0;
+    // second stream for copies that overlap kernels (created on first use) and events
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> sync_events;
     // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report
     bool trace = false;
     std::vector<SoapTraceSpan> spans;
@@ -82,6 +85,9 @@ int compact_cells(soapgb_ctx *ctx, int n_lists, int cells_per_list, const double
                   double lo, double hi, int key_stride, int *idx_out, int *count_out);
 
 int grid_for(soapgb_ctx *ctx, long long work, int block);
+
+// the context's copy stream and at least `count` synchronisation events (created once)
+int copy_resources(soapgb_ctx *ctx, int count);
 
 // Scope around a kernel launch: with tracing on, CUDA events on the context's stream
 // bracket the launch (records nothing otherwise).

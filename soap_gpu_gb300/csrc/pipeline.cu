@@ -5,6 +5,7 @@
 // float64 file per phase and type (SOAP_integration.cu:802-817 ->
 // SOAP_resolution.cu:398-412).  Here the deficits stay in device memory and all
 // phases go through each stage in one launch.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -105,19 +106,44 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
     int rc = ws.commit();
     if (rc) return rc;
+    // Host buffers with the FP32 form: the phases run in chunks, each chunk's spectra
+    // copied back on the copy stream while the next chunk is computed; the cubes are
+    // copied in on the copy stream while the geometry (maps, lists, plans) is built.
+    const bool chunked = host && form == SOAPGB_FAST32 && n_phase >= 2;
+    int n_chunk = 1, per_chunk = n_phase;
+    cudaStream_t cube_stream = ctx->stream;
+    if (chunked) {
+        n_chunk = std::min(n_phase, 8);
+        per_chunk = (n_phase + n_chunk - 1) / n_chunk;
+        n_chunk = (n_phase + per_chunk - 1) / per_chunk;
+        rc = copy_resources(ctx, n_chunk + 2);
+        if (rc) return rc;
+        // the copy stream starts after the work already queued on the main stream
+        SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[0], ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->sync_events[0], 0));
+        cube_stream = ctx->copy_stream;
+    }
 #define STAGE(dst, src, bytes, slot)                                               \
     dst = (decltype(dst))stage_in(ctx, mem, src, bytes, ws.get<void>(slot), &rc); \
     if (rc) return rc;
+#define STAGE_ON(stream, dst, src, bytes, slot)                                                       \
+    if (host) {                                                                                       \
+        SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<void>(slot), src, bytes, cudaMemcpyHostToDevice, stream)); \
+        dst = (decltype(dst))ws.get<void>(slot);                                                      \
+    } else {                                                                                          \
+        dst = (decltype(dst))(src);                                                                   \
+    }
     const double *d_wave;
     STAGE(d_wave, wave, sizeof(double) * n, s_wave);
     soapgb_cubes dc;
     dc.n_mu = n_mu;
-    STAGE(dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
-    STAGE(dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
-    STAGE(dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
-    STAGE(dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
-    STAGE(dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
-    STAGE(dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
+    STAGE_ON(cube_stream, dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
+    STAGE_ON(cube_stream, dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
+    STAGE_ON(cube_stream, dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
+    STAGE_ON(cube_stream, dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
+    STAGE_ON(cube_stream, dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
+    STAGE_ON(cube_stream, dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
+    if (chunked) SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[1], ctx->copy_stream));
     soapgb_maps dm;
     const double *cd;
     STAGE(cd, maps->delta, sizeof(double) * gm, s_m[0]);
@@ -134,6 +160,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     STAGE(d_qs, quiet_sed, sizeof(double) * n, s_qs);
     STAGE(d_qn, quiet_norm, sizeof(double) * n, s_qn);
 #undef STAGE
+#undef STAGE_ON
     char *d_raw = ws.get<char>(s_raw);
     int f32 = (form == SOAPGB_FAST32);
     double *d_temp = ws.get<double>(s_temp), *d_bi = ws.get<double>(s_bi);
@@ -141,6 +168,67 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp, d_bi,
                            ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
     if (rc) return rc;
+    if (chunked) {
+        FirPhaseArgs fa;
+        fa.n = n;
+        fa.n_eff = n_eff;
+        fa.wave = d_wave;
+        fa.cubes = &dc;
+        fa.n_phase = n_phase;
+        fa.temp = d_temp;
+        fa.bi = d_bi;
+        fa.delta = dm.delta;
+        fa.limb = dm.limb;
+        fa.lb = dm.lb;
+        fa.region = dm.region;
+        fa.gm = gm;
+        fa.step = step;
+        fa.act = act;
+        fa.flux = d_raw + esz * n;
+        fa.bconv = d_raw + esz * 2 * n;
+        fa.tot = d_raw;
+        fa.out_f32 = 1;
+        fa.out_stride = 3LL * n;
+        fa.lambda0 = w3[0];
+        fa.stage = FIR_STAGE_GEOMETRY;
+        rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+        if (rc) return rc;
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->sync_events[1], 0));   // cubes in
+        fa.stage = FIR_STAGE_CUBES;
+        rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+        if (rc) return rc;
+        Res32 R;
+        rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3, sigma_v,
+                                  50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
+        if (rc) return rc;
+        for (int c = 0; c < n_chunk; ++c) {
+            const int p0 = c * per_chunk, p1 = std::min(n_phase, p0 + per_chunk);
+            fa.stage = FIR_STAGE_RUN;
+            fa.l0 = p0;
+            fa.l1 = p1;
+            rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+            if (rc) return rc;
+            rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr);
+            if (rc) return rc;
+            cudaEvent_t ev = ctx->sync_events[2 + c];
+            SOAP_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
+            SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
+            const size_t off = (size_t)3 * p0 * n_eff, cnt = (size_t)3 * (p1 - p0) * n_eff;
+            SOAP_CUDA(ctx, cudaMemcpyAsync(lower + off, d_lower + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
+                                           ctx->copy_stream));
+        }
+        if (raw) {
+            double *dst = ws.get<double>(s_rawd);
+            long long tot_el = (long long)n_spec * n_eff;
+            SOAP_TRACED(ctx, "widen", k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(
+                                          n_spec, n, n_eff, (const float *)d_raw, dst));
+            SOAP_LAUNCHED(ctx);
+            SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return check_status(ctx, "soapgb_phase_pipeline");
+    }
     // deficits in [phase][tot, flux, bconv][n]
     rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act,
                           d_raw + esz * n /* flux */, d_raw + esz * 2 * n /* bconv */, d_raw /* tot */, f32, 3LL * n,

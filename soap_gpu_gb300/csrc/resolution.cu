@@ -876,22 +876,16 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     return SOAPGB_OK;
 }
 
-// FAST32 convolution of the spectra fused with the first extrema pass (k_conv32x)
-static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const float *spec,
-                          long long spec_stride, int n_spec, double sigma_v, int wid, double step_mult,
-                          double step_exp, double cut, double sig_max, char *param_scratch, const float *b32a,
-                          const float *b32b, const float *c32a, const float *c32b, int b_every, float *conv,
-                          unsigned *mm32, float *blk, const char *params64) {
-    constexpr int SB = 8;
+// FP32 tap constants (from the FP64 ones of the base convolution when given) and the
+// reach of every block of 1024 pixels; returns the staging halo
+static int conv32_params(soapgb_ctx *ctx, int n, int n_eff, const double *lam, double sigma_v, int wid,
+                         double step_mult, double step_exp, double cut, double sig_max, char *param_scratch,
+                         const char *params64, int *halo_out) {
     double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
     int r = (int)floor(sqrt(cut / cmin)) + 2;
     int halo = std::min(wid, r);
     if (halo < 1) halo = 1;
-    const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
-    size_t smem = sizeof(float) * (size_t)SB * win;
-    if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
-    if (smem > 48 * 1024)
-        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32x<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    *halo_out = halo;
     const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
     float *c2 = (float *)param_scratch;
     float *lk = (float *)(param_scratch + pb);
@@ -911,6 +905,22 @@ static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, 
                         n, n_eff, lam, sigma_v, wid, halo, step_mult, step_exp, cut, c2, lk, live, rblk));
     }
     SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+// FAST32 convolution of n_spec spectra fused with the first extrema pass (k_conv32t
+// with TMA staging for 16-byte aligned rows, else k_conv32x); tap constants from
+// conv32_params
+static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, const char *param_scratch,
+                      const float *spec, long long spec_stride, int n_spec, const float *b32a, const float *b32b,
+                      const float *c32a, const float *c32b, int b_every, float *conv, unsigned *mm32, float *blk) {
+    constexpr int SB = 8;
+    const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
+    const float *c2 = (const float *)param_scratch;
+    const float *lk = (const float *)(param_scratch + pb);
+    const int *live = (const int *)(param_scratch + 2 * pb);
+    const int *rblk = (const int *)(param_scratch + 3 * pb);
+    const int nbx = (n + FC_TILE - 1) / FC_TILE;
     const int nbatch = (n_spec + SB - 1) / SB;
     if (spec_stride % 4 == 0 && ((uintptr_t)spec & 15) == 0) {
         // TMA staging, double buffered: a block keeps its tile over several spectrum batches
@@ -924,6 +934,11 @@ static int launch_conv32x(soapgb_ctx *ctx, int n, int n_eff, const double *lam, 
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
                                                               n_eff, mm32, blk, nbx, ctx->d_status));
     } else {
+        const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
+        size_t smem = sizeof(float) * (size_t)SB * win;
+        if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
+        if (smem > 48 * 1024)
+            SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32x<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 g(nbx, nbatch);
         SOAP_TRACED(ctx, "conv32", k_conv32x<SB><<<g, FC_THREADS, smem, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                            n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv, n_eff,
@@ -944,11 +959,142 @@ static char *carve(char *&p, size_t bytes) {
     return r;
 }
 
+int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
+                         double wave1, double wave_last, const double *base_a, const double *base_b, int b_every,
+                         double sigma_v, double window, double step_mult, double step_exp, double sentinel,
+                         char *scratch, Res32 &R) {
+    if (!base_a) return set_error(ctx, SOAPGB_ERR_ARG, "FP32 resolution needs a base spectrum");
+    const int wid = conv_halfwidth(wave0, wave1, sigma_v, window);
+    char *p = scratch;
+    R.n = n;
+    R.n_eff = n_eff;
+    R.n_spec = n_spec;
+    R.wid = wid;
+    R.b_every = b_every;
+    R.sentinel = sentinel;
+    R.base_a = base_a;
+    R.base_b = (base_b && b_every > 0) ? base_b : nullptr;
+    R.conv32 = (float *)carve(p, sizeof(double) * (size_t)n_eff * n_spec);
+    R.mm = (unsigned long long *)carve(p, sizeof(unsigned long long) * 2 * n_spec);
+    // the largest sigma (sigma grows with wavelength) sets the widest reach
+    const double lmax = std::max(std::fabs(wave0), std::fabs(wave_last)) * 1.001;
+    const double sig_max = -1 * lmax * (1 - sqrt((1 + sigma_v / SOAP_C_LIGHT) / (1 - sigma_v / SOAP_C_LIGHT)));
+    if (!(sig_max > 0)) return set_error(ctx, SOAPGB_ERR_ARG, "non-positive instrument sigma");
+    char *pscr = carve(p, conv_param_bytes(n_eff));     // FP64 tap constants of the base convolution
+    char *pscr32 = carve(p, conv_param_bytes(n_eff));   // FP32 tap constants of the spectra's
+    int rc;
+    double *cb_a, *cb_b = nullptr;
+    if (R.base_b) {
+        // both bases in one launch (the FP64 weights are shared): staged as rows of one array
+        double *bb = (double *)carve(p, sizeof(double) * 2 * (size_t)n);
+        double *cb = (double *)carve(p, sizeof(double) * 2 * (size_t)n_eff);
+        SOAP_CUDA(ctx, cudaMemcpyAsync(bb, base_a, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(bb + n, base_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        rc = launch_conv_fast<double, 2>(ctx, n, n_eff, d_wave, bb, n, 2, 1, sigma_v, wid, step_mult, step_exp, 40.0,
+                                         cb, n_eff, sig_max, pscr);
+        if (rc) return rc;
+        cb_a = cb;
+        cb_b = cb + n_eff;
+    } else {
+        cb_a = (double *)carve(p, sizeof(double) * (size_t)n_eff);
+        rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult, step_exp,
+                                         40.0, cb_a, 0, sig_max, pscr);
+        if (rc) return rc;
+    }
+    R.cb_a = cb_a;
+    R.cb_b = cb_b;
+    float *b32a = (float *)carve(p, sizeof(float) * (size_t)n);
+    float *b32b = (float *)carve(p, sizeof(float) * (size_t)n);
+    float *c32a = (float *)carve(p, sizeof(float) * (size_t)n_eff);
+    float *c32b = (float *)carve(p, sizeof(float) * (size_t)n_eff);
+    R.mm32 = (unsigned *)carve(p, 16 * (size_t)n_spec);
+    R.fac = (float *)carve(p, 4 * (size_t)n_spec);
+    R.nbx = (n + FC_TILE - 1) / FC_TILE;   // extrema blocks of 1024 pixels
+    R.blk = (float *)carve(p, sizeof(float) * 2 * (size_t)R.nbx * n_spec);
+    k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_a, cb_a, b32a, c32a);
+    SOAP_LAUNCHED(ctx);
+    if (cb_b) {
+        k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_b, cb_b, b32b, c32b);
+        SOAP_LAUNCHED(ctx);
+    }
+    R.b32a = b32a;
+    R.b32b = cb_b ? b32b : b32a;
+    R.c32a = c32a;
+    R.c32b = cb_b ? c32b : c32a;
+    rc = conv32_params(ctx, n, n_eff, d_wave, sigma_v, wid, step_mult, step_exp, 30.0, sig_max, pscr32, pscr,
+                       &R.halo);
+    if (rc) return rc;
+    R.p32 = pscr32;
+    R.next = p;
+    return SOAPGB_OK;
+}
+
+int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
+                     double *d_out, long long out_stride, double *d_minmax) {
+    const int ns = s1 - s0;
+    if (ns <= 0) return SOAPGB_OK;
+    if (R.b_every > 0 && s0 % R.b_every != 0)
+        return set_error(ctx, SOAPGB_ERR_ARG, "resolution chunk must start at a multiple of %d spectra", R.b_every);
+    const int n = R.n, n_eff = R.n_eff;
+    const float *sp = spec32 + (long long)s0 * spec_stride;
+    float *conv = R.conv32 + (long long)s0 * n_eff;
+    unsigned *mm32 = R.mm32 + 4LL * s0;
+    unsigned long long *mm = R.mm + 2LL * s0;
+    float *fac = R.fac + s0;
+    float *blk = R.blk + 2LL * R.nbx * s0;
+    k_mm32_init<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, R.sentinel, mm32, mm);
+    SOAP_LAUNCHED(ctx);
+    int rc = conv32_run(ctx, n, n_eff, R.wid, R.halo, R.p32, sp, spec_stride, ns, R.b32a, R.b32b, R.c32a, R.c32b,
+                        R.b_every, conv, mm32, blk);
+    if (rc) return rc;
+    dim3 g2(R.nbx, ns);
+    SOAP_TRACED(ctx, "refine64",
+                k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, sp, spec_stride, R.base_a, R.base_b, R.cb_a,
+                                                         R.cb_b, R.b32a, R.b32b, R.c32a, R.c32b, R.b_every, conv,
+                                                         n_eff, mm32, blk, mm));
+    SOAP_LAUNCHED(ctx);
+    k_factor<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, mm, fac, d_minmax ? d_minmax + 2LL * s0 : nullptr);
+    SOAP_LAUNCHED(ctx);
+    double *out = d_out + (long long)s0 * out_stride;
+    if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)out & 15) == 0) {
+        dim3 g3(grid_for(ctx, n_eff / 4, 256), ns);
+        SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
+                                                                           n_eff, fac, out, out_stride));
+    } else {
+        dim3 g3(grid_for(ctx, n_eff, 256), ns);
+        SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
+                                                                          n_eff, fac, out, out_stride));
+    }
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
 int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
                       double wave1, double wave_last, const void *d_spec_v, int spec_f32, long long spec_stride,
                       const double *base_a, const double *base_b, int b_every, double sigma_v, double window,
                       double step_mult, double step_exp, double sentinel, double *d_out, long long out_stride,
                       double *d_minmax, char *scratch) {
+    if (form == SOAPGB_FAST32 && base_a) {
+        // ---- FP32 pipe throughout, exact FP64 normalisation constants ----------------
+        Res32 R;
+        int rc = resolution32_prepare(ctx, n, n_eff, n_spec, d_wave, wave0, wave1, wave_last, base_a, base_b,
+                                      b_every, sigma_v, window, step_mult, step_exp, sentinel, scratch, R);
+        if (rc) return rc;
+        const float *spec32 = (const float *)d_spec_v;
+        if (!spec_f32) {
+            char *p = R.next;
+            float *tmp = (float *)carve(p, sizeof(float) * (size_t)n * n_spec);
+            const double *ds = (const double *)d_spec_v;
+            for (int q = 0; q < n_spec; ++q) {
+                k_f64_to_f32<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ds + (long long)q * spec_stride,
+                                                                            tmp + (long long)q * n);
+                SOAP_LAUNCHED(ctx);
+            }
+            spec32 = tmp;
+            spec_stride = n;
+        }
+        return resolution32_run(ctx, R, spec32, spec_stride, 0, n_spec, d_out, out_stride, d_minmax);
+    }
     int wid = conv_halfwidth(wave0, wave1, sigma_v, window);
     char *p = scratch;
     double *conv = (double *)carve(p, sizeof(double) * (size_t)n_eff * n_spec);
@@ -987,58 +1133,6 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
             rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult,
                                              step_exp, 40.0, cb_a, 0, sig_max, pscr);
             if (rc) return rc;
-        }
-        if (form == SOAPGB_FAST32 && base_a) {
-            // ---- FP32 pipe throughout, exact FP64 normalisation constants ------------
-            const float *spec32 = (const float *)d_spec_v;
-            if (!spec_f32) {
-                float *tmp = (float *)carve(p, sizeof(float) * (size_t)n * n_spec);
-                for (int q = 0; q < n_spec; ++q) {
-                    k_f64_to_f32<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, d_spec + (long long)q * spec_stride,
-                                                                                tmp + (long long)q * n);
-                    SOAP_LAUNCHED(ctx);
-                }
-                spec32 = tmp;
-                spec_stride = n;
-            }
-            float *b32a = (float *)carve(p, sizeof(float) * (size_t)n);
-            float *b32b = (float *)carve(p, sizeof(float) * (size_t)n);
-            float *c32a = (float *)carve(p, sizeof(float) * (size_t)n_eff);
-            float *c32b = (float *)carve(p, sizeof(float) * (size_t)n_eff);
-            unsigned *mm32 = (unsigned *)carve(p, 16 * (size_t)n_spec);
-            float *fac = (float *)carve(p, 4 * (size_t)n_spec);
-            const int bx = (n + FC_TILE - 1) / FC_TILE;   // extrema blocks of 1024 pixels
-            float *blk = (float *)carve(p, sizeof(float) * 2 * (size_t)bx * n_spec);
-            k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_a, cb_a, b32a, c32a);
-            SOAP_LAUNCHED(ctx);
-            if (cb_b) {
-                k_base_prep<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_eff, base_b, cb_b, b32b, c32b);
-                SOAP_LAUNCHED(ctx);
-            }
-            float *conv32 = (float *)conv;
-            k_mm32_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm32, mm);
-            SOAP_LAUNCHED(ctx);
-            rc = launch_conv32x(ctx, n, n_eff, d_wave, spec32, spec_stride, n_spec, sigma_v, wid, step_mult, step_exp,
-                                cut, sig_max, pscr32, b32a, cb_b ? b32b : b32a, c32a, cb_b ? c32b : c32a, b_every,
-                                conv32, mm32, blk, pscr);
-            if (rc) return rc;
-            dim3 g2(bx, n_spec);
-            SOAP_TRACED(ctx, "refine64", k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, spec32, spec_stride, base_a, base_b, cb_a, cb_b, b32a,
-                                                     b32b, c32a, c32b, b_every, conv32, n_eff, mm32, blk, mm));
-            SOAP_LAUNCHED(ctx);
-            k_factor<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, mm, fac, d_minmax);
-            SOAP_LAUNCHED(ctx);
-            if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)d_out & 15) == 0) {
-                dim3 g3(grid_for(ctx, n_eff / 4, 256), n_spec);
-                SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
-                                                       out_stride));
-            } else {
-                dim3 g3(grid_for(ctx, n_eff, 256), n_spec);
-                SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, c32a, c32b, b_every, conv32, n_eff, fac, d_out,
-                                                      out_stride));
-            }
-            SOAP_LAUNCHED(ctx);
-            return SOAPGB_OK;
         }
         // FAST64, or no base (the whole (1 - A) is convolved): FP64
         rc = launch_conv_fast<double, 4>(ctx, n, n_eff, d_wave, d_spec, spec_stride, n_spec, base_a ? 0 : 1,

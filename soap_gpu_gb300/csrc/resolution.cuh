@@ -14,4 +14,27 @@ int resolution_device(soapgb_ctx *ctx, int form, int n, int n_eff, int n_spec, c
                       const double *base_a, const double *base_b, int b_every, double sigma_v, double window,
                       double step_mult, double step_exp, double sentinel, double *d_out, long long out_stride,
                       double *d_minmax, char *scratch);
+
+// The FP32 form in two steps, for callers that run the spectra in chunks: prepare
+// convolves the base spectra and sets up the per-spectrum state of all n_spec spectra in
+// scratch; run convolves and normalises spectra [s0, s1) (s0 a multiple of b_every) of
+// the FP32 rows spec32 into d_out rows [s0, s1).
+struct Res32 {
+    int n, n_eff, n_spec, wid, halo, nbx, b_every;
+    double sentinel;
+    const double *base_a, *base_b, *cb_a, *cb_b;
+    const float *b32a, *b32b, *c32a, *c32b;
+    const char *p32;
+    float *conv32;
+    unsigned *mm32;
+    unsigned long long *mm;
+    float *fac, *blk;
+    char *next;   // first scratch byte after the state
+};
+int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
+                         double wave1, double wave_last, const double *base_a, const double *base_b, int b_every,
+                         double sigma_v, double window, double step_mult, double step_exp, double sentinel,
+                         char *scratch, Res32 &R);
+int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
+                     double *d_out, long long out_stride, double *d_minmax);
 }  // namespace soapgb

@@ -1,0 +1,79 @@
+"""The composite per-phase pipeline (soapgb_phase_pipeline): maps -> integration ->
+convolution / normalisation in one call, against the separate stage calls, and its
+host-buffer path (phases in chunks, copies overlapping the next chunk) against its
+device-buffer path."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from soap_gpu_gb300 import synth
+from soap_gpu_gb300._lib import Star
+
+from _cases import activity, cubes, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _star(case, lb):
+    return Star(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                (ctypes.c_double * 4)(*lb))
+
+
+@pytest.fixture(scope="module")
+def setup(ctx):
+    case = synth.small_case(seed=11, grid=48, n=8300, n_phase=10, n_mu=6)
+    inp = synth.generate(case)
+    n_eff = (case.n // 512) * 512
+    maps = ctx.disk_maps(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                         inp.mu_boundary, inp.lb)
+    cb = cubes(inp)
+    cb["spot_sed"] = inp.spot_sed[0]
+    cb["fac_sed"] = inp.fac_sed[0]
+    act = activity(case)
+    regions = [case.regions for _ in case.phases]
+    return case, inp, n_eff, maps, cb, act, regions
+
+
+@pytest.mark.parametrize("form,tol", [("fast32", 2e-6), ("plain64", 1e-12)])
+def test_pipeline_matches_stages(ctx, setup, form, tol):
+    case, inp, n_eff, maps, cb, act, regions = setup
+    q_norm = ctx.quiet_disk(form, inp.wave, inp.q_norm, n_eff, maps, case.grid, case.step)
+    q_sed = ctx.quiet_disk(form, inp.wave, inp.q_sed, n_eff, maps, case.grid, case.step)
+    low, raw = ctx.phase_pipeline(form, inp.wave, n_eff, _star(case, inp.lb), maps, cb, case.step, act,
+                                  case.phases, regions, q_sed, q_norm, case.sigma_v, conv_step=case.step,
+                                  want_raw=True)
+    temp, bi = ctx.phase_maps(case.grid, case.incl, case.phases, regions, act)
+    flux, bconv, tot = ctx.phase_integrate(form, inp.wave, n_eff, case.grid, temp, bi, maps, cb, case.step, act)
+    assert np.sum(bi >= 0) > 0, "no active cell in the test case"
+    for k, spec in enumerate((tot, flux, bconv)):
+        for p in range(case.n_phase):
+            scale = max(np.max(np.abs(spec[p])), 1e-300)
+            assert rel_err(raw[p, k], spec[p, :n_eff], scale) <= tol
+    base = (q_sed, q_sed, q_norm)
+    for k, spec in enumerate((tot, flux, bconv)):
+        ref, _ = ctx.lower_resolution(form, inp.wave, spec, n_eff, case.sigma_v, base=base[k],
+                                      step_mult=case.step, step_exp=case.step)
+        assert rel_err(low[:, k], ref) <= tol
+
+
+def test_pipeline_host_chunks_equal_device(ctx, setup):
+    """The host path runs the phases in chunks with the copies on a second stream; every
+    kernel computes the same values as in the device path's single pass."""
+    torch = pytest.importorskip("torch")
+    case, inp, n_eff, maps, cb, act, regions = setup
+    q_norm = ctx.quiet_disk("fast32", inp.wave, inp.q_norm, n_eff, maps, case.grid, case.step)
+    q_sed = ctx.quiet_disk("fast32", inp.wave, inp.q_sed, n_eff, maps, case.grid, case.step)
+    star = _star(case, inp.lb)
+    low_h, raw_h = ctx.phase_pipeline("fast32", inp.wave, n_eff, star, maps, cb, case.step, act, case.phases,
+                                      regions, q_sed, q_norm, case.sigma_v, conv_step=case.step, want_raw=True)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda:0")
+    maps_d = {k: dev(v) for k, v in maps.items()}
+    cb_d = {k: dev(v) for k, v in cb.items()}
+    low_d, raw_d = ctx.phase_pipeline("fast32", dev(inp.wave), n_eff, star, maps_d, cb_d, case.step, act,
+                                      dev(case.phases), regions, dev(q_sed), dev(q_norm), case.sigma_v,
+                                      conv_step=case.step, want_raw=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(low_h, low_d.cpu().numpy())
+    assert np.array_equal(raw_h, raw_d.cpu().numpy())
+    assert np.all(np.isfinite(low_h)) and np.any(low_h != 1.0)
