@@ -85,10 +85,12 @@ static cudaEvent_t trace_event(soapgb_ctx *ctx) {
     return e;
 }
 
-TraceScope::TraceScope(soapgb_ctx *c, const char *n) : ctx(c), name(n) {
+TraceScope::TraceScope(soapgb_ctx *c, const char *n) : TraceScope(c, n, c ? c->stream : nullptr) {}
+
+TraceScope::TraceScope(soapgb_ctx *c, const char *n, cudaStream_t s) : ctx(c), name(n), stream(s) {
     if (!ctx || !ctx->trace) return;
     a = trace_event(ctx);
-    if (a) cudaEventRecord(a, ctx->stream);
+    if (a) cudaEventRecord(a, stream);
 }
 
 TraceScope::~TraceScope() {
@@ -98,7 +100,7 @@ TraceScope::~TraceScope() {
         ctx->ev_free.push_back(a);
         return;
     }
-    cudaEventRecord(b, ctx->stream);
+    cudaEventRecord(b, stream);
     ctx->spans.push_back(SoapTraceSpan{name, a, b});
 }
 

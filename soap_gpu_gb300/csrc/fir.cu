@@ -29,6 +29,7 @@
 #include <cmath>
 
 #include "fir.cuh"
+#include "regions.cuh"
 
 using namespace soapgb;
 
@@ -151,20 +152,28 @@ __device__ __forceinline__ bool bits_is_integral(double v) {
 // variant).  counts[l] = (n0, n1, n2, 0); class c occupies positions
 // [n0 + .. + n_{c-1}, + n_c) of the list.  Active cells are those whose type map value
 // lies in [-0.5, 1.5] (0 spot, otherwise facula), as in the per-cell form's compaction.
+// class of a visible cell of temperature t and type b (-1: not active)
+__device__ __forceinline__ int fir_class_tb(const CellGeo &g, double t, double b, int solar) {
+    if (!(g.L > -998.0)) return -1;
+    if (!(b >= -0.5 && b <= 1.5)) return -1;
+    if (bits_is_zero(b)) return bits_is_integral(t) ? CLS_SPOT : CLS_DIRECT;
+    return solar ? CLS_DIRECT : CLS_FAC;
+}
+
 __device__ __forceinline__ int fir_class(const CellGeo &g, const double *bi, const double *temp, long long idx,
                                          int solar) {
     if (!(g.L > -998.0)) return -1;
     if (!bi) return CLS_SPOT;
-    double b = bi[idx];
+    const double b = bi[idx];
     if (!(b >= -0.5 && b <= 1.5)) return -1;
-    if (bits_is_zero(b)) return bits_is_integral(temp[idx]) ? CLS_SPOT : CLS_DIRECT;
-    return solar ? CLS_DIRECT : CLS_FAC;
+    return fir_class_tb(g, bits_is_zero(b) ? temp[idx] : 0.0, b, solar);
 }
 
 __global__ void __launch_bounds__(1024) k_fir_lists(long long gm, const int *__restrict__ order,
                                                     const CellGeo *__restrict__ geo, const double *__restrict__ temp,
                                                     const double *__restrict__ bi, int solar, int *list_cell,
-                                                    double *list_dlt, int *counts, int only_flagged) {
+                                                    double *list_dlt, double2 *list_aux, int *counts,
+                                                    int only_flagged) {
     const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (only_flagged && counts[4 * l + 3] == 0) return;   // list already built by k_fir_plists
     const int nw = blockDim.x >> 5;
@@ -218,6 +227,7 @@ __global__ void __launch_bounds__(1024) k_fir_lists(long long gm, const int *__r
             for (int w = 0; w < warp; ++w) pos += wc[w][c];
             list_cell[mbase + pos] = cell;
             list_dlt[mbase + pos] = d;
+            if (c == CLS_DIRECT) list_aux[mbase + pos] = make_double2(temp[mbase + cell], bi[mbase + cell]);
         }
         __syncthreads();
         if (tid < 3) {
@@ -245,7 +255,8 @@ constexpr int FIR_PLIST_CAP = 4096;
 __global__ void __launch_bounds__(512) k_fir_plists(long long gm, const int *__restrict__ order,
                                                    const int *__restrict__ rank, const CellGeo *__restrict__ geo,
                                                    const double *__restrict__ temp, const double *__restrict__ bi,
-                                                   int solar, int *list_cell, double *list_dlt, int *counts) {
+                                                   int solar, int *list_cell, double *list_dlt, double2 *list_aux,
+                                                   int *counts) {
     __shared__ unsigned keys[FIR_PLIST_CAP];
     __shared__ int cnt[4];
     const int l = blockIdx.x, tid = threadIdx.x;
@@ -291,6 +302,7 @@ __global__ void __launch_bounds__(512) k_fir_plists(long long gm, const int *__r
         const int cell = order[keys[i] & 0xffffffu];
         list_cell[mbase + i] = cell;
         list_dlt[mbase + i] = geo[cell].dlt;
+        if ((int)(keys[i] >> 24) == CLS_DIRECT) list_aux[mbase + i] = make_double2(temp[mbase + cell], bi[mbase + cell]);
     }
     if (tid == 0) {
         int *o = counts + 4 * l;
@@ -300,6 +312,102 @@ __global__ void __launch_bounds__(512) k_fir_plists(long long gm, const int *__r
         o[3] = 0;
     }
 }
+
+// Phase lists without maps (the pipeline's collapsed forms): one block per phase visits
+// the cells of its regions' bounding boxes only -- a few thousand of the G*G -- and
+// keeps a cell in the box of the region that sets its final value (the last covering
+// one, region_cell_value), so every active cell is found once.  The active cells are
+// marked in three bitmaps over the velocity order (one per class) in shared memory; an
+// ordered compaction of the bitmaps gives the same lists as k_fir_lists / k_fir_plists
+// on the maps of k_phase_scan, with no sort and no G*G map per phase.
+constexpr int FIR_BLIST_THREADS = 512;
+constexpr size_t FIR_BLIST_SMEM_MAX = 180 * 1024;
+
+__global__ void __launch_bounds__(FIR_BLIST_THREADS)
+    k_fir_blists(int grid, double delta_grid, const RegionPhase *__restrict__ table, const int *__restrict__ reg_off,
+                 int t_star, int t_diff_spot, int t_diff_fac, int solar, const int *__restrict__ order,
+                 const int *__restrict__ rank, const CellGeo *__restrict__ geo, int *list_cell, double *list_dlt,
+                 double2 *list_aux, int *counts) {
+    extern __shared__ unsigned bm[];   // [class][W] bitmaps over the velocity order
+    __shared__ int wsum[FIR_BLIST_THREADS / 32];
+    __shared__ int ctot[3];
+    const long long gm = (long long)grid * grid;
+    const int W = (int)((gm + 31) >> 5);
+    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long mbase = (long long)l * gm;
+    for (int i = tid; i < 3 * W; i += FIR_BLIST_THREADS) bm[i] = 0u;
+    if (tid < 3) ctot[tid] = 0;
+    __syncthreads();
+    const int r0 = reg_off[l], r1 = reg_off[l + 1];
+    for (int r = r0; r < r1; ++r) {
+        const RegionPhase rp = table[r];
+        const int by = rp.iy1 - rp.iy0, bz = rp.iz1 - rp.iz0;
+        if (!rp.visible || by <= 0 || bz <= 0) continue;
+        const int nbox = by * bz;
+        for (int q = tid; q < nbox; q += FIR_BLIST_THREADS) {
+            const int iy = rp.iy0 + q / bz, iz = rp.iz0 + q % bz;
+            double t, b;
+            if (region_cell_value(table, r0, r1, iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b) != r)
+                continue;
+            const int k = iy * grid + iz;
+            const int c = fir_class_tb(geo[k], t, b, solar);
+            if (c < 0) continue;
+            const int rk = rank[k];
+            atomicOr(&bm[c * W + (rk >> 5)], 1u << (rk & 31));
+        }
+    }
+    __syncthreads();
+    // ordered compaction: thread tid owns words [w0, w1) of the concatenated bitmaps
+    const int nw3 = 3 * W;
+    const int per = (nw3 + FIR_BLIST_THREADS - 1) / FIR_BLIST_THREADS;
+    const int w0 = min(nw3, tid * per), w1 = min(nw3, w0 + per);
+    int my = 0, myc[3] = {0, 0, 0};
+    for (int w = w0; w < w1; ++w) {
+        const int pc = __popc(bm[w]);
+        my += pc;
+        myc[w / W] += pc;
+    }
+    int inc = my;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    for (int c = 0; c < 3; ++c)
+        if (myc[c]) atomicAdd(&ctot[c], myc[c]);
+    __syncthreads();
+    int pos = inc - my;
+    for (int w = 0; w < warp; ++w) pos += wsum[w];
+    for (int w = w0; w < w1; ++w) {
+        unsigned m = bm[w];
+        const int c = w / W, wr = w - c * W;
+        while (m) {
+            const int bit = __ffs(m) - 1;
+            m &= m - 1;
+            const int cell = order[wr * 32 + bit];
+            list_cell[mbase + pos] = cell;
+            list_dlt[mbase + pos] = geo[cell].dlt;
+            if (c == CLS_DIRECT) {
+                double t, b;
+                region_cell_value(table, r0, r1, cell / grid, cell % grid, delta_grid, t_star, t_diff_spot,
+                                  t_diff_fac, t, b);
+                list_aux[mbase + pos] = make_double2(t, b);
+            }
+            ++pos;
+        }
+    }
+    if (tid == 0) {
+        int *o = counts + 4 * l;
+        o[0] = ctot[0];
+        o[1] = ctot[1];
+        o[2] = ctot[2];
+        o[3] = 0;
+    }
+}
+
+static size_t fir_blists_smem(long long gm) { return sizeof(unsigned) * 3 * (size_t)((gm + 31) >> 5); }
+
+long long fir_box_lists_max_gm() { return (long long)(FIR_BLIST_SMEM_MAX / (3 * sizeof(unsigned))) * 32; }
 
 // --- prefix sums and segments -------------------------------------------------------
 template <int NV>
@@ -745,7 +853,7 @@ struct FirTileArgs {
     int seg_cap;
     const CellGeo *geo;
     const CellGeo32 *geo32;
-    const double *temp, *bi;    // [l][gm] (phase)
+    const double2 *list_aux;    // [l][gm]: (temperature, type) of the directly evaluated entries
     long long gm;
     int solar, t_norm_fac;
     void *out0, *out1, *out2;
@@ -1260,8 +1368,9 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
                 const CellGeo &gg = A.geo[cell];
                 x.row = gg.row;
                 x.zero_v = gg.zero_v;
-                x.temp = A.temp[lbase + cell];
-                x.kind = bits_is_zero(A.bi[lbase + cell]) ? 0 : 1;
+                const double2 ax = A.list_aux[lbase + c_start + b0 + tid];
+                x.temp = ax.x;
+                x.kind = bits_is_zero(ax.y) ? 0 : 1;
                 sh.excd[tid] = x;
             }
             __syncthreads();
@@ -1709,8 +1818,9 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     const CellGeo &gg = A.geo[cell];
                     x.row = gg.row;
                     x.zero_v = gg.zero_v;
-                    x.temp = A.temp[lbase + cell];
-                    x.kind = bits_is_zero(A.bi[lbase + cell]) ? 0 : 1;
+                    const double2 ax = A.list_aux[lbase + c_start + b0 + tid];
+                    x.temp = ax.x;
+                    x.kind = bits_is_zero(ax.y) ? 0 : 1;
                     sh.excd[tid] = x;
                 }
                 __syncthreads();
@@ -1823,8 +1933,8 @@ namespace {
 // workspace layout of the FAST forms
 struct FirLayout {
     enum {
-        GEO, GEO32, CUBE0, SED2A = CUBE0 + 6, SED2B, K1A, K1B, K2A, K2B, VA, VB, SORT_TMP, LCELL, LDLT, COUNTS,
-        PRE, SEGS, NSEG, PLAN, NSLOT
+        GEO, GEO32, CUBE0, SED2A = CUBE0 + 6, SED2B, K1A, K1B, K2A, K2B, VA, VB, SORT_TMP, LCELL, LDLT, LAUX,
+        COUNTS, PRE, SEGS, NSEG, PLAN, NSLOT
     };
     size_t off[NSLOT] = {0};
     size_t total = 0;
@@ -1846,6 +1956,7 @@ FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_l
     sz[FirLayout::SORT_TMP] = soapgb::fir_sort_temp_bytes(gm);
     sz[FirLayout::LCELL] = sizeof(int) * (size_t)gm * n_lists;
     sz[FirLayout::LDLT] = sizeof(double) * (size_t)gm * n_lists;
+    sz[FirLayout::LAUX] = (ncube == 6) ? sizeof(double2) * (size_t)gm * n_lists : 0;
     sz[FirLayout::COUNTS] = sizeof(int) * 4 * (size_t)n_lists;
     L.pre_stride = gm + 2;
     L.pre_comp = L.pre_stride * n_lists;
@@ -1894,7 +2005,7 @@ static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double st
 
 // velocity-ordered cell lists, prefix sums and segments for n_lists lists
 static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm, int n_lists, const double *temp,
-                     const double *bi, int solar) {
+                     const double *bi, int solar, const FirPhaseArgs *boxes = nullptr) {
     const CellGeo *geo = (const CellGeo *)(ws + L.off[FirLayout::GEO]);
     auto *k1a = (unsigned long long *)(ws + L.off[FirLayout::K1A]);
     auto *k1b = (unsigned long long *)(ws + L.off[FirLayout::K1B]);
@@ -1922,18 +2033,34 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
     if (rc) return rc;
     int *lcell = (int *)(ws + L.off[FirLayout::LCELL]);
     double *ldlt = (double *)(ws + L.off[FirLayout::LDLT]);
+    double2 *laux = (double2 *)(ws + L.off[FirLayout::LAUX]);
     int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
-    if (bi && gm < (1LL << 24)) {
+    if (boxes) {
+        // phases without maps: lists from the region boxes
+        if (gm > fir_box_lists_max_gm())
+            return set_error(ctx, SOAPGB_ERR_ARG, "box lists: grid of %lld cells above %lld", gm, fir_box_lists_max_gm());
+        int *rank = vb;   // free after the second sort
+        SOAP_TRACED(ctx, "fir_rank", k_fir_rank<<<g, 256, 0, ctx->stream>>>(gm, va, rank));
+        SOAP_LAUNCHED(ctx);
+        const size_t smem = fir_blists_smem(gm);
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_blists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const soapgb_activity *act = boxes->act;
+        SOAP_TRACED(ctx, "fir_lists",
+                    k_fir_blists<<<n_lists, FIR_BLIST_THREADS, smem, ctx->stream>>>(
+                        boxes->grid, 2. / boxes->grid, boxes->table, boxes->reg_off, act->t_star, act->t_diff_spot,
+                        act->t_diff_fac, solar, va, rank, geo, lcell, ldlt, laux, counts));
+        SOAP_LAUNCHED(ctx);
+    } else if (bi && gm < (1LL << 24)) {
         // phases: short lists by a per-phase sort of the active cells, the rest by a scan
         int *rank = vb;   // free after the second sort
         SOAP_TRACED(ctx, "fir_rank", k_fir_rank<<<g, 256, 0, ctx->stream>>>(gm, va, rank));
         SOAP_LAUNCHED(ctx);
-        SOAP_TRACED(ctx, "fir_lists", k_fir_plists<<<n_lists, 512, 0, ctx->stream>>>(gm, va, rank, geo, temp, bi, solar, lcell, ldlt, counts));
+        SOAP_TRACED(ctx, "fir_lists", k_fir_plists<<<n_lists, 512, 0, ctx->stream>>>(gm, va, rank, geo, temp, bi, solar, lcell, ldlt, laux, counts));
         SOAP_LAUNCHED(ctx);
-        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 1));
+        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, laux, counts, 1));
         SOAP_LAUNCHED(ctx);
     } else {
-        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, counts, 0));
+        SOAP_TRACED(ctx, "fir_lists_scan", k_fir_lists<<<n_lists, 1024, 0, ctx->stream>>>(gm, va, geo, temp, bi, solar, lcell, ldlt, laux, counts, 0));
         SOAP_LAUNCHED(ctx);
     }
     double *pre = (double *)(ws + L.off[FirLayout::PRE]);
@@ -1947,7 +2074,7 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
 
 template <typename T, int MODE, typename OutT>
 static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
-                        double los, const FirCubes &fc, const double *temp, const double *bi, long long gm, int solar,
+                        double los, const FirCubes &fc, long long gm, int solar,
                         int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists,
                         int stage = 7, int l0 = 0, int l1 = -1) {
     constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
@@ -1969,8 +2096,7 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.seg_cap = L.seg_cap;
     A.geo = (const CellGeo *)(ws + L.off[FirLayout::GEO]);
     A.geo32 = (const CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
-    A.temp = temp;
-    A.bi = bi;
+    A.list_aux = (const double2 *)(ws + L.off[FirLayout::LAUX]);
     A.gm = gm;
     A.solar = solar;
     A.t_norm_fac = t_norm_fac;
@@ -2038,12 +2164,12 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     if (form == SOAPGB_FAST32) {
         SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube));
         SOAP_LAUNCHED(ctx);
-        return launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr,
+        return launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc,
                                                        gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
     }
     SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (double *)cube));
     SOAP_LAUNCHED(ctx);
-    return launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, nullptr, nullptr, gm,
+    return launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, gm,
                                                     0, 0, a.out, nullptr, nullptr, 0, 1);
 }
 
@@ -2065,7 +2191,8 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, a.gm, a.delta, a.limb, a.lb, a.region, n_mu, geo, geo32,
                              &lambda0);
         if (rc) return rc;
-        rc = fir_lists(ctx, L, ws, a.gm, a.n_phase, a.temp, a.bi, a.act->solar);
+        if (!a.bi && !a.table) return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: neither maps nor a region table");
+        rc = fir_lists(ctx, L, ws, a.gm, a.n_phase, a.temp, a.bi, a.act->solar, a.bi ? nullptr : &a);
         if (rc) return rc;
     } else if (!(lambda0 > 0.0)) {
         return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: the run stage alone needs lambda0");
@@ -2100,10 +2227,10 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     const int st = (a.stage & FIR_STAGE_GEOMETRY ? 1 : 0) | (a.stage & FIR_STAGE_RUN ? 4 : 0);
     const int l1 = (a.l1 < 0) ? a.n_phase : a.l1;
     if (form == SOAPGB_FAST32)
-        return launch_tiles<float, MODE_PHASE, float>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
+        return launch_tiles<float, MODE_PHASE, float>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.gm,
                                                       a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
                                                       a.n_phase, st, a.l0, l1);
-    return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.temp, a.bi, a.gm,
+    return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.gm,
                                                     a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
                                                     a.n_phase, st, a.l0, l1);
 }

@@ -2,6 +2,8 @@
 #pragma once
 #include "internal.cuh"
 
+struct RegionPhase;
+
 struct FirPlanSizes {
     size_t bytes = 0;
 };
@@ -30,7 +32,12 @@ struct FirPhaseArgs {
     const double *wave;
     const soapgb_cubes *cubes;  // device pointers, FP64
     int n_phase;
-    const double *temp, *bi;    // n_phase x G*G
+    const double *temp = nullptr, *bi = nullptr;   // n_phase x G*G maps, or null with `table`
+    // without maps: the region table of the phases (regions.cuh); the lists are built
+    // from the regions' bounding boxes (grids of at most fir_box_lists_max_gm() cells)
+    const RegionPhase *table = nullptr;
+    const int *reg_off = nullptr;   // n_phase + 1 (device)
+    int grid = 0;
     const double *delta, *limb, *lb;
     const int *region;
     long long gm;               // G*G
@@ -49,6 +56,8 @@ struct FirPhaseArgs {
 enum { FIR_STAGE_GEOMETRY = 1, FIR_STAGE_CUBES = 2, FIR_STAGE_RUN = 4 };
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);
+// largest G*G whose phase lists can be built from the region boxes
+long long fir_box_lists_max_gm();
 
 namespace soapgb {
 // radix sorts of (key, cell) pairs on the context's stream (fir_sort.cu)

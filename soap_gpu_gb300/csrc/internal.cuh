@@ -94,8 +94,10 @@ int copy_resources(soapgb_ctx *ctx, int count);
 struct TraceScope {
     soapgb_ctx *ctx;
     const char *name;
+    cudaStream_t stream;
     cudaEvent_t a = nullptr;
-    TraceScope(soapgb_ctx *c, const char *n);
+    TraceScope(soapgb_ctx *c, const char *n);                    // on the context's stream
+    TraceScope(soapgb_ctx *c, const char *n, cudaStream_t s);    // on stream s (copies)
     ~TraceScope();
 };
 

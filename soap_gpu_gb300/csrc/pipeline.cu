@@ -11,6 +11,7 @@
 
 #include "internal.cuh"
 #include "fir.cuh"
+#include "regions.cuh"
 #include "resolution.cuh"
 
 using namespace soapgb;
@@ -19,7 +20,6 @@ namespace soapgb {
 int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                       const int *h_reg_off, const double *h_regions, const soapgb_activity *act, double *d_temp,
                       double *d_bi, char *scratch, size_t scratch_bytes);
-size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
 int integrate_device(soapgb_ctx *ctx, int form, int n, int n_eff, const double *d_wave, int grid, int n_phase,
                      const double *d_temp, const double *d_bi, const soapgb_maps &dm, const soapgb_cubes &dc,
                      double step, const soapgb_activity *act, void *d_flux, void *d_bconv, void *d_tot, int out_f32,
@@ -82,6 +82,10 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     }
     size_t cube_b = sizeof(double) * (size_t)n * n_mu;
     long long n_spec = 3LL * n_phase;
+    // the collapsed forms build their per-phase cell lists from the regions' bounding
+    // boxes (no G*G maps) when the grid allows; PLAIN64 integrates from the maps
+    const bool collapsed = (form != SOAPGB_PLAIN64);
+    const bool box_lists = collapsed && gm <= fir_box_lists_max_gm();
     Workspace ws(ctx);
     int s_wave = ws.add(host ? sizeof(double) * n : 0);
     int s_c[6];
@@ -96,9 +100,9 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     size_t esz = (form == SOAPGB_FAST32) ? sizeof(float) : sizeof(double);
     int s_raw = ws.add(esz * (size_t)n * n_spec);                // deficits [p][type][n]
     int s_rawd = ws.add(form == SOAPGB_FAST32 && raw && host ? sizeof(double) * (size_t)n_eff * n_spec : 0);
-    int s_temp = ws.add(sizeof(double) * gm * n_phase);
-    int s_bi = ws.add(sizeof(double) * gm * n_phase);
-    int s_cells = ws.add(sizeof(int) * gm * n_phase);
+    int s_temp = ws.add(box_lists ? 0 : sizeof(double) * gm * n_phase);
+    int s_bi = ws.add(box_lists ? 0 : sizeof(double) * gm * n_phase);
+    int s_cells = ws.add(collapsed ? 0 : sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
     int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
@@ -106,16 +110,20 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
     int rc = ws.commit();
     if (rc) return rc;
-    // Host buffers with the FP32 form: the phases run in chunks, each chunk's spectra
-    // copied back on the copy stream while the next chunk is computed; the cubes are
-    // copied in on the copy stream while the geometry (maps, lists, plans) is built.
-    const bool chunked = host && form == SOAPGB_FAST32 && n_phase >= 2;
+    // Host buffers with a collapsed form: the cubes are copied in on the copy stream
+    // while the geometry (cell order, lists, plans) is built; with FP32 the phases then
+    // run in chunks, each chunk's spectra copied back on the copy stream while the next
+    // chunk is computed.
+    const bool overlap = host && collapsed;
+    const bool chunked = overlap && form == SOAPGB_FAST32 && n_phase >= 2;
     int n_chunk = 1, per_chunk = n_phase;
     cudaStream_t cube_stream = ctx->stream;
     if (chunked) {
         n_chunk = std::min(n_phase, 8);
         per_chunk = (n_phase + n_chunk - 1) / n_chunk;
         n_chunk = (n_phase + per_chunk - 1) / per_chunk;
+    }
+    if (overlap) {
         rc = copy_resources(ctx, n_chunk + 2);
         if (rc) return rc;
         // the copy stream starts after the work already queued on the main stream
@@ -137,13 +145,16 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     STAGE(d_wave, wave, sizeof(double) * n, s_wave);
     soapgb_cubes dc;
     dc.n_mu = n_mu;
-    STAGE_ON(cube_stream, dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
-    STAGE_ON(cube_stream, dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
-    STAGE_ON(cube_stream, dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
-    STAGE_ON(cube_stream, dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
-    STAGE_ON(cube_stream, dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
-    STAGE_ON(cube_stream, dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
-    if (chunked) SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[1], ctx->copy_stream));
+    {
+        TraceScope ts(ctx, "h2d_cubes", cube_stream);
+        STAGE_ON(cube_stream, dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
+        STAGE_ON(cube_stream, dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
+        STAGE_ON(cube_stream, dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
+        STAGE_ON(cube_stream, dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
+        STAGE_ON(cube_stream, dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
+        STAGE_ON(cube_stream, dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
+    }
+    if (overlap) SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[1], ctx->copy_stream));
     soapgb_maps dm;
     const double *cd;
     STAGE(cd, maps->delta, sizeof(double) * gm, s_m[0]);
@@ -165,18 +176,27 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int f32 = (form == SOAPGB_FAST32);
     double *d_temp = ws.get<double>(s_temp), *d_bi = ws.get<double>(s_bi);
     double *d_lower = host ? ws.get<double>(s_lower) : lower;
-    rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp, d_bi,
-                           ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
+    const RegionPhase *d_table = nullptr;
+    const int *d_roff = nullptr;
+    if (box_lists)
+        rc = phase_table_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act,
+                                ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase), &d_table, &d_roff);
+    else
+        rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp,
+                               d_bi, ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
     if (rc) return rc;
-    if (chunked) {
+    if (collapsed) {
         FirPhaseArgs fa;
         fa.n = n;
         fa.n_eff = n_eff;
         fa.wave = d_wave;
         fa.cubes = &dc;
         fa.n_phase = n_phase;
-        fa.temp = d_temp;
-        fa.bi = d_bi;
+        fa.temp = box_lists ? nullptr : d_temp;
+        fa.bi = box_lists ? nullptr : d_bi;
+        fa.table = d_table;
+        fa.reg_off = d_roff;
+        fa.grid = grid;
         fa.delta = dm.delta;
         fa.limb = dm.limb;
         fa.lb = dm.lb;
@@ -187,69 +207,84 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.flux = d_raw + esz * n;
         fa.bconv = d_raw + esz * 2 * n;
         fa.tot = d_raw;
-        fa.out_f32 = 1;
+        fa.out_f32 = f32;
         fa.out_stride = 3LL * n;
         fa.lambda0 = w3[0];
         fa.stage = FIR_STAGE_GEOMETRY;
         rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
         if (rc) return rc;
-        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->sync_events[1], 0));   // cubes in
+        if (overlap) SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->sync_events[1], 0));   // cubes in
         fa.stage = FIR_STAGE_CUBES;
         rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
         if (rc) return rc;
-        Res32 R;
-        rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3, sigma_v,
-                                  50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
-        if (rc) return rc;
-        for (int c = 0; c < n_chunk; ++c) {
-            const int p0 = c * per_chunk, p1 = std::min(n_phase, p0 + per_chunk);
+        if (f32) {
+            Res32 R;
+            rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3, sigma_v,
+                                      50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
+            if (rc) return rc;
+            for (int c = 0; c < n_chunk; ++c) {
+                const int p0 = c * per_chunk, p1 = std::min(n_phase, p0 + per_chunk);
+                fa.stage = FIR_STAGE_RUN;
+                fa.l0 = p0;
+                fa.l1 = p1;
+                rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+                if (rc) return rc;
+                rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr);
+                if (rc) return rc;
+                if (host) {
+                    cudaEvent_t ev = ctx->sync_events[2 + c];
+                    SOAP_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
+                    SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
+                    const size_t off = (size_t)3 * p0 * n_eff, cnt = (size_t)3 * (p1 - p0) * n_eff;
+                    TraceScope ts(ctx, "d2h_lower", ctx->copy_stream);
+                    SOAP_CUDA(ctx, cudaMemcpyAsync(lower + off, d_lower + off, sizeof(double) * cnt,
+                                                   cudaMemcpyDeviceToHost, ctx->copy_stream));
+                }
+            }
+        } else {
             fa.stage = FIR_STAGE_RUN;
-            fa.l0 = p0;
-            fa.l1 = p1;
             rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
             if (rc) return rc;
-            rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr);
+            rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, 0, n, d_qs,
+                                   d_qn, 3, sigma_v, 50.0, conv_step, conv_step, sentinel, d_lower, n_eff, nullptr,
+                                   ws.get<char>(s_res));
             if (rc) return rc;
-            cudaEvent_t ev = ctx->sync_events[2 + c];
-            SOAP_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
-            SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
-            const size_t off = (size_t)3 * p0 * n_eff, cnt = (size_t)3 * (p1 - p0) * n_eff;
-            SOAP_CUDA(ctx, cudaMemcpyAsync(lower + off, d_lower + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
-                                           ctx->copy_stream));
+            if (host)
+                SOAP_CUDA(ctx, cudaMemcpyAsync(lower, d_lower, sizeof(double) * (size_t)n_eff * n_spec,
+                                               cudaMemcpyDeviceToHost, ctx->stream));
         }
         if (raw) {
-            double *dst = ws.get<double>(s_rawd);
             long long tot_el = (long long)n_spec * n_eff;
-            SOAP_TRACED(ctx, "widen", k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(
-                                          n_spec, n, n_eff, (const float *)d_raw, dst));
-            SOAP_LAUNCHED(ctx);
-            SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, cudaMemcpyDeviceToHost, ctx->stream));
+            cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+            if (f32) {
+                double *dst = host ? ws.get<double>(s_rawd) : raw;
+                SOAP_TRACED(ctx, "widen", k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(
+                                              n_spec, n, n_eff, (const float *)d_raw, dst));
+                SOAP_LAUNCHED(ctx);
+                if (host)
+                    SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, k, ctx->stream));
+            } else {
+                SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n,
+                                                 sizeof(double) * n_eff, n_spec, k, ctx->stream));
+            }
         }
+        if (!host) return SOAPGB_OK;
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return check_status(ctx, "soapgb_phase_pipeline");
     }
-    // deficits in [phase][tot, flux, bconv][n]
+    // PLAIN64: deficits in [phase][tot, flux, bconv][n] from the maps
     rc = integrate_device(ctx, form, n, n_eff, d_wave, grid, n_phase, d_temp, d_bi, dm, dc, step, act,
-                          d_raw + esz * n /* flux */, d_raw + esz * 2 * n /* bconv */, d_raw /* tot */, f32, 3LL * n,
+                          d_raw + esz * n /* flux */, d_raw + esz * 2 * n /* bconv */, d_raw /* tot */, 0, 3LL * n,
                           ws.get<int>(s_cells), ws.get<int>(s_counts), ws.get<char>(s_fir), fp);
     if (rc) return rc;
-    rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, f32, n, d_qs, d_qn, 3,
+    rc = resolution_device(ctx, form, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_raw, 0, n, d_qs, d_qn, 3,
                            sigma_v, 50.0, conv_step, conv_step, sentinel, d_lower, n_eff, nullptr, ws.get<char>(s_res));
     if (rc) return rc;
     if (raw) {
-        if (f32) {
-            double *dst = host ? ws.get<double>(s_rawd) : raw;
-            long long tot_el = (long long)n_spec * n_eff;
-            SOAP_TRACED(ctx, "widen", k_widen_rows<<<grid_for(ctx, tot_el, 256), 256, 0, ctx->stream>>>(n_spec, n, n_eff, (const float *)d_raw, dst));
-            SOAP_LAUNCHED(ctx);
-            if (host)
-                SOAP_CUDA(ctx, cudaMemcpyAsync(raw, dst, sizeof(double) * tot_el, cudaMemcpyDeviceToHost, ctx->stream));
-        } else {
-            cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-            SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n,
-                                             sizeof(double) * n_eff, n_spec, k, ctx->stream));
-        }
+        cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        SOAP_CUDA(ctx, cudaMemcpy2DAsync(raw, sizeof(double) * n_eff, d_raw, sizeof(double) * n,
+                                         sizeof(double) * n_eff, n_spec, k, ctx->stream));
     }
     if (host) {
         SOAP_CUDA(ctx, cudaMemcpyAsync(lower, d_lower, sizeof(double) * (size_t)n_eff * n_spec, cudaMemcpyDeviceToHost, ctx->stream));

@@ -12,17 +12,9 @@
 #include <cstring>
 #include <vector>
 
-#include "internal.cuh"
+#include "regions.cuh"
 
 using namespace soapgb;
-
-struct RegionPhase {
-    int iy0, iz0, iy1, iz1;  // bounding box [iy0, iy1) x [iz0, iz1), clamped to the grid
-    int visible;
-    int type;                // 0 spot, 1 facula
-    double s;                // cap chord radius
-    double r0, r1, r2;       // first row of the inverse rotation
-};
 
 // spot_init_gpu + spot_phase_gpu + spot_area for one region at one phase
 static void host_region_bbox(double s, double longitude, double latitude, double inclination, int nrho,
@@ -96,33 +88,8 @@ __global__ void k_phase_scan(int grid, double delta_grid, const RegionPhase *__r
     int p = blockIdx.y;
     if (k >= gm) return;
     int iy = (int)(k / grid), iz = (int)(k % grid);
-    double y = 0.0, z = 0.0;
-    bool have_yz = false;   // FP64 only for cells inside a bounding box
-    double t = -9999.0, b = -9999.0;
-    int r0 = reg_off[p], r1 = reg_off[p + 1];
-    for (int r = r0; r < r1; ++r) {
-        RegionPhase rp = table[r];
-        if (!rp.visible || iy < rp.iy0 || iy >= rp.iy1 || iz < rp.iz0 || iz >= rp.iz1) continue;
-        if (!have_yz) {
-            y = __dadd_rn(-1., __dmul_rn((double)iy, delta_grid));
-            z = __dadd_rn(-1., __dmul_rn((double)iz, delta_grid));
-            have_yz = true;
-        }
-        if (!(__dadd_rn(__dmul_rn(z, z), __dmul_rn(y, y)) < 1.)) continue;
-        double xa0 = __dsqrt_rn(__dsub_rn(1., __dadd_rn(__dmul_rn(y, y), __dmul_rn(z, z))));
-        double xi0 = __dadd_rn(__dadd_rn(__dmul_rn(rp.r0, xa0), __dmul_rn(rp.r1, y)), __dmul_rn(rp.r2, z));
-        if (__dmul_rn(xi0, xi0) >= __dsub_rn(1., __dmul_rn(rp.s, rp.s))) {
-            if (rp.type == 0) {
-                t = (double)(t_star - t_diff_spot);
-                b = 0.0;
-            } else {
-                double tp = __dadd_rn(__dsub_rn(__dadd_rn((double)(t_star + t_diff_fac), 0.9), __dmul_rn(407.7, xa0)),
-                                      __dmul_rn(190.9, __dmul_rn(xa0, xa0)));
-                t = (double)(int)tp;
-                b = 1.0;
-            }
-        }
-    }
+    double t, b;
+    region_cell_value(table, reg_off[p], reg_off[p + 1], iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b);
     temp[(long long)p * gm + k] = t;
     bi[(long long)p * gm + k] = b;
 }
@@ -163,26 +130,40 @@ static int build_region_table(soapgb_ctx *ctx, int grid, double incl, int n_phas
 }
 
 namespace soapgb {
-// Device-side phase maps for already-device temp/bi outputs; phases/regions/offsets on host.
-int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
-                      const int *h_reg_off, const double *h_regions, const soapgb_activity *act, double *d_temp,
-                      double *d_bi, char *scratch, size_t scratch_bytes) {
+int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
+                       const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
+                       size_t scratch_bytes, const RegionPhase **d_table, const int **d_off) {
     std::vector<RegionPhase> table;
     int rc = build_region_table(ctx, grid, incl, n_phase, h_phases, h_reg_off, h_regions, act->nrho, table);
     if (rc) return rc;
     size_t tb = sizeof(RegionPhase) * table.size();
     size_t ob = sizeof(int) * (n_phase + 1);
-    if (tb + ob + 256 > scratch_bytes) return set_error(ctx, SOAPGB_ERR_ARG, "phase maps scratch too small");
-    RegionPhase *d_table = (RegionPhase *)scratch;
-    int *d_off = (int *)(scratch + ((tb + 255) & ~size_t(255)));
-    SOAP_CUDA(ctx, cudaMemcpyAsync(d_table, table.data(), tb, cudaMemcpyHostToDevice, ctx->stream));
-    SOAP_CUDA(ctx, cudaMemcpyAsync(d_off, h_reg_off, ob, cudaMemcpyHostToDevice, ctx->stream));
+    if (((tb + 255) & ~size_t(255)) + ob > scratch_bytes)
+        return set_error(ctx, SOAPGB_ERR_ARG, "phase maps scratch too small");
+    RegionPhase *dt = (RegionPhase *)scratch;
+    int *dof = (int *)(scratch + ((tb + 255) & ~size_t(255)));
+    SOAP_CUDA(ctx, cudaMemcpyAsync(dt, table.data(), tb, cudaMemcpyHostToDevice, ctx->stream));
+    SOAP_CUDA(ctx, cudaMemcpyAsync(dof, h_reg_off, ob, cudaMemcpyHostToDevice, ctx->stream));
+    // `table` lives in pageable memory: cudaMemcpyAsync has staged it before returning
+    *d_table = dt;
+    *d_off = dof;
+    return SOAPGB_OK;
+}
+
+// Device-side phase maps for already-device temp/bi outputs; phases/regions/offsets on host.
+int phase_maps_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
+                      const int *h_reg_off, const double *h_regions, const soapgb_activity *act, double *d_temp,
+                      double *d_bi, char *scratch, size_t scratch_bytes) {
+    const RegionPhase *d_table;
+    const int *d_off;
+    int rc = phase_table_device(ctx, grid, incl, n_phase, h_phases, h_reg_off, h_regions, act, scratch, scratch_bytes,
+                                &d_table, &d_off);
+    if (rc) return rc;
     long long gm = (long long)grid * grid;
     dim3 g(grid_for(ctx, gm, 256), n_phase);
     SOAP_TRACED(ctx, "phase_scan", k_phase_scan<<<g, 256, 0, ctx->stream>>>(grid, 2. / grid, d_table, d_off, act->t_star, act->t_diff_spot,
                                              act->t_diff_fac, d_temp, d_bi));
     SOAP_LAUNCHED(ctx);
-    // `table` lives in pageable memory: cudaMemcpyAsync has staged it before returning
     return SOAPGB_OK;
 }
 
