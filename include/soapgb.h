@@ -205,7 +205,13 @@ int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double *x, const 
  * the n-long disk sums of a4-a7 (tail zero).  lower: n_phase x 3 x n_eff, types in
  * the order tot, flux, bconv (SOAP_resolution.cu:414-416); raw (optional):
  * n_phase x 3 x n_eff deficit spectra in the same order.  conv_step is the step
- * used in the Gaussian (0.005 in the reference binaries). */
+ * used in the Gaussian (0.005 in the reference binaries).
+ * With mem = SOAPGB_DEVICE the descriptors phases, reg_offsets and regions may be
+ * host or device memory: from host memory the call does not synchronise, so calls
+ * queue on the stream back to back.  wave[0], wave[1] and wave[n_eff - 1] of a device
+ * wavelength array are read (one synchronisation) the first time the array is seen
+ * and kept in the context; later calls confirm them on the device, and a changed
+ * array is reported by soapgb_synchronize (status 51). */
 int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
                           const soapgb_star *star, const soapgb_maps *maps,
                           const soapgb_cubes *cubes, double step, const soapgb_activity *act,

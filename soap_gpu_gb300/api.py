@@ -52,6 +52,17 @@ class _Args:
         self.keep.append(a)
         return ctypes.c_void_p(a.ctypes.data)
 
+    def desc(self, x, dtype):
+        """A small descriptor array (phases, region tables): kept in host memory when it
+        is given there, so that a device-buffer call need not synchronise to read it."""
+        if x is None:
+            return None
+        if _is_dev(x):
+            return self.inp(x, dtype)
+        a = np.ascontiguousarray(x, dtype=dtype)
+        self.keep.append(a)
+        return ctypes.c_void_p(a.ctypes.data)
+
     def out(self, shape, dtype):
         if self.dev:
             t = torch.empty(shape, dtype=torch.float64 if dtype == np.float64 else torch.int32,
@@ -282,8 +293,8 @@ class Context:
                 raw, rp = a.out((n_phase, 3, int(n_eff)), np.float64)
         self._check(self.L.soapgb_phase_pipeline(self.h, _form(form), n, int(n_eff), a.inp(wave, np.float64),
                                                  ctypes.byref(star), ctypes.byref(m), ctypes.byref(c), float(step),
-                                                 ctypes.byref(act), n_phase, a.inp(phases, np.float64),
-                                                 a.inp(off, np.int32), a.inp(reg, np.float64),
+                                                 ctypes.byref(act), n_phase, a.desc(phases, np.float64),
+                                                 a.desc(off, np.int32), a.desc(reg, np.float64),
                                                  a.inp(quiet_sed, np.float64), a.inp(quiet_norm, np.float64),
                                                  float(sigma_v), float(conv_step), float(sentinel), a.mem, lp, rp))
         return (lower, raw) if want_raw else lower

@@ -66,8 +66,69 @@ int check_status(soapgb_ctx *ctx, const char *what) {
     if (e != cudaSuccess) return cuda_check(ctx, e, what);
     if (h != 0) {
         cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+        if (h == SOAPGB_ST_EDGES) {
+            ctx->edge_wave = nullptr;
+            return set_error(ctx, SOAPGB_ERR_DEVICE,
+                             "%s: device status %d: the wavelength array changed after an earlier call read its "
+                             "first, second or last value; the calls since then used the old values",
+                             what, h);
+        }
         return set_error(ctx, SOAPGB_ERR_DEVICE, "%s: device status %d", what, h);
     }
+    return SOAPGB_OK;
+}
+
+bool host_readable(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;   // not known to CUDA: ordinary host memory
+    }
+    return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeUnregistered;
+}
+
+int read_descriptor(soapgb_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return SOAPGB_OK;
+    if (host_readable(src)) {
+        memcpy(dst, src, bytes);
+        return SOAPGB_OK;
+    }
+    SOAP_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SOAPGB_OK;
+}
+
+__global__ void k_check_edges(const double *__restrict__ wave, int n_eff, double w0, double w1, double wl,
+                              int *status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const bool same = __double_as_longlong(wave[0]) == __double_as_longlong(w0) &&
+                      __double_as_longlong(wave[1]) == __double_as_longlong(w1) &&
+                      __double_as_longlong(wave[n_eff - 1]) == __double_as_longlong(wl);
+    if (!same) atomicExch(status, SOAPGB_ST_EDGES);
+}
+
+int wave_edges(soapgb_ctx *ctx, int mem, const double *wave, int n, int n_eff, double *w3) {
+    if (mem == SOAPGB_HOST || host_readable(wave)) {
+        w3[0] = wave[0];
+        w3[1] = wave[1];
+        w3[2] = wave[n_eff - 1];
+        return SOAPGB_OK;
+    }
+    if (ctx->edge_wave == wave && ctx->edge_n == n && ctx->edge_n_eff == n_eff) {
+        w3[0] = ctx->edge_w3[0];
+        w3[1] = ctx->edge_w3[1];
+        w3[2] = ctx->edge_w3[2];
+        k_check_edges<<<1, 32, 0, ctx->stream>>>(wave, n_eff, w3[0], w3[1], w3[2], ctx->d_status);
+        SOAP_LAUNCHED(ctx);
+        return SOAPGB_OK;
+    }
+    SOAP_CUDA(ctx, cudaMemcpyAsync(w3, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaMemcpyAsync(w3 + 2, wave + n_eff - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->edge_wave = wave;
+    ctx->edge_n = n;
+    ctx->edge_n_eff = n_eff;
+    for (int q = 0; q < 3; ++q) ctx->edge_w3[q] = w3[q];
     return SOAPGB_OK;
 }
 

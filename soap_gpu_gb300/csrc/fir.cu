@@ -116,6 +116,41 @@ __global__ void k_to_type(long long count, const double *__restrict__ a, const d
     out[i] = (T)v;
 }
 
+// FP64 -> FP32 rounded to nearest even on the integer pipes: the 52-bit fraction is cut
+// to 23 bits, rounding up past half and at half to even (a carry into the exponent is
+// the correct next binade, and past the largest exponent gives infinity).  Results
+// outside the normal FP32 range (zero, subnormal) and NaN take the conversion
+// instruction.
+__device__ __forceinline__ float soap_f64_to_f32(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((u >> 52) & 0x7ff);
+    if (e < 1023 - 126 || e > 1023 + 127) return __double2float_rn(v);
+    const unsigned long long frac = u & 0xfffffffffffffULL;
+    const unsigned keep = (unsigned)(frac >> 29);
+    const unsigned long long rest = frac & 0x1fffffffULL;
+    unsigned bits = ((unsigned)(e - 1023 + 127) << 23) | keep;
+    if (rest > 0x10000000ULL || (rest == 0x10000000ULL && (keep & 1u))) bits += 1u;
+    return __uint_as_float(bits | ((unsigned)(u >> 32) & 0x80000000u));
+}
+
+// The six typed cubes of the FP32 phase integration in one pass over the four FP64
+// cubes (two values per thread and step): q_sed, q_norm, spot_norm, q_norm - spot_norm,
+// fac_norm, q_norm - fac_norm.  The two differences are formed in FP64 and rounded once.
+__global__ void __launch_bounds__(256) k_cube_types32(long long n2, const double2 *__restrict__ qs,
+                                                      const double2 *__restrict__ qn, const double2 *__restrict__ sn,
+                                                      const double2 *__restrict__ fn, float2 *o0, float2 *o1,
+                                                      float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
+        const double2 a = qs[i], b = qn[i], c = sn[i], d = fn[i];
+        o0[i] = make_float2(soap_f64_to_f32(a.x), soap_f64_to_f32(a.y));
+        o1[i] = make_float2(soap_f64_to_f32(b.x), soap_f64_to_f32(b.y));
+        o2[i] = make_float2(soap_f64_to_f32(c.x), soap_f64_to_f32(c.y));
+        o3[i] = make_float2(soap_f64_to_f32(b.x - c.x), soap_f64_to_f32(b.y - c.y));
+        o4[i] = make_float2(soap_f64_to_f32(d.x), soap_f64_to_f32(d.y));
+        o5[i] = make_float2(soap_f64_to_f32(b.x - d.x), soap_f64_to_f32(b.y - d.y));
+    }
+}
+
 // --- cell order ----------------------------------------------------------------
 // pass 1 keys: the slope dlt (order-preserving 64-bit image); pass 2 (stable): mu bin
 // and v == 0, invisible cells last
@@ -860,6 +895,8 @@ struct FirTileArgs {
     long long out_stride;
     int *status;
     const void *plan;           // FirPrePlan<T> per (list, tile), or null
+    const int *run_list;        // lists to integrate (ascending), or null for all of them
+    int n_lists_all;            // lists with a plan slot
 };
 
 // The list's (class, mu bin, v == 0) segments with their shift ranges at the tile
@@ -1073,9 +1110,10 @@ __global__ void __launch_bounds__(FIR_PLAN_THREADS) k_fir_plan(const FirTileArgs
     __shared__ int wsum[FIR_PLAN_THREADS / 32];
     __shared__ int nunit_sh;
     FirSeg *segs = reinterpret_cast<FirSeg *>(plan_smem + ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)));
-    const int l = blockIdx.y, j0 = blockIdx.x * FIR_TILE, tid = threadIdx.x;
+    const int l = A.run_list ? A.run_list[blockIdx.y] : (int)blockIdx.y;
+    const int j0 = blockIdx.x * FIR_TILE, tid = threadIdx.x;
     const long long tau = (long long)l * gridDim.x + blockIdx.x;
-    const long long ntot = (long long)gridDim.x * gridDim.y;
+    const long long ntot = (long long)gridDim.x * A.n_lists_all;
     char *rec = reinterpret_cast<char *>(const_cast<void *>(A.plan)) + tau * FirPlanSlot<T>::BYTES;
     int *psize = reinterpret_cast<int *>(reinterpret_cast<char *>(const_cast<void *>(A.plan)) +
                                          ntot * FirPlanSlot<T>::BYTES);
@@ -1477,7 +1515,8 @@ struct FirPPSmem {
 template <typename T>
 __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPSmem<T>) + 15) & ~size_t(15); }
 
-// Block b walks the (phase, tile) pairs tau = b, b + G, ... (tau = phase * ntile + tile).
+// Block b walks the (phase, tile) pairs tau = b, b + G, ... (tau = phase * ntile + tile;
+// with a run list, phase = run_list[tau / ntile]).
 // A tile's compact plan (k_fir_plan) is copied by TMA one tile ahead into the other plan
 // buffer; the cube windows of its work units stream through two buffers, and the first
 // unit of the next tile is issued while the current tile's last unit is applied, so the
@@ -1508,6 +1547,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     }
     __syncthreads();
 
+    // (phase, tile) index of walk position t
+    auto real = [&](int t) -> int { return A.run_list ? A.run_list[t / ntile] * ntile + t % ntile : t; };
     // (thread 0) copy the plan of tile tau (bytes long) into plan buffer b
     auto issue_plan = [&](int tau, int b, unsigned bytes) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -1679,8 +1720,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     // tiles tau in [tau0, ntot)
     if (tid == 0) {
         const int t0 = tau0 + (int)blockIdx.x;
-        if (t0 < ntot) issue_plan(t0, 0, (unsigned)psize[t0]);
-        if (t0 + G < ntot) issue_plan(t0 + G, 1, (unsigned)psize[t0 + G]);
+        if (t0 < ntot) issue_plan(real(t0), 0, (unsigned)psize[real(t0)]);
+        if (t0 + G < ntot) issue_plan(real(t0 + G), 1, (unsigned)psize[real(t0 + G)]);
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount & 1)
     bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
@@ -1690,14 +1731,15 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         const int pbuf = k & 1;
         // size of the plan issued at the end of this tile, read early (its latency hides
         // behind the tile's work)
-        const unsigned next_bytes = (tid == 0 && tau + 2 * G < ntot) ? (unsigned)psize[tau + 2 * G] : 0u;
+        const unsigned next_bytes = (tid == 0 && tau + 2 * G < ntot) ? (unsigned)psize[real(tau + 2 * G)] : 0u;
         if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1))) atomicExch(&sh.fail, 1);
         __syncthreads();
         if (sh.fail) {
             bad = 1;
             break;
         }
-        const int l = tau / ntile, j0 = (tau - l * ntile) * FIR_TILE;
+        const int tr = real(tau);
+        const int l = tr / ntile, j0 = (tr - l * ntile) * FIR_TILE;
         const int t_eff = min(FIR_TILE, n_eff - j0);
         const long long lbase = (long long)l * A.gm;
         const int *cn = A.counts + 4 * l;
@@ -1735,7 +1777,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                         if (tn < ntot && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
-                            const int ln = tn / ntile, jn = (tn - ln * ntile) * FIR_TILE;
+                            const int tnr = real(tn);
+                            const int ln = tnr / ntile, jn = (tnr - ln * ntile) * FIR_TILE;
                             if (hn.w && hn.x > 0 && jn < n_eff) {
                                 const FirPlanLayout<T> Ln(hn.x, hn.y, hn.z);
                                 issue_unit(u + 1, *reinterpret_cast<const FirUnit *>(rn + Ln.o_unit));
@@ -1902,7 +1945,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
             for (int a = 0; a < 7; ++a) acc[a][q].zero();
         }
         __syncthreads();   // plan buffer pbuf free
-        if (tid == 0 && tau + 2 * G < ntot) issue_plan(tau + 2 * G, pbuf, next_bytes);
+        if (tid == 0 && tau + 2 * G < ntot) issue_plan(real(tau + 2 * G), pbuf, next_bytes);
     }
     if (bad && tid == 0) {
         // a copy did not land in time: record it and give the copies possibly in flight a
@@ -1919,6 +1962,18 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
 // host side
 // ---------------------------------------------------------------------------
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// outputs [0, n) of the phases zero_list[0, count) set to zero (phases without a visible
+// region: no active cell, so their deficit spectra are zero)
+template <typename T>
+__global__ void k_fir_zero(int n, const int *__restrict__ zero_list, T *out0, T *out1, T *out2, long long out_stride) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const long long o = (long long)zero_list[blockIdx.y] * out_stride + j;
+    out0[o] = (T)0;
+    out1[o] = (T)0;
+    out2[o] = (T)0;
+}
 
 __global__ void k_pair_rows(int n, const double *__restrict__ a, const double *__restrict__ b, float2 *pa, float2 *pb) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2076,7 +2131,7 @@ template <typename T, int MODE, typename OutT>
 static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
                         double los, const FirCubes &fc, long long gm, int solar,
                         int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists,
-                        int stage = 7, int l0 = 0, int l1 = -1) {
+                        int stage = 7, int l0 = 0, int l1 = -1, const FirPhaseArgs *pa = nullptr) {
     constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
     if (l1 < 0) l1 = n_lists;
     FirTileArgs A;
@@ -2106,20 +2161,40 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.out_stride = out_stride;
     A.status = ctx->d_status;
     A.plan = nullptr;
+    A.run_list = nullptr;
+    A.n_lists_all = n_lists;
     const int ntile = (n + FIR_TILE - 1) / FIR_TILE;
     if constexpr (MODE == MODE_PHASE) {
         // plans of every (phase, tile) (stage 1), then the persistent tile kernel over the
         // phases [l0, l1) (stage 4)
         A.plan = ws + L.off[FirLayout::PLAN];
-        if (stage & 1) {
+        // with run / zero lists: only the listed phases are planned and integrated, the
+        // others zero-filled; [r0, r1) and [z0, z1) are the parts of the lists in [l0, l1)
+        const bool lists = pa && pa->run_list;
+        int r0 = l0, r1 = l1, z0 = 0, z1 = 0;
+        if (lists) {
+            A.run_list = pa->run_list;
+            r0 = (int)(std::lower_bound(pa->run_host, pa->run_host + pa->n_run, l0) - pa->run_host);
+            r1 = (int)(std::lower_bound(pa->run_host, pa->run_host + pa->n_run, l1) - pa->run_host);
+            z0 = (int)(std::lower_bound(pa->zero_host, pa->zero_host + pa->n_zero, l0) - pa->zero_host);
+            z1 = (int)(std::lower_bound(pa->zero_host, pa->zero_host + pa->n_zero, l1) - pa->zero_host);
+        }
+        const int n_plan = lists ? pa->n_run : n_lists;
+        if ((stage & 1) && n_plan > 0) {
             size_t smem_p = ((sizeof(FirPrePlan<T>) + 15) & ~size_t(15)) + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
             SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_plan<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
             SOAP_TRACED(ctx, "fir_plan",
-                        k_fir_plan<T><<<dim3(ntile, n_lists), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
+                        k_fir_plan<T><<<dim3(ntile, n_plan), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
             SOAP_LAUNCHED(ctx);
         }
-        if ((stage & 4) && l1 > l0) {
-            const int tau0 = ntile * l0, ntot = ntile * l1, nrun = ntot - tau0;
+        if ((stage & 4) && z1 > z0) {
+            SOAP_TRACED(ctx, "fir_zero",
+                        k_fir_zero<T><<<dim3((n + 255) / 256, z1 - z0), 256, 0, ctx->stream>>>(
+                            n, pa->zero_list + z0, (T *)o0, (T *)o1, (T *)o2, out_stride));
+            SOAP_LAUNCHED(ctx);
+        }
+        if ((stage & 4) && r1 > r0) {
+            const int tau0 = ntile * r0, ntot = ntile * r1, nrun = ntot - tau0;
             size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
             SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
             int per_sm = 0;
@@ -2208,7 +2283,21 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
         const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
         const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
-        for (int q = 0; q < 6; ++q) {
+        auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+        const bool fused = (tsz == 4) && (cube_elems % 2 == 0) && al16(c.q_sed) && al16(c.q_norm) &&
+                           al16(c.spot_norm) && al16(c.fac_norm);
+        if (fused) {
+            float2 *o[6];
+            for (int q = 0; q < 6; ++q) o[q] = (float2 *)const_cast<void *>(fc.c[q]);
+            const long long n2 = (long long)(cube_elems / 2);
+            const int nblk = (int)std::min<long long>((n2 + 255) / 256, 16LL * std::max(ctx->num_sms, 1));
+            SOAP_TRACED(ctx, "cube_types",
+                        k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
+                            n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,
+                            (const double2 *)c.fac_norm, o[0], o[1], o[2], o[3], o[4], o[5]));
+            SOAP_LAUNCHED(ctx);
+        }
+        for (int q = 0; q < 6 && !fused; ++q) {
             void *dst = const_cast<void *>(fc.c[q]);
             if (tsz == 4)
                 SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst));
@@ -2229,8 +2318,8 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     if (form == SOAPGB_FAST32)
         return launch_tiles<float, MODE_PHASE, float>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.gm,
                                                       a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
-                                                      a.n_phase, st, a.l0, l1);
+                                                      a.n_phase, st, a.l0, l1, &a);
     return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.gm,
                                                     a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
-                                                    a.n_phase, st, a.l0, l1);
+                                                    a.n_phase, st, a.l0, l1, &a);
 }

@@ -38,6 +38,12 @@ struct FirPhaseArgs {
     const RegionPhase *table = nullptr;
     const int *reg_off = nullptr;   // n_phase + 1 (device)
     int grid = 0;
+    // optional: the phases with a visible region (run) and the others (zero), ascending,
+    // on the device and the host; the run stage then integrates only the former and
+    // zero-fills the outputs of the latter (no active cell, so zero deficits)
+    const int *run_list = nullptr, *zero_list = nullptr;
+    const int *run_host = nullptr, *zero_host = nullptr;
+    int n_run = 0, n_zero = 0;
     const double *delta, *limb, *lb;
     const int *region;
     long long gm;               // G*G

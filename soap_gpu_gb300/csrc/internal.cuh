@@ -32,6 +32,11 @@ struct soapgb_ctx {
     // second stream for copies that overlap kernels (created on first use) and events
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> sync_events;
+    // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
+    // once; later calls with the same array confirm them on the device, status 51)
+    const double *edge_wave = nullptr;
+    int edge_n = 0, edge_n_eff = 0;
+    double edge_w3[3] = {0.0, 0.0, 0.0};
     // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report
     bool trace = false;
     std::vector<SoapTraceSpan> spans;
@@ -79,6 +84,16 @@ struct Workspace {
 const void *stage_in(soapgb_ctx *ctx, int mem, const void *p, size_t bytes, void *dst, int *rc);
 
 int check_status(soapgb_ctx *ctx, const char *what);
+// device status word: a cached wavelength edge value no longer matches the array
+constexpr int SOAPGB_ST_EDGES = 51;
+// true for memory the host can read directly (pageable or page-locked host memory)
+bool host_readable(const void *p);
+// copy a small descriptor array to the host: directly from host memory, or from device
+// memory with a synchronisation of the context's stream
+int read_descriptor(soapgb_ctx *ctx, void *dst, const void *src, size_t bytes);
+// w3 = (wave[0], wave[1], wave[n_eff - 1]) without a synchronisation when the same
+// device array was seen before (a one-thread kernel confirms the values on the device)
+int wave_edges(soapgb_ctx *ctx, int mem, const double *wave, int n, int n_eff, double *w3);
 
 // number of visible cells etc. via ordered compaction helpers (regions.cu)
 int compact_cells(soapgb_ctx *ctx, int n_lists, int cells_per_list, const double *key,

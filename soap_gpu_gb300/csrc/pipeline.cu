@@ -52,34 +52,25 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int grid = star->grid;
     long long gm = (long long)grid * grid;
     int n_mu = cubes->n_mu;
-    // small descriptors on the host
+    // small descriptors on the host: read directly from host memory (no synchronisation,
+    // so that a device-buffer call queues behind the previous one), or copied from device
+    // memory with a synchronisation
     std::vector<int> h_off(n_phase + 1);
     std::vector<double> h_ph(n_phase);
     double w3[3];
-    if (host) {
-        memcpy(h_off.data(), reg_offsets, sizeof(int) * (n_phase + 1));
-        memcpy(h_ph.data(), phases, sizeof(double) * n_phase);
-        w3[0] = wave[0];
-        w3[1] = wave[1];
-        w3[2] = wave[n_eff - 1];
-    } else {
-        SOAP_CUDA(ctx, cudaMemcpyAsync(h_off.data(), reg_offsets, sizeof(int) * (n_phase + 1), cudaMemcpyDeviceToHost, ctx->stream));
-        SOAP_CUDA(ctx, cudaMemcpyAsync(h_ph.data(), phases, sizeof(double) * n_phase, cudaMemcpyDeviceToHost, ctx->stream));
-        SOAP_CUDA(ctx, cudaMemcpyAsync(w3, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        SOAP_CUDA(ctx, cudaMemcpyAsync(w3 + 2, wave + n_eff - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    }
+    int rc0 = read_descriptor(ctx, h_off.data(), reg_offsets, sizeof(int) * (n_phase + 1));
+    if (!rc0) rc0 = read_descriptor(ctx, h_ph.data(), phases, sizeof(double) * n_phase);
+    if (rc0) return rc0;
     int n_rows = h_off[n_phase];
     if (h_off[0] != 0 || n_rows < 0) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: bad reg_offsets");
     std::vector<double> h_reg(4 * (size_t)(n_rows > 0 ? n_rows : 1));
     if (n_rows > 0) {
         if (!regions) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: null regions");
-        if (host) memcpy(h_reg.data(), regions, sizeof(double) * 4 * n_rows);
-        else {
-            SOAP_CUDA(ctx, cudaMemcpyAsync(h_reg.data(), regions, sizeof(double) * 4 * n_rows, cudaMemcpyDeviceToHost, ctx->stream));
-            SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        }
+        rc0 = read_descriptor(ctx, h_reg.data(), regions, sizeof(double) * 4 * n_rows);
+        if (rc0) return rc0;
     }
+    rc0 = wave_edges(ctx, mem, wave, n, n_eff, w3);
+    if (rc0) return rc0;
     size_t cube_b = sizeof(double) * (size_t)n * n_mu;
     long long n_spec = 3LL * n_phase;
     // the collapsed forms build their per-phase cell lists from the regions' bounding
@@ -105,6 +96,8 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_cells = ws.add(collapsed ? 0 : sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
     int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
+    int s_lists = ws.add(box_lists ? sizeof(int) * n_phase : 0);
+    int s_zspec = ws.add(box_lists ? (size_t)n_spec : 0);
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
     int s_fir = ws.add(fp.bytes);
     int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
@@ -178,10 +171,29 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     double *d_lower = host ? ws.get<double>(s_lower) : lower;
     const RegionPhase *d_table = nullptr;
     const int *d_roff = nullptr;
-    if (box_lists)
+    // phases with a visible region are integrated; the others have no active cell
+    std::vector<unsigned char> vis;
+    std::vector<int> h_lists;   // run list, then zero list
+    int n_run = 0;
+    if (box_lists) {
         rc = phase_table_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act,
-                                ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase), &d_table, &d_roff);
-    else
+                                ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase), &d_table, &d_roff,
+                                &vis);
+        if (rc) return rc;
+        for (int p = 0; p < n_phase; ++p)
+            if (vis[p]) h_lists.push_back(p);
+        n_run = (int)h_lists.size();
+        for (int p = 0; p < n_phase; ++p)
+            if (!vis[p]) h_lists.push_back(p);
+        // spectra of the phases without a visible region are zero
+        std::vector<unsigned char> zspec((size_t)n_spec);
+        for (int p = 0; p < n_phase; ++p) zspec[3 * p] = zspec[3 * p + 1] = zspec[3 * p + 2] = vis[p] ? 0 : 1;
+        // pageable sources: staged by the driver before the calls return
+        SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<int>(s_lists), h_lists.data(), sizeof(int) * n_phase,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<unsigned char>(s_zspec), zspec.data(), (size_t)n_spec,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+    } else
         rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp,
                                d_bi, ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
     if (rc) return rc;
@@ -197,6 +209,14 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.table = d_table;
         fa.reg_off = d_roff;
         fa.grid = grid;
+        if (box_lists) {
+            fa.run_list = ws.get<int>(s_lists);
+            fa.zero_list = fa.run_list + n_run;
+            fa.run_host = h_lists.data();
+            fa.zero_host = h_lists.data() + n_run;
+            fa.n_run = n_run;
+            fa.n_zero = n_phase - n_run;
+        }
         fa.delta = dm.delta;
         fa.limb = dm.limb;
         fa.lb = dm.lb;
@@ -229,7 +249,8 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 fa.l1 = p1;
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
                 if (rc) return rc;
-                rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr);
+                rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr,
+                                      box_lists ? ws.get<unsigned char>(s_zspec) : nullptr);
                 if (rc) return rc;
                 if (host) {
                     cudaEvent_t ev = ctx->sync_events[2 + c];

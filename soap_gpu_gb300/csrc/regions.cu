@@ -132,10 +132,17 @@ static int build_region_table(soapgb_ctx *ctx, int grid, double incl, int n_phas
 namespace soapgb {
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
-                       size_t scratch_bytes, const RegionPhase **d_table, const int **d_off) {
+                       size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
+                       std::vector<unsigned char> *phase_visible) {
     std::vector<RegionPhase> table;
     int rc = build_region_table(ctx, grid, incl, n_phase, h_phases, h_reg_off, h_regions, act->nrho, table);
     if (rc) return rc;
+    if (phase_visible) {
+        phase_visible->assign(n_phase, 0);
+        for (int p = 0; p < n_phase; ++p)
+            for (int r = h_reg_off[p]; r < h_reg_off[p + 1]; ++r)
+                if (table[r].visible) (*phase_visible)[p] = 1;
+    }
     size_t tb = sizeof(RegionPhase) * table.size();
     size_t ob = sizeof(int) * (n_phase + 1);
     if (((tb + 255) & ~size_t(255)) + ob > scratch_bytes)

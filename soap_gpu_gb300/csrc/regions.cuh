@@ -2,6 +2,8 @@
 // turns them into a cell's temperature and type (regions.cu; the collapsed integration
 // builds its per-phase cell lists from the same test in fir.cu).
 #pragma once
+#include <vector>
+
 #include "internal.cuh"
 
 struct RegionPhase {
@@ -54,9 +56,11 @@ __device__ __forceinline__ int region_cell_value(const RegionPhase *__restrict__
 
 namespace soapgb {
 // The region table of n_phase phases built on the host and copied to scratch:
-// *d_table (reg_off[n_phase] rows) and *d_off (n_phase + 1 offsets).
+// *d_table (reg_off[n_phase] rows) and *d_off (n_phase + 1 offsets); phase_visible
+// (optional) gets 1 for the phases with at least one visible region, else 0.
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
-                       size_t scratch_bytes, const RegionPhase **d_table, const int **d_off);
+                       size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
+                       std::vector<unsigned char> *phase_visible = nullptr);
 size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
 }  // namespace soapgb

@@ -603,7 +603,8 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
                                                         const float *__restrict__ b32b, const float *__restrict__ c32a,
                                                         const float *__restrict__ c32b, int b_every,
                                                         float *__restrict__ conv, long long conv_stride,
-                                                        unsigned *mm32, float *blk, int nbx, int *status) {
+                                                        unsigned *mm32, float *blk, int nbx, int *status,
+                                                        const unsigned char *__restrict__ zero_spec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[SB][4][FC_THREADS / 32];
     __shared__ unsigned long long bar[2];
@@ -696,7 +697,11 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
         for (int q = 0; q < SB; ++q)
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) acc[q][p] = 0.f;
-        if (R > 0)
+        // a batch of spectra known to be zero (phases without a visible region) has no
+        // taps to sum: its convolution is the base part alone
+        bool zero_batch = (zero_spec != nullptr);
+        for (int q = 0; q < nsb && zero_batch; ++q) zero_batch = zero_spec[s0 + q] != 0;
+        if (R > 0 && !zero_batch)
             conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
         conv32_finish<SB>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every,
                           conv, conv_stride, mm32, blk, nbx, red);
@@ -913,7 +918,8 @@ static int conv32_params(soapgb_ctx *ctx, int n, int n_eff, const double *lam, d
 // conv32_params
 static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, const char *param_scratch,
                       const float *spec, long long spec_stride, int n_spec, const float *b32a, const float *b32b,
-                      const float *c32a, const float *c32b, int b_every, float *conv, unsigned *mm32, float *blk) {
+                      const float *c32a, const float *c32b, int b_every, float *conv, unsigned *mm32, float *blk,
+                      const unsigned char *zero_spec) {
     constexpr int SB = 8;
     const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
     const float *c2 = (const float *)param_scratch;
@@ -932,7 +938,7 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         dim3 g(nbx, gy);
         SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
-                                                              n_eff, mm32, blk, nbx, ctx->d_status));
+                                                              n_eff, mm32, blk, nbx, ctx->d_status, zero_spec));
     } else {
         const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
         size_t smem = sizeof(float) * (size_t)SB * win;
@@ -1030,7 +1036,7 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
 }
 
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
-                     double *d_out, long long out_stride, double *d_minmax) {
+                     double *d_out, long long out_stride, double *d_minmax, const unsigned char *zero_spec) {
     const int ns = s1 - s0;
     if (ns <= 0) return SOAPGB_OK;
     if (R.b_every > 0 && s0 % R.b_every != 0)
@@ -1045,7 +1051,7 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     k_mm32_init<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, R.sentinel, mm32, mm);
     SOAP_LAUNCHED(ctx);
     int rc = conv32_run(ctx, n, n_eff, R.wid, R.halo, R.p32, sp, spec_stride, ns, R.b32a, R.b32b, R.c32a, R.c32b,
-                        R.b_every, conv, mm32, blk);
+                        R.b_every, conv, mm32, blk, zero_spec ? zero_spec + s0 : nullptr);
     if (rc) return rc;
     dim3 g2(R.nbx, ns);
     SOAP_TRACED(ctx, "refine64",

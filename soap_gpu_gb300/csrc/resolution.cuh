@@ -36,5 +36,6 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
                          double sigma_v, double window, double step_mult, double step_exp, double sentinel,
                          char *scratch, Res32 &R);
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
-                     double *d_out, long long out_stride, double *d_minmax);
+                     double *d_out, long long out_stride, double *d_minmax,
+                     const unsigned char *zero_spec = nullptr);   // [n_spec]: 1 = spectrum known to be zero
 }  // namespace soapgb

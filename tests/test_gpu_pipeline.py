@@ -81,3 +81,39 @@ def test_pipeline_host_chunks_equal_device(ctx, setup):
     assert np.array_equal(low_h, low_d.cpu().numpy())
     assert np.array_equal(raw_h, raw_d.cpu().numpy())
     assert np.all(np.isfinite(low_h)) and np.any(low_h != 1.0)
+
+
+def test_pipeline_descriptors_and_wave_edges(ctx, setup):
+    """Device buffers: phase descriptors from host memory (no synchronisation) and from
+    device memory give the same spectra; a device wavelength array changed in place
+    after its edge values were cached is reported by the next synchronisation, and the
+    call after that reads the array again."""
+    torch = pytest.importorskip("torch")
+    case, inp, n_eff, maps, cb, act, regions = setup
+    q_norm = ctx.quiet_disk("fast32", inp.wave, inp.q_norm, n_eff, maps, case.grid, case.step)
+    q_sed = ctx.quiet_disk("fast32", inp.wave, inp.q_sed, n_eff, maps, case.grid, case.step)
+    star = _star(case, inp.lb)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda:0")
+    maps_d = {k: dev(v) for k, v in maps.items()}
+    cb_d = {k: dev(v) for k, v in cb.items()}
+    wave_d = dev(inp.wave)
+
+    def run(phases):
+        out = ctx.phase_pipeline("fast32", wave_d, n_eff, star, maps_d, cb_d, case.step, act, phases, regions,
+                                 dev(q_sed), dev(q_norm), case.sigma_v, conv_step=case.step)
+        ctx.synchronize()
+        return out.cpu().numpy()
+
+    a = run(np.asarray(case.phases))        # host descriptors
+    b = run(dev(case.phases))               # device descriptors
+    c = run(np.asarray(case.phases))        # cached edges, confirmed on the device
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    w1 = wave_d[1].clone()
+    wave_d[1] = w1 + 1e-9                   # same array, new second value
+    ctx.phase_pipeline("fast32", wave_d, n_eff, star, maps_d, cb_d, case.step, act, np.asarray(case.phases),
+                       regions, dev(q_sed), dev(q_norm), case.sigma_v, conv_step=case.step)
+    with pytest.raises(RuntimeError, match="status 51"):
+        ctx.synchronize()
+    wave_d[1] = w1
+    d = run(np.asarray(case.phases))        # read again after the report
+    assert np.array_equal(a, d)

@@ -55,3 +55,35 @@ def test_reference_layout_round_trip(tmp_path):
         assert mask.shape[1] == 2
     finally:
         os.chdir(cwd)
+
+
+def _narrow_rne(v):
+    """The integer-pipe FP64 -> FP32 rounding of the FP32 cube conversion (fir.cu,
+    soap_f64_to_f32), restated with numpy integers for normal-range results."""
+    u = v.view(np.uint64)
+    e = ((u >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    frac = u & np.uint64(0xFFFFFFFFFFFFF)
+    keep = (frac >> np.uint64(29)).astype(np.uint64)
+    rest = frac & np.uint64(0x1FFFFFFF)
+    bits = (((e - 1023 + 127).astype(np.uint64)) << np.uint64(23)) | keep
+    half = np.uint64(0x10000000)
+    up = (rest > half) | ((rest == half) & ((keep & np.uint64(1)) == np.uint64(1)))
+    bits = bits + up.astype(np.uint64)
+    bits = bits | ((u >> np.uint64(32)) & np.uint64(0x80000000))
+    return bits.astype(np.uint32).view(np.float32)
+
+
+def test_fp32_narrowing_rounds_to_nearest_even():
+    rng = np.random.default_rng(3)
+    v = rng.uniform(-2.0, 2.0, 200000) * 10.0 ** rng.integers(-30, 30, 200000)
+    # exact halfway cases (odd and even kept bit) and one below / above half
+    base = rng.uniform(1.0, 2.0, 1000).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(base.astype(np.float32)).astype(np.float64)
+    v = np.concatenate([v, base + ulp / 2, base + ulp * 1.5, np.nextafter(base + ulp / 2, 0),
+                        np.nextafter(base + ulp / 2, 10), -(base + ulp / 2),
+                        [np.float64(np.finfo(np.float32).max) * (1 + 2.0 ** -25)]])
+    e = (v.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    v = v[(e >= 1023 - 126) & (e <= 1023 + 127)]
+    with np.errstate(over="ignore"):
+        ref = v.astype(np.float32)
+    assert np.array_equal(_narrow_rne(v).view(np.uint32), ref.view(np.uint32))
