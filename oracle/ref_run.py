@@ -6,7 +6,7 @@ contract run_all_SOAP.py uses (run_all_SOAP.py:160-250), and compares every file
 they write.  Usage (on a GPU host, after ``__graft_entry__.build()``):
 
     python -m oracle.ref_run --case 0 --out gpurun_out/ref_case0
-    python -m oracle.ref_run --case 1 --phases 4 --out gpurun_out/ref_case1 --only-time
+    python -m oracle.ref_run --case 1 --phases 10 --rot-step 0.1 --out gpurun_out/ref_case1
 
 Writes ``summary.json`` under --out with the per-file differences and the wall time
 of every stage of every implementation.
@@ -30,10 +30,14 @@ if ROOT not in sys.path:
 from soap_gpu_gb300 import config as cfgmod, synth  # noqa: E402
 
 
-def prepare(case, root, n_phase=None):
-    """Synthetic inputs + the driver's map files (run_all_SOAP.py:160-220)."""
+def prepare(case, root, n_phase=None, rot_step=None):
+    """Synthetic inputs + the driver's map files (run_all_SOAP.py:160-220).  n_phase and
+    rot_step override the case's (phases = arange(0, n_phase * rot_step, rot_step), as
+    run_all_SOAP.py:191 forms them), so that a short run can still span the rotation."""
     if n_phase is not None:
         case.n_phase = n_phase
+    if rot_step is not None:
+        case.rot_step = rot_step
     inp = synth.generate(case)
     os.makedirs(root, exist_ok=True)
     cfg_path = synth.write_reference_layout(inp, root)
@@ -169,6 +173,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", type=int, default=0)
     ap.add_argument("--phases", type=int, default=None)
+    ap.add_argument("--rot-step", type=float, default=None)
     ap.add_argument("--out", default="gpurun_out/ref_run")
     ap.add_argument("--work", default="/tmp/soap_ref_run")
     ap.add_argument("--only-time", action="store_true")
@@ -182,7 +187,7 @@ def main():
     roots = {}
     for impl in impls:
         root = os.path.join(args.work, impl)
-        inp, cfg_path = prepare(synth.make_case(args.case), root, args.phases)
+        inp, cfg_path = prepare(synth.make_case(args.case), root, args.phases, args.rot_step)
         rc = cfgmod.load_config(cfg_path)
         env = dict(os.environ)
         if impl in ("patched", "asis"):

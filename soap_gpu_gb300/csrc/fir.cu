@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(512) k_fir_plists(long long gm, const int *__r
 // marked in three bitmaps over the velocity order (one per class) in shared memory; an
 // ordered compaction of the bitmaps gives the same lists as k_fir_lists / k_fir_plists
 // on the maps of k_phase_scan, with no sort and no G*G map per phase.
-constexpr int FIR_BLIST_THREADS = 512;
+constexpr int FIR_BLIST_THREADS = 1024;
 constexpr size_t FIR_BLIST_SMEM_MAX = 180 * 1024;
 
 __global__ void __launch_bounds__(FIR_BLIST_THREADS)
@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(FIR_BLIST_THREADS)
     if (tid < 3) ctot[tid] = 0;
     __syncthreads();
     const int r0 = reg_off[l], r1 = reg_off[l + 1];
+    const float delta_f = (float)delta_grid;
     for (int r = r0; r < r1; ++r) {
         const RegionPhase rp = table[r];
         const int by = rp.iy1 - rp.iy0, bz = rp.iz1 - rp.iz0;
@@ -381,9 +382,15 @@ __global__ void __launch_bounds__(FIR_BLIST_THREADS)
         const int nbox = by * bz;
         for (int q = tid; q < nbox; q += FIR_BLIST_THREADS) {
             const int iy = rp.iy0 + q / bz, iz = rp.iz0 + q % bz;
-            double t, b;
-            if (region_cell_value(table, r0, r1, iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b) != r)
-                continue;
+            int owner = region_owner_fp32(table, r0, r1, iy, iz, delta_f);
+            if (owner == -2) {
+                double t, b;
+                owner = region_cell_value(table, r0, r1, iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b);
+            }
+            if (owner != r) continue;
+            // the class needs the type alone: a spot's temperature t_star - t_diff_spot is
+            // integral, a facula's class does not depend on its temperature
+            const double t = (double)(t_star - t_diff_spot), b = (rp.type == 0) ? 0.0 : 1.0;
             const int k = iy * grid + iz;
             const int c = fir_class_tb(geo[k], t, b, solar);
             if (c < 0) continue;

@@ -54,6 +54,39 @@ __device__ __forceinline__ int region_cell_value(const RegionPhase *__restrict__
     return owner;
 }
 
+// The index of the region that sets cell (iy, iz) -- the same answer as
+// region_cell_value -- from FP32 arithmetic where that answer is certain, or -2 when
+// a test lies within the FP32 error bound of its threshold (the caller then evaluates
+// region_cell_value in FP64).  Error bound: y and z differ from the FP64 values by at
+// most 3e-7, y^2 + z^2 by 1.6e-6; with 1 - y^2 - z^2 >= 1e-2 the square root differs
+// by 2.1e-5, xi0 by 2.3e-5 and xi0^2 - (1 - s^2) by 4.7e-5.  The margins below are 10x
+// (disk) and 4x (cap) those bounds; cells within 1e-2 of the limb go to FP64.
+__device__ __forceinline__ int region_owner_fp32(const RegionPhase *__restrict__ table, int r0, int r1, int iy, int iz,
+                                                 float delta_grid) {
+    const float y = fmaf((float)iy, delta_grid, -1.f), z = fmaf((float)iz, delta_grid, -1.f);
+    const float q = fmaf(y, y, z * z);
+    int owner = -1;
+    bool inside_disk = false, disk_known = false;
+    for (int r = r0; r < r1; ++r) {
+        const RegionPhase rp = table[r];
+        if (!rp.visible || iy < rp.iy0 || iy >= rp.iy1 || iz < rp.iz0 || iz >= rp.iz1) continue;
+        if (!disk_known) {
+            if (fabsf(q - 1.f) <= 4e-5f) return -2;
+            inside_disk = q < 1.f;
+            disk_known = true;
+        }
+        if (!inside_disk) continue;
+        const float rest = 1.f - q;
+        if (rest < 1e-2f) return -2;
+        const float xa = sqrtf(rest);
+        const float xi = fmaf((float)rp.r0, xa, fmaf((float)rp.r1, y, (float)rp.r2 * z));
+        const float d = fmaf(xi, xi, -(float)(1.0 - rp.s * rp.s));
+        if (fabsf(d) <= 2e-4f) return -2;
+        if (d > 0.f) owner = r;
+    }
+    return owner;
+}
+
 namespace soapgb {
 // The region table of n_phase phases built on the host and copied to scratch:
 // *d_table (reg_off[n_phase] rows) and *d_off (n_phase + 1 offsets); phase_visible
