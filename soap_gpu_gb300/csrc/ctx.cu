@@ -165,6 +165,13 @@ TraceScope::~TraceScope() {
     ctx->spans.push_back(SoapTraceSpan{name, a, b});
 }
 
+int aux_resources(soapgb_ctx *ctx) {
+    if (!ctx->aux_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+    for (int q = 0; q < 2; ++q)
+        if (!ctx->aux_events[q]) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_events[q], cudaEventDisableTiming));
+    return SOAPGB_OK;
+}
+
 int copy_resources(soapgb_ctx *ctx, int count) {
     if (!ctx->copy_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     while ((int)ctx->sync_events.size() < count) {
@@ -272,6 +279,12 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     }
     for (auto e : ctx->ev_free) cudaEventDestroy(e);
     for (auto e : ctx->sync_events) cudaEventDestroy(e);
+    for (auto e : ctx->aux_events)
+        if (e) cudaEventDestroy(e);
+    if (ctx->aux_stream) {
+        cudaStreamSynchronize(ctx->aux_stream);
+        cudaStreamDestroy(ctx->aux_stream);
+    }
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);

@@ -1505,11 +1505,12 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
 // true: a work unit's cube rows are staged in shared memory by TMA before it is applied;
 // false: the apply loops read them from global memory (L1-cached), with no per-unit barrier
 constexpr bool FIR_PP_STAGED = true;
+constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per cube row
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
 struct FirPPSmem {
-    T win[2][4][FIR_WIN];
+    T win[FIR_PP_STAGED ? 2 : 1][4][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
     unsigned long long wbar[2], pbar[2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
@@ -1522,14 +1523,16 @@ struct FirPPSmem {
 template <typename T>
 __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPSmem<T>) + 15) & ~size_t(15); }
 
-// Block b walks the (phase, tile) pairs tau = b, b + G, ... (tau = phase * ntile + tile;
-// with a run list, phase = run_list[tau / ntile]).
+// The (phase, tile) pairs of the phases [r0, r0 + nr) (of the run list, when there is
+// one) are walked tile by tile -- position v is tile v / nr of phase r0 + v % nr -- and
+// block b takes the consecutive positions [b per, (b + 1) per): one block works through
+// the phases of one tile, so consecutive phases read the same cube rows (L1 / L2).
 // A tile's compact plan (k_fir_plan) is copied by TMA one tile ahead into the other plan
 // buffer; the cube windows of its work units stream through two buffers, and the first
 // unit of the next tile is issued while the current tile's last unit is applied, so the
 // copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
 template <typename T>
-__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int tau0, int ntot,
+__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int r0, int nr,
                                                         int ntot_all) {
     constexpr int NC = 4;
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
@@ -1554,8 +1557,13 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     }
     __syncthreads();
 
-    // (phase, tile) index of walk position t
-    auto real = [&](int t) -> int { return A.run_list ? A.run_list[t / ntile] * ntile + t % ntile : t; };
+    // (phase, tile) index (phase * ntile + tile) of walk position v
+    auto real = [&](int v) -> int {
+        const int li = r0 + v % nr;
+        return (A.run_list ? A.run_list[li] : li) * ntile + v / nr;
+    };
+    const int total = nr * ntile, per = (total + G - 1) / G;
+    const int vb = min(total, (int)blockIdx.x * per), ve = min(total, vb + per);
     // (thread 0) copy the plan of tile tau (bytes long) into plan buffer b
     auto issue_plan = [&](int tau, int b, unsigned bytes) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -1623,7 +1631,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         int off;
         bool staged;
     };
-    auto src_of = [&](const T (*W)[FIR_WIN], const FirUnit &d) {
+    auto src_of = [&](const T (*W)[FIR_PP_WIN], const FirUnit &d) {
         Src sr;
         if (FIR_PP_STAGED) {
             for (int c = 0; c < 4; ++c) sr.p[c] = W[c];
@@ -1724,28 +1732,27 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         return sh.fail == 0;
     };
 
-    // tiles tau in [tau0, ntot)
+    // walk positions [vb, ve)
     if (tid == 0) {
-        const int t0 = tau0 + (int)blockIdx.x;
-        if (t0 < ntot) issue_plan(real(t0), 0, (unsigned)psize[real(t0)]);
-        if (t0 + G < ntot) issue_plan(real(t0 + G), 1, (unsigned)psize[real(t0 + G)]);
+        if (vb < ve) issue_plan(real(vb), 0, (unsigned)psize[real(vb)]);
+        if (vb + 1 < ve) issue_plan(real(vb + 1), 1, (unsigned)psize[real(vb + 1)]);
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount & 1)
     bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
     int k = 0;
     int bad = 0;
-    for (int tau = tau0 + (int)blockIdx.x; tau < ntot && !bad; tau += G, ++k) {
+    for (int v = vb; v < ve && !bad; ++v, ++k) {
         const int pbuf = k & 1;
         // size of the plan issued at the end of this tile, read early (its latency hides
         // behind the tile's work)
-        const unsigned next_bytes = (tid == 0 && tau + 2 * G < ntot) ? (unsigned)psize[real(tau + 2 * G)] : 0u;
+        const unsigned next_bytes = (tid == 0 && v + 2 < ve) ? (unsigned)psize[real(v + 2)] : 0u;
         if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1))) atomicExch(&sh.fail, 1);
         __syncthreads();
         if (sh.fail) {
             bad = 1;
             break;
         }
-        const int tr = real(tau);
+        const int tr = real(v);
         const int l = tr / ntile, j0 = (tr - l * ntile) * FIR_TILE;
         const int t_eff = min(FIR_TILE, n_eff - j0);
         const long long lbase = (long long)l * A.gm;
@@ -1780,8 +1787,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     } else {
                         // last unit: issue the next tile's first unit, from its plan
                         pre = false;
-                        const int tn = tau + G;
-                        if (tn < ntot && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
+                        const int tn = v + 1;
+                        if (tn < ve && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
                             const int tnr = real(tn);
@@ -1820,19 +1827,18 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                 const int nb = st.nb;
                 for (int ui = 0; ui < nb; ++ui) {
                     const int u = ucount;
-                    if (tid == 0) {
-                        if (ui == 0) issue_unit(u, st.unit[0]);
-                        if (ui + 1 < nb) issue_unit(u + 1, st.unit[ui + 1]);
-                    }
-                    if (!wait_unit(u)) {
-                        bad = 1;
-                        break;
+                    if (FIR_PP_STAGED) {
+                        if (tid == 0) {
+                            if (ui == 0) issue_unit(u, st.unit[0]);
+                            if (ui + 1 < nb) issue_unit(u + 1, st.unit[ui + 1]);
+                        }
+                        if (!wait_unit(u)) {
+                            bad = 1;
+                            break;
+                        }
                     }
                     const FirUnit d = st.unit[ui];
-                    Src sr;
-                    for (int c = 0; c < 4; ++c) sr.p[c] = sh.win[u & 1][c];
-                    sr.off = d.off - d.w0;
-                    sr.staged = true;
+                    const Src sr = src_of(sh.win[FIR_PP_STAGED ? (u & 1) : 0], d);
                     part_zero();
                     apply_groups(sr, d, st.grp, st.ut[ui], st.ut[ui + 1], j0, t_eff);
                     const int e_lo = st.woff[st.ut[ui]], e_hi = st.woff[st.ut[ui + 1]];
@@ -1952,14 +1958,16 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
             for (int a = 0; a < 7; ++a) acc[a][q].zero();
         }
         __syncthreads();   // plan buffer pbuf free
-        if (tid == 0 && tau + 2 * G < ntot) issue_plan(real(tau + 2 * G), pbuf, next_bytes);
+        if (tid == 0 && v + 2 < ve) issue_plan(real(v + 2), pbuf, next_bytes);
     }
     if (bad && tid == 0) {
         // a copy did not land in time: record it and give the copies possibly in flight a
         // bounded wait before leaving
         atomicExch(A.status, FIR_ST_WAIT);
-        mbar_wait_bounded(&sh.wbar[ucount & 1], (unsigned)((ucount >> 1) & 1));
-        mbar_wait_bounded(&sh.wbar[(ucount + 1) & 1], (unsigned)(((ucount + 1) >> 1) & 1));
+        if (FIR_PP_STAGED) {
+            mbar_wait_bounded(&sh.wbar[ucount & 1], (unsigned)((ucount >> 1) & 1));
+            mbar_wait_bounded(&sh.wbar[(ucount + 1) & 1], (unsigned)(((ucount + 1) >> 1) & 1));
+        }
         mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1));
         mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1));
     }
@@ -2201,14 +2209,14 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
             SOAP_LAUNCHED(ctx);
         }
         if ((stage & 4) && r1 > r0) {
-            const int tau0 = ntile * r0, ntot = ntile * r1, nrun = ntot - tau0;
+            const int nrun = ntile * (r1 - r0);
             size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
             SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
             int per_sm = 0;
             SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fir_pp<T>, FIR_THREADS, smem_t));
             const int nblk = std::max(1, std::min(nrun, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
             SOAP_TRACED(ctx, "fir_tile_phase",
-                        k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, tau0, ntot,
+                        k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, r0, r1 - r0,
                                                                                 ntile * n_lists));
             SOAP_LAUNCHED(ctx);
         }

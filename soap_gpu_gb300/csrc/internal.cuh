@@ -32,6 +32,10 @@ struct soapgb_ctx {
     // second stream for copies that overlap kernels (created on first use) and events
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> sync_events;
+    // second compute stream for independent stages (created on first use) and its two
+    // ordering events (main -> aux at the start, aux -> main at the join)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t aux_events[2] = {nullptr, nullptr};
     // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
     // once; later calls with the same array confirm them on the device, status 51)
     const double *edge_wave = nullptr;
@@ -103,6 +107,16 @@ int grid_for(soapgb_ctx *ctx, long long work, int block);
 
 // the context's copy stream and at least `count` synchronisation events (created once)
 int copy_resources(soapgb_ctx *ctx, int count);
+int aux_resources(soapgb_ctx *ctx);
+
+// Launches made while an AuxScope is alive go to the context's aux stream (the stream
+// member is switched and restored; every launch of the library reads ctx->stream).
+struct AuxScope {
+    soapgb_ctx *ctx;
+    cudaStream_t saved;
+    explicit AuxScope(soapgb_ctx *c) : ctx(c), saved(c->stream) { ctx->stream = ctx->aux_stream; }
+    ~AuxScope() { ctx->stream = saved; }
+};
 
 // Scope around a kernel launch: with tracing on, CUDA events on the context's stream
 // bracket the launch (records nothing otherwise).

@@ -230,18 +230,30 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.out_f32 = f32;
         fa.out_stride = 3LL * n;
         fa.lambda0 = w3[0];
+        // The typed cubes and the convolution set-up (tap constants, FP64 base
+        // convolutions) do not depend on the geometry stage (cell order, lists, plans),
+        // which is latency-bound: they run beside it on the aux stream.
+        rc = aux_resources(ctx);
+        if (rc) return rc;
+        SOAP_CUDA(ctx, cudaEventRecord(ctx->aux_events[0], ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_events[0], 0));
+        if (overlap) SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->sync_events[1], 0));   // cubes in
+        Res32 R;
+        {
+            AuxScope aux(ctx);
+            fa.stage = FIR_STAGE_CUBES;
+            rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+            if (!rc && f32)
+                rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3,
+                                          sigma_v, 50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
+            if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
+        }
+        if (rc) return rc;
         fa.stage = FIR_STAGE_GEOMETRY;
         rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
         if (rc) return rc;
-        if (overlap) SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->sync_events[1], 0));   // cubes in
-        fa.stage = FIR_STAGE_CUBES;
-        rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
-        if (rc) return rc;
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
         if (f32) {
-            Res32 R;
-            rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3, sigma_v,
-                                      50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
-            if (rc) return rc;
             for (int c = 0; c < n_chunk; ++c) {
                 const int p0 = c * per_chunk, p1 = std::min(n_phase, p0 + per_chunk);
                 fa.stage = FIR_STAGE_RUN;

@@ -727,9 +727,11 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
     }
 }
 
-// pass 2 of the fused form: exact FP64 extrema of the candidate pixels of the blocks
-// (1024 pixels each) that can hold one.  grid (blocks, spectra)
-__global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, const float *__restrict__ spec,
+// pass 2 of the fused form: exact FP64 extrema of the candidate pixels of the pixel
+// blocks (1024 pixels each) that can hold one.  grid (ceil(nbx / 8), spectra): warp w
+// of a block takes pixel block 8 blockIdx.x + w when its FP32 bounds make it a
+// candidate (most are not, and their warps leave at once).
+__global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, int nbx, const float *__restrict__ spec,
                                                    long long spec_stride, const double *__restrict__ ba,
                                                    const double *__restrict__ bb, const double *__restrict__ cba,
                                                    const double *__restrict__ cbb, const float *__restrict__ b32a,
@@ -739,12 +741,14 @@ __global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, const float
                                                    const unsigned *__restrict__ mm32, const float *__restrict__ blk,
                                                    unsigned long long *mm64) {
     const int s = blockIdx.y;
+    const int x = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (x >= nbx) return;
     const float mnA = soap_dec32(mm32[4 * s + 0]), mxC = soap_dec32(mm32[4 * s + 1]);
     const float tolA = ldexpf(soap_dec32(mm32[4 * s + 2]), -21), tolC = ldexpf(soap_dec32(mm32[4 * s + 3]), -21);
-    const float *bk = blk + ((long long)s * gridDim.x + blockIdx.x) * 2;
+    const float *bk = blk + ((long long)s * nbx + x) * 2;
     const bool needA = bk[0] <= mnA + tolA;
     const bool needC = (mm32[4 * s + 1] != 0u) && (bk[1] >= mxC - tolC);
-    if (!needA && !needC) return;          // uniform for the whole block
+    if (!needA && !needC) return;          // uniform for the warp
     const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
     const float *sp = spec + (long long)s * spec_stride;
     const float *bs = use_b ? b32b : b32a;
@@ -753,11 +757,11 @@ __global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, const float
     const double *c64 = use_b ? cbb : cba;
     const float *cv = conv + (long long)s * conv_stride;
     unsigned long long mn = ~0ULL, mx = 0ULL;
-    const int i_end = min(n, (int)(blockIdx.x + 1) * FC_TILE);
-    for (int i = blockIdx.x * FC_TILE + threadIdx.x; i < i_end; i += blockDim.x) {
-        const float x = sp[i];
-        if (needA && bs[i] - x <= mnA + tolA) {
-            const double a = b64[i] - (double)x;
+    const int i_end = min(n, (x + 1) * FC_TILE);
+    for (int i = x * FC_TILE + lane; i < i_end; i += 32) {
+        const float xv = sp[i];
+        if (needA && bs[i] - xv <= mnA + tolA) {
+            const double a = b64[i] - (double)xv;
             mn = min(mn, soap_ord_enc(a));
         }
         if (needC && i < n_eff) {
@@ -773,7 +777,7 @@ __global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, const float
         mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         if (mn != ~0ULL) atomicMin(&mm64[2 * s], mn);
         if (mx != 0ULL) atomicMax(&mm64[2 * s + 1], mx);
     }
@@ -1053,11 +1057,10 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     int rc = conv32_run(ctx, n, n_eff, R.wid, R.halo, R.p32, sp, spec_stride, ns, R.b32a, R.b32b, R.c32a, R.c32b,
                         R.b_every, conv, mm32, blk, zero_spec ? zero_spec + s0 : nullptr);
     if (rc) return rc;
-    dim3 g2(R.nbx, ns);
     SOAP_TRACED(ctx, "refine64",
-                k_refine64x<<<g2, 256, 0, ctx->stream>>>(n, n_eff, sp, spec_stride, R.base_a, R.base_b, R.cb_a,
-                                                         R.cb_b, R.b32a, R.b32b, R.c32a, R.c32b, R.b_every, conv,
-                                                         n_eff, mm32, blk, mm));
+                k_refine64x<<<dim3((R.nbx + 7) / 8, ns), 256, 0, ctx->stream>>>(n, n_eff, R.nbx, sp, spec_stride, R.base_a, R.base_b,
+                                                         R.cb_a, R.cb_b, R.b32a, R.b32b, R.c32a, R.c32b, R.b_every,
+                                                         conv, n_eff, mm32, blk, mm));
     SOAP_LAUNCHED(ctx);
     k_factor<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, mm, fac, d_minmax ? d_minmax + 2LL * s0 : nullptr);
     SOAP_LAUNCHED(ctx);
