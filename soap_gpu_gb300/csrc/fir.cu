@@ -1506,13 +1506,17 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
 // false: the apply loops read them from global memory (L1-cached), with no per-unit barrier
 constexpr bool FIR_PP_STAGED = true;
 constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per cube row
+// window buffers: unit u is staged in buffer u % 3, so the copy of unit u + 1 (issued
+// before unit u is applied) lands in the buffer of unit u - 2, which every thread left
+// before the barrier of unit u - 1: one barrier per unit
+constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
 struct FirPPSmem {
-    T win[FIR_PP_STAGED ? 2 : 1][4][FIR_PP_WIN];
+    T win[FIR_PP_NBUF][4][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
-    unsigned long long wbar[2], pbar[2];
+    unsigned long long wbar[3], pbar[2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
     FirExcD<T> excd[64];
     int wsum[FIR_THREADS / 32];
@@ -1550,6 +1554,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     if (tid == 0) {
         mbar_init(&sh.wbar[0], 1);
         mbar_init(&sh.wbar[1], 1);
+        mbar_init(&sh.wbar[2], 1);
         mbar_init(&sh.pbar[0], 1);
         mbar_init(&sh.pbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1570,9 +1575,9 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         mbar_expect_tx(&sh.pbar[b], bytes);
         bulk_g2s(&sh.pb[b][0], plans + (size_t)tau * SLOT, bytes, &sh.pbar[b]);
     };
-    // (thread 0) stage the rows of unit number u (buffer u & 1)
+    // (thread 0) stage the rows of unit number u (buffer u % 3)
     auto issue_unit = [&](int u, const FirUnit &d) {
-        const int b = u & 1;
+        const int b = FIR_PP_STAGED ? u % 3 : 0;
         unsigned bytes = 0;
         uintptr_t rel = 0;
         if (d.w1 > d.w0) {
@@ -1727,7 +1732,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     };
     // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
     auto wait_unit = [&](int u) {
-        if (!mbar_wait_bounded(&sh.wbar[u & 1], (unsigned)((u >> 1) & 1))) atomicExch(&sh.fail, 1);
+        if (!mbar_wait_bounded(&sh.wbar[u % 3], (unsigned)((u / 3) & 1))) atomicExch(&sh.fail, 1);
         __syncthreads();
         return sh.fail == 0;
     };
@@ -1737,7 +1742,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         if (vb < ve) issue_plan(real(vb), 0, (unsigned)psize[real(vb)]);
         if (vb + 1 < ve) issue_plan(real(vb + 1), 1, (unsigned)psize[real(vb + 1)]);
     }
-    int ucount = 0;        // units staged and applied so far (window buffer ucount & 1)
+    int ucount = 0;        // units staged and applied so far (window buffer ucount % 3)
     bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
     int k = 0;
     int bad = 0;
@@ -1806,14 +1811,13 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     break;
                 }
                 const FirUnit d = units[ui];
-                const Src sr = src_of(sh.win[u & 1], d);
+                const Src sr = src_of(sh.win[FIR_PP_STAGED ? u % 3 : 0], d);
                 part_zero();
                 apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
                 const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
                 apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
                 part_fold(d.cls);
-                __syncthreads();
-                ++ucount;
+                ++ucount;   // no barrier: the next copies go to other buffers
             }
         } else if (t_eff > 0) {
             // --- tile that plans itself, batch by batch ----------------------------------
@@ -1838,7 +1842,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                         }
                     }
                     const FirUnit d = st.unit[ui];
-                    const Src sr = src_of(sh.win[FIR_PP_STAGED ? (u & 1) : 0], d);
+                    const Src sr = src_of(sh.win[FIR_PP_STAGED ? u % 3 : 0], d);
                     part_zero();
                     apply_groups(sr, d, st.grp, st.ut[ui], st.ut[ui + 1], j0, t_eff);
                     const int e_lo = st.woff[st.ut[ui]], e_hi = st.woff[st.ut[ui + 1]];
@@ -1965,8 +1969,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         // bounded wait before leaving
         atomicExch(A.status, FIR_ST_WAIT);
         if (FIR_PP_STAGED) {
-            mbar_wait_bounded(&sh.wbar[ucount & 1], (unsigned)((ucount >> 1) & 1));
-            mbar_wait_bounded(&sh.wbar[(ucount + 1) & 1], (unsigned)(((ucount + 1) >> 1) & 1));
+            mbar_wait_bounded(&sh.wbar[ucount % 3], (unsigned)((ucount / 3) & 1));
+            mbar_wait_bounded(&sh.wbar[(ucount + 1) % 3], (unsigned)(((ucount + 1) / 3) & 1));
         }
         mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1));
         mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1));
