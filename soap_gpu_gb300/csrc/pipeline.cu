@@ -172,7 +172,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     const RegionPhase *d_table = nullptr;
     const int *d_roff = nullptr;
     // phases with a visible region are integrated; the others have no active cell
-    std::vector<unsigned char> vis;
+    std::vector<unsigned char> vis, zspec;
     std::vector<int> h_lists;   // run list, then zero list
     int n_run = 0;
     if (box_lists) {
@@ -186,7 +186,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         for (int p = 0; p < n_phase; ++p)
             if (!vis[p]) h_lists.push_back(p);
         // spectra of the phases without a visible region are zero
-        std::vector<unsigned char> zspec((size_t)n_spec);
+        zspec.assign((size_t)n_spec, 0);
         for (int p = 0; p < n_phase; ++p) zspec[3 * p] = zspec[3 * p + 1] = zspec[3 * p + 2] = vis[p] ? 0 : 1;
         // pageable sources: staged by the driver before the calls return
         SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<int>(s_lists), h_lists.data(), sizeof(int) * n_phase,
@@ -262,7 +262,8 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
                 if (rc) return rc;
                 rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr,
-                                      box_lists ? ws.get<unsigned char>(s_zspec) : nullptr);
+                                      box_lists ? ws.get<unsigned char>(s_zspec) : nullptr,
+                                      box_lists ? zspec.data() : nullptr);
                 if (rc) return rc;
                 if (host) {
                     cudaEvent_t ev = ctx->sync_events[2 + c];

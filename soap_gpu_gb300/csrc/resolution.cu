@@ -17,6 +17,7 @@
 //               (deterministic), then an FP64 normalisation pass.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "internal.cuh"
 #include "resolution.cuh"
@@ -341,10 +342,12 @@ __global__ void k_base_prep(int n, int n_eff, const double *__restrict__ base, c
 __global__ void k_mm32_init(int n_spec, double sentinel, unsigned *mm32, unsigned long long *mm64) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n_spec) {
-        mm32[4 * s + 0] = 0xffffffffu;                 // min A (FP32 key)
-        mm32[4 * s + 1] = 0u;                          // max C (FP32 key)
-        mm32[4 * s + 2] = 0u;                          // max(|base| + |spec|)
-        mm32[4 * s + 3] = 0u;                          // max(|cb| + |conv|)
+        if (mm32) {
+            mm32[4 * s + 0] = 0xffffffffu;             // min A (FP32 key)
+            mm32[4 * s + 1] = 0u;                      // max C (FP32 key)
+            mm32[4 * s + 2] = 0u;                      // max(|base| + |spec|)
+            mm32[4 * s + 3] = 0u;                      // max(|cb| + |conv|)
+        }
         mm64[2 * s + 0] = ~0ULL;
         mm64[2 * s + 1] = soap_ord_enc(sentinel);
     }
@@ -604,7 +607,8 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
                                                         const float *__restrict__ c32b, int b_every,
                                                         float *__restrict__ conv, long long conv_stride,
                                                         unsigned *mm32, float *blk, int nbx, int *status,
-                                                        const unsigned char *__restrict__ zero_spec) {
+                                                        const unsigned char *__restrict__ zero_spec,
+                                                        const int *__restrict__ blist, int nlist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[SB][4][FC_THREADS / 32];
     __shared__ unsigned long long bar[2];
@@ -620,7 +624,9 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
     const int ca = max(mb, 0);
     const int cb = min(mb + win, (n + 3) & ~3);
     const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
-    const int nbatch = (n_spec + SB - 1) / SB;
+    // the batches to convolve: blist[0, nlist) (batches of zero spectra left out), or all
+    const int nwalk = blist ? nlist : (n_spec + SB - 1) / SB;
+    auto batch_of = [&](int it) { return blist ? blist[it] : it; };
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[0])));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[1])));
@@ -660,10 +666,11 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
     const int R = (i0 < n_eff) ? rblk[blockIdx.x] : 0;
     const int sh = (halo - R + xo) & 3;
     int k = 0, k_fail = -1;
-    if (threadIdx.x == 0 && blockIdx.y < nbatch) issue(blockIdx.y, 0);
-    for (int bt = blockIdx.y; bt < nbatch; bt += gridDim.y, ++k) {
+    if (threadIdx.x == 0 && (int)blockIdx.y < nwalk) issue(batch_of(blockIdx.y), 0);
+    for (int it = blockIdx.y; it < nwalk; it += gridDim.y, ++k) {
+        const int bt = batch_of(it);
         const int buf = k & 1;
-        if (threadIdx.x == 0 && bt + (int)gridDim.y < nbatch) issue(bt + gridDim.y, buf ^ 1);
+        if (threadIdx.x == 0 && it + (int)gridDim.y < nwalk) issue(batch_of(it + gridDim.y), buf ^ 1);
         const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
         float *xs = xbuf + (size_t)buf * SB * win;
         bool ok = false;
@@ -710,7 +717,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
         // a staged copy did not land in time: record it and give the next batch's copy,
         // if one was issued, a bounded wait before leaving
         atomicExch(status, 42);
-        if (blockIdx.y + (k_fail + 1) * (int)gridDim.y < nbatch) {
+        if ((int)blockIdx.y + (k_fail + 1) * (int)gridDim.y < nwalk) {
             const int kb = k_fail + 1;
             const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[kb & 1]);
             for (long long it = 0; it < (1LL << 24); ++it) {
@@ -739,10 +746,11 @@ __global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, int nbx, co
                                                    const float *__restrict__ c32b, int b_every,
                                                    const float *__restrict__ conv, long long conv_stride,
                                                    const unsigned *__restrict__ mm32, const float *__restrict__ blk,
-                                                   unsigned long long *mm64) {
+                                                   unsigned long long *mm64, const unsigned char *__restrict__ zero_spec) {
     const int s = blockIdx.y;
     const int x = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (x >= nbx) return;
+    if (zero_spec && zero_spec[s]) return;   // extrema of the base alone (k_zero_extrema)
     const float mnA = soap_dec32(mm32[4 * s + 0]), mxC = soap_dec32(mm32[4 * s + 1]);
     const float tolA = ldexpf(soap_dec32(mm32[4 * s + 2]), -21), tolC = ldexpf(soap_dec32(mm32[4 * s + 3]), -21);
     const float *bk = blk + ((long long)s * nbx + x) * 2;
@@ -783,6 +791,47 @@ __global__ void __launch_bounds__(256) k_refine64x(int n, int n_eff, int nbx, co
     }
 }
 
+// Exact FP64 extrema of the spectra whose deficit is zero, one per base: what
+// k_refine64x finds for such a spectrum (its candidates hold the extremes of the base
+// alone): min over [0, n) of base, max over [0, n_eff) of the base convolution where
+// its FP32 and FP64 values are non-zero.  mmz[2 q] / mmz[2 q + 1] for base q, set to
+// (~0, sentinel) by k_mm32_init's rule beforehand.  grid (blocks, bases)
+__global__ void __launch_bounds__(256) k_zero_extrema(int n, int n_eff, const double *__restrict__ ba,
+                                                      const double *__restrict__ bb, const double *__restrict__ cba,
+                                                      const double *__restrict__ cbb, const float *__restrict__ c32a,
+                                                      const float *__restrict__ c32b, unsigned long long *mmz) {
+    const int q = blockIdx.y;
+    const double *b64 = q ? bb : ba;
+    const double *c64 = q ? cbb : cba;
+    const float *c32 = q ? c32b : c32a;
+    unsigned long long mn = ~0ULL, mx = 0ULL;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        mn = min(mn, soap_ord_enc(b64[i] - 0.0));
+        if (i < n_eff && c32[i] != 0.f) {
+            const double cx = c64[i] + 0.0;
+            if (cx != 0.0) mx = max(mx, soap_ord_enc(cx));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mn != ~0ULL) atomicMin(&mmz[2 * q], mn);
+        if (mx != 0ULL) atomicMax(&mmz[2 * q + 1], mx);
+    }
+}
+
+// extrema of the zero spectra of a chunk from the per-base values
+__global__ void k_zero_mm(int n_spec, const unsigned char *__restrict__ zero_spec, int b_every,
+                          const unsigned long long *__restrict__ mmz, unsigned long long *mm64) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_spec || !zero_spec[s]) return;
+    const int q = (b_every > 0 && (s % b_every) == b_every - 1) ? 1 : 0;
+    mm64[2 * s] = mmz[2 * q];
+    mm64[2 * s + 1] = mmz[2 * q + 1];
+}
+
 // FP64 normalisation constants per spectrum -> FP32 factor
 __global__ void k_factor(int n_spec, const unsigned long long *__restrict__ mm64, float *fac, double *minmax_out) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -800,13 +849,14 @@ __global__ void __launch_bounds__(256) k_norm32(int n_eff, const float *__restri
                                                 const float *__restrict__ c32b, int b_every,
                                                 const float *__restrict__ conv, long long conv_stride,
                                                 const float *__restrict__ fac, double *__restrict__ out,
-                                                long long out_stride) {
+                                                long long out_stride, const unsigned char *__restrict__ zero_spec) {
     int s = blockIdx.y;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_eff) return;
     bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
     const float *cbs = use_b ? c32b : c32a;
-    float c = cbs[i] + conv[(long long)s * conv_stride + i];
+    const float cd = (zero_spec && zero_spec[s]) ? 0.f : conv[(long long)s * conv_stride + i];
+    float c = cbs[i] + cd;
     out[(long long)s * out_stride + i] = soap_f32_to_f64(fmaf(-c, fac[s], 1.0f));
 }
 
@@ -816,13 +866,15 @@ __global__ void __launch_bounds__(256) k_norm32v(int n_eff, const float *__restr
                                                  const float *__restrict__ c32b, int b_every,
                                                  const float *__restrict__ conv, long long conv_stride,
                                                  const float *__restrict__ fac, double *__restrict__ out,
-                                                 long long out_stride) {
+                                                 long long out_stride, const unsigned char *__restrict__ zero_spec) {
     const int s = blockIdx.y;
     const int i = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n_eff) return;
     const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
     const float4 cb = *reinterpret_cast<const float4 *>((use_b ? c32b : c32a) + i);
-    const float4 cd = *reinterpret_cast<const float4 *>(conv + (long long)s * conv_stride + i);
+    // a zero spectrum's convolution is zero (not computed, not stored)
+    const float4 cd = (zero_spec && zero_spec[s]) ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                  : *reinterpret_cast<const float4 *>(conv + (long long)s * conv_stride + i);
     const float f = fac[s];
     double2 *o = reinterpret_cast<double2 *>(out + (long long)s * out_stride + i);
     o[0] = make_double2(soap_f32_to_f64(fmaf(-(cb.x + cd.x), f, 1.0f)), soap_f32_to_f64(fmaf(-(cb.y + cd.y), f, 1.0f)));
@@ -840,6 +892,7 @@ static size_t conv_param_bytes(int n_eff) {
 size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
     size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
     b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
+    b += sizeof(unsigned long long) * 4 + 256 + sizeof(int) * ((size_t)n_spec / 8 + 2) + 256;   // zero spectra
     if (form != SOAPGB_PLAIN64)
         b += 2 * (sizeof(double) * (size_t)n_eff + 256) + 2 * (conv_param_bytes(n_eff) + 256) +
              2 * sizeof(double) * (size_t)n + 256;   // base convolutions, tap constants, staged bases
@@ -923,7 +976,7 @@ static int conv32_params(soapgb_ctx *ctx, int n, int n_eff, const double *lam, d
 static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, const char *param_scratch,
                       const float *spec, long long spec_stride, int n_spec, const float *b32a, const float *b32b,
                       const float *c32a, const float *c32b, int b_every, float *conv, unsigned *mm32, float *blk,
-                      const unsigned char *zero_spec) {
+                      const unsigned char *zero_spec, const int *blist, int nlist) {
     constexpr int SB = 8;
     const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
     const float *c2 = (const float *)param_scratch;
@@ -938,11 +991,14 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         size_t smem_t = sizeof(float) * 2 * (size_t)SB * win_t;
         if (smem_t > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32t<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
-        int gy = std::max(1, std::min(nbatch, (2 * std::max(ctx->num_sms, 1) + nbx - 1) / nbx));
+        const int nwalk = blist ? nlist : nbatch;
+        if (nwalk == 0) return SOAPGB_OK;   // every spectrum is zero
+        int gy = std::max(1, std::min(nwalk, (2 * std::max(ctx->num_sms, 1) + nbx - 1) / nbx));
         dim3 g(nbx, gy);
         SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
-                                                              n_eff, mm32, blk, nbx, ctx->d_status, zero_spec));
+                                                              n_eff, mm32, blk, nbx, ctx->d_status, zero_spec,
+                                                              blist, nlist));
     } else {
         const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
         size_t smem = sizeof(float) * (size_t)SB * win;
@@ -1035,12 +1091,22 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
                        &R.halo);
     if (rc) return rc;
     R.p32 = pscr32;
+    // extrema of the zero spectra, per base
+    R.mmz = (unsigned long long *)carve(p, sizeof(unsigned long long) * 4);
+    R.blist = (int *)carve(p, sizeof(int) * ((size_t)n_spec / 8 + 2));
+    k_mm32_init<<<1, 32, 0, ctx->stream>>>(2, sentinel, nullptr, R.mmz);
+    SOAP_LAUNCHED(ctx);
+    k_zero_extrema<<<dim3(std::max(1, std::min(grid_for(ctx, n, 256), 4 * std::max(ctx->num_sms, 1))), R.base_b ? 2 : 1),
+                     256, 0, ctx->stream>>>(n, n_eff, base_a, R.base_b ? R.base_b : base_a, cb_a, cb_b ? cb_b : cb_a,
+                                            c32a, cb_b ? c32b : c32a, R.mmz);
+    SOAP_LAUNCHED(ctx);
     R.next = p;
     return SOAPGB_OK;
 }
 
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
-                     double *d_out, long long out_stride, double *d_minmax, const unsigned char *zero_spec) {
+                     double *d_out, long long out_stride, double *d_minmax, const unsigned char *zero_spec,
+                     const unsigned char *zero_host) {
     const int ns = s1 - s0;
     if (ns <= 0) return SOAPGB_OK;
     if (R.b_every > 0 && s0 % R.b_every != 0)
@@ -1054,13 +1120,32 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     float *blk = R.blk + 2LL * R.nbx * s0;
     k_mm32_init<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, R.sentinel, mm32, mm);
     SOAP_LAUNCHED(ctx);
+    // spectra known to be zero (both flag copies given): their batches are left out of
+    // the convolution and their extrema come from the bases
+    const unsigned char *zs = (zero_spec && zero_host) ? zero_spec + s0 : nullptr;
+    const int *blist = nullptr;
+    int nlist = 0;
+    if (zs) {
+        std::vector<int> bl;
+        for (int b = 0; b * 8 < ns; ++b) {
+            bool all0 = true;
+            for (int q = b * 8; q < std::min(ns, b * 8 + 8) && all0; ++q) all0 = zero_host[s0 + q] != 0;
+            if (!all0) bl.push_back(b);
+        }
+        nlist = (int)bl.size();
+        if (nlist > 0)   // pageable source: staged by the driver before the call returns
+            SOAP_CUDA(ctx, cudaMemcpyAsync(R.blist, bl.data(), sizeof(int) * nlist, cudaMemcpyHostToDevice, ctx->stream));
+        blist = R.blist;
+        k_zero_mm<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, zs, R.b_every, R.mmz, mm);
+        SOAP_LAUNCHED(ctx);
+    }
     int rc = conv32_run(ctx, n, n_eff, R.wid, R.halo, R.p32, sp, spec_stride, ns, R.b32a, R.b32b, R.c32a, R.c32b,
-                        R.b_every, conv, mm32, blk, zero_spec ? zero_spec + s0 : nullptr);
+                        R.b_every, conv, mm32, blk, zs, blist, nlist);
     if (rc) return rc;
     SOAP_TRACED(ctx, "refine64",
                 k_refine64x<<<dim3((R.nbx + 7) / 8, ns), 256, 0, ctx->stream>>>(n, n_eff, R.nbx, sp, spec_stride, R.base_a, R.base_b,
                                                          R.cb_a, R.cb_b, R.b32a, R.b32b, R.c32a, R.c32b, R.b_every,
-                                                         conv, n_eff, mm32, blk, mm));
+                                                         conv, n_eff, mm32, blk, mm, zs));
     SOAP_LAUNCHED(ctx);
     k_factor<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, mm, fac, d_minmax ? d_minmax + 2LL * s0 : nullptr);
     SOAP_LAUNCHED(ctx);
@@ -1068,11 +1153,11 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)out & 15) == 0) {
         dim3 g3(grid_for(ctx, n_eff / 4, 256), ns);
         SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
-                                                                           n_eff, fac, out, out_stride));
+                                                                           n_eff, fac, out, out_stride, zs));
     } else {
         dim3 g3(grid_for(ctx, n_eff, 256), ns);
         SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
-                                                                          n_eff, fac, out, out_stride));
+                                                                          n_eff, fac, out, out_stride, zs));
     }
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;

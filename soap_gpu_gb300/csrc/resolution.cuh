@@ -29,6 +29,8 @@ struct Res32 {
     unsigned *mm32;
     unsigned long long *mm;
     float *fac, *blk;
+    unsigned long long *mmz;   // exact extrema of a zero spectrum, per base: [base][min, max]
+    int *blist;                // batch list of a chunk's convolution
     char *next;   // first scratch byte after the state
 };
 int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
@@ -37,5 +39,6 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
                          char *scratch, Res32 &R);
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
                      double *d_out, long long out_stride, double *d_minmax,
-                     const unsigned char *zero_spec = nullptr);   // [n_spec]: 1 = spectrum known to be zero
+                     const unsigned char *zero_spec = nullptr,    // [n_spec] device: 1 = spectrum known to be zero
+                     const unsigned char *zero_host = nullptr);   // the same flags on the host (both or neither)
 }  // namespace soapgb
