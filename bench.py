@@ -260,6 +260,21 @@ def run_own(args):
         tdist.all_reduce(te_t, op=tdist.ReduceOp.MAX)
     e2e_value = n_units / (float(te_t.item()) / 1e3)
 
+    # --- seed preparation: bisector injection of one 20 x 310k cube (CB_injection_faculae) ---
+    rng_b = np.random.default_rng(11)
+    bis_coeffs = T(rng_b.uniform(-300.0, 300.0, (n_mu, 4)))
+    bis_flux = T(inp.q_norm[0])
+    for _ in range(2):
+        ctx.bisector_inject(wave_d, bis_flux, bis_coeffs)
+    torch.cuda.synchronize()
+    eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eb0.record(stream)
+    for _ in range(5):
+        ctx.bisector_inject(wave_d, bis_flux, bis_coeffs)
+    eb1.record(stream)
+    eb1.synchronize()
+    bis_ms = eb0.elapsed_time(eb1) / 5
+
     # --- per-kernel CUDA-event times of one step, roofline of the dominant kernel -------
     ctx.trace(True)
     for _ in range(2):
@@ -296,6 +311,8 @@ def run_own(args):
             "cpu_baseline": cpu,
             "accuracy": err,
             "kernels_ms_per_step": {k: round(v[1], 4) for k, v in sorted(ktab.items(), key=lambda x: -x[1][1])},
+            "seed_preparation": {"bisector_injection_ms_per_cube": round(bis_ms, 4),
+                                 "cube": "%d mu bins x %d px, quiet form, inputs resident" % (n_mu, n)},
             "clocks": clk,
         }
     if dist:

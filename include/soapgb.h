@@ -220,6 +220,28 @@ int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const dou
                           const double *quiet_norm, double sigma_v, double conv_step,
                           double sentinel, int mem, double *lower, double *raw);
 
+/* ---- bisector injection of the seed spectra --------------------------------
+ * Replaces BIS_inject_spectral_quiet / BIS_inject_spectral_active
+ * (CB_injection_faculae.py:191-244, with Delta_wavelength :119-123), which the
+ * reference runs in a Python loop over pixels once per seed spectrum and mu bin.
+ * For every mu bin b < n_mu, pixel k of flux moves by the relativistic shift of
+ * rv_b(flux[k]) and the spectrum is re-sampled on wave: linear interpolation as
+ * scipy's interp1d does it (numpy.interp), 0 outside the shifted range.  out is
+ * n_mu x n.  Polynomials have n_coef (<= 16) coefficients per bin, highest power
+ * first (numpy.poly1d), rows of n_mu x n_coef.
+ *   SOAPGB_BIS_QUIET:  rv = poly(coeffs_b)(f) * scale.
+ *   SOAPGB_BIS_ACTIVE: rv = (poly(coeffs_b)(f) + vshift_b) * scale for 0.5 < f < dep_cut_b,
+ *     (poly(coeffs_low_b)(f) + vshift_b) * scale for f <= 0.5,
+ *     (vcut_b + vshift_b) * scale for f > dep_cut_b, and no shift otherwise.
+ * A shifted grid that does not increase is an error (device status 61), where the
+ * reference's interp1d would sort it. */
+#define SOAPGB_BIS_QUIET 0
+#define SOAPGB_BIS_ACTIVE 1
+int soapgb_bisector_inject(soapgb_ctx *ctx, int mode, int n, int n_mu, int n_coef, const double *wave,
+                           const double *flux, const double *coeffs, const double *coeffs_low,
+                           const double *dep_cut, const double *vcut, const double *vshift, double scale,
+                           int mem, double *out);
+
 /* ---- allocation-free convolution + normalisation --------------------------
  * No counterpart in the reference: an extra entry point of this library.  The
  * same computation as soapgb_lower_resolution in the PLAIN64 form, for callers

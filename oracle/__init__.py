@@ -238,3 +238,51 @@ def lb_params(t_star, lb_g2, lb_k0, lb_m0, temp_array):
         p = np.polyfit(temp_array[bnd], der[bnd], 1)
         lb[i] = np.poly1d(p)(t_star)
     return np.polyfit(mu, lb, 3)[::-1]
+
+
+def bisector_inject(wave, flux, mode, coeffs, coeffs_low=None, dep_cut=None, vcut=None, vshift=None, scale=1.0):
+    """Bisector injection of one spectrum into every mu bin (numpy restatement).
+
+    Follows CB_injection_faculae.py:191-244 (BIS_inject_spectral_active for mode 1,
+    BIS_inject_spectral_quiet for mode 0) with Delta_wavelength (:119-123):
+    * rv of pixel k from np.poly1d (Horner, highest power first);
+    * in mode 1 the branches are taken in the reference's order:
+      0.5 < f < dep_cut -> (up(f) + vshift) scale; f <= 0.5 -> (low(f) + vshift) scale;
+      f > dep_cut -> (vcut + vshift) scale; otherwise no shift;
+    * wave_new = wave + wave (sqrt((1 + b) / (1 - b)) - 1), b = rv / c;
+    * the spectrum is re-sampled at wave by scipy's linear interp1d, which for 1-D
+      float64 data delegates to numpy.interp: interval j with wn[j] <= x < wn[j + 1];
+      y = f[j] where x == wn[j], else ((f[j + 1] - f[j]) / (wn[j + 1] - wn[j])) (x - wn[j])
+      + f[j] (separate multiply and add), on the pixels strictly inside
+      (min wave_new, max wave_new), 0 elsewhere.
+    Returns n_mu x n.  Raises ValueError for a non-increasing shifted grid (scipy
+    would sort it)."""
+    wave = np.asarray(wave, dtype=np.float64)
+    f = np.asarray(flux, dtype=np.float64)
+    coeffs = np.atleast_2d(np.asarray(coeffs, dtype=np.float64))
+    n_mu, n = coeffs.shape[0], wave.size
+    out = np.zeros((n_mu, n))
+    for b in range(n_mu):
+        if mode == 0:
+            rv = np.polyval(coeffs[b], f) * scale
+            moved = np.ones(n, dtype=bool)
+        else:
+            up = (f < dep_cut[b]) & (f > 0.5)
+            low = ~up & (f <= 0.5)
+            cut = ~up & ~low & (f > dep_cut[b])
+            rv = np.zeros(n)
+            rv[up] = (np.polyval(coeffs[b], f[up]) + vshift[b]) * scale
+            rv[low] = (np.polyval(np.asarray(coeffs_low)[b], f[low]) + vshift[b]) * scale
+            rv[cut] = (vcut[b] + vshift[b]) * scale
+            moved = up | low | cut
+        beta = rv / C_LIGHT
+        wn = np.where(moved, wave + wave * (np.sqrt((1 + beta) / (1 - beta)) - 1), wave)
+        if not np.all(np.diff(wn) > 0):
+            raise ValueError("bisector injection: shifted grid not increasing")
+        sel = (wave < wn.max()) & (wave > wn.min())
+        x = wave[sel]
+        j = np.searchsorted(wn, x, side="right") - 1
+        slope = (f[j + 1] - f[j]) / (wn[j + 1] - wn[j])
+        y = slope * (x - wn[j]) + f[j]
+        out[b, sel] = np.where(wn[j] == x, f[j], y)
+    return out

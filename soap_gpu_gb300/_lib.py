@@ -76,6 +76,8 @@ SIGNATURES = [
                                              ctypes.c_double, ctypes.POINTER(Activity), ctypes.c_int, _vp, _vp, _vp,
                                              _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_int, _vp, _vp]),
+    ("soapgb_bisector_inject", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
+                                              _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp]),
     ("soapgb_noalloc_capacity", ctypes.c_size_t, [ctypes.c_int]),
     ("soapgb_lower_resolution_noalloc", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
      + [ctypes.c_double] * 5 + [_vp, _vp]),

@@ -185,6 +185,27 @@ class Context:
                                                    sentinel, a.mem, op, mp))
         return (out[0] if single else out), mm
 
+    # -- seed preparation: bisector injection (CB_injection_faculae.py:191-244) ----------
+    def bisector_inject(self, wave, flux, coeffs, coeffs_low=None, dep_cut=None, vcut=None, vshift=None,
+                        scale=1.0):
+        """Inject a per-mu-bin bisector into one spectrum: out[n_mu, n].
+
+        coeffs (n_mu x n_coef, highest power first) alone gives the quiet form
+        (BIS_inject_spectral_quiet); with coeffs_low, dep_cut, vcut and vshift (one row
+        or value per mu bin) the active form (BIS_inject_spectral_active)."""
+        a = self._args(wave, flux, coeffs)
+        active = coeffs_low is not None
+        c = coeffs if a.dev else np.atleast_2d(np.asarray(coeffs, dtype=np.float64))
+        n_mu, n_coef = int(c.shape[0]), int(c.shape[1])
+        n = int(wave.shape[0])
+        out, op = a.out((n_mu, n), np.float64)
+        self._check(self.L.soapgb_bisector_inject(
+            self.h, 1 if active else 0, n, n_mu, n_coef, a.inp(wave, np.float64), a.inp(flux, np.float64),
+            a.inp(c, np.float64), a.inp(coeffs_low, np.float64) if active else None,
+            a.inp(dep_cut, np.float64) if active else None, a.inp(vcut, np.float64) if active else None,
+            a.inp(vshift, np.float64) if active else None, float(scale), a.mem, op))
+        return out
+
     # -- a9-a10 -----------------------------------------------------------------
     @staticmethod
     def _regions(regions_per_phase: Sequence[np.ndarray]):
