@@ -33,8 +33,21 @@ def _write(path, arr, dtype=np.float64):
     np.ascontiguousarray(arr, dtype=dtype).tofile(path)
 
 
-def run(config_path: str, form: str = "plain64", write_spectra: bool = True, device: int = 0, verbose=True):
+def evolving_sizes(phases, sizes, period, area_rate):
+    """Region sizes per phase for a linear change of area, as run_all_SOAP_evo.py:16-20,
+    213-230 forms them: t = (phase - phase_min) * P [d], area = size^2 - area_rate * t,
+    size = sqrt(area).  Returns an n_phase x n_region array."""
+    t = (np.asarray(phases, dtype=np.float64) - np.min(phases)) * period
+    area = np.asarray(sizes, dtype=np.float64)[None, :] ** 2 - area_rate * t[:, None]
+    return np.sqrt(area)
+
+
+def run(config_path: str, form: str = "plain64", write_spectra: bool = True, device: int = 0, verbose=True,
+        area_rate: float = None):
+    """area_rate: the spot-size evolution of run_all_SOAP_evo.py (change of region area
+    per day); None keeps the sizes of the configuration."""
     rc = cfgmod.load_config(config_path)
+    rc.area_rate = area_rate
     base_dir = os.path.dirname(os.path.abspath(config_path))
     cwd = os.getcwd()
     os.chdir(base_dir)
@@ -67,13 +80,17 @@ def _run(rc, form, write_spectra, device, verbose):
     else:                                                     # run_all_SOAP.py:178-220
         phases = rc.phases
         np.savetxt(rc.output_prefix + '/' + rc.file_prefix + '_phase_locator.txt', phases.T)
+        regions = [rc.regions for _ in phases]
+        if getattr(rc, "area_rate", None) is not None:        # run_all_SOAP_evo.py:213-230
+            sizes = evolving_sizes(phases, rc.regions[:, 2], rc.period, rc.area_rate)
+            regions = [np.column_stack((rc.regions[:, 0], rc.regions[:, 1], sizes[i], rc.regions[:, 3]))
+                       for i in range(phases.size)]
         info = np.zeros((phases.size, 2))
         for i in range(phases.size):
-            np.savetxt(rc.maps_dir + 'maps' + str(int(i)) + '_for_all.txt', rc.regions)
-            info[i] = (i, rc.regions.shape[0])
+            np.savetxt(rc.maps_dir + 'maps' + str(int(i)) + '_for_all.txt', regions[i])
+            info[i] = (i, regions[i].shape[0])
         np.savetxt(rc.maps_dir + 'final_info.txt', info)
         ids = np.arange(phases.size)
-        regions = [rc.regions for _ in phases]
     prefix = rc.output_prefix + "/" + rc.file_prefix
     act = Activity(rc.t_star, rc.t_diff_spot, rc.t_diff_fac, rc.nrho, 0)
     star = Star(rc.grid, rc.period, rc.omega_ratio, rc.incl, rc.radius_km, rc.limb1, rc.limb2, (
@@ -135,8 +152,10 @@ def main():
     ap.add_argument("--form", default="plain64", choices=["plain64", "fast64", "fast32"])
     ap.add_argument("--no-spectra", action="store_true", help="do not write the per-phase spectra files")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--area-rate", type=float, default=None,
+                    help="spot-size evolution: change of region area per day (run_all_SOAP_evo.py)")
     a = ap.parse_args()
-    run(a.config, a.form, not a.no_spectra, a.device)
+    run(a.config, a.form, not a.no_spectra, a.device, area_rate=a.area_rate)
 
 
 if __name__ == "__main__":

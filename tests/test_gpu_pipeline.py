@@ -117,3 +117,27 @@ def test_pipeline_descriptors_and_wave_edges(ctx, setup):
     wave_d[1] = w1
     d = run(np.asarray(case.phases))        # read again after the report
     assert np.array_equal(a, d)
+
+
+def test_pipeline_per_phase_regions(ctx, setup):
+    """Region tables that change from phase to phase -- sizes that evolve as in
+    run_all_SOAP_evo.py, a phase without regions, a phase with three -- through the
+    pipeline's box lists agree bit for bit with the map-based stage calls."""
+    from soap_gpu_gb300.driver import evolving_sizes
+    case, inp, n_eff, maps, cb, act, _ = setup
+    sizes = evolving_sizes(case.phases, case.regions[:, 2], 1.0, 0.002)
+    regions = [np.column_stack((case.regions[:, 0], case.regions[:, 1], sizes[p], case.regions[:, 3]))
+               for p in range(case.n_phase)]
+    regions[1] = np.zeros((0, 4))
+    regions[2] = np.vstack([regions[2], [[-30.0, 90.0, 0.15, 0.0]]])
+    q_norm = ctx.quiet_disk("fast32", inp.wave, inp.q_norm, n_eff, maps, case.grid, case.step)
+    q_sed = ctx.quiet_disk("fast32", inp.wave, inp.q_sed, n_eff, maps, case.grid, case.step)
+    low, raw = ctx.phase_pipeline("fast32", inp.wave, n_eff, _star(case, inp.lb), maps, cb, case.step, act,
+                                  case.phases, regions, q_sed, q_norm, case.sigma_v, conv_step=case.step,
+                                  want_raw=True)
+    temp, bi = ctx.phase_maps(case.grid, case.incl, case.phases, regions, act)
+    flux, bconv, tot = ctx.phase_integrate("fast32", inp.wave, n_eff, case.grid, temp, bi, maps, cb, case.step, act)
+    assert not np.any((bi[1] >= -0.5) & (bi[1] <= 1.5)), "phase 1 has no region"
+    for k, spec in enumerate((tot, flux, bconv)):
+        assert np.array_equal(raw[:, k], spec[:, :n_eff])
+    assert np.all(raw[1] == 0.0)

@@ -87,3 +87,16 @@ def test_fp32_narrowing_rounds_to_nearest_even():
     with np.errstate(over="ignore"):
         ref = v.astype(np.float32)
     assert np.array_equal(_narrow_rne(v).view(np.uint32), ref.view(np.uint32))
+
+
+def test_evolving_sizes_follow_the_evolution_driver():
+    """run_all_SOAP_evo.py:16-20,213-230: t = (phase - phase_min) P, area = size^2 -
+    rate t (spot_evo), size = sqrt(area)."""
+    from soap_gpu_gb300.driver import evolving_sizes
+    phases = np.arange(0.0, 2.0, 0.25)
+    sizes = np.array([0.1, 0.17])
+    got = evolving_sizes(phases, sizes, 25.0, -0.002)
+    t = (phases - phases.min()) * 25.0
+    for r, s0 in enumerate(sizes):
+        amax = s0 ** 2
+        assert np.array_equal(got[:, r], (amax - (-0.002) * t) ** 0.5)
