@@ -1506,19 +1506,22 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
 // false: the apply loops read them from global memory (L1-cached), with no per-unit barrier
 constexpr bool FIR_PP_STAGED = true;
 constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per cube row
-// window buffers: unit u is staged in buffer u % 3, so the copy of unit u + 1 (issued
-// before unit u is applied) lands in the buffer of unit u - 2, which every thread left
-// before the barrier of unit u - 1: one barrier per unit
+// window buffers: unit u is staged in buffer u % NBUF.  With three, the copy of unit
+// u + 1 (issued before unit u is applied) lands in the buffer of unit u - 2, which every
+// thread left before the barrier of unit u - 1: one barrier per unit.  With two, a
+// second barrier after each unit frees its buffer.
 constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
+constexpr int FIR_PP_MINB = 2;   // resident blocks per SM the kernel is compiled for
+constexpr int FIR_PP_EXC = 64;   // directly evaluated cells per staged batch
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
 struct FirPPSmem {
     T win[FIR_PP_NBUF][4][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
-    unsigned long long wbar[3], pbar[2];
+    unsigned long long wbar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2], pbar[2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
-    FirExcD<T> excd[64];
+    FirExcD<T> excd[FIR_PP_EXC];
     int wsum[FIR_THREADS / 32];
     int fail, nunit_sh;
     // followed by FirSeg seg[2 * seg_cap] (dynamic, 16-byte aligned)
@@ -1536,7 +1539,7 @@ __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPS
 // unit of the next tile is issued while the current tile's last unit is applied, so the
 // copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
 template <typename T>
-__global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int ntile, int r0, int nr,
+__global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTileArgs A, int ntile, int r0, int nr,
                                                         int ntot_all) {
     constexpr int NC = 4;
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
@@ -1552,9 +1555,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     const char *plans = reinterpret_cast<const char *>(A.plan);
     const int *psize = reinterpret_cast<const int *>(plans + (size_t)ntot_all * SLOT);
     if (tid == 0) {
-        mbar_init(&sh.wbar[0], 1);
-        mbar_init(&sh.wbar[1], 1);
-        mbar_init(&sh.wbar[2], 1);
+        for (int q = 0; q < (FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2); ++q) mbar_init(&sh.wbar[q], 1);
         mbar_init(&sh.pbar[0], 1);
         mbar_init(&sh.pbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1577,7 +1578,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     };
     // (thread 0) stage the rows of unit number u (buffer u % 3)
     auto issue_unit = [&](int u, const FirUnit &d) {
-        const int b = FIR_PP_STAGED ? u % 3 : 0;
+        const int b = u % FIR_PP_NBUF;
         unsigned bytes = 0;
         uintptr_t rel = 0;
         if (d.w1 > d.w0) {
@@ -1597,16 +1598,35 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         }
     };
 
-    Acc<T> acc[7][FIR_PIX];
+    // compensated sums of the three outputs per pixel: flux, tot, bconv
+    Acc<T> acc[3][FIR_PIX];
 #pragma unroll
-    for (int a = 0; a < 7; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) acc[a][q].zero();
+    // the outputs' terms of one class at pixel j: flux S - I Q, tot S - I A, bconv B, with
+    // I the class's continuum (spot or facula SED row); the products I Q and I A are
+    // formed exactly inside fma (FP32: I as a float pair) and rounded once with S
+    auto add_out = [&](int q, int j, bool spot, T S, T Q, T Aa, T B) {
+        T f, t;
+        if constexpr (sizeof(T) == 4) {
+            const float2 w = (spot ? A.cubes.spot_sed2 : A.cubes.fac_sed2)[j];
+            f = fmaf(-w.y, Q, fmaf(-w.x, Q, S));
+            t = fmaf(-w.y, Aa, fmaf(-w.x, Aa, S));
+        } else {
+            const double w = (spot ? A.cubes.spot_sed : A.cubes.fac_sed)[j];
+            f = fma(-w, Q, S);
+            t = fma(-w, Aa, S);
+        }
+        acc[0][q].add(f);
+        acc[1][q].add(t);
+        acc[2][q].add(B);
+    };
 
     // A unit's terms are summed in plain registers (part[slot][pixel]; slots per class:
-    // spot S, Qs, As, Bs; facula S, Bf, Qf, Af) and folded into the compensated
-    // accumulators once per unit: a unit holds a few percent of a pixel's sum, so its
-    // FP32 partial carries rounding well below the compensated total's.
+    // spot S, Qs, As, Bs; facula S, Bf, Qf, Af) and folded into the compensated output
+    // sums once per unit: a unit holds a few percent of a pixel's sum, so its FP32
+    // partial carries rounding well below the compensated total's.
     T part[4][FIR_PIX];
     auto part_zero = [&]() {
 #pragma unroll
@@ -1614,19 +1634,13 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
 #pragma unroll
             for (int q = 0; q < FIR_PIX; ++q) part[a][q] = (T)0;
     };
-    auto part_fold = [&](int cls) {
+    auto part_fold = [&](int cls, int j0) {
+        const bool spot = (cls == CLS_SPOT);
 #pragma unroll
         for (int q = 0; q < FIR_PIX; ++q) {
-            acc[0][q].add(part[0][q]);
-            if (cls == CLS_SPOT) {
-                acc[1][q].add(part[1][q]);
-                acc[2][q].add(part[2][q]);
-                acc[3][q].add(part[3][q]);
-            } else {
-                acc[6][q].add(part[1][q]);
-                acc[4][q].add(part[2][q]);
-                acc[5][q].add(part[3][q]);
-            }
+            const int j = min(j0 + tid + q * FIR_THREADS, n - 1);   // pixels past n are not written
+            if (spot) add_out(q, j, true, part[0][q], part[1][q], part[2][q], part[3][q]);
+            else add_out(q, j, false, part[0][q], part[2][q], part[3][q], part[1][q]);
         }
     };
     // source rows of a unit: staged windows (value of source pixel i at p[c][i + off]) or
@@ -1732,7 +1746,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
     };
     // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
     auto wait_unit = [&](int u) {
-        if (!mbar_wait_bounded(&sh.wbar[u % 3], (unsigned)((u / 3) & 1))) atomicExch(&sh.fail, 1);
+        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1))) atomicExch(&sh.fail, 1);
         __syncthreads();
         return sh.fail == 0;
     };
@@ -1782,7 +1796,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
                     const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
                     apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
-                    part_fold(d.cls);
+                    part_fold(d.cls, j0);
                     continue;
                 }
                 if (tid == 0) {
@@ -1811,13 +1825,14 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     break;
                 }
                 const FirUnit d = units[ui];
-                const Src sr = src_of(sh.win[FIR_PP_STAGED ? u % 3 : 0], d);
+                const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
                 part_zero();
                 apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
                 const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
                 apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
-                part_fold(d.cls);
-                ++ucount;   // no barrier: the next copies go to other buffers
+                part_fold(d.cls, j0);
+                if (FIR_PP_NBUF == 2) __syncthreads();   // buffer u % 2 free for unit u + 2
+                ++ucount;
             }
         } else if (t_eff > 0) {
             // --- tile that plans itself, batch by batch ----------------------------------
@@ -1842,7 +1857,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                         }
                     }
                     const FirUnit d = st.unit[ui];
-                    const Src sr = src_of(sh.win[FIR_PP_STAGED ? u % 3 : 0], d);
+                    const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
                     part_zero();
                     apply_groups(sr, d, st.grp, st.ut[ui], st.ut[ui + 1], j0, t_eff);
                     const int e_lo = st.woff[st.ut[ui]], e_hi = st.woff[st.ut[ui + 1]];
@@ -1857,7 +1872,7 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                         }
                         apply_exc(sr, d, ex, ce - cb, j0);
                     }
-                    part_fold(d.cls);
+                    part_fold(d.cls, j0);
                     __syncthreads();
                     ++ucount;
                 }
@@ -1869,8 +1884,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         // --- directly evaluated cells (spots of non-integral temperature, solar faculae)
         if (t_eff > 0 && cn[2] > 0) {
             const int c_start = cn[0] + cn[1], c_cnt = cn[2];
-            for (int b0 = 0; b0 < c_cnt; b0 += 64) {
-                const int nbd = min(64, c_cnt - b0);
+            for (int b0 = 0; b0 < c_cnt; b0 += FIR_PP_EXC) {
+                const int nbd = min(FIR_PP_EXC, c_cnt - b0);
                 if (tid < nbd) {
                     const int cell = A.list_cell[lbase + c_start + b0 + tid];
                     FirExcD<T> x;
@@ -1911,17 +1926,12 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                             return rowp[i] + (rowp[i + 1] - rowp[i]) * w;
                         };
                         const T Lc = xc.L;
-                        acc[0][q].add(Lc * val(0));
                         if (xc.kind == 0) {
                             T Lq = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)(int)xc.temp));
-                            acc[1][q].add(Lq * val(1));
-                            acc[2][q].add(Lq * val(2));
-                            acc[3][q].add(Lc * val(3));
+                            add_out(q, j, true, Lc * val(0), Lq * val(1), Lq * val(2), Lc * val(3));
                         } else {
-                            acc[6][q].add(Lc * val(5));
                             T w2 = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)A.t_norm_fac));
-                            acc[4][q].add(w2 * val(1));
-                            acc[5][q].add(w2 * val(4));
+                            add_out(q, j, false, Lc * val(0), w2 * val(1), w2 * val(4), Lc * val(5));
                         }
                     }
                 }
@@ -1938,28 +1948,15 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
                     out0[o] = (T)0;
                     out1[o] = (T)0;
                     out2[o] = (T)0;
-                } else if constexpr (sizeof(T) == 4) {
-                    F2 S{acc[0][q].s, -acc[0][q].c}, Qs{acc[1][q].s, -acc[1][q].c}, As{acc[2][q].s, -acc[2][q].c};
-                    F2 Qf{acc[4][q].s, -acc[4][q].c}, Af{acc[5][q].s, -acc[5][q].c};
-                    float2 is2 = A.cubes.spot_sed2[j], fs2 = A.cubes.fac_sed2[j];
-                    F2 is{is2.x, is2.y}, fs{fs2.x, fs2.y};
-                    F2 fl = f2_add(f2_add(S, f2_neg(f2_mul(is, Qs))), f2_neg(f2_mul(fs, Qf)));
-                    F2 tt = f2_add(f2_add(S, f2_neg(f2_mul(is, As))), f2_neg(f2_mul(fs, Af)));
-                    F2 bc = f2_add(F2{acc[3][q].s, -acc[3][q].c}, F2{acc[6][q].s, -acc[6][q].c});
-                    out0[o] = (T)(fl.hi + fl.lo);   // flux
-                    out1[o] = (T)(bc.hi + bc.lo);   // bconv
-                    out2[o] = (T)(tt.hi + tt.lo);   // tot
                 } else {
-                    double S = acc[0][q].get(), Qs = acc[1][q].get(), As = acc[2][q].get(), Bs = acc[3][q].get();
-                    double Qf = acc[4][q].get(), Af = acc[5][q].get(), Bf = acc[6][q].get();
-                    double is = A.cubes.spot_sed[j], fs = A.cubes.fac_sed[j];
-                    out0[o] = (T)(S - is * Qs - fs * Qf);
-                    out1[o] = (T)(Bs + Bf);
-                    out2[o] = (T)(S - is * As - fs * Af);
+                    // the compensated sums, rounded once to the output type
+                    out0[o] = (T)(acc[0][q].s - acc[0][q].c);   // flux
+                    out1[o] = (T)(acc[2][q].s - acc[2][q].c);   // bconv
+                    out2[o] = (T)(acc[1][q].s - acc[1][q].c);   // tot
                 }
             }
 #pragma unroll
-            for (int a = 0; a < 7; ++a) acc[a][q].zero();
+            for (int a = 0; a < 3; ++a) acc[a][q].zero();
         }
         __syncthreads();   // plan buffer pbuf free
         if (tid == 0 && v + 2 < ve) issue_plan(real(v + 2), pbuf, next_bytes);
@@ -1969,8 +1966,8 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir_pp(const FirTileArgs A, int
         // bounded wait before leaving
         atomicExch(A.status, FIR_ST_WAIT);
         if (FIR_PP_STAGED) {
-            mbar_wait_bounded(&sh.wbar[ucount % 3], (unsigned)((ucount / 3) & 1));
-            mbar_wait_bounded(&sh.wbar[(ucount + 1) % 3], (unsigned)(((ucount + 1) / 3) & 1));
+            mbar_wait_bounded(&sh.wbar[ucount % FIR_PP_NBUF], (unsigned)((ucount / FIR_PP_NBUF) & 1));
+            mbar_wait_bounded(&sh.wbar[(ucount + 1) % FIR_PP_NBUF], (unsigned)(((ucount + 1) / FIR_PP_NBUF) & 1));
         }
         mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1));
         mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1));
