@@ -572,12 +572,12 @@ __global__ void __launch_bounds__(256) k_fir_prefix(long long gm, const int *__r
 // per-pixel sums of the FP32 form: compensated (Kahan) when set
 constexpr bool FIR_COMPENSATED = true;
 
-template <typename T>
+template <typename T, bool COMP = FIR_COMPENSATED>
 struct Acc {
     T s, c;
     __device__ __forceinline__ void zero() { s = (T)0; c = (T)0; }
     __device__ __forceinline__ void add(T x) {
-        if constexpr (sizeof(T) == 4 && FIR_COMPENSATED) {
+        if constexpr (sizeof(T) == 4 && COMP) {
             T y = x - c;
             T t = s + y;
             c = (t - s) - y;
@@ -1513,6 +1513,8 @@ constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per c
 constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
 constexpr int FIR_PP_MINB = 2;   // resident blocks per SM the kernel is compiled for
 constexpr int FIR_PP_EXC = 64;   // directly evaluated cells per staged batch
+constexpr bool FIR_PP_COMP = false;  // compensated output sums (per tile a pixel adds about 9 unit deficits, each rounded once)
+constexpr int FIR_FOLD = 4;          // work units per fold of the partial sums
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
@@ -1599,7 +1601,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     };
 
     // compensated sums of the three outputs per pixel: flux, tot, bconv
-    Acc<T> acc[3][FIR_PIX];
+    Acc<T, FIR_PP_COMP> acc[3][FIR_PIX];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -1787,6 +1789,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
             const int *woff = reinterpret_cast<const int *>(rec + L.o_woff);
             const FirGrp<T> *grp = reinterpret_cast<const FirGrp<T> *>(rec + L.o_grp);
             const FirExcW<T> *exc = reinterpret_cast<const FirExcW<T> *>(rec + L.o_exc);
+            int nfold = 0;   // units summed in part[] since the last fold
             for (int ui = 0; ui < nb; ++ui) {
                 const int u = ucount;
                 if (!FIR_PP_STAGED) {   // rows read from global memory: no staging, no barrier
@@ -1826,11 +1829,15 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 }
                 const FirUnit d = units[ui];
                 const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
-                part_zero();
+                if (nfold == 0) part_zero();
                 apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
                 const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
                 apply_exc(sr, d, exc + e_lo, e_hi - e_lo, j0);
-                part_fold(d.cls, j0);
+                // the partial sums cover up to FIR_FOLD units of one class
+                if (++nfold == FIR_FOLD || ui + 1 == nb || units[ui + 1].cls != d.cls) {
+                    part_fold(d.cls, j0);
+                    nfold = 0;
+                }
                 if (FIR_PP_NBUF == 2) __syncthreads();   // buffer u % 2 free for unit u + 2
                 ++ucount;
             }
