@@ -9,7 +9,7 @@ it as (l_j - l'_i) / (l'_{i+1} - l'_i) from ~5000 A values 0.005 A apart, which
 carries ~1e-10 relative rounding per cell (the PLAIN64 form reproduces that
 rounding bit for bit);
 FAST32 within 2e-6 of scale (the precision form's flux budget is 1e-6 on the final
-normalised spectra, checked at full size in test_gpu_fullsize.py).
+normalised spectra, checked at full size by bench.py's accuracy report).
 """
 import numpy as np
 import pytest
