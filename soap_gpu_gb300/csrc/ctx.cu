@@ -174,6 +174,7 @@ int aux_resources(soapgb_ctx *ctx) {
 
 int copy_resources(soapgb_ctx *ctx, int count) {
     if (!ctx->copy_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->d2h_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking));
     while ((int)ctx->sync_events.size() < count) {
         cudaEvent_t e = nullptr;
         SOAP_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -284,6 +285,10 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     if (ctx->aux_stream) {
         cudaStreamSynchronize(ctx->aux_stream);
         cudaStreamDestroy(ctx->aux_stream);
+    }
+    if (ctx->d2h_stream) {
+        cudaStreamSynchronize(ctx->d2h_stream);
+        cudaStreamDestroy(ctx->d2h_stream);
     }
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);

@@ -31,6 +31,7 @@ struct soapgb_ctx {
     int num_sms = 0;
     // second stream for copies that overlap kernels (created on first use) and events
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t d2h_stream = nullptr;   // device-to-host copies beside the copy stream's uploads
     std::vector<cudaEvent_t> sync_events;
     // second compute stream for independent stages (created on first use) and its two
     // ordering events (main -> aux at the start, aux -> main at the join)

@@ -6,6 +6,7 @@
 // SOAP_resolution.cu:398-412).  Here the deficits stay in device memory and all
 // phases go through each stage in one launch.
 #include <algorithm>
+#include <memory>
 #include <cstring>
 #include <vector>
 
@@ -98,6 +99,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
     int s_lists = ws.add(box_lists ? sizeof(int) * n_phase : 0);
     int s_zspec = ws.add(box_lists ? (size_t)n_spec : 0);
+    int s_ztmpl = ws.add(host && box_lists && form == SOAPGB_FAST32 ? sizeof(double) * 3 * (size_t)n_eff : 0);
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
     int s_fir = ws.add(fp.bytes);
     int s_res = ws.add(resolution_scratch_bytes(form, n, n_eff, (int)n_spec));
@@ -116,9 +118,15 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         per_chunk = (n_phase + n_chunk - 1) / n_chunk;
         n_chunk = (n_phase + per_chunk - 1) / per_chunk;
     }
+    // call-long spans per stream (tracing only): from the call's start to each stream's
+    // last operation
+    std::unique_ptr<TraceScope> span_main, span_copy, span_d2h;
     if (overlap) {
-        rc = copy_resources(ctx, n_chunk + 2);
+        rc = copy_resources(ctx, n_chunk + 3);
         if (rc) return rc;
+        span_main.reset(new TraceScope(ctx, "call_main"));
+        span_copy.reset(new TraceScope(ctx, "call_copy", ctx->copy_stream));
+        span_d2h.reset(new TraceScope(ctx, "call_d2h", ctx->d2h_stream));
         // the copy stream starts after the work already queued on the main stream
         SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[0], ctx->stream));
         SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->sync_events[0], 0));
@@ -138,16 +146,10 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     STAGE(d_wave, wave, sizeof(double) * n, s_wave);
     soapgb_cubes dc;
     dc.n_mu = n_mu;
-    {
-        TraceScope ts(ctx, "h2d_cubes", cube_stream);
-        STAGE_ON(cube_stream, dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
-        STAGE_ON(cube_stream, dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
-        STAGE_ON(cube_stream, dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
-        STAGE_ON(cube_stream, dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
-        STAGE_ON(cube_stream, dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
-        STAGE_ON(cube_stream, dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
-    }
-    if (overlap) SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[1], ctx->copy_stream));
+    // small inputs first: copies share the host-to-device engine in issue order, so
+    // the geometry's inputs must not queue behind the cubes
+    STAGE(dc.spot_sed, cubes->spot_sed, sizeof(double) * n, s_c[4]);
+    STAGE(dc.fac_sed, cubes->fac_sed, sizeof(double) * n, s_c[5]);
     soapgb_maps dm;
     const double *cd;
     STAGE(cd, maps->delta, sizeof(double) * gm, s_m[0]);
@@ -163,8 +165,6 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     const double *d_qs, *d_qn;
     STAGE(d_qs, quiet_sed, sizeof(double) * n, s_qs);
     STAGE(d_qn, quiet_norm, sizeof(double) * n, s_qn);
-#undef STAGE
-#undef STAGE_ON
     char *d_raw = ws.get<char>(s_raw);
     int f32 = (form == SOAPGB_FAST32);
     double *d_temp = ws.get<double>(s_temp), *d_bi = ws.get<double>(s_bi);
@@ -197,6 +197,17 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp,
                                d_bi, ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
     if (rc) return rc;
+    // the cubes last, after every small upload (table, lists, flags) of the call
+    {
+        TraceScope ts(ctx, "h2d_cubes", cube_stream);
+        STAGE_ON(cube_stream, dc.q_norm, cubes->q_norm, cube_b, s_c[0]);
+        STAGE_ON(cube_stream, dc.q_sed, cubes->q_sed, cube_b, s_c[1]);
+        STAGE_ON(cube_stream, dc.spot_norm, cubes->spot_norm, cube_b, s_c[2]);
+        STAGE_ON(cube_stream, dc.fac_norm, cubes->fac_norm, cube_b, s_c[3]);
+    }
+    if (overlap) SOAP_CUDA(ctx, cudaEventRecord(ctx->sync_events[1], ctx->copy_stream));
+#undef STAGE
+#undef STAGE_ON
     if (collapsed) {
         FirPhaseArgs fa;
         fa.n = n;
@@ -232,30 +243,64 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.lambda0 = w3[0];
         // The typed cubes and the convolution set-up (tap constants, FP64 base
         // convolutions) do not depend on the geometry stage (cell order, lists, plans),
-        // which is latency-bound: they run beside it on the aux stream.
+        // which is latency-bound: they run beside it on the aux stream.  With host
+        // buffers the convolution set-up needs only the small inputs, so it runs before
+        // the cubes are in; the phases without a visible region then have their output
+        // at once (the base alone, the same rows for every such phase), and it is copied
+        // back on the d2h stream while the cubes are still coming in on the copy stream.
+        const int n_zero = n_phase - n_run;
+        const bool early_zero = host && f32 && box_lists && n_zero > 0;
         rc = aux_resources(ctx);
         if (rc) return rc;
         SOAP_CUDA(ctx, cudaEventRecord(ctx->aux_events[0], ctx->stream));
         SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_events[0], 0));
-        if (overlap) SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->sync_events[1], 0));   // cubes in
         Res32 R;
         {
             AuxScope aux(ctx);
-            fa.stage = FIR_STAGE_CUBES;
-            rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
-            if (!rc && f32)
+            if (f32)
                 rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3,
                                           sigma_v, 50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
+            if (!rc && early_zero) {
+                rc = resolution32_zero_rows(ctx, R, 3, ws.get<double>(s_ztmpl));
+                if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->sync_events[2], ctx->aux_stream), "zero rows");
+            }
+            if (!rc && overlap) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->sync_events[1], 0),
+                                                "cubes in");
+            if (!rc) {
+                fa.stage = FIR_STAGE_CUBES;
+                rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+            }
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
         }
         if (rc) return rc;
+        if (early_zero) {
+            SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->sync_events[2], 0));
+            TraceScope ts(ctx, "d2h_zero", ctx->d2h_stream);
+            const double *tmpl = ws.get<double>(s_ztmpl);
+            for (int q = 0; q < n_zero; ++q) {
+                const int p = h_lists[n_run + q];
+                SOAP_CUDA(ctx, cudaMemcpyAsync(lower + (size_t)3 * p * n_eff, tmpl, sizeof(double) * 3 * n_eff,
+                                               cudaMemcpyDeviceToHost, ctx->d2h_stream));
+            }
+        }
         fa.stage = FIR_STAGE_GEOMETRY;
         rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
         if (rc) return rc;
         SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
         if (f32) {
-            for (int c = 0; c < n_chunk; ++c) {
-                const int p0 = c * per_chunk, p1 = std::min(n_phase, p0 + per_chunk);
+            // phase range of the chunks: with the zero phases' rows already on their way,
+            // only the visible phases' span is computed (unless the raw deficits are wanted)
+            int c_lo = 0, c_hi = n_phase;
+            if (early_zero && !raw) {
+                c_lo = n_run > 0 ? h_lists[0] : 0;
+                c_hi = n_run > 0 ? h_lists[n_run - 1] + 1 : 0;
+            }
+            const int span = c_hi - c_lo;
+            const int nc = chunked ? std::max(1, std::min(n_chunk, span)) : 1;
+            const int per = span > 0 ? (span + nc - 1) / nc : 0;
+            for (int c = 0; c < nc && span > 0; ++c) {
+                const int p0 = c_lo + c * per, p1 = std::min(c_hi, p0 + per);
+                if (p0 >= p1) break;
                 fa.stage = FIR_STAGE_RUN;
                 fa.l0 = p0;
                 fa.l1 = p1;
@@ -266,13 +311,23 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                                       box_lists ? zspec.data() : nullptr);
                 if (rc) return rc;
                 if (host) {
-                    cudaEvent_t ev = ctx->sync_events[2 + c];
+                    cudaEvent_t ev = ctx->sync_events[3 + c];
                     SOAP_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
-                    SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
-                    const size_t off = (size_t)3 * p0 * n_eff, cnt = (size_t)3 * (p1 - p0) * n_eff;
-                    TraceScope ts(ctx, "d2h_lower", ctx->copy_stream);
-                    SOAP_CUDA(ctx, cudaMemcpyAsync(lower + off, d_lower + off, sizeof(double) * cnt,
-                                                   cudaMemcpyDeviceToHost, ctx->copy_stream));
+                    SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ev, 0));
+                    TraceScope ts(ctx, "d2h_lower", ctx->d2h_stream);
+                    // the chunk's phases, in runs; the zero phases' rows came from the template
+                    for (int a = p0; a < p1;) {
+                        if (early_zero && !vis[a]) {
+                            ++a;
+                            continue;
+                        }
+                        int b = a + 1;
+                        while (b < p1 && !(early_zero && !vis[b])) ++b;
+                        const size_t off = (size_t)3 * a * n_eff, cnt = (size_t)3 * (b - a) * n_eff;
+                        SOAP_CUDA(ctx, cudaMemcpyAsync(lower + off, d_lower + off, sizeof(double) * cnt,
+                                                       cudaMemcpyDeviceToHost, ctx->d2h_stream));
+                        a = b;
+                    }
                 }
             }
         } else {
@@ -303,7 +358,11 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
             }
         }
         if (!host) return SOAPGB_OK;
+        span_main.reset();
+        span_copy.reset();
+        span_d2h.reset();
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->d2h_stream));
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return check_status(ctx, "soapgb_phase_pipeline");
     }

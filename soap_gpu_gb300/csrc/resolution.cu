@@ -822,6 +822,20 @@ __global__ void __launch_bounds__(256) k_zero_extrema(int n, int n_eff, const do
     }
 }
 
+// The normalised output of a zero spectrum for each of the b_every types (the same for
+// every phase: the base alone), as k_factor and k_norm32 form it: out3[t][i], t < 3.
+__global__ void k_zero_rows(int n_eff, int b_every, const float *__restrict__ c32a, const float *__restrict__ c32b,
+                            const unsigned long long *__restrict__ mmz, double *__restrict__ out3) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.y;
+    if (i >= n_eff) return;
+    const int q = (b_every > 0 && (t % b_every) == b_every - 1) ? 1 : 0;
+    const double mn = soap_ord_dec(mmz[2 * q]), mx = soap_ord_dec(mmz[2 * q + 1]);
+    const float f = (float)((1.0 - mn) / mx);
+    const float c = (q ? c32b : c32a)[i] + 0.f;
+    out3[(size_t)t * n_eff + i] = soap_f32_to_f64(fmaf(-c, f, 1.0f));
+}
+
 // extrema of the zero spectra of a chunk from the per-base values
 __global__ void k_zero_mm(int n_spec, const unsigned char *__restrict__ zero_spec, int b_every,
                           const unsigned long long *__restrict__ mmz, unsigned long long *mm64) {
@@ -1159,6 +1173,13 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
         SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
                                                                           n_eff, fac, out, out_stride, zs));
     }
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
+int resolution32_zero_rows(soapgb_ctx *ctx, const Res32 &R, int n_types, double *out) {
+    k_zero_rows<<<dim3(grid_for(ctx, R.n_eff, 256), n_types), 256, 0, ctx->stream>>>(R.n_eff, R.b_every, R.c32a,
+                                                                                       R.c32b, R.mmz, out);
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;
 }

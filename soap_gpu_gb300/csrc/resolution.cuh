@@ -37,6 +37,9 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
                          double wave1, double wave_last, const double *base_a, const double *base_b, int b_every,
                          double sigma_v, double window, double step_mult, double step_exp, double sentinel,
                          char *scratch, Res32 &R);
+// the normalised rows of a zero spectrum for the n_types spectrum types (tot, flux,
+// bconv with b_every 3): out[n_types][n_eff], the same values resolution32_run writes
+int resolution32_zero_rows(soapgb_ctx *ctx, const Res32 &R, int n_types, double *out);
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
                      double *d_out, long long out_stride, double *d_minmax,
                      const unsigned char *zero_spec = nullptr,    // [n_spec] device: 1 = spectrum known to be zero
