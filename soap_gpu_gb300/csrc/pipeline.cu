@@ -256,10 +256,17 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_events[0], 0));
         Res32 R;
         {
+            // host buffers: the convolution set-up first (its inputs are in long before
+            // the cubes); device buffers: the typed cubes first (the FP64 base
+            // convolution would slow the geometry stage it runs beside)
             AuxScope aux(ctx);
-            if (f32)
-                rc = resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn, 3,
-                                          sigma_v, 50.0, conv_step, conv_step, sentinel, ws.get<char>(s_res), R);
+            auto prepare = [&]() {
+                return f32 ? resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn,
+                                                  3, sigma_v, 50.0, conv_step, conv_step, sentinel,
+                                                  ws.get<char>(s_res), R)
+                           : SOAPGB_OK;
+            };
+            if (overlap) rc = prepare();
             if (!rc && early_zero) {
                 rc = resolution32_zero_rows(ctx, R, 3, ws.get<double>(s_ztmpl));
                 if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->sync_events[2], ctx->aux_stream), "zero rows");
@@ -270,6 +277,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 fa.stage = FIR_STAGE_CUBES;
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
             }
+            if (!rc && !overlap) rc = prepare();
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
         }
         if (rc) return rc;
