@@ -447,6 +447,119 @@ __global__ void __launch_bounds__(FIR_BLIST_THREADS)
     }
 }
 
+// Phase lists without maps and without a cell order: one block per phase collects the
+// active cells of its region boxes (as k_fir_blists) and sorts them in shared memory by
+// (class, mu bin key, order-preserving image of the slope, cell index) -- a bitonic
+// network over a power-of-two capacity at least the phase's box cells.  That is the
+// order the two radix sorts of the cell order give (by slope, then stably by mu bin),
+// so the lists are the same as k_fir_blists's, without the G*G sort.
+constexpr int FIR_SLIST_THREADS = 1024;
+constexpr int FIR_SLIST_CAP_MAX = 8192;
+
+__global__ void __launch_bounds__(FIR_SLIST_THREADS)
+    k_fir_slists(int grid, double delta_grid, const RegionPhase *__restrict__ table, const int *__restrict__ reg_off,
+                 int t_star, int t_diff_spot, int t_diff_fac, int solar, int cap, const CellGeo *__restrict__ geo,
+                 int *list_cell, double *list_dlt, double2 *list_aux, int *counts, int *status) {
+    extern __shared__ __align__(16) unsigned char sl_smem[];
+    unsigned long long *kb = reinterpret_cast<unsigned long long *>(sl_smem);   // [cap] slope keys
+    unsigned *ka = reinterpret_cast<unsigned *>(kb + cap);                      // [cap] class << 16 | bin key
+    int *kc = reinterpret_cast<int *>(ka + cap);                                // [cap] cell
+    __shared__ int cnt, ccnt[3];
+    const long long gm = (long long)grid * grid;
+    const int l = blockIdx.x, tid = threadIdx.x;
+    const long long mbase = (long long)l * gm;
+    if (tid == 0) cnt = 0;
+    if (tid < 3) ccnt[tid] = 0;
+    __syncthreads();
+    const int r0 = reg_off[l], r1 = reg_off[l + 1];
+    const float delta_f = (float)delta_grid;
+    for (int r = r0; r < r1; ++r) {
+        const RegionPhase rp = table[r];
+        const int by = rp.iy1 - rp.iy0, bz = rp.iz1 - rp.iz0;
+        if (!rp.visible || by <= 0 || bz <= 0) continue;
+        const int nbox = by * bz;
+        for (int q = tid; q < nbox; q += FIR_SLIST_THREADS) {
+            const int iy = rp.iy0 + q / bz, iz = rp.iz0 + q % bz;
+            int owner = region_owner_fp32(table, r0, r1, iy, iz, delta_f);
+            if (owner == -2) {
+                double t, b;
+                owner = region_cell_value(table, r0, r1, iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b);
+            }
+            if (owner != r) continue;
+            const double t = (double)(t_star - t_diff_spot), b = (rp.type == 0) ? 0.0 : 1.0;
+            const int k = iy * grid + iz;
+            const CellGeo &g = geo[k];
+            const int c = fir_class_tb(g, t, b, solar);
+            if (c < 0) continue;
+            atomicAdd(&ccnt[c], 1);
+            const int pos = atomicAdd(&cnt, 1);
+            if (pos < cap) {
+                ka[pos] = ((unsigned)c << 16) | (unsigned)(g.row * 2 + g.zero_v);
+                kb[pos] = soap_ord64(g.dlt);
+                kc[pos] = k;
+            }
+        }
+    }
+    __syncthreads();
+    const int n = cnt;
+    if (n > cap) {   // the host sizes cap from the boxes: cannot happen
+        if (tid == 0) atomicExch(status, FIR_ST_SEGMENTS);
+        if (tid < 4) counts[4 * l + tid] = 0;
+        return;
+    }
+    int np = 1;
+    while (np < n) np <<= 1;
+    for (int i = n + tid; i < np; i += FIR_SLIST_THREADS) {
+        ka[i] = 0xffffffffu;
+        kb[i] = ~0ULL;
+        kc[i] = 0x7fffffff;
+    }
+    __syncthreads();
+    for (int k = 2; k <= np; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < np; i += FIR_SLIST_THREADS) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const unsigned a0 = ka[i], a1 = ka[p];
+                    const unsigned long long b0 = kb[i], b1 = kb[p];
+                    const int c0 = kc[i], c1 = kc[p];
+                    const bool gt = (a0 != a1) ? (a0 > a1) : (b0 != b1) ? (b0 > b1) : (c0 > c1);
+                    if (gt == ((i & k) == 0)) {
+                        ka[i] = a1; ka[p] = a0;
+                        kb[i] = b1; kb[p] = b0;
+                        kc[i] = c1; kc[p] = c0;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < n; i += FIR_SLIST_THREADS) {
+        const int cell = kc[i];
+        list_cell[mbase + i] = cell;
+        list_dlt[mbase + i] = geo[cell].dlt;
+        if ((int)(ka[i] >> 16) == CLS_DIRECT) {
+            double t, b;
+            region_cell_value(table, r0, r1, cell / grid, cell % grid, delta_grid, t_star, t_diff_spot, t_diff_fac, t,
+                              b);
+            list_aux[mbase + i] = make_double2(t, b);
+        }
+    }
+    if (tid == 0) {
+        int *o = counts + 4 * l;
+        o[0] = ccnt[0];
+        o[1] = ccnt[1];
+        o[2] = ccnt[2];
+        o[3] = 0;
+    }
+}
+
+int fir_sorted_box_capacity(long long max_box_cells) {
+    int cap = 32;
+    while (cap < max_box_cells) cap <<= 1;
+    return cap <= FIR_SLIST_CAP_MAX ? cap : 0;
+}
+
 static size_t fir_blists_smem(long long gm) { return sizeof(unsigned) * 3 * (size_t)((gm + 31) >> 5); }
 
 long long fir_box_lists_max_gm() { return (long long)(FIR_BLIST_SMEM_MAX / (3 * sizeof(unsigned))) * 32; }
@@ -2085,6 +2198,30 @@ static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double st
 static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm, int n_lists, const double *temp,
                      const double *bi, int solar, const FirPhaseArgs *boxes = nullptr) {
     const CellGeo *geo = (const CellGeo *)(ws + L.off[FirLayout::GEO]);
+    if (boxes && boxes->box_cap > 0) {
+        // phases sort their own active cells: no cell order needed
+        int *lcell = (int *)(ws + L.off[FirLayout::LCELL]);
+        double *ldlt = (double *)(ws + L.off[FirLayout::LDLT]);
+        double2 *laux = (double2 *)(ws + L.off[FirLayout::LAUX]);
+        int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
+        const int cap = boxes->box_cap;
+        const size_t smem = (size_t)cap * (sizeof(unsigned long long) + sizeof(unsigned) + sizeof(int));
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_slists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const soapgb_activity *act = boxes->act;
+        SOAP_TRACED(ctx, "fir_lists",
+                    k_fir_slists<<<n_lists, FIR_SLIST_THREADS, smem, ctx->stream>>>(
+                        boxes->grid, 2. / boxes->grid, boxes->table, boxes->reg_off, act->t_star, act->t_diff_spot,
+                        act->t_diff_fac, solar, cap, geo, lcell, ldlt, laux, counts, ctx->d_status));
+        SOAP_LAUNCHED(ctx);
+        double *pre = (double *)(ws + L.off[FirLayout::PRE]);
+        int2 *segs = (int2 *)(ws + L.off[FirLayout::SEGS]);
+        int *nseg = (int *)(ws + L.off[FirLayout::NSEG]);
+        SOAP_TRACED(ctx, "fir_prefix", k_fir_prefix<<<dim3(n_lists, 2), 256, 0, ctx->stream>>>(
+                                           gm, counts, lcell, geo, pre, L.pre_stride, L.pre_comp, segs, nseg,
+                                           L.seg_cap, ctx->d_status));
+        SOAP_LAUNCHED(ctx);
+        return SOAPGB_OK;
+    }
     auto *k1a = (unsigned long long *)(ws + L.off[FirLayout::K1A]);
     auto *k1b = (unsigned long long *)(ws + L.off[FirLayout::K1B]);
     auto *k2a = (unsigned *)(ws + L.off[FirLayout::K2A]);

@@ -38,6 +38,7 @@ struct FirPhaseArgs {
     const RegionPhase *table = nullptr;
     const int *reg_off = nullptr;   // n_phase + 1 (device)
     int grid = 0;
+    int box_cap = 0;                // > 0: each phase sorts its active cells (capacity, from the boxes)
     // optional: the phases with a visible region (run) and the others (zero), ascending,
     // on the device and the host; the run stage then integrates only the former and
     // zero-fills the outputs of the latter (no active cell, so zero deficits)
@@ -64,6 +65,8 @@ enum { FIR_STAGE_GEOMETRY = 1, FIR_STAGE_CUBES = 2, FIR_STAGE_RUN = 4 };
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);
 // largest G*G whose phase lists can be built from the region boxes
 long long fir_box_lists_max_gm();
+// capacity of the per-phase sort for phases of at most max_box_cells box cells (0: too many)
+int fir_sorted_box_capacity(long long max_box_cells);
 
 namespace soapgb {
 // radix sorts of (key, cell) pairs on the context's stream (fir_sort.cu)

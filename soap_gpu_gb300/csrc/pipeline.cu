@@ -174,11 +174,12 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     // phases with a visible region are integrated; the others have no active cell
     std::vector<unsigned char> vis, zspec;
     std::vector<int> h_lists;   // run list, then zero list
+    long long max_box = 0;      // most box cells of a phase
     int n_run = 0;
     if (box_lists) {
         rc = phase_table_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act,
                                 ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase), &d_table, &d_roff,
-                                &vis);
+                                &vis, &max_box);
         if (rc) return rc;
         for (int p = 0; p < n_phase; ++p)
             if (vis[p]) h_lists.push_back(p);
@@ -220,6 +221,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.table = d_table;
         fa.reg_off = d_roff;
         fa.grid = grid;
+        fa.box_cap = box_lists ? fir_sorted_box_capacity(max_box) : 0;
         if (box_lists) {
             fa.run_list = ws.get<int>(s_lists);
             fa.zero_list = fa.run_list + n_run;

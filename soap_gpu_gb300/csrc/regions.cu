@@ -8,6 +8,7 @@
 // cell of every phase, applying the regions in order (later regions overwrite).
 // The rim bounding box is computed from all nrho points at once, which is the
 // deterministic form of spot_area's cross-block reduction (:61-93).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -133,7 +134,7 @@ namespace soapgb {
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
                        size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
-                       std::vector<unsigned char> *phase_visible) {
+                       std::vector<unsigned char> *phase_visible, long long *max_box_cells) {
     std::vector<RegionPhase> table;
     int rc = build_region_table(ctx, grid, incl, n_phase, h_phases, h_reg_off, h_regions, act->nrho, table);
     if (rc) return rc;
@@ -142,6 +143,18 @@ int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, cons
         for (int p = 0; p < n_phase; ++p)
             for (int r = h_reg_off[p]; r < h_reg_off[p + 1]; ++r)
                 if (table[r].visible) (*phase_visible)[p] = 1;
+    }
+    if (max_box_cells) {
+        long long mx = 0;
+        for (int p = 0; p < n_phase; ++p) {
+            long long sum = 0;
+            for (int r = h_reg_off[p]; r < h_reg_off[p + 1]; ++r) {
+                const RegionPhase &t = table[r];
+                if (t.visible && t.iy1 > t.iy0 && t.iz1 > t.iz0) sum += (long long)(t.iy1 - t.iy0) * (t.iz1 - t.iz0);
+            }
+            mx = std::max(mx, sum);
+        }
+        *max_box_cells = mx;
     }
     size_t tb = sizeof(RegionPhase) * table.size();
     size_t ob = sizeof(int) * (n_phase + 1);

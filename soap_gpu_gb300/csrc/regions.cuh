@@ -90,10 +90,12 @@ __device__ __forceinline__ int region_owner_fp32(const RegionPhase *__restrict__
 namespace soapgb {
 // The region table of n_phase phases built on the host and copied to scratch:
 // *d_table (reg_off[n_phase] rows) and *d_off (n_phase + 1 offsets); phase_visible
-// (optional) gets 1 for the phases with at least one visible region, else 0.
+// (optional) gets 1 for the phases with at least one visible region, else 0;
+// max_box_cells (optional) the largest sum over a phase's visible regions of their
+// bounding-box cells (a bound on the phase's active cells).
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
                        size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
-                       std::vector<unsigned char> *phase_visible = nullptr);
+                       std::vector<unsigned char> *phase_visible = nullptr, long long *max_box_cells = nullptr);
 size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
 }  // namespace soapgb
