@@ -98,7 +98,9 @@ int soapgb_ctx_create(int device, soapgb_ctx **out);
 int soapgb_ctx_destroy(soapgb_ctx *ctx);
 const char *soapgb_last_error(const soapgb_ctx *ctx);
 /* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores the
- * context's own stream. */
+ * context's own stream, a non-blocking stream that is not ordered with the legacy
+ * default stream.  A caller whose work is on the legacy default stream (torch's
+ * default stream, handle 0) passes cudaStreamLegacy. */
 int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream);
 int soapgb_synchronize(soapgb_ctx *ctx);
 /* Number of kernel launches issued by this context since creation. */

@@ -26,6 +26,20 @@ def _is_dev(x):
     return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
 
 
+# cudaStreamLegacy: the handle that names the legacy default stream explicitly
+_CUDA_STREAM_LEGACY = 0x1
+
+
+def torch_stream_handle(device: int) -> int:
+    """The cudaStream_t of torch's current stream on ``device``, for soapgb_set_stream.
+
+    torch's default stream is the legacy default stream, whose handle is 0; the C
+    interface reads a null stream as "the context's own stream", a non-blocking stream
+    with no ordering against the caller's work, so 0 becomes cudaStreamLegacy."""
+    h = torch.cuda.current_stream(device).cuda_stream
+    return h if h else _CUDA_STREAM_LEGACY
+
+
 def _form(form):
     if isinstance(form, str):
         return FORMS[form]
@@ -114,7 +128,7 @@ class Context:
     def _args(self, *xs):
         dev = any(_is_dev(x) for x in xs if x is not None)
         if dev:
-            self.L.soapgb_set_stream(self.h, ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+            self.L.soapgb_set_stream(self.h, ctypes.c_void_p(torch_stream_handle(self.device)))
         else:
             self.L.soapgb_set_stream(self.h, None)
         return _Args(dev, self.device)

@@ -50,3 +50,28 @@ def test_folded_grid_reports_status(ctx):
     # the context stays usable
     q = ctx.bisector_inject(GOLD["wave"], GOLD["flux"], GOLD["q_coeffs"], scale=float(GOLD["scale"]))
     assert np.array_equal(q, GOLD["quiet"])
+
+
+@pytest.mark.parametrize("side_stream", [False, True])
+def test_device_calls_follow_the_torch_stream(ctx, side_stream):
+    # the input is written on torch's current stream behind a long spin, and the result
+    # read there, with no synchronisation in between: a call that ran on a stream of its
+    # own would read the input before the copy or be read before it finished
+    torch = pytest.importorskip("torch")
+    dev = "cuda:0"
+    w = torch.as_tensor(GOLD["wave"], device=dev)
+    c = torch.as_tensor(GOLD["q_coeffs"], device=dev)
+    src = torch.as_tensor(GOLD["flux"], device=dev)
+    f = torch.zeros_like(src)
+    s = torch.cuda.Stream() if side_stream else torch.cuda.default_stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            f.zero_()
+            torch.cuda._sleep(50_000_000)   # about 25 ms of spinning on this stream
+            f.copy_(src)
+            q = ctx.bisector_inject(w, f, c, scale=float(GOLD["scale"]))
+            got = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
+            got.copy_(q, non_blocking=True)
+            s.synchronize()
+            assert np.array_equal(got.numpy(), GOLD["quiet"])

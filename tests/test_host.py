@@ -2,6 +2,7 @@
 import os
 
 import numpy as np
+import pytest
 
 from soap_gpu_gb300 import config, synth
 
@@ -100,3 +101,17 @@ def test_evolving_sizes_follow_the_evolution_driver():
     for r, s0 in enumerate(sizes):
         amax = s0 ** 2
         assert np.array_equal(got[:, r], (amax - (-0.002) * t) ** 0.5)
+
+
+def test_torch_default_stream_maps_to_the_legacy_handle(monkeypatch):
+    torch = pytest.importorskip("torch")
+    from soap_gpu_gb300 import api
+
+    class _S:
+        def __init__(self, h):
+            self.cuda_stream = h
+
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda device=None: _S(0))
+    assert api.torch_stream_handle(0) == 0x1      # cudaStreamLegacy, never the null handle
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda device=None: _S(0x5678))
+    assert api.torch_stream_handle(0) == 0x5678

@@ -28,7 +28,7 @@ def _ptr(t):
 def test_noalloc_matches_allocating_entry_point_twice():
     torch = pytest.importorskip("torch")
     from soap_gpu_gb300 import _lib
-    from soap_gpu_gb300.api import Context
+    from soap_gpu_gb300.api import Context, torch_stream_handle
 
     L = _lib.load()
     inp = small_inputs()
@@ -44,7 +44,7 @@ def test_noalloc_matches_allocating_entry_point_twice():
     spec_d = torch.as_tensor(spec, device=dev)
     sigma_v = inp.case.sigma_v
     with Context(0) as ctx:
-        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        stream = ctypes.c_void_p(torch_stream_handle(0))
         assert L.soapgb_set_stream(ctx.h, stream) == 0
         ref = torch.empty((3, n_eff), dtype=torch.float64, device=dev)
         ref_mm = torch.empty((3, 2), dtype=torch.float64, device=dev)
