@@ -167,7 +167,7 @@ TraceScope::~TraceScope() {
 
 int aux_resources(soapgb_ctx *ctx) {
     if (!ctx->aux_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
-    for (int q = 0; q < 2; ++q)
+    for (int q = 0; q < 3; ++q)
         if (!ctx->aux_events[q]) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_events[q], cudaEventDisableTiming));
     return SOAPGB_OK;
 }

@@ -134,20 +134,37 @@ __device__ __forceinline__ float soap_f64_to_f32(double v) {
 }
 
 // The six typed cubes of the FP32 phase integration in one pass over the four FP64
-// cubes (two values per thread and step): q_sed, q_norm, spot_norm, q_norm - spot_norm,
-// fac_norm, q_norm - fac_norm.  The two differences are formed in FP64 and rounded once.
+// cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm.  The
+// two differences are formed in FP64 and rounded once.  The grid is small (a few blocks
+// per SM, so the geometry kernels on the other stream find room beside it), and each
+// thread keeps two steps' loads (eight 16-byte loads) in flight to cover HBM latency.
+__device__ __forceinline__ void cube_types_store(long long i, double2 a, double2 b, double2 c, double2 d, float2 *o0,
+                                                 float2 *o1, float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
+    o0[i] = make_float2(soap_f64_to_f32(a.x), soap_f64_to_f32(a.y));
+    o1[i] = make_float2(soap_f64_to_f32(b.x), soap_f64_to_f32(b.y));
+    o2[i] = make_float2(soap_f64_to_f32(c.x), soap_f64_to_f32(c.y));
+    o3[i] = make_float2(soap_f64_to_f32(b.x - c.x), soap_f64_to_f32(b.y - c.y));
+    o4[i] = make_float2(soap_f64_to_f32(d.x), soap_f64_to_f32(d.y));
+    o5[i] = make_float2(soap_f64_to_f32(b.x - d.x), soap_f64_to_f32(b.y - d.y));
+}
+
 __global__ void __launch_bounds__(256) k_cube_types32(long long n2, const double2 *__restrict__ qs,
                                                       const double2 *__restrict__ qn, const double2 *__restrict__ sn,
                                                       const double2 *__restrict__ fn, float2 *o0, float2 *o1,
                                                       float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
-        const double2 a = qs[i], b = qn[i], c = sn[i], d = fn[i];
-        o0[i] = make_float2(soap_f64_to_f32(a.x), soap_f64_to_f32(a.y));
-        o1[i] = make_float2(soap_f64_to_f32(b.x), soap_f64_to_f32(b.y));
-        o2[i] = make_float2(soap_f64_to_f32(c.x), soap_f64_to_f32(c.y));
-        o3[i] = make_float2(soap_f64_to_f32(b.x - c.x), soap_f64_to_f32(b.y - c.y));
-        o4[i] = make_float2(soap_f64_to_f32(d.x), soap_f64_to_f32(d.y));
-        o5[i] = make_float2(soap_f64_to_f32(b.x - d.x), soap_f64_to_f32(b.y - d.y));
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += 2 * stride) {
+        const long long j = i + stride;
+        const double2 a0 = __ldcs(qs + i), b0 = __ldcs(qn + i), c0 = __ldcs(sn + i), d0 = __ldcs(fn + i);
+        double2 a1 = make_double2(0.0, 0.0), b1 = a1, c1 = a1, d1 = a1;
+        if (j < n2) {
+            a1 = __ldcs(qs + j);
+            b1 = __ldcs(qn + j);
+            c1 = __ldcs(sn + j);
+            d1 = __ldcs(fn + j);
+        }
+        cube_types_store(i, a0, b0, c0, d0, o0, o1, o2, o3, o4, o5);
+        if (j < n2) cube_types_store(j, a1, b1, c1, d1, o0, o1, o2, o3, o4, o5);
     }
 }
 
@@ -2347,7 +2364,7 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
                         k_fir_plan<T><<<dim3(ntile, n_plan), FIR_PLAN_THREADS, smem_p, ctx->stream>>>(A));
             SOAP_LAUNCHED(ctx);
         }
-        if ((stage & 4) && z1 > z0) {
+        if ((stage & 4) && z1 > z0 && pa->zero_fill) {
             SOAP_TRACED(ctx, "fir_zero",
                         k_fir_zero<T><<<dim3((n + 255) / 256, z1 - z0), 256, 0, ctx->stream>>>(
                             n, pa->zero_list + z0, (T *)o0, (T *)o1, (T *)o2, out_stride));
@@ -2450,7 +2467,7 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
             float2 *o[6];
             for (int q = 0; q < 6; ++q) o[q] = (float2 *)const_cast<void *>(fc.c[q]);
             const long long n2 = (long long)(cube_elems / 2);
-            const int nblk = (int)std::min<long long>((n2 + 255) / 256, 16LL * std::max(ctx->num_sms, 1));
+            const int nblk = (int)std::min<long long>((n2 + 255) / 256, 3LL * std::max(ctx->num_sms, 1));
             SOAP_TRACED(ctx, "cube_types",
                         k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
                             n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,

@@ -45,6 +45,8 @@ struct FirPhaseArgs {
     const int *run_list = nullptr, *zero_list = nullptr;
     const int *run_host = nullptr, *zero_host = nullptr;
     int n_run = 0, n_zero = 0;
+    // 0: the zero phases' outputs are left unwritten (their consumer knows them as zero)
+    int zero_fill = 1;
     const double *delta, *limb, *lb;
     const int *region;
     long long gm;               // G*G

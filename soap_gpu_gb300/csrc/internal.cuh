@@ -33,10 +33,11 @@ struct soapgb_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaStream_t d2h_stream = nullptr;   // device-to-host copies beside the copy stream's uploads
     std::vector<cudaEvent_t> sync_events;
-    // second compute stream for independent stages (created on first use) and its two
-    // ordering events (main -> aux at the start, aux -> main at the join)
+    // second compute stream for independent stages (created on first use) and its
+    // ordering events: main -> aux at the start, aux -> main at the join, and a second
+    // aux -> main point where the main stream needs only the first part of the aux work
     cudaStream_t aux_stream = nullptr;
-    cudaEvent_t aux_events[2] = {nullptr, nullptr};
+    cudaEvent_t aux_events[3] = {nullptr, nullptr, nullptr};
     // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
     // once; later calls with the same array confirm them on the device, status 51)
     const double *edge_wave = nullptr;

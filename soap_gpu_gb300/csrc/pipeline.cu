@@ -229,6 +229,9 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
             fa.zero_host = h_lists.data() + n_run;
             fa.n_run = n_run;
             fa.n_zero = n_phase - n_run;
+            // the FP32 resolution stage takes the zero phases as zero without reading
+            // their rows; only the raw deficits, when wanted, need them written
+            fa.zero_fill = (!f32 || raw) ? 1 : 0;
         }
         fa.delta = dm.delta;
         fa.limb = dm.limb;
@@ -279,6 +282,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 fa.stage = FIR_STAGE_CUBES;
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
             }
+            if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[2], ctx->aux_stream), "typed cubes");
             if (!rc && !overlap) rc = prepare();
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
         }
@@ -296,8 +300,12 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.stage = FIR_STAGE_GEOMETRY;
         rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
         if (rc) return rc;
-        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
+        // the integration needs the typed cubes; the convolution set-up is joined
+        // before the first convolution, so with device buffers it runs on beside the
+        // integration
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[2], 0));
         if (f32) {
+            bool joined = false;
             // phase range of the chunks: with the zero phases' rows already on their way,
             // only the visible phases' span is computed (unless the raw deficits are wanted)
             int c_lo = 0, c_hi = n_phase;
@@ -316,6 +324,10 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 fa.l1 = p1;
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
                 if (rc) return rc;
+                if (!joined) {
+                    SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
+                    joined = true;
+                }
                 rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr,
                                       box_lists ? ws.get<unsigned char>(s_zspec) : nullptr,
                                       box_lists ? zspec.data() : nullptr);
@@ -340,7 +352,9 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                     }
                 }
             }
+            if (!joined) SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
         } else {
+            SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->aux_events[1], 0));
             fa.stage = FIR_STAGE_RUN;
             rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
             if (rc) return rc;

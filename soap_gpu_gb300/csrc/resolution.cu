@@ -609,6 +609,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
                                                         unsigned *mm32, float *blk, int nbx, int *status,
                                                         const unsigned char *__restrict__ zero_spec,
                                                         const int *__restrict__ blist, int nlist) {
+    static_assert(SB <= 31, "one bit per spectrum of a batch");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[SB][4][FC_THREADS / 32];
     __shared__ unsigned long long bar[2];
@@ -634,15 +635,21 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
         fail = 0;
     }
     __syncthreads();
+    // rows of spectra known to be zero (phases without a visible region) are not copied
+    // but zeroed in shared memory: their raw rows need not be written
+    auto zero_row = [&](int s) { return zero_spec != nullptr && zero_spec[s] != 0; };
     auto issue = [&](int bt, int buf) {   // thread 0
         const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
+        int ncopy = 0;
+        for (int q = 0; q < nsb; ++q) ncopy += zero_row(s0 + q) ? 0 : 1;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
-                     "r"(bytes * (unsigned)nsb)
+                     "r"(bytes * (unsigned)ncopy)
                      : "memory");
         if (bytes) {
             for (int q = 0; q < nsb; ++q) {
+                if (zero_row(s0 + q)) continue;
                 const float *src = spec + (long long)(s0 + q) * spec_stride + ca;
                 float *dst = xbuf + ((size_t)buf * SB + q) * win + (ca - mb);
                 asm volatile(
@@ -686,12 +693,14 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
             ok = (r != 0);
         }
         if (!ok) atomicExch(&fail, 1);
-        // zero the staged pixels outside [0, n) (and the rows of absent spectra)
-        if (ca > mb || cb < mb + win || nsb < SB) {
+        unsigned zmask = 0;   // rows of zero spectra in this batch
+        for (int q = 0; q < nsb; ++q) zmask |= zero_row(s0 + q) ? (1u << q) : 0u;
+        // zero the staged pixels outside [0, n), and the rows of absent and zero spectra
+        if (ca > mb || cb < mb + win || nsb < SB || zmask) {
             for (int q = 0; q < SB; ++q)
                 for (int t = threadIdx.x; t < win; t += FC_THREADS) {
                     const int m = mb + t;
-                    if (q >= nsb || m < 0 || m >= n) xs[q * win + t] = 0.f;
+                    if (q >= nsb || ((zmask >> q) & 1u) || m < 0 || m >= n) xs[q * win + t] = 0.f;
                 }
         }
         __syncthreads();
@@ -706,8 +715,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
             for (int p = 0; p < FC_PIX; ++p) acc[q][p] = 0.f;
         // a batch of spectra known to be zero (phases without a visible region) has no
         // taps to sum: its convolution is the base part alone
-        bool zero_batch = (zero_spec != nullptr);
-        for (int q = 0; q < nsb && zero_batch; ++q) zero_batch = zero_spec[s0 + q] != 0;
+        const bool zero_batch = (zmask == (1u << nsb) - 1u);
         if (R > 0 && !zero_batch)
             conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
         conv32_finish<SB>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every,

@@ -141,3 +141,43 @@ def test_pipeline_per_phase_regions(ctx, setup):
     for k, spec in enumerate((tot, flux, bconv)):
         assert np.array_equal(raw[:, k], spec[:, :n_eff])
     assert np.all(raw[1] == 0.0)
+
+
+@pytest.mark.parametrize("device_mode", [False, True])
+def test_zero_phases_need_no_raw_rows(ctx, setup, device_mode):
+    """Phases without a visible region: the FP32 resolution stage takes their deficits
+    as zero without reading their rows, which are then left unwritten.  A first call
+    leaves non-zero rows behind in the context's buffers; a call in which those phases
+    have no region gives, without raw outputs, the same spectra bit for bit as with
+    them (when their rows are zero-filled)."""
+    torch = pytest.importorskip("torch")
+    case, inp, n_eff, maps, cb, act, regions = setup
+    q_norm = ctx.quiet_disk("fast32", inp.wave, inp.q_norm, n_eff, maps, case.grid, case.step)
+    q_sed = ctx.quiet_disk("fast32", inp.wave, inp.q_sed, n_eff, maps, case.grid, case.step)
+    star = _star(case, inp.lb)
+    if device_mode:
+        dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda:0")
+        back = lambda t: t.cpu().numpy()
+    else:
+        dev = back = lambda a: a
+    maps_x = {k: dev(v) for k, v in maps.items()}
+    cb_x = {k: dev(v) for k, v in cb.items()}
+    args = (dev(inp.wave), n_eff, star, maps_x, cb_x, case.step, act)
+
+    def run(regs, want_raw):
+        r = ctx.phase_pipeline("fast32", *args, np.asarray(case.phases), regs, dev(q_sed), dev(q_norm),
+                               case.sigma_v, conv_step=case.step, want_raw=want_raw)
+        ctx.synchronize()
+        return tuple(back(x) for x in r) if want_raw else back(r)
+
+    _, raw_a = run(regions, True)
+    lit = [p for p in range(case.n_phase) if np.any(raw_a[p] != 0.0)]
+    assert len(lit) >= 4, "the case needs phases with a visible region"
+    empty = lit[1::3]                      # interior phases: their batches mix zero and non-zero rows
+    regs_b = [np.zeros((0, 4)) if p in empty else regions[p] for p in range(case.n_phase)]
+    low_b = run(regs_b, False)             # rows of `empty` still hold the first call's deficits
+    low_c, raw_c = run(regs_b, True)       # zero-filled rows
+    assert all(np.all(raw_c[p] == 0.0) for p in empty)
+    assert np.array_equal(low_b, low_c)
+    for p in empty[1:]:                    # a zero phase's spectra are the base's alone
+        assert np.array_equal(low_b[p], low_b[empty[0]])
