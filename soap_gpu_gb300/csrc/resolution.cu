@@ -469,66 +469,101 @@ __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff
                                               const float (&acc)[SB][FC_PIX], const float *__restrict__ b32a,
                                               const float *__restrict__ b32b, const float *__restrict__ c32a,
                                               const float *__restrict__ c32b, int b_every, float *__restrict__ conv,
-                                              long long conv_stride, unsigned *mm32, float *blk, int nbx,
-                                              float (*red)[4][FC_THREADS / 32]) {
+                                              long long conv_stride, unsigned *mm32, float *blk, int nbx, int bx,
+                                              unsigned (*red)[4][FC_THREADS / 32]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the two bases and their convolutions at the thread's pixels, once for all spectra
+    float ba[FC_PIX], bb[FC_PIX], ka[FC_PIX], kb[FC_PIX];
+    const bool al_b = (((uintptr_t)b32a | (uintptr_t)b32b) & 15) == 0;
+    const bool al_c = (((uintptr_t)c32a | (uintptr_t)c32b) & 15) == 0;
+    if (al_b && ib + FC_PIX <= n) {
+        const float4 u = *reinterpret_cast<const float4 *>(b32a + ib), v = *reinterpret_cast<const float4 *>(b32b + ib);
+        ba[0] = u.x, ba[1] = u.y, ba[2] = u.z, ba[3] = u.w;
+        bb[0] = v.x, bb[1] = v.y, bb[2] = v.z, bb[3] = v.w;
+    } else {
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            ba[p] = (ib + p < n) ? b32a[ib + p] : 0.f;
+            bb[p] = (ib + p < n) ? b32b[ib + p] : 0.f;
+        }
+    }
+    const bool full_e = (ib + FC_PIX <= n_eff);
+    if (al_c && full_e) {
+        const float4 u = *reinterpret_cast<const float4 *>(c32a + ib), v = *reinterpret_cast<const float4 *>(c32b + ib);
+        ka[0] = u.x, ka[1] = u.y, ka[2] = u.z, ka[3] = u.w;
+        kb[0] = v.x, kb[1] = v.y, kb[2] = v.z, kb[3] = v.w;
+    } else {
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            ka[p] = (ib + p < n_eff) ? c32a[ib + p] : 0.f;
+            kb[p] = (ib + p < n_eff) ? c32b[ib + p] : 0.f;
+        }
+    }
+    const bool vec_out = full_e && (conv_stride % FC_PIX) == 0 && ((uintptr_t)conv & 15) == 0;
 #pragma unroll
     for (int q = 0; q < SB; ++q) {
         float mn = INFINITY, mx = -INFINITY, ma = 0.f, mc = 0.f;
         if (q < nsb) {
             const int s = s0 + q;
             const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
-            const float *bs = use_b ? b32b : b32a;
-            const float *cbs = use_b ? c32b : c32a;
             float *cp = conv + (long long)s * conv_stride;
+            float cdv[FC_PIX];
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) {
                 const int i = ib + p;
                 if (i < n) {
-                    const float b = bs[i], x = xs[q * win + (i - i0) + xoff];
+                    const float b = use_b ? bb[p] : ba[p], x = xs[q * win + (i - i0) + xoff];
                     mn = fminf(mn, b - x);
                     ma = fmaxf(ma, fabsf(b) + fabsf(x));
                 }
+                cdv[p] = 0.f;
                 if (i < n_eff) {
                     const float cd = lv[p] ? acc[q][p] : 0.f;
-                    cp[i] = cd;
-                    const float cb = cbs[i];
+                    cdv[p] = cd;
+                    const float cb = use_b ? kb[p] : ka[p];
                     const float c = cb + cd;
                     if (c != 0.f) mx = fmaxf(mx, c);
                     mc = fmaxf(mc, fabsf(cb) + fabsf(cd));
                 }
             }
+            if (vec_out) {
+                *reinterpret_cast<float4 *>(cp + ib) = make_float4(cdv[0], cdv[1], cdv[2], cdv[3]);
+            } else {
+#pragma unroll
+                for (int p = 0; p < FC_PIX; ++p)
+                    if (ib + p < n_eff) cp[ib + p] = cdv[p];
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
-            mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, o));
-        }
+        // warp extrema on the order-preserving integer images (exact; the per-thread
+        // values hold no NaN, which fminf / fmaxf drop)
+        const unsigned rmn = __reduce_min_sync(0xffffffffu, soap_ord32(mn));
+        const unsigned rmx = __reduce_max_sync(0xffffffffu, soap_ord32(mx));
+        const unsigned rma = __reduce_max_sync(0xffffffffu, soap_ord32(ma));
+        const unsigned rmc = __reduce_max_sync(0xffffffffu, soap_ord32(mc));
         if (lane == 0) {
-            red[q][0][warp] = mn;
-            red[q][1][warp] = mx;
-            red[q][2][warp] = ma;
-            red[q][3][warp] = mc;
+            red[q][0][warp] = rmn;
+            red[q][1][warp] = rmx;
+            red[q][2][warp] = rma;
+            red[q][3][warp] = rmc;
         }
     }
     __syncthreads();
     if (threadIdx.x < nsb) {
         const int q = threadIdx.x, s = s0 + q;
-        float mn = red[q][0][0], mx = red[q][1][0], ma = red[q][2][0], mc = red[q][3][0];
+        unsigned mn = red[q][0][0], mx = red[q][1][0], ma = red[q][2][0], mc = red[q][3][0];
         for (int w = 1; w < FC_THREADS / 32; ++w) {
-            mn = fminf(mn, red[q][0][w]);
-            mx = fmaxf(mx, red[q][1][w]);
-            ma = fmaxf(ma, red[q][2][w]);
-            mc = fmaxf(mc, red[q][3][w]);
+            mn = min(mn, red[q][0][w]);
+            mx = max(mx, red[q][1][w]);
+            ma = max(ma, red[q][2][w]);
+            mc = max(mc, red[q][3][w]);
         }
-        float *bk = blk + ((long long)s * nbx + blockIdx.x) * 2;
-        bk[0] = mn;
-        bk[1] = mx;
-        if (mn < INFINITY) atomicMin(&mm32[4 * s + 0], soap_ord32(mn));
-        if (mx > -INFINITY) atomicMax(&mm32[4 * s + 1], soap_ord32(mx));
-        atomicMax(&mm32[4 * s + 2], soap_ord32(ma));
-        atomicMax(&mm32[4 * s + 3], soap_ord32(mc));
+        float *bk = blk + ((long long)s * nbx + bx) * 2;
+        bk[0] = soap_dec32(mn);
+        bk[1] = soap_dec32(mx);
+        if (mn != soap_ord32(INFINITY)) atomicMin(&mm32[4 * s + 0], mn);
+        if (mx != soap_ord32(-INFINITY)) atomicMax(&mm32[4 * s + 1], mx);
+        atomicMax(&mm32[4 * s + 2], ma);
+        atomicMax(&mm32[4 * s + 3], mc);
     }
     __syncthreads();
 }
@@ -554,7 +589,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const 
                                                         unsigned *mm32, float *blk) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *xs = reinterpret_cast<float *>(smem_raw);
-    __shared__ float red[SB][4][FC_THREADS / 32];
+    __shared__ unsigned red[SB][4][FC_THREADS / 32];
     const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
     const int i0 = blockIdx.x * FC_TILE;
     const int s0 = blockIdx.y * SB;
@@ -588,46 +623,52 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const 
         conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh, R, sh, wid, c2, lk, acc);
     }
     conv32_finish<SB>(xs, win, halo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every, conv,
-                      conv_stride, mm32, blk, gridDim.x, red);
+                      conv_stride, mm32, blk, gridDim.x, blockIdx.x, red);
 }
 
-// The same with TMA staging (spectra rows 16-byte aligned, stride a multiple of 4): a
-// block keeps its pixel tile and walks spectrum batches blockIdx.y, + gridDim.y, ...;
-// the next batch's rows are copied by cp.async.bulk into the other buffer while the
-// current one is convolved.  Staged row r of a batch starts at source pixel
-// mb = floor4(i0 - halo); pixels outside [0, n) are zeroed by the threads once the
-// copy has landed.
+// The same with TMA staging (spectra rows 16-byte aligned, stride a multiple of 4), on a
+// persistent grid: block b walks the items b, b + gridDim.x, ... of (spectrum batch,
+// pixel tile), batch-major, and copies the next item's rows by cp.async.bulk into the
+// other buffer while the current one is convolved.  Staged row r of an item starts at
+// source pixel mb = floor4(i0 - halo); pixels outside [0, n) are zeroed by the threads
+// once the copy has landed.
 template <int SB>
-__global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
-                                                        const float *__restrict__ lka, const int *__restrict__ livea,
-                                                        const int *__restrict__ rblk, int wid,
-                                                        const float *__restrict__ spec, long long spec_stride,
-                                                        int n_spec, int halo, const float *__restrict__ b32a,
-                                                        const float *__restrict__ b32b, const float *__restrict__ c32a,
-                                                        const float *__restrict__ c32b, int b_every,
-                                                        float *__restrict__ conv, long long conv_stride,
-                                                        unsigned *mm32, float *blk, int nbx, int *status,
-                                                        const unsigned char *__restrict__ zero_spec,
-                                                        const int *__restrict__ blist, int nlist) {
+__global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
+                                                           const float *__restrict__ lka,
+                                                           const int *__restrict__ livea, const int *__restrict__ rblk,
+                                                           int wid, const float *__restrict__ spec,
+                                                           long long spec_stride, int n_spec, int halo,
+                                                           const float *__restrict__ b32a,
+                                                           const float *__restrict__ b32b,
+                                                           const float *__restrict__ c32a,
+                                                           const float *__restrict__ c32b, int b_every,
+                                                           float *__restrict__ conv, long long conv_stride,
+                                                           unsigned *mm32, float *blk, int nbx, int *status,
+                                                           const unsigned char *__restrict__ zero_spec,
+                                                           const int *__restrict__ blist, int nlist) {
     static_assert(SB <= 31, "one bit per spectrum of a batch");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float red[SB][4][FC_THREADS / 32];
+    __shared__ unsigned red[SB][4][FC_THREADS / 32];
     __shared__ unsigned long long bar[2];
     __shared__ int fail;
     const int win = (FC_TILE + 2 * halo + 12 + 3) & ~3;
     float *xbuf = reinterpret_cast<float *>(smem_raw);   // [2][SB][win]
-    const int i0 = blockIdx.x * FC_TILE;
-    const int wm0 = i0 - halo;                          // source pixel of window index 0
-    const int mb = (wm0 >= 0) ? (wm0 & ~3) : -((-wm0 + 3) & ~3);
-    const int xo = wm0 - mb;                            // staged index of wm0, in [0, 3]
-    // in-range part [ca, cb) of the staged row, 16-byte aligned at both ends (the row's
-    // allocation is padded beyond n to a multiple of 16 bytes)
-    const int ca = max(mb, 0);
-    const int cb = min(mb + win, (n + 3) & ~3);
-    const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
     // the batches to convolve: blist[0, nlist) (batches of zero spectra left out), or all
     const int nwalk = blist ? nlist : (n_spec + SB - 1) / SB;
-    auto batch_of = [&](int it) { return blist ? blist[it] : it; };
+    const int nitem = nwalk * nbx;   // the host checks that it fits an int
+    auto batch_of = [&](int it) { return blist ? blist[it / nbx] : it / nbx; };
+    // staged window of tile x: first source pixel mb (16-byte aligned, <= i0 - halo) and
+    // the in-range part [ca, cb) of the staged row, 16-byte aligned at both ends (the
+    // row's allocation is padded beyond n to a multiple of 16 bytes)
+    auto window = [&](int x, int &mb, int &ca, int &cb) {
+        const int wm0 = x * FC_TILE - halo;
+        mb = (wm0 >= 0) ? (wm0 & ~3) : -((-wm0 + 3) & ~3);
+        ca = max(mb, 0);
+        cb = min(mb + win, (n + 3) & ~3);
+    };
+    // rows of spectra known to be zero (phases without a visible region) are not copied
+    // but zeroed in shared memory: their raw rows need not be written
+    auto zero_row = [&](int s) { return zero_spec != nullptr && zero_spec[s] != 0; };
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[0])));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&bar[1])));
@@ -635,11 +676,12 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
         fail = 0;
     }
     __syncthreads();
-    // rows of spectra known to be zero (phases without a visible region) are not copied
-    // but zeroed in shared memory: their raw rows need not be written
-    auto zero_row = [&](int s) { return zero_spec != nullptr && zero_spec[s] != 0; };
-    auto issue = [&](int bt, int buf) {   // thread 0
+    auto issue = [&](int it, int buf) {   // thread 0
+        const int bt = batch_of(it), x = it % nbx;
         const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        int mb, ca, cb;
+        window(x, mb, ca, cb);
+        const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
         int ncopy = 0;
         for (int q = 0; q < nsb; ++q) ncopy += zero_row(s0 + q) ? 0 : 1;
@@ -660,29 +702,33 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
             }
         }
     };
-    const int ib = i0 + threadIdx.x * FC_PIX;
-    float c2[FC_PIX], lk[FC_PIX];
-    bool lv[FC_PIX];
-#pragma unroll
-    for (int p = 0; p < FC_PIX; ++p) {
-        const int i = ib + p;
-        lv[p] = (i < n_eff) && livea[i];
-        c2[p] = lv[p] ? c2a[i] : 0.f;
-        lk[p] = lv[p] ? lka[i] : -200.f;
-    }
-    const int R = (i0 < n_eff) ? rblk[blockIdx.x] : 0;
-    const int sh = (halo - R + xo) & 3;
     int k = 0, k_fail = -1;
-    if (threadIdx.x == 0 && (int)blockIdx.y < nwalk) issue(batch_of(blockIdx.y), 0);
-    for (int it = blockIdx.y; it < nwalk; it += gridDim.y, ++k) {
-        const int bt = batch_of(it);
+    if (threadIdx.x == 0 && (int)blockIdx.x < nitem) issue(blockIdx.x, 0);
+    for (int it = blockIdx.x; it < nitem; it += gridDim.x, ++k) {
+        const int bt = batch_of(it), x = it % nbx;
         const int buf = k & 1;
-        if (threadIdx.x == 0 && it + (int)gridDim.y < nwalk) issue(batch_of(it + gridDim.y), buf ^ 1);
+        if (threadIdx.x == 0 && it + (int)gridDim.x < nitem) issue(it + gridDim.x, buf ^ 1);
         const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        const int i0 = x * FC_TILE;
+        int mb, ca, cb;
+        window(x, mb, ca, cb);
+        const int xo = (i0 - halo) - mb;   // staged index of source pixel i0 - halo, in [0, 3]
+        const int ib = i0 + threadIdx.x * FC_PIX;
+        float c2[FC_PIX], lk[FC_PIX];
+        bool lv[FC_PIX];
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            const int i = ib + p;
+            lv[p] = (i < n_eff) && livea[i];
+            c2[p] = lv[p] ? c2a[i] : 0.f;
+            lk[p] = lv[p] ? lka[i] : -200.f;
+        }
+        const int R = (i0 < n_eff) ? rblk[x] : 0;
+        const int sh = (halo - R + xo) & 3;
         float *xs = xbuf + (size_t)buf * SB * win;
         bool ok = false;
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
-        for (long long it = 0; it < (1LL << 24) && !ok; ++it) {
+        for (long long w = 0; w < (1LL << 24) && !ok; ++w) {
             unsigned r;
             asm volatile(
                 "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -713,22 +759,22 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32t(int n, int n_eff, const 
         for (int q = 0; q < SB; ++q)
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) acc[q][p] = 0.f;
-        // a batch of spectra known to be zero (phases without a visible region) has no
-        // taps to sum: its convolution is the base part alone
+        // a batch of spectra known to be zero has no taps to sum: its convolution is
+        // the base part alone
         const bool zero_batch = (zmask == (1u << nsb) - 1u);
         if (R > 0 && !zero_batch)
             conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
         conv32_finish<SB>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every,
-                          conv, conv_stride, mm32, blk, nbx, red);
+                          conv, conv_stride, mm32, blk, nbx, x, red);
     }
     if (k_fail >= 0 && threadIdx.x == 0) {
-        // a staged copy did not land in time: record it and give the next batch's copy,
+        // a staged copy did not land in time: record it and give the next item's copy,
         // if one was issued, a bounded wait before leaving
         atomicExch(status, 42);
-        if ((int)blockIdx.y + (k_fail + 1) * (int)gridDim.y < nwalk) {
+        if ((long long)blockIdx.x + (long long)(k_fail + 1) * gridDim.x < (long long)nitem) {
             const int kb = k_fail + 1;
             const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[kb & 1]);
-            for (long long it = 0; it < (1LL << 24); ++it) {
+            for (long long w = 0; w < (1LL << 24); ++w) {
                 unsigned r;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -1015,8 +1061,12 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32t<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
         const int nwalk = blist ? nlist : nbatch;
         if (nwalk == 0) return SOAPGB_OK;   // every spectrum is zero
-        int gy = std::max(1, std::min(nwalk, (2 * std::max(ctx->num_sms, 1) + nbx - 1) / nbx));
-        dim3 g(nbx, gy);
+        int per_sm = 0;
+        SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv32t<SB>, FC_THREADS, smem_t));
+        const long long nitem = (long long)nwalk * nbx;
+        if (nitem > 0x7fffffffLL) return set_error(ctx, SOAPGB_ERR_ARG, "convolution: too many (batch, tile) items");
+        const int g = (int)std::max<long long>(1, std::min<long long>(nitem, (long long)std::max(per_sm, 1) *
+                                                                                  std::max(ctx->num_sms, 1)));
         SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
                                                               n_eff, mm32, blk, nbx, ctx->d_status, zero_spec,
