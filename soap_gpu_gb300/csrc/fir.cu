@@ -135,9 +135,8 @@ __device__ __forceinline__ float soap_f64_to_f32(double v) {
 
 // The six typed cubes of the FP32 phase integration in one pass over the four FP64
 // cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm.  The
-// two differences are formed in FP64 and rounded once.  The grid is small (a few blocks
-// per SM, so the geometry kernels on the other stream find room beside it), and each
-// thread keeps two steps' loads (eight 16-byte loads) in flight to cover HBM latency.
+// two differences are formed in FP64 and rounded once.  Each thread keeps two steps'
+// loads (eight 16-byte loads) in flight to cover HBM latency.
 __device__ __forceinline__ void cube_types_store(long long i, double2 a, double2 b, double2 c, double2 d, float2 *o0,
                                                  float2 *o1, float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
     o0[i] = make_float2(soap_f64_to_f32(a.x), soap_f64_to_f32(a.y));
@@ -478,9 +477,10 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
                  int t_star, int t_diff_spot, int t_diff_fac, int solar, int cap, const CellGeo *__restrict__ geo,
                  int *list_cell, double *list_dlt, double2 *list_aux, int *counts, int *status) {
     extern __shared__ __align__(16) unsigned char sl_smem[];
-    unsigned long long *kb = reinterpret_cast<unsigned long long *>(sl_smem);   // [cap] slope keys
-    unsigned *ka = reinterpret_cast<unsigned *>(kb + cap);                      // [cap] class << 16 | bin key
-    int *kc = reinterpret_cast<int *>(ka + cap);                                // [cap] cell
+    // the sort record of an active cell in two words, compared as one 128-bit key:
+    // k1 = (class << 16 | bin key) << 32 | ord64(dlt) >> 32, k2 = ord64(dlt) << 32 | cell
+    unsigned long long *k1 = reinterpret_cast<unsigned long long *>(sl_smem);   // [cap]
+    unsigned long long *k2 = k1 + cap;                                         // [cap]
     __shared__ int cnt, ccnt[3];
     const long long gm = (long long)grid * grid;
     const int l = blockIdx.x, tid = threadIdx.x;
@@ -511,9 +511,10 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
             atomicAdd(&ccnt[c], 1);
             const int pos = atomicAdd(&cnt, 1);
             if (pos < cap) {
-                ka[pos] = ((unsigned)c << 16) | (unsigned)(g.row * 2 + g.zero_v);
-                kb[pos] = soap_ord64(g.dlt);
-                kc[pos] = k;
+                const unsigned long long od = soap_ord64(g.dlt);
+                const unsigned ka = ((unsigned)c << 16) | (unsigned)(g.row * 2 + g.zero_v);
+                k1[pos] = ((unsigned long long)ka << 32) | (od >> 32);
+                k2[pos] = (od << 32) | (unsigned)k;
             }
         }
     }
@@ -524,38 +525,39 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
         if (tid < 4) counts[4 * l + tid] = 0;
         return;
     }
-    int np = 1;
-    while (np < n) np <<= 1;
-    for (int i = n + tid; i < np; i += FIR_SLIST_THREADS) {
-        ka[i] = 0xffffffffu;
-        kb[i] = ~0ULL;
-        kc[i] = 0x7fffffff;
+    int np = 1, lnp = 0;
+    while (np < n) np <<= 1, ++lnp;
+    for (int i = n + tid; i < np; i += FIR_SLIST_THREADS) {   // padding sorts last
+        k1[i] = ~0ULL;
+        k2[i] = ~0ULL;
     }
     __syncthreads();
-    for (int k = 2; k <= np; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < np; i += FIR_SLIST_THREADS) {
-                const int p = i ^ j;
-                if (p > i) {
-                    const unsigned a0 = ka[i], a1 = ka[p];
-                    const unsigned long long b0 = kb[i], b1 = kb[p];
-                    const int c0 = kc[i], c1 = kc[p];
-                    const bool gt = (a0 != a1) ? (a0 > a1) : (b0 != b1) ? (b0 > b1) : (c0 > c1);
-                    if (gt == ((i & k) == 0)) {
-                        ka[i] = a1; ka[p] = a0;
-                        kb[i] = b1; kb[p] = b0;
-                        kc[i] = c1; kc[p] = c0;
-                    }
+    // bitonic network over the np / 2 compare-exchange pairs of each stage: pair m of
+    // stage (k, j) joins i (m with a zero bit inserted at bit log2 j) and i + j
+    const int half = np >> 1;
+    for (int lk = 1; lk <= lnp; ++lk) {
+        for (int lj = lk - 1; lj >= 0; --lj) {
+            const int j = 1 << lj;
+            for (int m = tid; m < half; m += FIR_SLIST_THREADS) {
+                const int i = ((m >> lj) << (lj + 1)) | (m & (j - 1));
+                const int p = i + j;
+                const unsigned long long a1 = k1[i], b1 = k1[p], a2 = k2[i], b2 = k2[p];
+                const bool gt = (a1 != b1) ? (a1 > b1) : (a2 > b2);
+                if (gt == (((i >> lk) & 1) == 0)) {
+                    k1[i] = b1;
+                    k1[p] = a1;
+                    k2[i] = b2;
+                    k2[p] = a2;
                 }
             }
             __syncthreads();
         }
     }
     for (int i = tid; i < n; i += FIR_SLIST_THREADS) {
-        const int cell = kc[i];
+        const int cell = (int)(unsigned)k2[i];
         list_cell[mbase + i] = cell;
         list_dlt[mbase + i] = geo[cell].dlt;
-        if ((int)(ka[i] >> 16) == CLS_DIRECT) {
+        if ((int)(k1[i] >> 48) == CLS_DIRECT) {
             double t, b;
             region_cell_value(table, r0, r1, cell / grid, cell % grid, delta_grid, t_star, t_diff_spot, t_diff_fac, t,
                               b);
@@ -2222,7 +2224,7 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
         double2 *laux = (double2 *)(ws + L.off[FirLayout::LAUX]);
         int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
         const int cap = boxes->box_cap;
-        const size_t smem = (size_t)cap * (sizeof(unsigned long long) + sizeof(unsigned) + sizeof(int));
+        const size_t smem = (size_t)cap * 2 * sizeof(unsigned long long);
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_slists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const soapgb_activity *act = boxes->act;
         SOAP_TRACED(ctx, "fir_lists",
@@ -2467,7 +2469,9 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
             float2 *o[6];
             for (int q = 0; q < 6; ++q) o[q] = (float2 *)const_cast<void *>(fc.c[q]);
             const long long n2 = (long long)(cube_elems / 2);
-            const int nblk = (int)std::min<long long>((n2 + 255) / 256, 3LL * std::max(ctx->num_sms, 1));
+            // short blocks (two steps per thread): SMs free up quickly for the
+            // higher-priority geometry kernels that run beside this one
+            const int nblk = (int)std::max<long long>(1, (n2 + 511) / 512);
             SOAP_TRACED(ctx, "cube_types",
                         k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
                             n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,
