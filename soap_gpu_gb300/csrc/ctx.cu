@@ -169,6 +169,14 @@ int aux_resources(soapgb_ctx *ctx) {
     if (!ctx->aux_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
     for (int q = 0; q < 3; ++q)
         if (!ctx->aux_events[q]) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_events[q], cudaEventDisableTiming));
+    if (!ctx->geo_stream) {
+        int least = 0, greatest = 0;
+        SOAP_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SOAP_CUDA(ctx, cudaStreamCreateWithPriority(&ctx->geo_stream, cudaStreamNonBlocking, greatest));
+    }
+    if (!ctx->geo_event) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->geo_event, cudaEventDisableTiming));
+    if (!ctx->aux2_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux2_stream, cudaStreamNonBlocking));
+    if (!ctx->aux2_event) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux2_event, cudaEventDisableTiming));
     return SOAPGB_OK;
 }
 
@@ -285,6 +293,16 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     if (ctx->aux_stream) {
         cudaStreamSynchronize(ctx->aux_stream);
         cudaStreamDestroy(ctx->aux_stream);
+    }
+    if (ctx->geo_event) cudaEventDestroy(ctx->geo_event);
+    if (ctx->aux2_event) cudaEventDestroy(ctx->aux2_event);
+    if (ctx->aux2_stream) {
+        cudaStreamSynchronize(ctx->aux2_stream);
+        cudaStreamDestroy(ctx->aux2_stream);
+    }
+    if (ctx->geo_stream) {
+        cudaStreamSynchronize(ctx->geo_stream);
+        cudaStreamDestroy(ctx->geo_stream);
     }
     if (ctx->d2h_stream) {
         cudaStreamSynchronize(ctx->d2h_stream);

@@ -38,6 +38,13 @@ struct soapgb_ctx {
     // aux -> main point where the main stream needs only the first part of the aux work
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t aux_events[3] = {nullptr, nullptr, nullptr};
+    // stream of the highest priority for latency-bound stages on the critical path (the
+    // block scheduler dispatches its pending blocks first) and its join event
+    cudaStream_t geo_stream = nullptr;
+    cudaEvent_t geo_event = nullptr;
+    // a second aux stream (independent set-up work beside the first) and its join event
+    cudaStream_t aux2_stream = nullptr;
+    cudaEvent_t aux2_event = nullptr;
     // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
     // once; later calls with the same array confirm them on the device, status 51)
     const double *edge_wave = nullptr;
@@ -117,6 +124,7 @@ struct AuxScope {
     soapgb_ctx *ctx;
     cudaStream_t saved;
     explicit AuxScope(soapgb_ctx *c) : ctx(c), saved(c->stream) { ctx->stream = ctx->aux_stream; }
+    AuxScope(soapgb_ctx *c, cudaStream_t s) : ctx(c), saved(c->stream) { ctx->stream = s; }
     ~AuxScope() { ctx->stream = saved; }
 };
 

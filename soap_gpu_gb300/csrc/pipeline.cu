@@ -259,11 +259,14 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         if (rc) return rc;
         SOAP_CUDA(ctx, cudaEventRecord(ctx->aux_events[0], ctx->stream));
         SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_events[0], 0));
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->geo_stream, ctx->aux_events[0], 0));
         Res32 R;
         {
-            // host buffers: the convolution set-up first (its inputs are in long before
-            // the cubes); device buffers: the typed cubes first (the FP64 base
-            // convolution would slow the geometry stage it runs beside)
+            // host buffers: the convolution set-up first on the aux stream (its inputs
+            // are in long before the cubes), then the typed cubes; device buffers: the
+            // typed cubes on the aux stream and the convolution set-up on a second one,
+            // both from the start, so that the FP64 base convolution overlaps the phase
+            // lists (one block per phase, most SMs free) rather than the tile plans
             AuxScope aux(ctx);
             auto prepare = [&]() {
                 return f32 ? resolution32_prepare(ctx, n, n_eff, (int)n_spec, d_wave, w3[0], w3[1], w3[2], d_qs, d_qn,
@@ -271,7 +274,16 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                                                   ws.get<char>(s_res), R)
                            : SOAPGB_OK;
             };
-            if (overlap) rc = prepare();
+            if (overlap) {
+                rc = prepare();
+            } else {
+                rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->aux2_stream, ctx->aux_events[0], 0), "set-up fork");
+                if (!rc) {
+                    AuxScope aux2(ctx, ctx->aux2_stream);
+                    rc = prepare();
+                    if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux2_event, ctx->aux2_stream), "set-up join");
+                }
+            }
             if (!rc && early_zero) {
                 rc = resolution32_zero_rows(ctx, R, 3, ws.get<double>(s_ztmpl));
                 if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->sync_events[2], ctx->aux_stream), "zero rows");
@@ -283,7 +295,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
             }
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[2], ctx->aux_stream), "typed cubes");
-            if (!rc && !overlap) rc = prepare();
+            if (!rc && !overlap) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux2_event, 0), "set-up");
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
         }
         if (rc) return rc;
@@ -297,9 +309,17 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                                                cudaMemcpyDeviceToHost, ctx->d2h_stream));
             }
         }
-        fa.stage = FIR_STAGE_GEOMETRY;
-        rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+        {
+            // the geometry (lists, prefix sums, tile plans) is latency-bound and on the
+            // critical path: on the high-priority stream, its blocks are dispatched ahead
+            // of the aux stream's
+            AuxScope geo(ctx, ctx->geo_stream);
+            fa.stage = FIR_STAGE_GEOMETRY;
+            rc = fir_phase(ctx, form, fa, ws.get<char>(s_fir), fp);
+            if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->geo_event, ctx->geo_stream), "geometry join");
+        }
         if (rc) return rc;
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->geo_event, 0));
         // the integration needs the typed cubes; the convolution set-up is joined
         // before the first convolution, so with device buffers it runs on beside the
         // integration
@@ -330,7 +350,8 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                 }
                 rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr,
                                       box_lists ? ws.get<unsigned char>(s_zspec) : nullptr,
-                                      box_lists ? zspec.data() : nullptr);
+                                      box_lists ? zspec.data() : nullptr,
+                                      early_zero ? ZeroRows::SKIP : ZeroRows::NORM);
                 if (rc) return rc;
                 if (host) {
                     cudaEvent_t ev = ctx->sync_events[3 + c];

@@ -917,8 +917,10 @@ __global__ void __launch_bounds__(256) k_norm32(int n_eff, const float *__restri
                                                 const float *__restrict__ c32b, int b_every,
                                                 const float *__restrict__ conv, long long conv_stride,
                                                 const float *__restrict__ fac, double *__restrict__ out,
-                                                long long out_stride, const unsigned char *__restrict__ zero_spec) {
+                                                long long out_stride, const unsigned char *__restrict__ zero_spec,
+                                                int skip_zero) {
     int s = blockIdx.y;
+    if (skip_zero && zero_spec && zero_spec[s]) return;   // rows the caller has already
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_eff) return;
     bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
@@ -934,8 +936,10 @@ __global__ void __launch_bounds__(256) k_norm32v(int n_eff, const float *__restr
                                                  const float *__restrict__ c32b, int b_every,
                                                  const float *__restrict__ conv, long long conv_stride,
                                                  const float *__restrict__ fac, double *__restrict__ out,
-                                                 long long out_stride, const unsigned char *__restrict__ zero_spec) {
+                                                 long long out_stride, const unsigned char *__restrict__ zero_spec,
+                                                 int skip_zero) {
     const int s = blockIdx.y;
+    if (skip_zero && zero_spec && zero_spec[s]) return;   // rows the caller has already
     const int i = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n_eff) return;
     const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
@@ -1178,7 +1182,7 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
 
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
                      double *d_out, long long out_stride, double *d_minmax, const unsigned char *zero_spec,
-                     const unsigned char *zero_host) {
+                     const unsigned char *zero_host, ZeroRows zero_rows) {
     const int ns = s1 - s0;
     if (ns <= 0) return SOAPGB_OK;
     if (R.b_every > 0 && s0 % R.b_every != 0)
@@ -1214,6 +1218,9 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     int rc = conv32_run(ctx, n, n_eff, R.wid, R.halo, R.p32, sp, spec_stride, ns, R.b32a, R.b32b, R.c32a, R.c32b,
                         R.b_every, conv, mm32, blk, zs, blist, nlist);
     if (rc) return rc;
+    // the zero spectra's rows are left unwritten where the caller has them already
+    const bool skip_zero = zs && zero_rows == ZeroRows::SKIP;
+    double *out = d_out + (long long)s0 * out_stride;
     SOAP_TRACED(ctx, "refine64",
                 k_refine64x<<<dim3((R.nbx + 7) / 8, ns), 256, 0, ctx->stream>>>(n, n_eff, R.nbx, sp, spec_stride, R.base_a, R.base_b,
                                                          R.cb_a, R.cb_b, R.b32a, R.b32b, R.c32a, R.c32b, R.b_every,
@@ -1221,15 +1228,16 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     SOAP_LAUNCHED(ctx);
     k_factor<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, mm, fac, d_minmax ? d_minmax + 2LL * s0 : nullptr);
     SOAP_LAUNCHED(ctx);
-    double *out = d_out + (long long)s0 * out_stride;
     if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)out & 15) == 0) {
         dim3 g3(grid_for(ctx, n_eff / 4, 256), ns);
         SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
-                                                                           n_eff, fac, out, out_stride, zs));
+                                                                           n_eff, fac, out, out_stride, zs,
+                                                                           skip_zero ? 1 : 0));
     } else {
         dim3 g3(grid_for(ctx, n_eff, 256), ns);
         SOAP_TRACED(ctx, "norm32", k_norm32<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
-                                                                          n_eff, fac, out, out_stride, zs));
+                                                                          n_eff, fac, out, out_stride, zs,
+                                                                          skip_zero ? 1 : 0));
     }
     SOAP_LAUNCHED(ctx);
     return SOAPGB_OK;

@@ -40,8 +40,12 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
 // the normalised rows of a zero spectrum for the n_types spectrum types (tot, flux,
 // bconv with b_every 3): out[n_types][n_eff], the same values resolution32_run writes
 int resolution32_zero_rows(soapgb_ctx *ctx, const Res32 &R, int n_types, double *out);
+// the normalised rows of the zero spectra (with zero_spec / zero_host): written by the
+// normalisation (NORM), or not at all, the caller having them already (SKIP)
+enum class ZeroRows { NORM, SKIP };
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
                      double *d_out, long long out_stride, double *d_minmax,
                      const unsigned char *zero_spec = nullptr,    // [n_spec] device: 1 = spectrum known to be zero
-                     const unsigned char *zero_host = nullptr);   // the same flags on the host (both or neither)
+                     const unsigned char *zero_host = nullptr,    // the same flags on the host (both or neither)
+                     ZeroRows zero_rows = ZeroRows::NORM);
 }  // namespace soapgb
