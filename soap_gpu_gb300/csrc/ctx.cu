@@ -169,13 +169,13 @@ int aux_resources(soapgb_ctx *ctx) {
     if (!ctx->aux_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
     for (int q = 0; q < 3; ++q)
         if (!ctx->aux_events[q]) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux_events[q], cudaEventDisableTiming));
-    if (!ctx->geo_stream) {
-        int least = 0, greatest = 0;
-        SOAP_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    int least = 0, greatest = 0;
+    SOAP_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    if (!ctx->geo_stream)
         SOAP_CUDA(ctx, cudaStreamCreateWithPriority(&ctx->geo_stream, cudaStreamNonBlocking, greatest));
-    }
     if (!ctx->geo_event) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->geo_event, cudaEventDisableTiming));
-    if (!ctx->aux2_stream) SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux2_stream, cudaStreamNonBlocking));
+    if (!ctx->aux2_stream)
+        SOAP_CUDA(ctx, cudaStreamCreateWithPriority(&ctx->aux2_stream, cudaStreamNonBlocking, greatest));
     if (!ctx->aux2_event) SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->aux2_event, cudaEventDisableTiming));
     return SOAPGB_OK;
 }

@@ -42,7 +42,8 @@ struct soapgb_ctx {
     // block scheduler dispatches its pending blocks first) and its join event
     cudaStream_t geo_stream = nullptr;
     cudaEvent_t geo_event = nullptr;
-    // a second aux stream (independent set-up work beside the first) and its join event
+    // a second aux stream (independent set-up work beside the first, dispatched ahead of
+    // it at the highest priority) and its join event
     cudaStream_t aux2_stream = nullptr;
     cudaEvent_t aux2_event = nullptr;
     // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
