@@ -82,8 +82,30 @@ __global__ void k_bis_resample(int n, const double *__restrict__ wave, const dou
     const double x = wave[i];
     double y = 0.0;
     if (x > g[0] && x < g[n - 1]) {
-        // g[lo] <= x < g[hi]: at most ceil(log2 n) steps
-        int lo = 0, hi = n - 1;
+        // the interval g[lo] <= x < g[lo + 1] (unique: g increases strictly, checked by
+        // k_bis_order).  The shifted grid lies a few pixels from the unshifted one, so
+        // a galloping search from i brackets it in O(log shift) loads, then bisection
+        // inside the bracket [lo, hi] with g[lo] <= x < g[hi].
+        int lo, hi;
+        if (g[i] <= x) {
+            lo = i;
+            int step = 1;
+            hi = min(n - 1, i + step);
+            while (g[hi] <= x) {   // g[n - 1] > x ends it
+                lo = hi;
+                step <<= 1;
+                hi = min(n - 1, lo + step);
+            }
+        } else {
+            hi = i;
+            int step = 1;
+            lo = max(0, i - step);
+            while (g[lo] > x) {    // g[0] < x ends it
+                hi = lo;
+                step <<= 1;
+                lo = max(0, hi - step);
+            }
+        }
         while (hi - lo > 1) {
             const int mid = lo + ((hi - lo) >> 1);
             if (g[mid] <= x) lo = mid;
