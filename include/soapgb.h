@@ -100,7 +100,8 @@ const char *soapgb_last_error(const soapgb_ctx *ctx);
 /* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores the
  * context's own stream, a non-blocking stream that is not ordered with the legacy
  * default stream.  A caller whose work is on the legacy default stream (torch's
- * default stream, handle 0) passes cudaStreamLegacy. */
+ * default stream, handle 0) passes cudaStreamLegacy.  Switching streams orders the
+ * new stream after the work the context queued on the previous one. */
 int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream);
 int soapgb_synchronize(soapgb_ctx *ctx);
 /* Number of kernel launches issued by this context since creation. */

@@ -295,6 +295,7 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
         cudaStreamDestroy(ctx->aux_stream);
     }
     if (ctx->geo_event) cudaEventDestroy(ctx->geo_event);
+    if (ctx->switch_event) cudaEventDestroy(ctx->switch_event);
     if (ctx->aux2_event) cudaEventDestroy(ctx->aux2_event);
     if (ctx->aux2_stream) {
         cudaStreamSynchronize(ctx->aux2_stream);
@@ -326,7 +327,17 @@ const char *soapgb_last_error(const soapgb_ctx *ctx) {
 
 int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream) {
     if (!ctx) return SOAPGB_ERR_ARG;
-    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    cudaStream_t next = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    if (next != ctx->stream && ctx->stream) {
+        // every call's work ends on the context's stream and may still be queued there,
+        // using the context's scratch: the new stream starts after it
+        SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+        if (!ctx->switch_event)
+            SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->switch_event, cudaEventDisableTiming));
+        SOAP_CUDA(ctx, cudaEventRecord(ctx->switch_event, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamWaitEvent(next, ctx->switch_event, 0));
+    }
+    ctx->stream = next;
     return SOAPGB_OK;
 }
 

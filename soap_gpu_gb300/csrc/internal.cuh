@@ -46,6 +46,9 @@ struct soapgb_ctx {
     // it at the highest priority) and its join event
     cudaStream_t aux2_stream = nullptr;
     cudaEvent_t aux2_event = nullptr;
+    // recorded on the previous stream when soapgb_set_stream switches streams: work the
+    // context queued there (which may still use its scratch) precedes the new stream's
+    cudaEvent_t switch_event = nullptr;
     // wave[0], wave[1], wave[n_eff - 1] of the last device wavelength array seen (read
     // once; later calls with the same array confirm them on the device, status 51)
     const double *edge_wave = nullptr;
