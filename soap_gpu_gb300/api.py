@@ -266,6 +266,35 @@ class Context:
                                                   float(step), ctypes.byref(act), a.mem, fp, bp, tp))
         return flux, bconv, tot
 
+    def phase_integrate_adjoint(self, wave, n_eff, grid, temp, bi, maps, cubes: dict, step, act: Activity,
+                                g_flux, g_bconv, g_tot):
+        """Gradients of a scalar through phase_integrate (PLAIN64 arithmetic), given its
+        gradients g_flux, g_bconv, g_tot (n_phase x n) w.r.t. the outputs: a dict with the
+        four cubes (n_mu x n), the two continuum rows ("spot_sed", "fac_sed", n) and the
+        limb map ("limb", G*G), each summed over the phases."""
+        a = self._args(wave, temp, cubes["q_norm"])
+        n = int(wave.shape[0])
+        n_phase = int(temp.shape[0])
+        n_mu = int(cubes["q_norm"].shape[0])
+        m = Maps(a.inp(maps["delta"], np.float64), a.inp(maps["limb"], np.float64), None,
+                 a.inp(maps["region"], np.int32), a.inp(maps["lb"], np.float64))
+        c = Cubes(*[a.inp(cubes[k], np.float64) for k in ("q_norm", "q_sed", "spot_norm", "fac_norm")],
+                  a.inp(cubes["spot_sed"][0] if len(cubes["spot_sed"].shape) == 2 else cubes["spot_sed"],
+                        np.float64),
+                  a.inp(cubes["fac_sed"][0] if len(cubes["fac_sed"].shape) == 2 else cubes["fac_sed"], np.float64),
+                  n_mu)
+        out = {}
+        ptrs = []
+        for k, shape in (("q_norm", (n_mu, n)), ("q_sed", (n_mu, n)), ("spot_norm", (n_mu, n)),
+                         ("fac_norm", (n_mu, n)), ("spot_sed", (n,)), ("fac_sed", (n,)), ("limb", (int(grid) ** 2,))):
+            out[k], pk = a.out(shape, np.float64)
+            ptrs.append(pk)
+        self._check(self.L.soapgb_phase_integrate_adjoint(
+            self.h, n, int(n_eff), a.inp(wave, np.float64), int(grid), n_phase, a.inp(temp, np.float64),
+            a.inp(bi, np.float64), ctypes.byref(m), ctypes.byref(c), float(step), ctypes.byref(act),
+            a.inp(g_flux, np.float64), a.inp(g_bconv, np.float64), a.inp(g_tot, np.float64), a.mem, *ptrs))
+        return out
+
     # -- a15-a16 ----------------------------------------------------------------
     def ccf(self, form, vel, line_wave, line_weight, wave_trim, step_size, spectra, normalise=True,
             wave_extend=100.0, mask_step=0.005, index_old=20000):

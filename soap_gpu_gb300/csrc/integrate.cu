@@ -152,6 +152,298 @@ __global__ void __launch_bounds__(256) k_phase_plain64(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the PLAIN64 integration.  The outputs are linear in every cube row and
+// in every cell's limb value L:
+//   flux += s - I q,  bconv += q - a,  tot += s - I a,   q, s, a = L lerp(row)
+// with lerp(row)[j] = row[o] + (row[o+1] - row[o]) (dl / dd) at the owner o of j.
+// Given gF, gB, gT (gradients of a scalar w.r.t. flux, bconv, tot), the gradients
+// are gathers in a fixed order (no atomics):
+//   row grads: source pixel i collects from the output pixels it owns as o (weight
+//     1 - dl/dd) and as o + 1 (weight dl/dd), times L and the combination of
+//     gF, gB, gT the row enters with (q_sed: gF + gT; q_norm: gB - I gF;
+//     spot / facula rows: -gB - I gT);
+//   continuum rows: I = ratio x sed[j], so d/dsed[j] = sum over cells of
+//     ratio (-q gF - a gT);
+//   limb: d/dL = sum over j of the cell's unit-L contribution dotted with g.
+// ---------------------------------------------------------------------------
+
+constexpr int ADJ_MAX_MU = 256;   // mu rows the adjoint's per-phase regrouping handles
+
+// per phase, the active cells regrouped by mu row (stable: map order within a row);
+// roff[p][b .. b + 1] delimits row b.  One thread per phase (a few thousand cells).
+__global__ void k_adj_bucket(int n_mu, long long gm, const int *__restrict__ cells, const int *__restrict__ counts,
+                             const int *__restrict__ region_m, int *__restrict__ rcells, int *__restrict__ roff,
+                             int *status) {
+    __shared__ int cur[ADJ_MAX_MU + 1];
+    const int p = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    const int *pc = cells + (long long)p * gm;
+    const int nc = counts[p];
+    int *off = roff + (long long)p * (n_mu + 1);
+    for (int b = 0; b <= n_mu; ++b) cur[b] = 0;
+    for (int c = 0; c < nc; ++c) {
+        int row = region_m[pc[c]];
+        if ((unsigned)row >= (unsigned)n_mu) {
+            atomicExch(status, 21);
+            row = 0;
+        }
+        cur[row + 1]++;
+    }
+    for (int b = 1; b <= n_mu; ++b) cur[b] += cur[b - 1];
+    for (int b = 0; b <= n_mu; ++b) off[b] = cur[b];
+    int *pr = rcells + (long long)p * gm;
+    for (int c = 0; c < nc; ++c) {
+        int row = region_m[pc[c]];
+        if ((unsigned)row >= (unsigned)n_mu) row = 0;
+        pr[cur[row]++] = pc[c];
+    }
+}
+
+// cell intensity I at pixel j (fast_intensity / fast_intensity_fac / the solar form)
+__device__ __forceinline__ double soap_intensity(int type, double T, double lbk, double lj, double ssed, double fsed,
+                                                 int solar, int t_norm_fac) {
+    if (type == 0) {
+        const int tn = (int)T;
+        const double ratio = ((double)tn == T) ? 1.0 : soap_planck(lj, T) / soap_planck(lj, (double)tn);
+        return __dmul_rn(ratio, ssed);
+    }
+    if (solar) {
+        const double ratio = ((double)t_norm_fac == T) ? 1.0 : soap_planck(lj, T) / soap_planck(lj, (double)t_norm_fac);
+        return __dmul_rn(ratio, fsed);
+    }
+    return __dmul_rn(__dadd_rn(1.0, lbk), fsed);
+}
+
+// row gradients: grid (ceil(n / 256), n_mu); thread = source pixel i of row b
+__global__ void __launch_bounds__(256) k_adj_rows(
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ spot_sed,
+    const double *__restrict__ fac_sed, int n_phase, long long gm, const int *__restrict__ rcells,
+    const int *__restrict__ roff, int n_mu, const double *__restrict__ temp, const double *__restrict__ bi,
+    const double *__restrict__ delta_m, const double *__restrict__ limb_m, const double *__restrict__ lb_m,
+    double step, int solar, int t_star, int t_diff_fac, const double *__restrict__ gF, const double *__restrict__ gB,
+    const double *__restrict__ gT, long long g_stride, double *__restrict__ d_qn, double *__restrict__ d_qs,
+    double *__restrict__ d_sn, double *__restrict__ d_fn) {
+    __shared__ double s_delta[PHASE_CHUNK], s_limb[PHASE_CHUNK], s_fb[PHASE_CHUNK], s_sq[PHASE_CHUNK],
+        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK];
+    __shared__ int s_type[PHASE_CHUNK];
+    const int b = blockIdx.y;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double lambda0 = lam[0];
+    const int t_norm_fac = (int)(t_star + t_diff_fac + 0.9 - 216.8);
+    double aqn = 0.0, aqs = 0.0, asn = 0.0, afn = 0.0;
+    for (int p = 0; p < n_phase; ++p) {
+        const int *off = roff + (long long)p * (n_mu + 1);
+        const int c_lo = off[b], c_hi = off[b + 1];
+        const int *pr = rcells + (long long)p * gm;
+        const double *pt = temp + (long long)p * gm, *pb = bi + (long long)p * gm;
+        const double *gf = gF + (long long)p * g_stride, *gb = gB + (long long)p * g_stride,
+                     *gt = gT + (long long)p * g_stride;
+        for (int c0 = c_lo; c0 < c_hi; c0 += PHASE_CHUNK) {
+            const int nc = min(PHASE_CHUNK, c_hi - c0);
+            __syncthreads();
+            for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+                const int k = pr[c0 + t];
+                const double d = delta_m[k];
+                const CellShift cs = soap_cell_shift(d, lambda0, step);
+                s_delta[t] = d;
+                s_limb[t] = limb_m[k];
+                s_fb[t] = cs.fbeta;
+                s_sq[t] = cs.sq;
+                s_off[t] = cs.off;
+                s_lb[t] = lb_m[k];
+                s_temp[t] = pt[k];
+                s_type[t] = (pb[k] == 0.0) ? 0 : 1;
+            }
+            __syncthreads();
+            if (i >= n_eff) continue;
+            for (int t = 0; t < nc; ++t) {
+                const double L = s_limb[t];
+                const int type = s_type[t];
+                // contributions of output pixel j with weight w on source i
+                auto add = [&](long long j, double w) {
+                    const double lj = lam[j];
+                    const double I = soap_intensity(type, s_temp[t], s_lb[t], lj, spot_sed[j], fac_sed[j], solar,
+                                                    t_norm_fac);
+                    const double lw = __dmul_rn(L, w);
+                    aqs = fma(lw, __dadd_rn(gf[j], gt[j]), aqs);
+                    aqn = fma(lw, __dsub_rn(gb[j], __dmul_rn(I, gf[j])), aqn);
+                    const double ha = __dsub_rn(-gb[j], __dmul_rn(I, gt[j]));
+                    if (type == 0) asn = fma(lw, ha, asn);
+                    else afn = fma(lw, ha, afn);
+                };
+                if (s_delta[t] == 0.0) {   // v == 0: output pixel i copies source i
+                    add(i, 1.0);
+                    continue;
+                }
+                CellShift cs;
+                cs.fbeta = s_fb[t];
+                cs.sq = s_sq[t];
+                cs.off = s_off[t];
+                // owner o = i - 1 (source i is its upper neighbour) and o = i (lower)
+                for (int side = 0; side < 2; ++side) {
+                    const long long o = i - 1 + side;
+                    if (o < 0 || o > n_eff - 2) continue;
+                    const long long ja = max(soap_ceil_pos(o, cs), 0LL);
+                    const long long jb = min(soap_ceil_pos(o + 1, cs), (long long)n_eff);
+                    if (ja >= jb) continue;
+                    const double lo0 = lam[o], lo1 = lam[o + 1];
+                    const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
+                    const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
+                    const double dd = __dsub_rn(ls1, ls0);
+                    for (long long j = ja; j < jb; ++j) {
+                        const double r = __ddiv_rn(__dsub_rn(lam[j], ls0), dd);
+                        add(j, side == 0 ? r : __dsub_rn(1.0, r));
+                    }
+                }
+            }
+        }
+    }
+    if (i < n) {
+        const long long o = (long long)b * n + i;
+        d_qn[o] = aqn;
+        d_qs[o] = aqs;
+        d_sn[o] = asn;
+        d_fn[o] = afn;
+    }
+}
+
+// continuum-row gradients: thread = output pixel j; all active cells of all phases
+__global__ void __launch_bounds__(256) k_adj_continuum(
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ q_norm,
+    const double *__restrict__ spot_norm, const double *__restrict__ fac_norm, const double *__restrict__ spot_sed,
+    const double *__restrict__ fac_sed, int n_phase, long long gm, const int *__restrict__ cells,
+    const int *__restrict__ counts, const double *__restrict__ temp, const double *__restrict__ bi,
+    const double *__restrict__ delta_m, const double *__restrict__ limb_m, const double *__restrict__ lb_m,
+    const int *__restrict__ region_m, int n_mu, double step, int solar, int t_star, int t_diff_fac,
+    const double *__restrict__ gF, const double *__restrict__ gT, long long g_stride, double *__restrict__ d_ss,
+    double *__restrict__ d_fs) {
+    __shared__ double s_delta[PHASE_CHUNK], s_limb[PHASE_CHUNK], s_fb[PHASE_CHUNK], s_sq[PHASE_CHUNK],
+        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK];
+    __shared__ int s_row[PHASE_CHUNK], s_type[PHASE_CHUNK];
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double lambda0 = lam[0];
+    const int t_norm_fac = (int)(t_star + t_diff_fac + 0.9 - 216.8);
+    const double lj = (j < n_eff) ? lam[j] : 0.0;
+    double ass = 0.0, afs = 0.0;
+    for (int p = 0; p < n_phase; ++p) {
+        const int *pc = cells + (long long)p * gm;
+        const int nc_all = counts[p];
+        const double *pt = temp + (long long)p * gm, *pb = bi + (long long)p * gm;
+        const double gf = (j < n_eff) ? gF[(long long)p * g_stride + j] : 0.0;
+        const double gt = (j < n_eff) ? gT[(long long)p * g_stride + j] : 0.0;
+        for (int c0 = 0; c0 < nc_all; c0 += PHASE_CHUNK) {
+            const int nc = min(PHASE_CHUNK, nc_all - c0);
+            __syncthreads();
+            for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+                const int k = pc[c0 + t];
+                const double d = delta_m[k];
+                const CellShift cs = soap_cell_shift(d, lambda0, step);
+                s_delta[t] = d;
+                s_limb[t] = limb_m[k];
+                s_fb[t] = cs.fbeta;
+                s_sq[t] = cs.sq;
+                s_off[t] = cs.off;
+                int row = region_m[k];
+                s_row[t] = ((unsigned)row < (unsigned)n_mu) ? row : 0;
+                s_lb[t] = lb_m[k];
+                s_temp[t] = pt[k];
+                s_type[t] = (pb[k] == 0.0) ? 0 : 1;
+            }
+            __syncthreads();
+            if (j >= n_eff) continue;
+            for (int t = 0; t < nc; ++t) {
+                CellShift cs;
+                cs.fbeta = s_fb[t];
+                cs.sq = s_sq[t];
+                cs.off = s_off[t];
+                const double d = s_delta[t], L = s_limb[t];
+                const long long off = (long long)s_row[t] * n;
+                CellAt at;
+                if (d != 0.0) at = soap_cell_at(j, n_eff, lam, cs);
+                const double q = soap_lerp_at(at, j, q_norm + off, d, L);
+                const double h = -__dmul_rn(q, gf);
+                if (s_type[t] == 0) {
+                    const double a = soap_lerp_at(at, j, spot_norm + off, d, L);
+                    const double ratio = soap_intensity(0, s_temp[t], 0.0, lj, 1.0, 0.0, solar, t_norm_fac);
+                    ass = fma(ratio, __dsub_rn(h, __dmul_rn(a, gt)), ass);
+                } else {
+                    const double a = soap_lerp_at(at, j, fac_norm + off, d, L);
+                    const double ratio = soap_intensity(1, s_temp[t], s_lb[t], lj, 0.0, 1.0, solar, t_norm_fac);
+                    afs = fma(ratio, __dsub_rn(h, __dmul_rn(a, gt)), afs);
+                }
+            }
+        }
+    }
+    if (j < n) {
+        d_ss[j] = ass;
+        d_fs[j] = afs;
+    }
+}
+
+// limb gradients per (phase, cell): block (x, p) takes the phase's cells x, x + gridDim.x,
+// ...; the dot product over the pixels is reduced in a fixed order (warp shuffles,
+// then warps in order) into buf[p][k]
+__global__ void __launch_bounds__(256) k_adj_limb(
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ q_norm,
+    const double *__restrict__ q_sed, const double *__restrict__ spot_norm, const double *__restrict__ fac_norm,
+    const double *__restrict__ spot_sed, const double *__restrict__ fac_sed, long long gm,
+    const int *__restrict__ cells, const int *__restrict__ counts, const double *__restrict__ temp,
+    const double *__restrict__ bi, const double *__restrict__ delta_m, const double *__restrict__ lb_m,
+    const int *__restrict__ region_m, int n_mu, double step, int solar, int t_star, int t_diff_fac,
+    const double *__restrict__ gF, const double *__restrict__ gB, const double *__restrict__ gT, long long g_stride,
+    double *__restrict__ buf) {
+    __shared__ double red[256 / 32];
+    const int p = blockIdx.y;
+    const double lambda0 = lam[0];
+    const int t_norm_fac = (int)(t_star + t_diff_fac + 0.9 - 216.8);
+    const int *pc = cells + (long long)p * gm;
+    const int nc = counts[p];
+    const double *gf = gF + (long long)p * g_stride, *gb = gB + (long long)p * g_stride,
+                 *gt = gT + (long long)p * g_stride;
+    for (int c = blockIdx.x; c < nc; c += gridDim.x) {
+        const int k = pc[c];
+        const double d = delta_m[k];
+        const CellShift cs = soap_cell_shift(d, lambda0, step);
+        int row = region_m[k];
+        row = ((unsigned)row < (unsigned)n_mu) ? row : 0;
+        const long long off = (long long)row * n;
+        const int type = (bi[(long long)p * gm + k] == 0.0) ? 0 : 1;
+        const double T = temp[(long long)p * gm + k], lbk = lb_m[k];
+        const double *arow = (type == 0 ? spot_norm : fac_norm) + off;
+        double acc = 0.0;
+        for (long long j = threadIdx.x; j < n_eff; j += blockDim.x) {
+            CellAt at;
+            if (d != 0.0) at = soap_cell_at(j, n_eff, lam, cs);
+            const double q = soap_lerp_at(at, j, q_norm + off, d, 1.0);
+            const double s = soap_lerp_at(at, j, q_sed + off, d, 1.0);
+            const double a = soap_lerp_at(at, j, arow, d, 1.0);
+            const double I = soap_intensity(type, T, lbk, lam[j], spot_sed[j], fac_sed[j], solar, t_norm_fac);
+            acc = fma(gf[j], __dsub_rn(s, __dmul_rn(I, q)), acc);
+            acc = fma(gb[j], __dsub_rn(q, a), acc);
+            acc = fma(gt[j], __dsub_rn(s, __dmul_rn(I, a)), acc);
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w];
+            buf[(long long)p * gm + k] = sum;
+        }
+    }
+}
+
+// grad_limb[k] = sum over phases, in order, of buf[p][k]
+__global__ void k_adj_sum_phases(int n_phase, long long gm, const double *__restrict__ buf, double *out) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= gm) return;
+    double s = 0.0;
+    for (int p = 0; p < n_phase; ++p) s += buf[(long long)p * gm + k];
+    out[k] = s;
+}
+
 // float -> double copy without FP64 instructions
 __global__ void k_f32_widen(long long count, const float *__restrict__ a, double *__restrict__ out) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -303,4 +595,130 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return host ? check_status(ctx, "soapgb_phase_integrate") : SOAPGB_OK;
+}
+
+extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff, const double *wave, int grid,
+                                              int n_phase, const double *temp, const double *bi,
+                                              const soapgb_maps *maps, const soapgb_cubes *cubes, double step,
+                                              const soapgb_activity *act, const double *g_flux,
+                                              const double *g_bconv, const double *g_tot, int mem,
+                                              double *grad_q_norm, double *grad_q_sed, double *grad_spot_norm,
+                                              double *grad_fac_norm, double *grad_spot_sed, double *grad_fac_sed,
+                                              double *grad_limb) {
+    if (!ctx || !maps || !cubes || !act) return SOAPGB_ERR_ARG;
+    if (n < 2 || n_eff < 2 || n_eff > n || grid < 1 || n_phase < 0 || cubes->n_mu < 1 ||
+        cubes->n_mu > ADJ_MAX_MU || !(step > 0) || !wave || !temp || !bi || !maps->delta || !maps->limb ||
+        !maps->lb || !maps->region || !cubes->q_norm || !cubes->q_sed || !cubes->spot_norm || !cubes->fac_norm ||
+        !cubes->spot_sed || !cubes->fac_sed || !g_flux || !g_bconv || !g_tot || !grad_q_norm || !grad_q_sed ||
+        !grad_spot_norm || !grad_fac_norm || !grad_spot_sed || !grad_fac_sed || !grad_limb)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_integrate_adjoint: bad arguments");
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    const long long gm = (long long)grid * grid;
+    const int n_mu = cubes->n_mu;
+    const size_t cube_b = sizeof(double) * (size_t)n * n_mu, row_b = sizeof(double) * (size_t)n;
+    const size_t g_b = sizeof(double) * (size_t)n * std::max(n_phase, 1);
+    const size_t map_b = sizeof(double) * (size_t)gm * std::max(n_phase, 1);
+    const bool host = (mem == SOAPGB_HOST);
+    Workspace ws(ctx);
+    int s_wave = ws.add(host ? row_b : 0);
+    int s_c[6];
+    for (int q = 0; q < 4; ++q) s_c[q] = ws.add(host ? cube_b : 0);
+    for (int q = 4; q < 6; ++q) s_c[q] = ws.add(host ? row_b : 0);
+    int s_temp = ws.add(host ? map_b : 0), s_bi = ws.add(host ? map_b : 0);
+    int s_m[4];
+    for (int q = 0; q < 3; ++q) s_m[q] = ws.add(host ? sizeof(double) * gm : 0);
+    s_m[3] = ws.add(host ? sizeof(int) * gm : 0);
+    int s_g[3];
+    for (int q = 0; q < 3; ++q) s_g[q] = ws.add(host ? g_b : 0);
+    int s_o[7];
+    for (int q = 0; q < 4; ++q) s_o[q] = ws.add(host ? cube_b : 0);
+    for (int q = 4; q < 6; ++q) s_o[q] = ws.add(host ? row_b : 0);
+    s_o[6] = ws.add(host ? sizeof(double) * gm : 0);
+    int s_cells = ws.add(sizeof(int) * gm * std::max(n_phase, 1));
+    int s_rcells = ws.add(sizeof(int) * gm * std::max(n_phase, 1));
+    int s_counts = ws.add(sizeof(int) * std::max(n_phase, 1));
+    int s_roff = ws.add(sizeof(int) * (size_t)(n_mu + 1) * std::max(n_phase, 1));
+    int s_buf = ws.add(map_b);
+    int rc = ws.commit();
+    if (rc) return rc;
+#define STAGE(dst, src, bytes, slot)                                                           \
+    dst = (decltype(dst))stage_in(ctx, mem, src, bytes, ws.get<void>(slot), &rc);             \
+    if (rc) return rc;
+    const double *d_wave, *d_qn, *d_qs, *d_sn, *d_fn, *d_ss, *d_fs, *d_temp, *d_bi, *d_delta, *d_limb, *d_lb;
+    const int *d_region;
+    const double *d_gf, *d_gb, *d_gt;
+    STAGE(d_wave, wave, row_b, s_wave);
+    STAGE(d_qn, cubes->q_norm, cube_b, s_c[0]);
+    STAGE(d_qs, cubes->q_sed, cube_b, s_c[1]);
+    STAGE(d_sn, cubes->spot_norm, cube_b, s_c[2]);
+    STAGE(d_fn, cubes->fac_norm, cube_b, s_c[3]);
+    STAGE(d_ss, cubes->spot_sed, row_b, s_c[4]);
+    STAGE(d_fs, cubes->fac_sed, row_b, s_c[5]);
+    STAGE(d_temp, temp, map_b, s_temp);
+    STAGE(d_bi, bi, map_b, s_bi);
+    STAGE(d_delta, maps->delta, sizeof(double) * gm, s_m[0]);
+    STAGE(d_limb, maps->limb, sizeof(double) * gm, s_m[1]);
+    STAGE(d_lb, maps->lb, sizeof(double) * gm, s_m[2]);
+    STAGE(d_region, maps->region, sizeof(int) * gm, s_m[3]);
+    STAGE(d_gf, g_flux, g_b, s_g[0]);
+    STAGE(d_gb, g_bconv, g_b, s_g[1]);
+    STAGE(d_gt, g_tot, g_b, s_g[2]);
+#undef STAGE
+    double *o_qn = host ? ws.get<double>(s_o[0]) : grad_q_norm;
+    double *o_qs = host ? ws.get<double>(s_o[1]) : grad_q_sed;
+    double *o_sn = host ? ws.get<double>(s_o[2]) : grad_spot_norm;
+    double *o_fn = host ? ws.get<double>(s_o[3]) : grad_fac_norm;
+    double *o_ss = host ? ws.get<double>(s_o[4]) : grad_spot_sed;
+    double *o_fs = host ? ws.get<double>(s_o[5]) : grad_fac_sed;
+    double *o_lm = host ? ws.get<double>(s_o[6]) : grad_limb;
+    int *d_cells = ws.get<int>(s_cells), *d_rcells = ws.get<int>(s_rcells);
+    int *d_counts = ws.get<int>(s_counts), *d_roff = ws.get<int>(s_roff);
+    double *d_buf = ws.get<double>(s_buf);
+    if (n_phase == 0) {
+        for (double *o : {o_qn, o_qs, o_sn, o_fn})
+            SOAP_CUDA(ctx, cudaMemsetAsync(o, 0, cube_b, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemsetAsync(o_ss, 0, row_b, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemsetAsync(o_fs, 0, row_b, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemsetAsync(o_lm, 0, sizeof(double) * gm, ctx->stream));
+    } else {
+        rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
+        if (rc) return rc;
+        k_adj_bucket<<<n_phase, 32, 0, ctx->stream>>>(n_mu, gm, d_cells, d_counts, d_region, d_rcells, d_roff,
+                                                      ctx->d_status);
+        SOAP_LAUNCHED(ctx);
+        SOAP_TRACED(ctx, "adjoint_rows",
+                    k_adj_rows<<<dim3(grid_for(ctx, n, 256), n_mu), 256, 0, ctx->stream>>>(
+                        n, n_eff, d_wave, d_ss, d_fs, n_phase, gm, d_rcells, d_roff, n_mu, d_temp, d_bi, d_delta,
+                        d_limb, d_lb, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb, d_gt, n, o_qn, o_qs,
+                        o_sn, o_fn));
+        SOAP_LAUNCHED(ctx);
+        SOAP_TRACED(ctx, "adjoint_continuum",
+                    k_adj_continuum<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+                        n, n_eff, d_wave, d_qn, d_sn, d_fn, d_ss, d_fs, n_phase, gm, d_cells, d_counts, d_temp, d_bi,
+                        d_delta, d_limb, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf,
+                        d_gt, n, o_ss, o_fs));
+        SOAP_LAUNCHED(ctx);
+        SOAP_CUDA(ctx, cudaMemsetAsync(d_buf, 0, map_b, ctx->stream));
+        const int gx = (int)std::min<long long>(gm, 4LL * std::max(ctx->num_sms, 1));
+        SOAP_TRACED(ctx, "adjoint_limb",
+                    k_adj_limb<<<dim3(gx, n_phase), 256, 0, ctx->stream>>>(
+                        n, n_eff, d_wave, d_qn, d_qs, d_sn, d_fn, d_ss, d_fs, gm, d_cells, d_counts, d_temp, d_bi,
+                        d_delta, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb,
+                        d_gt, n, d_buf));
+        SOAP_LAUNCHED(ctx);
+        k_adj_sum_phases<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(n_phase, gm, d_buf, o_lm);
+        SOAP_LAUNCHED(ctx);
+    }
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_q_norm, o_qn, cube_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_q_sed, o_qs, cube_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_spot_norm, o_sn, cube_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_fac_norm, o_fn, cube_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_spot_sed, o_ss, row_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_fac_sed, o_fs, row_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_limb, o_lm, sizeof(double) * gm, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return check_status(ctx, "soapgb_phase_integrate_adjoint");
+    }
+    return SOAPGB_OK;
 }
