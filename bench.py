@@ -313,6 +313,7 @@ def run_own(args):
             "kernels_ms_per_step": {k: round(v[1], 4) for k, v in sorted(ktab.items(), key=lambda x: -x[1][1])},
             "seed_preparation": {"bisector_injection_ms_per_cube": round(bis_ms, 4),
                                  "cube": "%d mu bins x %d px, quiet form, inputs resident" % (n_mu, n)},
+            "differentiable": adjoint_timing(ctx, dev),
             "clocks": clk,
         }
     if dist:
@@ -342,6 +343,59 @@ def algorithmic_bytes(kernel, case, phases, regions, act, ctx, maps_d, form):
     if kernel == "norm32":
         return {"bytes": 3 * n_phase * n_eff * (4 + 8), "formula": "3 n_phase x N_eff x (4 + 8) B"}
     return {"bytes": 0, "formula": "not modelled"}
+
+
+def adjoint_timing(ctx, dev, reps=3):
+    """Forward and forward + adjoint of the differentiable integration (PLAIN64,
+    soap_gpu_gb300.differentiable) on one star of the differentiable-form shape: 200x200
+    grid, 100,000 px, 3 regions, 5 phases over one rotation (of its 50); CUDA events,
+    inputs resident."""
+    import dataclasses
+    import torch
+    from soap_gpu_gb300 import synth
+    from soap_gpu_gb300.differentiable import IntegrationSetup, deficit_spectra
+    from soap_gpu_gb300._lib import Activity
+    case = synth.small_case(seed=4, grid=200, n=100000, n_phase=5, n_mu=10)
+    case = dataclasses.replace(case, regions=np.array([[20.0, 180.0, 0.1, 0.0], [-15.0, 200.0, 0.1732, 1.0],
+                                                       [35.0, 160.0, 0.1, 1.0]]), rot_step=0.2)
+    inp = synth.generate(case)
+    n_eff = (case.n // 512) * 512
+    setup = IntegrationSetup.build(ctx, inp.wave, n_eff, case.grid, case.period, case.w_ratio, case.incl,
+                                   case.radius_km, inp.mu_boundary, inp.lb, case.phases,
+                                   [case.regions for _ in case.phases],
+                                   Activity(case.t_star, case.t_diff_spot, case.t_diff_fac, case.nrho, 0), case.step,
+                                   device=dev)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    cubes = [T(inp.q_norm), T(inp.q_sed), T(inp.spot_norm), T(inp.fac_norm), T(inp.spot_sed[0]), T(inp.fac_sed[0])]
+    u = T([case.u1, case.u2])
+    W = torch.ones((case.n_phase, 3, case.n), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def fwd():
+        with torch.no_grad():
+            deficit_spectra(u, *cubes, setup)
+
+    def fwd_bwd():
+        ug = u.clone().requires_grad_(True)
+        cg = [c.clone().requires_grad_(True) for c in cubes]
+        (deficit_spectra(ug, *cg, setup) * W).sum().backward()
+
+    f_ms, fb_ms = timed(fwd), timed(fwd_bwd)
+    return {"case": "200x200 grid, 100,000 px, 10 mu bins, 3 regions, 5 phases over one rotation, PLAIN64; "
+                    "gradients w.r.t. "
+                    "u1, u2, 4 seed cubes, 2 continuum rows",
+            "forward_ms": round(f_ms, 3), "forward_adjoint_ms": round(fb_ms, 3), "ratio": round(fb_ms / f_ms, 2)}
 
 
 def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, regions, act, star):

@@ -215,6 +215,38 @@ __device__ __forceinline__ double soap_intensity(int type, double T, double lbk,
     return __dmul_rn(__dadd_rn(1.0, lbk), fsed);
 }
 
+// unit-limb values of a cell's three rows at output pixel j (q_norm, q_sed and the
+// spot or facula row), from one division: w = dl / dd at the owner o, then
+// row[o] + (row[o+1] - row[o]) w.  The forward forms ((row[o+1] - row[o]) / dd) dl per
+// row; the adjoint needs the values, not that rounding.
+struct AdjRows {
+    double q, s, a;
+};
+__device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const double *__restrict__ lam,
+                                               const CellShift &cs, double d, const double *__restrict__ rq,
+                                               const double *__restrict__ rs, const double *__restrict__ ra) {
+    AdjRows v;
+    if (d == 0.0) {
+        v.q = rq[j];
+        v.s = rs[j];
+        v.a = ra[j];
+        return v;
+    }
+    const long long o = soap_owner(j, n_eff, cs);
+    if (o < 0) {
+        v.q = v.s = v.a = 0.0;
+        return v;
+    }
+    const double lo0 = lam[o], lo1 = lam[o + 1];
+    const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
+    const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
+    const double w = __ddiv_rn(__dsub_rn(lam[j], ls0), __dsub_rn(ls1, ls0));
+    v.q = fma(rq[o + 1] - rq[o], w, rq[o]);
+    v.s = fma(rs[o + 1] - rs[o], w, rs[o]);
+    v.a = fma(ra[o + 1] - ra[o], w, ra[o]);
+    return v;
+}
+
 // row gradients: grid (ceil(n / 256), n_mu); thread = source pixel i of row b
 __global__ void __launch_bounds__(256) k_adj_rows(
     int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ spot_sed,
@@ -359,19 +391,14 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
                 cs.off = s_off[t];
                 const double d = s_delta[t], L = s_limb[t];
                 const long long off = (long long)s_row[t] * n;
-                CellAt at;
-                if (d != 0.0) at = soap_cell_at(j, n_eff, lam, cs);
-                const double q = soap_lerp_at(at, j, q_norm + off, d, L);
-                const double h = -__dmul_rn(q, gf);
-                if (s_type[t] == 0) {
-                    const double a = soap_lerp_at(at, j, spot_norm + off, d, L);
-                    const double ratio = soap_intensity(0, s_temp[t], 0.0, lj, 1.0, 0.0, solar, t_norm_fac);
-                    ass = fma(ratio, __dsub_rn(h, __dmul_rn(a, gt)), ass);
-                } else {
-                    const double a = soap_lerp_at(at, j, fac_norm + off, d, L);
-                    const double ratio = soap_intensity(1, s_temp[t], s_lb[t], lj, 0.0, 1.0, solar, t_norm_fac);
-                    afs = fma(ratio, __dsub_rn(h, __dmul_rn(a, gt)), afs);
-                }
+                const int type = s_type[t];
+                const AdjRows v = adj_rows_at(j, n_eff, lam, cs, d, q_norm + off, q_norm + off,
+                                              (type == 0 ? spot_norm : fac_norm) + off);
+                // d/dsed[j] of (-I q gF - I a gT) with I = ratio sed[j]; q, a carry L
+                const double h = __dmul_rn(L, fma(-v.q, gf, -__dmul_rn(v.a, gt)));
+                const double ratio = soap_intensity(type, s_temp[t], s_lb[t], lj, 1.0, 1.0, solar, t_norm_fac);
+                if (type == 0) ass = fma(ratio, h, ass);
+                else afs = fma(ratio, h, afs);
             }
         }
     }
@@ -413,15 +440,11 @@ __global__ void __launch_bounds__(256) k_adj_limb(
         const double *arow = (type == 0 ? spot_norm : fac_norm) + off;
         double acc = 0.0;
         for (long long j = threadIdx.x; j < n_eff; j += blockDim.x) {
-            CellAt at;
-            if (d != 0.0) at = soap_cell_at(j, n_eff, lam, cs);
-            const double q = soap_lerp_at(at, j, q_norm + off, d, 1.0);
-            const double s = soap_lerp_at(at, j, q_sed + off, d, 1.0);
-            const double a = soap_lerp_at(at, j, arow, d, 1.0);
+            const AdjRows v = adj_rows_at(j, n_eff, lam, cs, d, q_norm + off, q_sed + off, arow);
             const double I = soap_intensity(type, T, lbk, lam[j], spot_sed[j], fac_sed[j], solar, t_norm_fac);
-            acc = fma(gf[j], __dsub_rn(s, __dmul_rn(I, q)), acc);
-            acc = fma(gb[j], __dsub_rn(q, a), acc);
-            acc = fma(gt[j], __dsub_rn(s, __dmul_rn(I, a)), acc);
+            acc = fma(gf[j], __dsub_rn(v.s, __dmul_rn(I, v.q)), acc);
+            acc = fma(gb[j], __dsub_rn(v.q, v.a), acc);
+            acc = fma(gt[j], __dsub_rn(v.s, __dmul_rn(I, v.a)), acc);
         }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         __syncthreads();
