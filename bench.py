@@ -367,7 +367,7 @@ def adjoint_timing(ctx, dev, reps=3):
                                    device=dev)
     T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
     cubes = [T(inp.q_norm), T(inp.q_sed), T(inp.spot_norm), T(inp.fac_norm), T(inp.spot_sed[0]), T(inp.fac_sed[0])]
-    u = T([case.u1, case.u2])
+    u = T([case.u1, case.u2, case.vsini])
     W = torch.ones((case.n_phase, 3, case.n), dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream()
 

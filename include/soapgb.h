@@ -180,9 +180,11 @@ int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_eff, const do
  * form; the reference has no counterpart).  Given the gradients g_flux, g_bconv, g_tot
  * (n_phase x n each) of a scalar with respect to the three outputs, writes its
  * gradients with respect to the four cubes (n_mu x n each), the two continuum rows
- * (spot_sed, fac_sed: n each) and the limb map (G*G), each summed over the phases.
- * The outputs are linear in all of them.  The chain rule to the limb-darkening
- * coefficients is dL/du1 = -(1 - mu), dL/du2 = -(1 - mu)^2 on visible cells.
+ * (spot_sed, fac_sed: n each), the limb map and the velocity map (G*G each), each
+ * summed over the phases.  The outputs are linear in the cubes, rows and limb values;
+ * in a cell's velocity they are continuous and piecewise smooth (the derivative of the
+ * interpolation weight inside each owner interval).  Chain rules: dL/du1 = -(1 - mu),
+ * dL/du2 = -(1 - mu)^2 on visible cells; the velocity map is proportional to vsini.
  * Deterministic: every sum runs in a fixed order, without atomics. */
 int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff, const double *wave,
                                    int grid, int n_phase, const double *temp, const double *bi,
@@ -191,7 +193,7 @@ int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff, const doub
                                    const double *g_bconv, const double *g_tot, int mem,
                                    double *grad_q_norm, double *grad_q_sed, double *grad_spot_norm,
                                    double *grad_fac_norm, double *grad_spot_sed, double *grad_fac_sed,
-                                   double *grad_limb);
+                                   double *grad_limb, double *grad_delta);
 
 /* ---- a15-a16: mask CCF ---------------------------------------------------
  * Replaces calculate_CCF_1 / calc_mask / calculate_CCF_2, CCF_func.py:5-91, with

@@ -69,7 +69,7 @@ SIGNATURES = [
     ("soapgb_phase_integrate_adjoint", ctypes.c_int,
      [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.POINTER(Maps),
       ctypes.POINTER(Cubes), ctypes.c_double, ctypes.POINTER(Activity), _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp,
-      _vp, _vp, _vp, _vp]),
+      _vp, _vp, _vp, _vp, _vp]),
     ("soapgb_ccf", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                   _vp, ctypes.c_int, ctypes.c_int, _vp]),

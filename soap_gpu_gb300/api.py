@@ -270,8 +270,8 @@ class Context:
                                 g_flux, g_bconv, g_tot):
         """Gradients of a scalar through phase_integrate (PLAIN64 arithmetic), given its
         gradients g_flux, g_bconv, g_tot (n_phase x n) w.r.t. the outputs: a dict with the
-        four cubes (n_mu x n), the two continuum rows ("spot_sed", "fac_sed", n) and the
-        limb map ("limb", G*G), each summed over the phases."""
+        four cubes (n_mu x n), the two continuum rows ("spot_sed", "fac_sed", n), the limb
+        map ("limb", G*G) and the velocity map ("delta", G*G), each summed over the phases."""
         a = self._args(wave, temp, cubes["q_norm"])
         n = int(wave.shape[0])
         n_phase = int(temp.shape[0])
@@ -286,7 +286,8 @@ class Context:
         out = {}
         ptrs = []
         for k, shape in (("q_norm", (n_mu, n)), ("q_sed", (n_mu, n)), ("spot_norm", (n_mu, n)),
-                         ("fac_norm", (n_mu, n)), ("spot_sed", (n,)), ("fac_sed", (n,)), ("limb", (int(grid) ** 2,))):
+                         ("fac_norm", (n_mu, n)), ("spot_sed", (n,)), ("fac_sed", (n,)), ("limb", (int(grid) ** 2,)),
+                         ("delta", (int(grid) ** 2,))):
             out[k], pk = a.out(shape, np.float64)
             ptrs.append(pk)
         self._check(self.L.soapgb_phase_integrate_adjoint(

@@ -165,7 +165,11 @@ __global__ void __launch_bounds__(256) k_phase_plain64(
 //     spot / facula rows: -gB - I gT);
 //   continuum rows: I = ratio x sed[j], so d/dsed[j] = sum over cells of
 //     ratio (-q gF - a gT);
-//   limb: d/dL = sum over j of the cell's unit-L contribution dotted with g.
+//   limb: d/dL = sum over j of the cell's unit-L contribution dotted with g;
+//   velocity: the weight w = (l_j / S - l_o) / (l_{o+1} - l_o) of the owner o moves
+//     with the Doppler factor S = sqrt((1 + b) / (1 - b)), b = delta 1000 / c:
+//     dw/ddelta = -l_j / (S^2 (l_{o+1} - l_o)) x 1 / (S (1 - b)^2) x 1000 / c, and each
+//     row's value moves by (row[o+1] - row[o]) dw/ddelta (continuous across owners).
 // ---------------------------------------------------------------------------
 
 constexpr int ADJ_MAX_MU = 256;   // mu rows the adjoint's per-phase regrouping handles
@@ -221,29 +225,39 @@ __device__ __forceinline__ double soap_intensity(int type, double T, double lbk,
 // row; the adjoint needs the values, not that rounding.
 struct AdjRows {
     double q, s, a;
+    double dq, ds, da;   // d/ddelta of the three values (unit limb)
 };
 __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const double *__restrict__ lam,
                                                const CellShift &cs, double d, const double *__restrict__ rq,
                                                const double *__restrict__ rs, const double *__restrict__ ra) {
     AdjRows v;
-    if (d == 0.0) {
-        v.q = rq[j];
-        v.s = rs[j];
-        v.a = ra[j];
-        return v;
-    }
-    const long long o = soap_owner(j, n_eff, cs);
+    // the owner interval of j; with v == 0 the forward copies pixel j (owner j, w = 0)
+    const long long o = (d == 0.0) ? ((j <= n_eff - 2) ? j : -1) : soap_owner(j, n_eff, cs);
+    const double beta = d * 1000. / SOAP_C_LIGHT;
     if (o < 0) {
-        v.q = v.s = v.a = 0.0;
+        v.q = (d == 0.0) ? rq[j] : 0.0;
+        v.s = (d == 0.0) ? rs[j] : 0.0;
+        v.a = (d == 0.0) ? ra[j] : 0.0;
+        v.dq = v.ds = v.da = 0.0;
         return v;
     }
     const double lo0 = lam[o], lo1 = lam[o + 1];
-    const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
-    const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
-    const double w = __ddiv_rn(__dsub_rn(lam[j], ls0), __dsub_rn(ls1, ls0));
-    v.q = fma(rq[o + 1] - rq[o], w, rq[o]);
-    v.s = fma(rs[o + 1] - rs[o], w, rs[o]);
-    v.a = fma(ra[o + 1] - ra[o], w, ra[o]);
+    double w = 0.0;
+    if (d != 0.0) {
+        const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
+        const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
+        w = __ddiv_rn(__dsub_rn(lam[j], ls0), __dsub_rn(ls1, ls0));
+    }
+    const double eq = rq[o + 1] - rq[o], es = rs[o + 1] - rs[o], ea = ra[o + 1] - ra[o];
+    v.q = fma(eq, w, rq[o]);
+    v.s = fma(es, w, rs[o]);
+    v.a = fma(ea, w, ra[o]);
+    const double S = (d == 0.0) ? 1.0 : cs.sq;
+    const double omb = 1.0 - beta;
+    const double dw = -lam[j] / (S * S * (lo1 - lo0)) / (S * omb * omb) * (1000. / SOAP_C_LIGHT);
+    v.dq = eq * dw;
+    v.ds = es * dw;
+    v.da = ea * dw;
     return v;
 }
 
@@ -419,8 +433,8 @@ __global__ void __launch_bounds__(256) k_adj_limb(
     const double *__restrict__ bi, const double *__restrict__ delta_m, const double *__restrict__ lb_m,
     const int *__restrict__ region_m, int n_mu, double step, int solar, int t_star, int t_diff_fac,
     const double *__restrict__ gF, const double *__restrict__ gB, const double *__restrict__ gT, long long g_stride,
-    double *__restrict__ buf) {
-    __shared__ double red[256 / 32];
+    const double *__restrict__ limb_m, double *__restrict__ buf, double *__restrict__ buf_d) {
+    __shared__ double red[2][256 / 32];
     const int p = blockIdx.y;
     const double lambda0 = lam[0];
     const int t_norm_fac = (int)(t_star + t_diff_fac + 0.9 - 216.8);
@@ -438,22 +452,35 @@ __global__ void __launch_bounds__(256) k_adj_limb(
         const int type = (bi[(long long)p * gm + k] == 0.0) ? 0 : 1;
         const double T = temp[(long long)p * gm + k], lbk = lb_m[k];
         const double *arow = (type == 0 ? spot_norm : fac_norm) + off;
-        double acc = 0.0;
+        double acc = 0.0, accd = 0.0;
         for (long long j = threadIdx.x; j < n_eff; j += blockDim.x) {
             const AdjRows v = adj_rows_at(j, n_eff, lam, cs, d, q_norm + off, q_sed + off, arow);
             const double I = soap_intensity(type, T, lbk, lam[j], spot_sed[j], fac_sed[j], solar, t_norm_fac);
             acc = fma(gf[j], __dsub_rn(v.s, __dmul_rn(I, v.q)), acc);
             acc = fma(gb[j], __dsub_rn(v.q, v.a), acc);
             acc = fma(gt[j], __dsub_rn(v.s, __dmul_rn(I, v.a)), acc);
+            accd = fma(gf[j], v.ds - I * v.dq, accd);
+            accd = fma(gb[j], v.dq - v.da, accd);
+            accd = fma(gt[j], v.ds - I * v.da, accd);
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            accd += __shfl_xor_sync(0xffffffffu, accd, o);
+        }
         __syncthreads();
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        if ((threadIdx.x & 31) == 0) {
+            red[0][threadIdx.x >> 5] = acc;
+            red[1][threadIdx.x >> 5] = accd;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double sum = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w];
+            double sum = 0.0, sumd = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                sum += red[0][w];
+                sumd += red[1][w];
+            }
             buf[(long long)p * gm + k] = sum;
+            buf_d[(long long)p * gm + k] = __dmul_rn(limb_m[k], sumd);   // the values carry L
         }
     }
 }
@@ -627,13 +654,13 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
                                               const double *g_bconv, const double *g_tot, int mem,
                                               double *grad_q_norm, double *grad_q_sed, double *grad_spot_norm,
                                               double *grad_fac_norm, double *grad_spot_sed, double *grad_fac_sed,
-                                              double *grad_limb) {
+                                              double *grad_limb, double *grad_delta) {
     if (!ctx || !maps || !cubes || !act) return SOAPGB_ERR_ARG;
     if (n < 2 || n_eff < 2 || n_eff > n || grid < 1 || n_phase < 0 || cubes->n_mu < 1 ||
         cubes->n_mu > ADJ_MAX_MU || !(step > 0) || !wave || !temp || !bi || !maps->delta || !maps->limb ||
         !maps->lb || !maps->region || !cubes->q_norm || !cubes->q_sed || !cubes->spot_norm || !cubes->fac_norm ||
         !cubes->spot_sed || !cubes->fac_sed || !g_flux || !g_bconv || !g_tot || !grad_q_norm || !grad_q_sed ||
-        !grad_spot_norm || !grad_fac_norm || !grad_spot_sed || !grad_fac_sed || !grad_limb)
+        !grad_spot_norm || !grad_fac_norm || !grad_spot_sed || !grad_fac_sed || !grad_limb || !grad_delta)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_integrate_adjoint: bad arguments");
     SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
     const long long gm = (long long)grid * grid;
@@ -653,15 +680,16 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     s_m[3] = ws.add(host ? sizeof(int) * gm : 0);
     int s_g[3];
     for (int q = 0; q < 3; ++q) s_g[q] = ws.add(host ? g_b : 0);
-    int s_o[7];
+    int s_o[8];
     for (int q = 0; q < 4; ++q) s_o[q] = ws.add(host ? cube_b : 0);
     for (int q = 4; q < 6; ++q) s_o[q] = ws.add(host ? row_b : 0);
     s_o[6] = ws.add(host ? sizeof(double) * gm : 0);
+    s_o[7] = ws.add(host ? sizeof(double) * gm : 0);
     int s_cells = ws.add(sizeof(int) * gm * std::max(n_phase, 1));
     int s_rcells = ws.add(sizeof(int) * gm * std::max(n_phase, 1));
     int s_counts = ws.add(sizeof(int) * std::max(n_phase, 1));
     int s_roff = ws.add(sizeof(int) * (size_t)(n_mu + 1) * std::max(n_phase, 1));
-    int s_buf = ws.add(map_b);
+    int s_buf = ws.add(map_b), s_bufd = ws.add(map_b);
     int rc = ws.commit();
     if (rc) return rc;
 #define STAGE(dst, src, bytes, slot)                                                           \
@@ -694,15 +722,17 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     double *o_ss = host ? ws.get<double>(s_o[4]) : grad_spot_sed;
     double *o_fs = host ? ws.get<double>(s_o[5]) : grad_fac_sed;
     double *o_lm = host ? ws.get<double>(s_o[6]) : grad_limb;
+    double *o_dl = host ? ws.get<double>(s_o[7]) : grad_delta;
     int *d_cells = ws.get<int>(s_cells), *d_rcells = ws.get<int>(s_rcells);
     int *d_counts = ws.get<int>(s_counts), *d_roff = ws.get<int>(s_roff);
-    double *d_buf = ws.get<double>(s_buf);
+    double *d_buf = ws.get<double>(s_buf), *d_bufd = ws.get<double>(s_bufd);
     if (n_phase == 0) {
         for (double *o : {o_qn, o_qs, o_sn, o_fn})
             SOAP_CUDA(ctx, cudaMemsetAsync(o, 0, cube_b, ctx->stream));
         SOAP_CUDA(ctx, cudaMemsetAsync(o_ss, 0, row_b, ctx->stream));
         SOAP_CUDA(ctx, cudaMemsetAsync(o_fs, 0, row_b, ctx->stream));
         SOAP_CUDA(ctx, cudaMemsetAsync(o_lm, 0, sizeof(double) * gm, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemsetAsync(o_dl, 0, sizeof(double) * gm, ctx->stream));
     } else {
         rc = compact_cells(ctx, n_phase, (int)gm, d_bi, -0.5, 1.5, (int)gm, d_cells, d_counts);
         if (rc) return rc;
@@ -722,14 +752,17 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
                         d_gt, n, o_ss, o_fs));
         SOAP_LAUNCHED(ctx);
         SOAP_CUDA(ctx, cudaMemsetAsync(d_buf, 0, map_b, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemsetAsync(d_bufd, 0, map_b, ctx->stream));
         const int gx = (int)std::min<long long>(gm, 4LL * std::max(ctx->num_sms, 1));
         SOAP_TRACED(ctx, "adjoint_limb",
                     k_adj_limb<<<dim3(gx, n_phase), 256, 0, ctx->stream>>>(
                         n, n_eff, d_wave, d_qn, d_qs, d_sn, d_fn, d_ss, d_fs, gm, d_cells, d_counts, d_temp, d_bi,
                         d_delta, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb,
-                        d_gt, n, d_buf));
+                        d_gt, n, d_limb, d_buf, d_bufd));
         SOAP_LAUNCHED(ctx);
         k_adj_sum_phases<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(n_phase, gm, d_buf, o_lm);
+        SOAP_LAUNCHED(ctx);
+        k_adj_sum_phases<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(n_phase, gm, d_bufd, o_dl);
         SOAP_LAUNCHED(ctx);
     }
     if (host) {
@@ -740,6 +773,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         SOAP_CUDA(ctx, cudaMemcpyAsync(grad_spot_sed, o_ss, row_b, cudaMemcpyDeviceToHost, ctx->stream));
         SOAP_CUDA(ctx, cudaMemcpyAsync(grad_fac_sed, o_fs, row_b, cudaMemcpyDeviceToHost, ctx->stream));
         SOAP_CUDA(ctx, cudaMemcpyAsync(grad_limb, o_lm, sizeof(double) * gm, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_delta, o_dl, sizeof(double) * gm, cudaMemcpyDeviceToHost, ctx->stream));
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return check_status(ctx, "soapgb_phase_integrate_adjoint");
     }

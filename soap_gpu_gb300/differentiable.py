@@ -5,17 +5,21 @@ the PLAIN64 arithmetic (SOAP_integration.cu:392-447, spot_integrate): the three 
 spectra (flux, bconv, tot) of every phase as a function of
 
 * the limb-darkening coefficients u1, u2 (through the limb map of the disk,
-  L = 1 - u1 (1 - mu) - u2 (1 - mu)^2, SOAP_initialize.cu:365-366), and
+  L = 1 - u1 (1 - mu) - u2 (1 - mu)^2, SOAP_initialize.cu:365-366),
+* vsini (the cells' velocities scale with it: the rotation period is
+  2 pi R / (vsini 86400)), and
 * the seed spectra: the quiet normalised and SED cubes, the spot and facula
   normalised cubes, and the spot and facula continuum rows.
 
 Its backward runs the hand-written adjoint kernels of ``soapgb_phase_integrate_adjoint``
-(deterministic gathers, no atomics) and applies the chain rule dL/du1 = -(1 - mu),
-dL/du2 = -(1 - mu)^2 to the limb-map gradient.  The outputs are linear in every one of
-these inputs, so the gradients are exact up to rounding; the tests check them against
-FP64 central differences and a dot-product identity.
+(deterministic gathers, no atomics) and applies the chain rules dL/du1 = -(1 - mu),
+dL/du2 = -(1 - mu)^2 to the limb-map gradient and d delta / d vsini = delta / vsini to
+the velocity-map gradient.  The outputs are linear in the limb values and the seed
+spectra (gradients exact up to rounding) and continuous, piecewise smooth in the
+velocities; the tests check them against FP64 central differences and a dot-product
+identity.
 
-Region positions and sizes stay discrete (cell coverage), as in the reference; vsini,
+Region positions and sizes stay discrete (cell coverage), as in the reference; the
 inclination and the region contrast are not differentiated yet.
 """
 from __future__ import annotations
@@ -59,18 +63,27 @@ class IntegrationSetup:
                    float(radius_km), dev(mu_boundary), tuple(float(x) for x in lb), dev(temp), dev(bi), float(step),
                    act)
 
-    def maps(self, u1: float, u2: float) -> dict:
-        """The disk maps for limb-darkening coefficients (u1, u2), on the device."""
-        return self.ctx.disk_maps(self.grid, self.period, self.omega_ratio, self.incl, self.radius_km, u1, u2,
+    @property
+    def vsini(self) -> float:
+        """Equatorial velocity [km/s] of the setup's rotation period."""
+        return 2 * np.pi * self.radius_km / (self.period * 86400.0)
+
+    def maps(self, u1: float, u2: float, vsini: float) -> dict:
+        """The disk maps for limb-darkening coefficients (u1, u2) and vsini, on the device."""
+        period = 2 * np.pi * self.radius_km / (vsini * 86400.0)
+        return self.ctx.disk_maps(self.grid, period, self.omega_ratio, self.incl, self.radius_km, u1, u2,
                                   self.mu_boundary, self.lb)
 
 
 class DeficitSpectra(torch.autograd.Function):
-    """out[p, (flux, bconv, tot), :] = phase_integrate(u, cubes); see the module text."""
+    """out[p, (flux, bconv, tot), :] = phase_integrate(star, cubes), star = (u1, u2, vsini);
+    see the module text."""
 
     @staticmethod
-    def forward(fctx, u, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup: IntegrationSetup):
-        maps = setup.maps(float(u[0]), float(u[1]))
+    def forward(fctx, star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup: IntegrationSetup):
+        vsini = float(star[2])
+        maps = setup.maps(float(star[0]), float(star[1]), vsini)
+        fctx.vsini = vsini
         cubes = dict(zip(CUBE_KEYS, (q_norm.detach(), q_sed.detach(), spot_norm.detach(), fac_norm.detach(),
                                      spot_sed.detach(), fac_sed.detach())))
         flux, bconv, tot = setup.ctx.phase_integrate("plain64", setup.wave, setup.n_eff, setup.grid, setup.temp,
@@ -87,15 +100,18 @@ class DeficitSpectra(torch.autograd.Function):
         gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, setup.temp, setup.bi, maps,
                                                fctx.cubes, setup.step, setup.act, g[:, 0].contiguous(),
                                                g[:, 1].contiguous(), g[:, 2].contiguous())
-        # chain rule to the limb-darkening coefficients over the visible cells
+        # chain rules over the visible cells: limb-darkening coefficients, vsini
         vis = maps["limb"] > -998.0
-        om = torch.where(vis, 1.0 - maps["mu"], torch.zeros_like(maps["mu"]))
+        zero = torch.zeros_like(maps["mu"])
+        om = torch.where(vis, 1.0 - maps["mu"], zero)
         gl = gr["limb"]
-        grad_u = torch.stack((-(gl * om).sum(), -(gl * om * om).sum()))
-        return (grad_u, gr["q_norm"], gr["q_sed"], gr["spot_norm"], gr["fac_norm"], gr["spot_sed"], gr["fac_sed"],
-                None)
+        dv = torch.where(vis, maps["delta"], zero) / fctx.vsini
+        grad_star = torch.stack((-(gl * om).sum(), -(gl * om * om).sum(), (gr["delta"] * dv).sum()))
+        return (grad_star, gr["q_norm"], gr["q_sed"], gr["spot_norm"], gr["fac_norm"], gr["spot_sed"],
+                gr["fac_sed"], None)
 
 
-def deficit_spectra(u, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup: IntegrationSetup):
-    """Differentiable (n_phase, 3, n) deficit spectra; see ``DeficitSpectra``."""
-    return DeficitSpectra.apply(u, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup)
+def deficit_spectra(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup: IntegrationSetup):
+    """Differentiable (n_phase, 3, n) deficit spectra, star = (u1, u2, vsini); see
+    ``DeficitSpectra``."""
+    return DeficitSpectra.apply(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup)
