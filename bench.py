@@ -393,8 +393,7 @@ def adjoint_timing(ctx, dev, reps=3):
 
     f_ms, fb_ms = timed(fwd), timed(fwd_bwd)
     return {"case": "200x200 grid, 100,000 px, 10 mu bins, 3 regions, 5 phases over one rotation, PLAIN64; "
-                    "gradients w.r.t. "
-                    "u1, u2, 4 seed cubes, 2 continuum rows",
+                    "gradients w.r.t. u1, u2, vsini, 4 seed cubes, 2 continuum rows",
             "forward_ms": round(f_ms, 3), "forward_adjoint_ms": round(fb_ms, 3), "ratio": round(fb_ms / f_ms, 2)}
 
 
