@@ -1832,10 +1832,11 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 const T fdj = (T)dj;
                 const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
                 const T e0 = b0 - bb * fdj, e1 = b1 + bb * fdj;
-                part[0][q] += c0 * r0[x] + c1 * r0[x + 1];
-                part[1][q] += c0 * r1[x] + c1 * r1[x + 1];
-                part[2][q] += e0 * r2[x] + e1 * r2[x + 1];
-                part[3][q] += e0 * r3[x] + e1 * r3[x + 1];
+                // two chained FMAs per row (no separate product and sum)
+                part[0][q] = fma(c1, r0[x + 1], fma(c0, r0[x], part[0][q]));
+                part[1][q] = fma(c1, r1[x + 1], fma(c0, r1[x], part[1][q]));
+                part[2][q] = fma(e1, r2[x + 1], fma(e0, r2[x], part[2][q]));
+                part[3][q] = fma(e1, r3[x + 1], fma(e0, r3[x], part[3][q]));
             }
         }
     };
