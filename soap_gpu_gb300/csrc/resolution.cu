@@ -930,8 +930,10 @@ __global__ void __launch_bounds__(256) k_norm32(int n_eff, const float *__restri
     out[(long long)s * out_stride + i] = soap_f32_to_f64(fmaf(-c, fac[s], 1.0f));
 }
 
-// k_norm32 four pixels per thread: 16-byte loads and stores (n_eff % 4 == 0, strides
-// multiples of 4, 16-byte aligned rows)
+// k_norm32 in groups of four pixels: 16-byte loads and stores (n_eff % 4 == 0, strides
+// multiples of 4, 16-byte aligned rows); each thread takes NORM_GROUPS groups a block
+// apart, their loads issued before their stores
+constexpr int NORM_GROUPS = 4;
 __global__ void __launch_bounds__(256) k_norm32v(int n_eff, const float *__restrict__ c32a,
                                                  const float *__restrict__ c32b, int b_every,
                                                  const float *__restrict__ conv, long long conv_stride,
@@ -939,18 +941,36 @@ __global__ void __launch_bounds__(256) k_norm32v(int n_eff, const float *__restr
                                                  long long out_stride, const unsigned char *__restrict__ zero_spec,
                                                  int skip_zero) {
     const int s = blockIdx.y;
-    if (skip_zero && zero_spec && zero_spec[s]) return;   // rows the caller has already
-    const int i = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= n_eff) return;
+    const bool zs = zero_spec && zero_spec[s];
+    if (skip_zero && zs) return;   // rows the caller has already
     const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
-    const float4 cb = *reinterpret_cast<const float4 *>((use_b ? c32b : c32a) + i);
-    // a zero spectrum's convolution is zero (not computed, not stored)
-    const float4 cd = (zero_spec && zero_spec[s]) ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                                  : *reinterpret_cast<const float4 *>(conv + (long long)s * conv_stride + i);
+    const float *cbs = use_b ? c32b : c32a;
+    const float *cr = conv + (long long)s * conv_stride;
     const float f = fac[s];
-    double2 *o = reinterpret_cast<double2 *>(out + (long long)s * out_stride + i);
-    o[0] = make_double2(soap_f32_to_f64(fmaf(-(cb.x + cd.x), f, 1.0f)), soap_f32_to_f64(fmaf(-(cb.y + cd.y), f, 1.0f)));
-    o[1] = make_double2(soap_f32_to_f64(fmaf(-(cb.z + cd.z), f, 1.0f)), soap_f32_to_f64(fmaf(-(cb.w + cd.w), f, 1.0f)));
+    double *orow = out + (long long)s * out_stride;
+    const int i0 = 4 * (blockIdx.x * blockDim.x * NORM_GROUPS + threadIdx.x);
+    float4 cb[NORM_GROUPS], cd[NORM_GROUPS];
+#pragma unroll
+    for (int g = 0; g < NORM_GROUPS; ++g) {
+        const int i = i0 + 4 * g * (int)blockDim.x;
+        cb[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        cd[g] = cb[g];
+        if (i < n_eff) {
+            cb[g] = *reinterpret_cast<const float4 *>(cbs + i);
+            // a zero spectrum's convolution is zero (not computed, not stored)
+            if (!zs) cd[g] = *reinterpret_cast<const float4 *>(cr + i);
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < NORM_GROUPS; ++g) {
+        const int i = i0 + 4 * g * (int)blockDim.x;
+        if (i >= n_eff) continue;
+        double2 *o = reinterpret_cast<double2 *>(orow + i);
+        o[0] = make_double2(soap_f32_to_f64(fmaf(-(cb[g].x + cd[g].x), f, 1.0f)),
+                            soap_f32_to_f64(fmaf(-(cb[g].y + cd[g].y), f, 1.0f)));
+        o[1] = make_double2(soap_f32_to_f64(fmaf(-(cb[g].z + cd[g].z), f, 1.0f)),
+                            soap_f32_to_f64(fmaf(-(cb[g].w + cd[g].w), f, 1.0f)));
+    }
 }
 
 namespace soapgb {
@@ -1229,7 +1249,7 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     k_factor<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, mm, fac, d_minmax ? d_minmax + 2LL * s0 : nullptr);
     SOAP_LAUNCHED(ctx);
     if (n_eff % 4 == 0 && out_stride % 2 == 0 && ((uintptr_t)out & 15) == 0) {
-        dim3 g3(grid_for(ctx, n_eff / 4, 256), ns);
+        dim3 g3((unsigned)((n_eff / 4 + 256 * NORM_GROUPS - 1) / (256 * NORM_GROUPS)), ns);
         SOAP_TRACED(ctx, "norm32", k_norm32v<<<g3, 256, 0, ctx->stream>>>(n_eff, R.c32a, R.c32b, R.b_every, conv,
                                                                            n_eff, fac, out, out_stride, zs,
                                                                            skip_zero ? 1 : 0));
