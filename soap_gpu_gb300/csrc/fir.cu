@@ -27,6 +27,7 @@
 // buffered so that the next unit's rows arrive while the current one is applied.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "fir.cuh"
 #include "regions.cuh"
@@ -1808,21 +1809,19 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         const T *__restrict__ r1 = sr.p[1] + sr.off;
         const T *__restrict__ r2 = sr.p[2] + sr.off;
         const T *__restrict__ r3 = sr.p[3] + sr.off;
-        for (int t = t_lo; t < t_hi; ++t) {
-            const FirGrp<T> gr = grp[t];
-            if (!gr.ok) continue;
+        // one group at the thread's pixels; CHECKED: some pixels of the tile fall outside
+        // [jlo, jhi] (tile edges, the grid's end), else none and no test is needed
+        auto group_at = [&](auto checked_c, auto zv_c, const FirGrp<T> &gr, int jlo, int jhi, T b0, T b1, T bb) {
+            constexpr bool CHECKED = decltype(checked_c)::value;
+            constexpr bool ZV = decltype(zv_c)::value;
             const int m = gr.m;
-            const int jlo = max(j0, -m);
-            const int jhi = zv ? j0 + t_eff - 1 : min(j0 + t_eff - 1, n_eff - 2 - m);
-            // facula slots 2, 3 carry the (1 + LB) L weights, spot slots 2, 3 the L weights
-            const T b0 = fac ? gr.a0w : gr.a0, b1 = fac ? gr.a1w : gr.a1, bb = fac ? gr.bw : gr.b;
 #pragma unroll
             for (int q = 0; q < FIR_PIX; ++q) {
                 const int dj = tid + q * FIR_THREADS;
                 const int j = j0 + dj;
-                if (j < jlo || j > jhi) continue;
+                if (CHECKED && (j < jlo || j > jhi)) continue;
                 const int x = j + m;
-                if (zv) {   // single tap: w == 0
+                if (ZV) {   // single tap: w == 0
                     part[0][q] += gr.a0 * r0[x];
                     part[1][q] += gr.a0 * r1[x];
                     part[2][q] += b0 * r2[x];
@@ -1837,6 +1836,25 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 part[1][q] = fma(c1, r1[x + 1], fma(c0, r1[x], part[1][q]));
                 part[2][q] = fma(e1, r2[x + 1], fma(e0, r2[x], part[2][q]));
                 part[3][q] = fma(e1, r3[x + 1], fma(e0, r3[x], part[3][q]));
+            }
+        };
+        using yes = std::integral_constant<bool, true>;
+        using no = std::integral_constant<bool, false>;
+        for (int t = t_lo; t < t_hi; ++t) {
+            const FirGrp<T> gr = grp[t];
+            if (!gr.ok) continue;
+            const int m = gr.m;
+            const int jlo = max(j0, -m);
+            const int jhi = zv ? j0 + t_eff - 1 : min(j0 + t_eff - 1, n_eff - 2 - m);
+            // facula slots 2, 3 carry the (1 + LB) L weights, spot slots 2, 3 the L weights
+            const T b0 = fac ? gr.a0w : gr.a0, b1 = fac ? gr.a1w : gr.a1, bb = fac ? gr.bw : gr.b;
+            const bool inside = (jlo <= j0) && (jhi >= j0 + FIR_TILE - 1);   // uniform for the block
+            if (zv) {
+                if (inside) group_at(no(), yes(), gr, jlo, jhi, b0, b1, bb);
+                else group_at(yes(), yes(), gr, jlo, jhi, b0, b1, bb);
+            } else {
+                if (inside) group_at(no(), no(), gr, jlo, jhi, b0, b1, bb);
+                else group_at(yes(), no(), gr, jlo, jhi, b0, b1, bb);
             }
         }
     };
