@@ -1863,20 +1863,21 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     auto apply_exc = [&](const Src &sr, const FirUnit &d, const FirExcW<T> *exc, int ne, int j0) {
         const int cls = d.cls;
         const bool fac = (cls != CLS_SPOT);
-        for (int e = 0; e < ne; ++e) {
-            const FirExcW<T> xc = exc[e];
-            const T w23 = fac ? xc.w2 : xc.L;
+        // one wrap cell at the thread's pixels; CHECKED: a pixel may lie past n_eff or
+        // read a source outside [0, n_eff - 2] or outside the staged window; else none can
+        auto cell_at = [&](auto checked_c, const FirExcW<T> &xc, T w23) {
+            constexpr bool CHECKED = decltype(checked_c)::value;
 #pragma unroll
             for (int q = 0; q < FIR_PIX; ++q) {
                 const int dj = tid + q * FIR_THREADS;
                 const int j = j0 + dj;
-                if (j >= n_eff) continue;
+                if (CHECKED && j >= n_eff) continue;
                 T wd = xc.phi + xc.dlt * (T)dj;
                 int i = xc.i0 + dj;
                 if (wd >= (T)1) { wd -= (T)1; i += 1; }
                 else if (wd < (T)0) { wd += (T)1; i -= 1; }
-                if (i < 0 || i > n_eff - 2) continue;
-                const bool inwin = !sr.staged || ((i >= d.w0) && (i + 1 < d.w1));
+                if (CHECKED && (i < 0 || i > n_eff - 2)) continue;
+                const bool inwin = !CHECKED || !sr.staged || ((i >= d.w0) && (i + 1 < d.w1));
                 auto lv = [&](int c) -> T {
                     T s0, s1;
                     if (inwin) {
@@ -1895,6 +1896,17 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 part[2][q] += w23 * lv(2);
                 part[3][q] += w23 * lv(3);
             }
+        };
+        // the sources of a cell span [i0 - 1, i0 + FIR_TILE] over the tile
+        const bool full = (j0 + FIR_TILE <= n_eff);
+        for (int e = 0; e < ne; ++e) {
+            const FirExcW<T> xc = exc[e];
+            const T w23 = fac ? xc.w2 : xc.L;
+            const int ilo = xc.i0 - 1, ihi = xc.i0 + FIR_TILE;
+            const bool inside = full && ilo >= 0 && ihi <= n_eff - 2 &&
+                                (!sr.staged || (ilo >= d.w0 && ihi + 1 < d.w1));   // uniform for the block
+            if (inside) cell_at(std::integral_constant<bool, false>(), xc, w23);
+            else cell_at(std::integral_constant<bool, true>(), xc, w23);
         }
     };
     // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
