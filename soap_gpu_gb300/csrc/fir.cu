@@ -1001,16 +1001,28 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int *wsum, int &total)
 // order-preserving integer images of the doubles (no FP64 instruction per step).  A cell
 // within rounding of a boundary may be classified one group away from floor(t); its
 // weight is then within rounding of 0 or 1 and its contribution unchanged.
-__device__ __forceinline__ int fir_lower_bound(const double *__restrict__ dl, int lo, int hi, double invX, int m) {
-    const unsigned long long th = soap_ord64((double)m * invX);
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (soap_ord64(dl[mid]) >= th)
-            hi = mid;
-        else
-            lo = mid + 1;
+// Four lower-bound searches over the same range [lo, hi) of a list's slopes (sorted):
+// out[q] = the first position whose slope's ord64 image is >= th[q] (th[q] = the image
+// of m / X for a boundary shift m and a pixel position X).  In lock-step, so the four
+// loads of a step are in flight together; each search halves its own interval.
+__device__ __forceinline__ void fir_lower_bound4(const double *__restrict__ dl, int lo, int hi,
+                                                 const unsigned long long (&th)[4], int (&out)[4]) {
+    int l[4] = {lo, lo, lo, lo}, h[4] = {hi, hi, hi, hi};
+    while (l[0] < h[0] || l[1] < h[1] || l[2] < h[2] || l[3] < h[3]) {
+        unsigned long long v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = (l[q] < h[q]) ? soap_ord64(dl[(l[q] + h[q]) >> 1]) : 0ULL;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (l[q] < h[q]) {
+                const int mid = (l[q] + h[q]) >> 1;
+                if (v[q] >= th[q]) h[q] = mid;
+                else l[q] = mid + 1;
+            }
+        }
     }
-    return lo;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[q] = l[q];
 }
 
 struct FirTileArgs {
@@ -1164,19 +1176,14 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
         }
         const FirUnit d = st.unit[ui];
         const int m = d.ma + (k - st.ut[ui]);
-        int lowA, lowB, highA, highB;
-        if (m == d.m_lo) {
-            lowA = lowB = d.start;
-        } else {
-            lowA = fir_lower_bound(sl, d.start, d.end, iXa, m);
-            lowB = fir_lower_bound(sl, d.start, d.end, iXb, m);
-        }
-        if (m == d.m_hi) {
-            highA = highB = d.end;
-        } else {
-            highA = fir_lower_bound(sl, d.start, d.end, iXa, m + 1);
-            highB = fir_lower_bound(sl, d.start, d.end, iXb, m + 1);
-        }
+        // the four boundaries in lock-step (those at the unit's first and last shift are
+        // the range's ends)
+        const unsigned long long th[4] = {soap_ord64((double)m * iXa), soap_ord64((double)m * iXb),
+                                          soap_ord64((double)(m + 1) * iXa), soap_ord64((double)(m + 1) * iXb)};
+        int bnd[4];
+        fir_lower_bound4(sl, d.start, d.end, th, bnd);
+        const int lowA = (m == d.m_lo) ? d.start : bnd[0], lowB = (m == d.m_lo) ? d.start : bnd[1];
+        const int highA = (m == d.m_hi) ? d.end : bnd[2], highB = (m == d.m_hi) ? d.end : bnd[3];
         const int rlo = max(lowA, lowB), rhi = min(highA, highB);
         FirGrp<T> gr;
         gr.m = m;
