@@ -463,7 +463,7 @@ __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, in
 // conv(spec) (over [0, n_eff), C != 0) and the magnitudes that bound their rounding
 // (blk, order-preserving atomics into mm32).  xs + xi(i) is the staged spectrum value
 // of pixel i.  Ends with a block barrier.
-template <int SB>
+template <int SB, bool FULL = false>   // FULL: the tile lies below n_eff (no pixel test needed)
 __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff, int i0, int ib, int n, int n_eff,
                                               int s0, int nsb, const bool (&lv)[FC_PIX],
                                               const float (&acc)[SB][FC_PIX], const float *__restrict__ b32a,
@@ -511,13 +511,13 @@ __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) {
                 const int i = ib + p;
-                if (i < n) {
+                if (FULL || i < n) {
                     const float b = use_b ? bb[p] : ba[p], x = xs[q * win + (i - i0) + xoff];
                     mn = fminf(mn, b - x);
                     ma = fmaxf(ma, fabsf(b) + fabsf(x));
                 }
                 cdv[p] = 0.f;
-                if (i < n_eff) {
+                if (FULL || i < n_eff) {
                     const float cd = lv[p] ? acc[q][p] : 0.f;
                     cdv[p] = cd;
                     const float cb = use_b ? kb[p] : ka[p];
@@ -764,8 +764,12 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         const bool zero_batch = (zmask == (1u << nsb) - 1u);
         if (R > 0 && !zero_batch)
             conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
-        conv32_finish<SB>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every,
-                          conv, conv_stride, mm32, blk, nbx, x, red);
+        if (i0 + FC_TILE <= n_eff)   // uniform for the block
+            conv32_finish<SB, true>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b,
+                                    b_every, conv, conv_stride, mm32, blk, nbx, x, red);
+        else
+            conv32_finish<SB, false>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b,
+                                     b_every, conv, conv_stride, mm32, blk, nbx, x, red);
     }
     if (k_fail >= 0 && threadIdx.x == 0) {
         // a staged copy did not land in time: record it and give the next item's copy,
