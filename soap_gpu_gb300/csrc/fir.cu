@@ -478,10 +478,14 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
                  int t_star, int t_diff_spot, int t_diff_fac, int solar, int cap, const CellGeo *__restrict__ geo,
                  int *list_cell, double *list_dlt, double2 *list_aux, int *counts, int *status) {
     extern __shared__ __align__(16) unsigned char sl_smem[];
-    // the sort record of an active cell in two words, compared as one 128-bit key:
-    // k1 = (class << 16 | bin key) << 32 | ord64(dlt) >> 32, k2 = ord64(dlt) << 32 | cell
+    // the record of an active cell in two words, compared as one 128-bit key:
+    // k1 = (class << 16 | bin key) << 32 | ord64(dlt) >> 32, k2 = ord64(dlt) << 32 | cell;
+    // sorted through one 64-bit word per record, sk = class and bin (12 bits) | the slope
+    // image's top 32 bits | the record's index (20 bits), then each run of equal
+    // (class, bin, top slope bits) is put in k2 order
     unsigned long long *k1 = reinterpret_cast<unsigned long long *>(sl_smem);   // [cap]
     unsigned long long *k2 = k1 + cap;                                         // [cap]
+    unsigned long long *sk = k2 + cap;                                         // [cap]
     __shared__ int cnt, ccnt[3];
     const long long gm = (long long)grid * grid;
     const int l = blockIdx.x, tid = threadIdx.x;
@@ -513,9 +517,12 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
             const int pos = atomicAdd(&cnt, 1);
             if (pos < cap) {
                 const unsigned long long od = soap_ord64(g.dlt);
-                const unsigned ka = ((unsigned)c << 16) | (unsigned)(g.row * 2 + g.zero_v);
+                const unsigned bin = (unsigned)(g.row * 2 + g.zero_v);
+                const unsigned ka = ((unsigned)c << 16) | bin;
                 k1[pos] = ((unsigned long long)ka << 32) | (od >> 32);
                 k2[pos] = (od << 32) | (unsigned)k;
+                sk[pos] = ((unsigned long long)(((unsigned)c << 9) | bin) << 52) | ((od >> 32) << 20) |
+                          (unsigned long long)pos;
             }
         }
     }
@@ -528,10 +535,7 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
     }
     int np = 1, lnp = 0;
     while (np < n) np <<= 1, ++lnp;
-    for (int i = n + tid; i < np; i += FIR_SLIST_THREADS) {   // padding sorts last
-        k1[i] = ~0ULL;
-        k2[i] = ~0ULL;
-    }
+    for (int i = n + tid; i < np; i += FIR_SLIST_THREADS) sk[i] = ~0ULL;   // padding sorts last
     __syncthreads();
     // bitonic network over the np / 2 compare-exchange pairs of each stage: pair m of
     // stage (k, j) joins i (m with a zero bit inserted at bit log2 j) and i + j
@@ -542,23 +546,41 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
             for (int m = tid; m < half; m += FIR_SLIST_THREADS) {
                 const int i = ((m >> lj) << (lj + 1)) | (m & (j - 1));
                 const int p = i + j;
-                const unsigned long long a1 = k1[i], b1 = k1[p], a2 = k2[i], b2 = k2[p];
-                const bool gt = (a1 != b1) ? (a1 > b1) : (a2 > b2);
-                if (gt == (((i >> lk) & 1) == 0)) {
-                    k1[i] = b1;
-                    k1[p] = a1;
-                    k2[i] = b2;
-                    k2[p] = a2;
+                const unsigned long long a = sk[i], b = sk[p];
+                if ((a > b) == (((i >> lk) & 1) == 0)) {
+                    sk[i] = b;
+                    sk[p] = a;
                 }
             }
             __syncthreads();
         }
     }
+    // runs of equal (class, bin, top slope bits): order by k2 (the slope's low bits, then
+    // the cell); a run is sorted by the thread at its start (runs are short: mostly the
+    // cells mirrored across the equator, whose slopes are equal)
     for (int i = tid; i < n; i += FIR_SLIST_THREADS) {
-        const int cell = (int)(unsigned)k2[i];
+        const unsigned long long key = sk[i] >> 20;
+        if (i > 0 && (sk[i - 1] >> 20) == key) continue;
+        int e = i + 1;
+        while (e < n && (sk[e] >> 20) == key) ++e;
+        for (int a = i + 1; a < e; ++a) {   // insertion sort of [i, e) by k2
+            const unsigned long long v = sk[a];
+            const unsigned long long kv = k2[v & 0xfffffULL];
+            int b = a - 1;
+            while (b >= i && k2[sk[b] & 0xfffffULL] > kv) {
+                sk[b + 1] = sk[b];
+                --b;
+            }
+            sk[b + 1] = v;
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += FIR_SLIST_THREADS) {
+        const int rec = (int)(sk[i] & 0xfffffULL);
+        const int cell = (int)(unsigned)k2[rec];
         list_cell[mbase + i] = cell;
         list_dlt[mbase + i] = geo[cell].dlt;
-        if ((int)(k1[i] >> 48) == CLS_DIRECT) {
+        if ((int)(k1[rec] >> 48) == CLS_DIRECT) {
             double t, b;
             region_cell_value(table, r0, r1, cell / grid, cell % grid, delta_grid, t_star, t_diff_spot, t_diff_fac, t,
                               b);
@@ -2262,7 +2284,7 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
         double2 *laux = (double2 *)(ws + L.off[FirLayout::LAUX]);
         int *counts = (int *)(ws + L.off[FirLayout::COUNTS]);
         const int cap = boxes->box_cap;
-        const size_t smem = (size_t)cap * 2 * sizeof(unsigned long long);
+        const size_t smem = (size_t)cap * 3 * sizeof(unsigned long long);
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_slists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const soapgb_activity *act = boxes->act;
         SOAP_TRACED(ctx, "fir_lists",
