@@ -244,6 +244,129 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv_fast(int n, int n_eff, cons
     }
 }
 
+// --- the base convolution in double-float arithmetic on the FP32 pipe -------------------
+// A value is the unevaluated sum hi + lo of two floats (about 48 significant bits).
+// Products and sums use the error-free transforms of the published double-float
+// arithmetic: TwoProduct through FMA (the rounding error of a * b is fma(a, b, -a*b))
+// and Knuth's TwoSum, each followed by a renormalisation.
+struct DFloat {
+    float hi, lo;
+};
+__device__ __forceinline__ DFloat df_of(double v) {
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ DFloat df_renorm(float s, float e) {
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_renorm(p, e);
+}
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+    const float s = a.hi + b.hi;
+    const float bv = s - a.hi;
+    float e = (a.hi - (s - bv)) + (b.hi - bv);
+    e += a.lo + b.lo;
+    return df_renorm(s, e);
+}
+
+// k_conv_fast's FP64 form (Gaussian weights by the exact-product recurrence, the same
+// per-pixel ranges, conv(1 - base)) in double-float: the base convolution of the FP32
+// form without FP64 arithmetic in the tap loop (the FP64 pipe is 1/64 of the FP32 one,
+// and the kernel runs beside the FP64 geometry stages).  Results agree with the FP64
+// form to about 1e-13 relative.  grid (tiles of 1024 px, bases / SB).
+template <int SB>
+__global__ void __launch_bounds__(FC_THREADS) k_conv_base_df(int n, int n_eff, const double *__restrict__ kqa,
+                                                             const double *__restrict__ cqa,
+                                                             const int2 *__restrict__ rnga,
+                                                             const double *__restrict__ spec, long long spec_stride,
+                                                             int n_spec, int halo, double *__restrict__ conv,
+                                                             long long conv_stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *xs = reinterpret_cast<float2 *>(smem_raw);   // staged 1 - base as (hi, lo)
+    const int win = FC_TILE + 2 * halo;
+    const int i0 = blockIdx.x * FC_TILE;
+    const int s0 = blockIdx.y * SB;
+    const int nsb = min(SB, n_spec - s0);
+    for (int q = 0; q < nsb; ++q) {
+        const double *sp = spec + (long long)(s0 + q) * spec_stride;
+        for (int t = threadIdx.x; t < win; t += FC_THREADS) {
+            const int m = i0 - halo + t;
+            const DFloat d = df_of((m >= 0 && m < n) ? 1.0 - sp[m] : 0.0);
+            xs[q * win + t] = make_float2(d.hi, d.lo);
+        }
+    }
+    __syncthreads();
+    const int ib = i0 + threadIdx.x * FC_PIX;
+    DFloat acc[SB][FC_PIX];
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) acc[q][p] = {0.f, 0.f};
+    DFloat wcur[FC_PIX], rcur[FC_PIX], e2[FC_PIX];
+    int dlo[FC_PIX], dhi[FC_PIX];
+    int elo = 1 << 30, ehi = -(1 << 30);
+#pragma unroll
+    for (int p = 0; p < FC_PIX; ++p) {
+        const int i = ib + p;
+        dlo[p] = 0;
+        dhi[p] = -1;
+        wcur[p] = rcur[p] = e2[p] = {0.f, 0.f};
+        if (i < n_eff) {
+            const int2 r = rnga[i];
+            dlo[p] = r.x;
+            dhi[p] = r.y;
+            if (r.x <= r.y) {
+                elo = min(elo, i + r.x);
+                ehi = max(ehi, i + r.y);
+                const double c = cqa[i], d0 = (double)r.x;
+                wcur[p] = df_of(kqa[i] * exp(-d0 * d0 * c));
+                rcur[p] = df_of(exp(-(2.0 * d0 + 1.0) * c));
+                e2[p] = df_of(exp(-2.0 * c));
+            }
+        }
+    }
+    for (int e = elo; e <= ehi; ++e) {
+        DFloat w[FC_PIX];
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            const int d = e - (ib + p);
+            if (d >= dlo[p] && d <= dhi[p]) {
+                w[p] = wcur[p];
+                wcur[p] = df_mul(wcur[p], rcur[p]);
+                rcur[p] = df_mul(rcur[p], e2[p]);
+            } else {
+                w[p] = {0.f, 0.f};
+            }
+        }
+        const int li = e - (i0 - halo);
+#pragma unroll
+        for (int q = 0; q < SB; ++q) {
+            if (q < nsb) {
+                const float2 xv = xs[q * win + li];
+                const DFloat x = {xv.x, xv.y};
+#pragma unroll
+                for (int p = 0; p < FC_PIX; ++p) acc[q][p] = df_add(acc[q][p], df_mul(w[p], x));
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < SB; ++q) {
+        if (q >= nsb) continue;
+        double *cp = conv + (long long)(s0 + q) * conv_stride;
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) {
+            const int i = ib + p;
+            if (i < n_eff) cp[i] = (dlo[p] <= dhi[p]) ? (double)acc[q][p].hi + (double)acc[q][p].lo : 0.0;
+        }
+    }
+}
+
 // C_s += Cbase (FP64) where the reference has a C value; fused with min/max.
 // grid (blocks, spectra).  A_s = base - spec over [0, n); C over [0, n_eff).
 __global__ void __launch_bounds__(256) k_minmax(int n, int n_eff, const double *__restrict__ spec,
@@ -1034,6 +1157,38 @@ static int launch_conv_fast(soapgb_ctx *ctx, int n, int n_eff, const double *lam
     return SOAPGB_OK;
 }
 
+// The base convolution of the FP32 form: FP64 tap constants (k_conv_params), then
+// k_conv_base_df.  Same constants and ranges as launch_conv_fast<double>.
+template <int SB>
+static int launch_conv_base_df(soapgb_ctx *ctx, int n, int n_eff, const double *lam, const double *spec,
+                               long long spec_stride, int n_spec, double sigma_v, int wid, double step_mult,
+                               double step_exp, double cut, double *conv, long long conv_stride, double sig_max,
+                               char *param_scratch) {
+    const double cmin = step_exp * step_exp / (2.0 * sig_max * sig_max);
+    const int r = (int)floor(sqrt(cut / cmin)) + 2;
+    int halo = std::min(wid, r);
+    if (halo < 1) halo = 1;
+    const size_t smem = sizeof(float2) * (size_t)SB * (FC_TILE + 2 * halo);
+    if (smem > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
+    if (smem > 48 * 1024)
+        SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv_base_df<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    double *kq = (double *)param_scratch;
+    double *cq = (double *)(param_scratch + ((sizeof(double) * (size_t)n_eff + 255) & ~size_t(255)));
+    int2 *rng = (int2 *)(param_scratch + 2 * ((sizeof(double) * (size_t)n_eff + 255) & ~size_t(255)));
+    const double s1 = soap_sigma_per_lambda(sigma_v);
+    const double ka = step_mult / (s1 * sqrt(2. * SOAP_PI)), kb = step_exp * step_exp / (2.0 * s1 * s1);
+    const double kr = sqrt(cut / kb);
+    SOAP_TRACED(ctx, "conv_params",
+                k_conv_params<double><<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, lam, ka, kb, kr,
+                                                                                         wid, halo, kq, cq, rng));
+    SOAP_LAUNCHED(ctx);
+    const dim3 g((n_eff + FC_TILE - 1) / FC_TILE, (n_spec + SB - 1) / SB);
+    SOAP_TRACED(ctx, "conv_base", k_conv_base_df<SB><<<g, FC_THREADS, smem, ctx->stream>>>(
+                                      n, n_eff, kq, cq, rng, spec, spec_stride, n_spec, halo, conv, conv_stride));
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+
 // FP32 tap constants (from the FP64 ones of the base convolution when given) and the
 // reach of every block of 1024 pixels; returns the staging halo
 static int conv32_params(soapgb_ctx *ctx, int n, int n_eff, const double *lam, double sigma_v, int wid,
@@ -1156,15 +1311,15 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
         double *cb = (double *)carve(p, sizeof(double) * 2 * (size_t)n_eff);
         SOAP_CUDA(ctx, cudaMemcpyAsync(bb, base_a, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
         SOAP_CUDA(ctx, cudaMemcpyAsync(bb + n, base_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-        rc = launch_conv_fast<double, 2>(ctx, n, n_eff, d_wave, bb, n, 2, 1, sigma_v, wid, step_mult, step_exp, 40.0,
-                                         cb, n_eff, sig_max, pscr);
+        rc = launch_conv_base_df<2>(ctx, n, n_eff, d_wave, bb, n, 2, sigma_v, wid, step_mult, step_exp, 40.0, cb,
+                                    n_eff, sig_max, pscr);
         if (rc) return rc;
         cb_a = cb;
         cb_b = cb + n_eff;
     } else {
         cb_a = (double *)carve(p, sizeof(double) * (size_t)n_eff);
-        rc = launch_conv_fast<double, 1>(ctx, n, n_eff, d_wave, base_a, 0, 1, 1, sigma_v, wid, step_mult, step_exp,
-                                         40.0, cb_a, 0, sig_max, pscr);
+        rc = launch_conv_base_df<1>(ctx, n, n_eff, d_wave, base_a, 0, 1, sigma_v, wid, step_mult, step_exp, 40.0,
+                                    cb_a, 0, sig_max, pscr);
         if (rc) return rc;
     }
     R.cb_a = cb_a;
