@@ -6,8 +6,8 @@
 // SOAP_resolution.cu:398-412).  Here the deficits stay in device memory and all
 // phases go through each stage in one launch.
 #include <algorithm>
-#include <memory>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "internal.cuh"
@@ -96,9 +96,14 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_bi = ws.add(box_lists ? 0 : sizeof(double) * gm * n_phase);
     int s_cells = ws.add(collapsed ? 0 : sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
-    int s_pm = ws.add(phase_maps_scratch_bytes(n_rows, n_phase));
-    int s_lists = ws.add(box_lists ? sizeof(int) * n_phase : 0);
-    int s_zspec = ws.add(box_lists ? (size_t)n_spec : 0);
+    // the region table and, after it, the small per-call lists (run / zero phases, zero
+    // spectra, the convolution's batch list): one upload
+    const size_t pm_bytes = phase_maps_scratch_bytes(n_rows, n_phase);
+    auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t off_lists = al256(pm_bytes), off_zspec = off_lists + al256(sizeof(int) * n_phase);
+    const size_t off_blist = off_zspec + al256((size_t)n_spec);
+    const size_t small_bytes = off_blist + al256(sizeof(int) * ((size_t)n_spec / 8 + 2));
+    int s_pm = ws.add(small_bytes);
     int s_ztmpl = ws.add(host && box_lists && form == SOAPGB_FAST32 ? sizeof(double) * 3 * (size_t)n_eff : 0);
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
     int s_fir = ws.add(fp.bytes);
@@ -176,10 +181,13 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     std::vector<int> h_lists;   // run list, then zero list
     long long max_box = 0;      // most box cells of a phase
     int n_run = 0;
+    std::vector<char> pack;   // image of the small-upload region
+    int *d_lists = nullptr, *d_blist = nullptr;
+    unsigned char *d_zspec = nullptr;
+    int n_blist = -1;          // batches of the convolution's single chunk, when computed here
     if (box_lists) {
         rc = phase_table_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act,
-                                ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase), &d_table, &d_roff,
-                                &vis, &max_box);
+                                ws.get<char>(s_pm), pm_bytes, &d_table, &d_roff, &vis, &max_box, &pack);
         if (rc) return rc;
         for (int p = 0; p < n_phase; ++p)
             if (vis[p]) h_lists.push_back(p);
@@ -189,14 +197,34 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         // spectra of the phases without a visible region are zero
         zspec.assign((size_t)n_spec, 0);
         for (int p = 0; p < n_phase; ++p) zspec[3 * p] = zspec[3 * p + 1] = zspec[3 * p + 2] = vis[p] ? 0 : 1;
-        // pageable sources: staged by the driver before the calls return
-        SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<int>(s_lists), h_lists.data(), sizeof(int) * n_phase,
-                                       cudaMemcpyHostToDevice, ctx->stream));
-        SOAP_CUDA(ctx, cudaMemcpyAsync(ws.get<unsigned char>(s_zspec), zspec.data(), (size_t)n_spec,
-                                       cudaMemcpyHostToDevice, ctx->stream));
+        // the lists after the table, then one upload (a pageable source: staged by the
+        // driver before the call returns)
+        char *pm = ws.get<char>(s_pm);
+        d_lists = (int *)(pm + off_lists);
+        d_zspec = (unsigned char *)(pm + off_zspec);
+        d_blist = (int *)(pm + off_blist);
+        size_t used = off_zspec + (size_t)n_spec;
+        std::vector<int> bl;
+        if (!(host && collapsed) && form == SOAPGB_FAST32) {
+            // device buffers: one chunk of all the spectra; the batches of 8 that hold a
+            // non-zero spectrum (the others are left out of the convolution)
+            for (long long b = 0; b * 8 < n_spec; ++b) {
+                bool all0 = true;
+                for (long long q = b * 8; q < std::min<long long>(n_spec, b * 8 + 8) && all0; ++q)
+                    all0 = zspec[q] != 0;
+                if (!all0) bl.push_back((int)b);
+            }
+            n_blist = (int)bl.size();
+            used = off_blist + sizeof(int) * bl.size();
+        }
+        pack.resize(used, 0);
+        memcpy(pack.data() + off_lists, h_lists.data(), sizeof(int) * n_phase);
+        memcpy(pack.data() + off_zspec, zspec.data(), (size_t)n_spec);
+        if (!bl.empty()) memcpy(pack.data() + off_blist, bl.data(), sizeof(int) * bl.size());
+        SOAP_CUDA(ctx, cudaMemcpyAsync(pm, pack.data(), pack.size(), cudaMemcpyHostToDevice, ctx->stream));
     } else
         rc = phase_maps_device(ctx, grid, star->incl, n_phase, h_ph.data(), h_off.data(), h_reg.data(), act, d_temp,
-                               d_bi, ws.get<char>(s_pm), phase_maps_scratch_bytes(n_rows, n_phase));
+                               d_bi, ws.get<char>(s_pm), pm_bytes);
     if (rc) return rc;
     // the cubes last, after every small upload (table, lists, flags) of the call
     {
@@ -223,7 +251,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         fa.grid = grid;
         fa.box_cap = box_lists ? fir_sorted_box_capacity(max_box) : 0;
         if (box_lists) {
-            fa.run_list = ws.get<int>(s_lists);
+            fa.run_list = d_lists;
             fa.zero_list = fa.run_list + n_run;
             fa.run_host = h_lists.data();
             fa.zero_host = h_lists.data() + n_run;
@@ -349,9 +377,9 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
                     joined = true;
                 }
                 rc = resolution32_run(ctx, R, (const float *)d_raw, n, 3 * p0, 3 * p1, d_lower, n_eff, nullptr,
-                                      box_lists ? ws.get<unsigned char>(s_zspec) : nullptr,
-                                      box_lists ? zspec.data() : nullptr,
-                                      early_zero ? ZeroRows::SKIP : ZeroRows::NORM);
+                                      box_lists ? d_zspec : nullptr, box_lists ? zspec.data() : nullptr,
+                                      early_zero ? ZeroRows::SKIP : ZeroRows::NORM,
+                                      (n_blist >= 0 && p0 == 0 && p1 == n_phase) ? d_blist : nullptr, n_blist);
                 if (rc) return rc;
                 if (host) {
                     cudaEvent_t ev = ctx->sync_events[3 + c];

@@ -134,7 +134,8 @@ namespace soapgb {
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
                        size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
-                       std::vector<unsigned char> *phase_visible, long long *max_box_cells) {
+                       std::vector<unsigned char> *phase_visible, long long *max_box_cells,
+                       std::vector<char> *pack) {
     std::vector<RegionPhase> table;
     int rc = build_region_table(ctx, grid, incl, n_phase, h_phases, h_reg_off, h_regions, act->nrho, table);
     if (rc) return rc;
@@ -162,9 +163,15 @@ int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, cons
         return set_error(ctx, SOAPGB_ERR_ARG, "phase maps scratch too small");
     RegionPhase *dt = (RegionPhase *)scratch;
     int *dof = (int *)(scratch + ((tb + 255) & ~size_t(255)));
-    SOAP_CUDA(ctx, cudaMemcpyAsync(dt, table.data(), tb, cudaMemcpyHostToDevice, ctx->stream));
-    SOAP_CUDA(ctx, cudaMemcpyAsync(dof, h_reg_off, ob, cudaMemcpyHostToDevice, ctx->stream));
-    // `table` lives in pageable memory: cudaMemcpyAsync has staged it before returning
+    if (pack) {   // the caller copies the scratch image in one go
+        pack->assign(((tb + 255) & ~size_t(255)) + ob, 0);
+        memcpy(pack->data(), table.data(), tb);
+        memcpy(pack->data() + ((tb + 255) & ~size_t(255)), h_reg_off, ob);
+    } else {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(dt, table.data(), tb, cudaMemcpyHostToDevice, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(dof, h_reg_off, ob, cudaMemcpyHostToDevice, ctx->stream));
+        // `table` lives in pageable memory: cudaMemcpyAsync has staged it before returning
+    }
     *d_table = dt;
     *d_off = dof;
     return SOAPGB_OK;

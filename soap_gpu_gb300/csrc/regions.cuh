@@ -92,10 +92,13 @@ namespace soapgb {
 // *d_table (reg_off[n_phase] rows) and *d_off (n_phase + 1 offsets); phase_visible
 // (optional) gets 1 for the phases with at least one visible region, else 0;
 // max_box_cells (optional) the largest sum over a phase's visible regions of their
-// bounding-box cells (a bound on the phase's active cells).
+// bounding-box cells (a bound on the phase's active cells).  With `pack` the copies are
+// not issued: *pack receives the image of the scratch bytes, for the caller to copy
+// (with its own small uploads) in one go.
 int phase_table_device(soapgb_ctx *ctx, int grid, double incl, int n_phase, const double *h_phases,
                        const int *h_reg_off, const double *h_regions, const soapgb_activity *act, char *scratch,
                        size_t scratch_bytes, const RegionPhase **d_table, const int **d_off,
-                       std::vector<unsigned char> *phase_visible = nullptr, long long *max_box_cells = nullptr);
+                       std::vector<unsigned char> *phase_visible = nullptr, long long *max_box_cells = nullptr,
+                       std::vector<char> *pack = nullptr);
 size_t phase_maps_scratch_bytes(int n_rows, int n_phase);
 }  // namespace soapgb

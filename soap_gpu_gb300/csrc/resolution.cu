@@ -1361,7 +1361,7 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
 
 int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long long spec_stride, int s0, int s1,
                      double *d_out, long long out_stride, double *d_minmax, const unsigned char *zero_spec,
-                     const unsigned char *zero_host, ZeroRows zero_rows) {
+                     const unsigned char *zero_host, ZeroRows zero_rows, const int *blist_pre, int nlist_pre) {
     const int ns = s1 - s0;
     if (ns <= 0) return SOAPGB_OK;
     if (R.b_every > 0 && s0 % R.b_every != 0)
@@ -1380,7 +1380,12 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     const unsigned char *zs = (zero_spec && zero_host) ? zero_spec + s0 : nullptr;
     const int *blist = nullptr;
     int nlist = 0;
-    if (zs) {
+    if (zs && blist_pre) {   // the caller uploaded the batch list with its own small inputs
+        blist = blist_pre;
+        nlist = nlist_pre;
+        k_zero_mm<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, zs, R.b_every, R.mmz, mm);
+        SOAP_LAUNCHED(ctx);
+    } else if (zs) {
         std::vector<int> bl;
         for (int b = 0; b * 8 < ns; ++b) {
             bool all0 = true;

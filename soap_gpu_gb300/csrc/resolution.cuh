@@ -47,5 +47,7 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
                      double *d_out, long long out_stride, double *d_minmax,
                      const unsigned char *zero_spec = nullptr,    // [n_spec] device: 1 = spectrum known to be zero
                      const unsigned char *zero_host = nullptr,    // the same flags on the host (both or neither)
-                     ZeroRows zero_rows = ZeroRows::NORM);
+                     ZeroRows zero_rows = ZeroRows::NORM,
+                     const int *blist_pre = nullptr,   // device batch list of [s0, s1) made by the caller
+                     int nlist_pre = 0);
 }  // namespace soapgb
