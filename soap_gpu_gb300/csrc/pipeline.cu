@@ -97,12 +97,12 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     int s_cells = ws.add(collapsed ? 0 : sizeof(int) * gm * n_phase);
     int s_counts = ws.add(sizeof(int) * n_phase);
     // the region table and, after it, the small per-call lists (run / zero phases, zero
-    // spectra, the convolution's batch list): one upload
+    // spectra, the convolution's row list): one upload
     const size_t pm_bytes = phase_maps_scratch_bytes(n_rows, n_phase);
     auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t off_lists = al256(pm_bytes), off_zspec = off_lists + al256(sizeof(int) * n_phase);
     const size_t off_blist = off_zspec + al256((size_t)n_spec);
-    const size_t small_bytes = off_blist + al256(sizeof(int) * ((size_t)n_spec / 8 + 2));
+    const size_t small_bytes = off_blist + al256(sizeof(int) * ((size_t)n_spec + 2));
     int s_pm = ws.add(small_bytes);
     int s_ztmpl = ws.add(host && box_lists && form == SOAPGB_FAST32 ? sizeof(double) * 3 * (size_t)n_eff : 0);
     FirPlanSizes fp = fir_plan_sizes(form, n, n_mu, gm, true, n_phase);
@@ -206,14 +206,10 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
         size_t used = off_zspec + (size_t)n_spec;
         std::vector<int> bl;
         if (!(host && collapsed) && form == SOAPGB_FAST32) {
-            // device buffers: one chunk of all the spectra; the batches of 8 that hold a
-            // non-zero spectrum (the others are left out of the convolution)
-            for (long long b = 0; b * 8 < n_spec; ++b) {
-                bool all0 = true;
-                for (long long q = b * 8; q < std::min<long long>(n_spec, b * 8 + 8) && all0; ++q)
-                    all0 = zspec[q] != 0;
-                if (!all0) bl.push_back((int)b);
-            }
+            // device buffers: one chunk of all the spectra; its non-zero ones, the rows the
+            // convolution takes
+            for (long long q = 0; q < n_spec; ++q)
+                if (!zspec[q]) bl.push_back((int)q);
             n_blist = (int)bl.size();
             used = off_blist + sizeof(int) * bl.size();
         }

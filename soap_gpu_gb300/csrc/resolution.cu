@@ -588,7 +588,7 @@ __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, in
 // of pixel i.  Ends with a block barrier.
 template <int SB, bool FULL = false>   // FULL: the tile lies below n_eff (no pixel test needed)
 __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff, int i0, int ib, int n, int n_eff,
-                                              int s0, int nsb, const bool (&lv)[FC_PIX],
+                                              const int *srow, int nsb, const bool (&lv)[FC_PIX],
                                               const float (&acc)[SB][FC_PIX], const float *__restrict__ b32a,
                                               const float *__restrict__ b32b, const float *__restrict__ c32a,
                                               const float *__restrict__ c32b, int b_every, float *__restrict__ conv,
@@ -627,7 +627,7 @@ __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff
     for (int q = 0; q < SB; ++q) {
         float mn = INFINITY, mx = -INFINITY, ma = 0.f, mc = 0.f;
         if (q < nsb) {
-            const int s = s0 + q;
+            const int s = srow[q];
             const bool use_b = (b_every > 0 && (s % b_every) == b_every - 1);
             float *cp = conv + (long long)s * conv_stride;
             float cdv[FC_PIX];
@@ -672,7 +672,7 @@ __device__ __forceinline__ void conv32_finish(const float *xs, int win, int xoff
     }
     __syncthreads();
     if (threadIdx.x < nsb) {
-        const int q = threadIdx.x, s = s0 + q;
+        const int q = threadIdx.x, s = srow[q];
         unsigned mn = red[q][0][0], mx = red[q][1][0], ma = red[q][2][0], mc = red[q][3][0];
         for (int w = 1; w < FC_THREADS / 32; ++w) {
             mn = min(mn, red[q][0][w]);
@@ -745,7 +745,10 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const 
         const int sh = (halo - R) & 3;
         conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh, R, sh, wid, c2, lk, acc);
     }
-    conv32_finish<SB>(xs, win, halo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every, conv,
+    __shared__ int srow[SB];   // the spectra of the batch
+    if (threadIdx.x < SB) srow[threadIdx.x] = s0 + threadIdx.x;
+    __syncthreads();
+    conv32_finish<SB>(xs, win, halo, i0, ib, n, n_eff, srow, nsb, lv, acc, b32a, b32b, c32a, c32b, b_every, conv,
                       conv_stride, mm32, blk, gridDim.x, blockIdx.x, red);
 }
 
@@ -768,18 +771,22 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
                                                            float *__restrict__ conv, long long conv_stride,
                                                            unsigned *mm32, float *blk, int nbx, int *status,
                                                            const unsigned char *__restrict__ zero_spec,
-                                                           const int *__restrict__ blist, int nlist) {
+                                                           const int *__restrict__ rows, int nrows) {
     static_assert(SB <= 31, "one bit per spectrum of a batch");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned red[SB][4][FC_THREADS / 32];
+    __shared__ int srow[SB];
     __shared__ unsigned long long bar[2];
     __shared__ int fail;
     const int win = (FC_TILE + 2 * halo + 12 + 3) & ~3;
     float *xbuf = reinterpret_cast<float *>(smem_raw);   // [2][SB][win]
-    // the batches to convolve: blist[0, nlist) (batches of zero spectra left out), or all
-    const int nwalk = blist ? nlist : (n_spec + SB - 1) / SB;
+    // the spectra to convolve: rows[0, nrows) (the non-zero ones), or all n_spec; batch
+    // bt holds the listed spectra bt * SB ...
+    const int nlisted = rows ? nrows : n_spec;
+    const int nwalk = (nlisted + SB - 1) / SB;
     const int nitem = nwalk * nbx;   // the host checks that it fits an int
-    auto batch_of = [&](int it) { return blist ? blist[it / nbx] : it / nbx; };
+    auto batch_of = [&](int it) { return it / nbx; };
+    auto row_id = [&](int bt, int q) { return rows ? rows[bt * SB + q] : bt * SB + q; };
     // staged window of tile x: first source pixel mb (16-byte aligned, <= i0 - halo) and
     // the in-range part [ca, cb) of the staged row, 16-byte aligned at both ends (the
     // row's allocation is padded beyond n to a multiple of 16 bytes)
@@ -801,21 +808,22 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
     __syncthreads();
     auto issue = [&](int it, int buf) {   // thread 0
         const int bt = batch_of(it), x = it % nbx;
-        const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        const int nsb = min(SB, nlisted - bt * SB);
         int mb, ca, cb;
         window(x, mb, ca, cb);
         const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
         int ncopy = 0;
-        for (int q = 0; q < nsb; ++q) ncopy += zero_row(s0 + q) ? 0 : 1;
+        for (int q = 0; q < nsb; ++q) ncopy += zero_row(row_id(bt, q)) ? 0 : 1;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
                      "r"(bytes * (unsigned)ncopy)
                      : "memory");
         if (bytes) {
             for (int q = 0; q < nsb; ++q) {
-                if (zero_row(s0 + q)) continue;
-                const float *src = spec + (long long)(s0 + q) * spec_stride + ca;
+                const int sq = row_id(bt, q);
+                if (zero_row(sq)) continue;
+                const float *src = spec + (long long)sq * spec_stride + ca;
                 float *dst = xbuf + ((size_t)buf * SB + q) * win + (ca - mb);
                 asm volatile(
                     "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -831,7 +839,11 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         const int bt = batch_of(it), x = it % nbx;
         const int buf = k & 1;
         if (threadIdx.x == 0 && it + (int)gridDim.x < nitem) issue(it + gridDim.x, buf ^ 1);
-        const int s0 = bt * SB, nsb = min(SB, n_spec - s0);
+        const int nsb = min(SB, nlisted - bt * SB);
+        // the item's spectra (shared: the epilogue's last step indexes them by thread);
+        // written before the barrier below, read after it, rewritten after the epilogue's
+        // closing barrier
+        if (threadIdx.x < SB) srow[threadIdx.x] = ((int)threadIdx.x < nsb) ? row_id(bt, threadIdx.x) : 0;
         const int i0 = x * FC_TILE;
         int mb, ca, cb;
         window(x, mb, ca, cb);
@@ -863,7 +875,7 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         }
         if (!ok) atomicExch(&fail, 1);
         unsigned zmask = 0;   // rows of zero spectra in this batch
-        for (int q = 0; q < nsb; ++q) zmask |= zero_row(s0 + q) ? (1u << q) : 0u;
+        for (int q = 0; q < nsb; ++q) zmask |= zero_row(row_id(bt, q)) ? (1u << q) : 0u;
         // zero the staged pixels outside [0, n), and the rows of absent and zero spectra
         if (ca > mb || cb < mb + win || nsb < SB || zmask) {
             for (int q = 0; q < SB; ++q)
@@ -888,11 +900,11 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         if (R > 0 && !zero_batch)
             conv32_taps<SB>(xs, win, threadIdx.x * FC_PIX + halo - R - sh + xo, R, sh, wid, c2, lk, acc);
         if (i0 + FC_TILE <= n_eff)   // uniform for the block
-            conv32_finish<SB, true>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b,
-                                    b_every, conv, conv_stride, mm32, blk, nbx, x, red);
+            conv32_finish<SB, true>(xs, win, halo + xo, i0, ib, n, n_eff, srow, nsb, lv, acc, b32a, b32b, c32a,
+                                    c32b, b_every, conv, conv_stride, mm32, blk, nbx, x, red);
         else
-            conv32_finish<SB, false>(xs, win, halo + xo, i0, ib, n, n_eff, s0, nsb, lv, acc, b32a, b32b, c32a, c32b,
-                                     b_every, conv, conv_stride, mm32, blk, nbx, x, red);
+            conv32_finish<SB, false>(xs, win, halo + xo, i0, ib, n, n_eff, srow, nsb, lv, acc, b32a, b32b, c32a,
+                                     c32b, b_every, conv, conv_stride, mm32, blk, nbx, x, red);
     }
     if (k_fail >= 0 && threadIdx.x == 0) {
         // a staged copy did not land in time: record it and give the next item's copy,
@@ -1111,7 +1123,7 @@ static size_t conv_param_bytes(int n_eff) {
 size_t resolution_scratch_bytes(int form, int n, int n_eff, int n_spec) {
     size_t b = sizeof(double) * (size_t)n_eff * n_spec + 256;   // conv
     b += sizeof(unsigned long long) * 2 * n_spec + 256;          // min/max
-    b += sizeof(unsigned long long) * 4 + 256 + sizeof(int) * ((size_t)n_spec / 8 + 2) + 256;   // zero spectra
+    b += sizeof(unsigned long long) * 4 + 256 + sizeof(int) * ((size_t)n_spec + 2) + 256;   // zero spectra
     if (form != SOAPGB_PLAIN64)
         b += 2 * (sizeof(double) * (size_t)n_eff + 256) + 2 * (conv_param_bytes(n_eff) + 256) +
              2 * sizeof(double) * (size_t)n + 256;   // base convolutions, tap constants, staged bases
@@ -1227,7 +1239,7 @@ static int conv32_params(soapgb_ctx *ctx, int n, int n_eff, const double *lam, d
 static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, const char *param_scratch,
                       const float *spec, long long spec_stride, int n_spec, const float *b32a, const float *b32b,
                       const float *c32a, const float *c32b, int b_every, float *conv, unsigned *mm32, float *blk,
-                      const unsigned char *zero_spec, const int *blist, int nlist) {
+                      const unsigned char *zero_spec, const int *rows, int nrows) {
     constexpr int SB = 8;
     const size_t pb = (sizeof(float) * (size_t)n_eff + 255) & ~size_t(255);
     const float *c2 = (const float *)param_scratch;
@@ -1242,7 +1254,7 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         size_t smem_t = sizeof(float) * 2 * (size_t)SB * win_t;
         if (smem_t > 200 * 1024) return set_error(ctx, SOAPGB_ERR_ARG, "convolution window too wide (%d px)", halo);
         SOAP_CUDA(ctx, cudaFuncSetAttribute(k_conv32t<SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
-        const int nwalk = blist ? nlist : nbatch;
+        const int nwalk = rows ? (nrows + SB - 1) / SB : nbatch;
         if (nwalk == 0) return SOAPGB_OK;   // every spectrum is zero
         int per_sm = 0;
         SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv32t<SB>, FC_THREADS, smem_t));
@@ -1253,7 +1265,7 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
                                                               n_eff, mm32, blk, nbx, ctx->d_status, zero_spec,
-                                                              blist, nlist));
+                                                              rows, nrows));
     } else {
         const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
         size_t smem = sizeof(float) * (size_t)SB * win;
@@ -1348,7 +1360,7 @@ int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const do
     R.p32 = pscr32;
     // extrema of the zero spectra, per base
     R.mmz = (unsigned long long *)carve(p, sizeof(unsigned long long) * 4);
-    R.blist = (int *)carve(p, sizeof(int) * ((size_t)n_spec / 8 + 2));
+    R.blist = (int *)carve(p, sizeof(int) * ((size_t)n_spec + 2));
     k_mm32_init<<<1, 32, 0, ctx->stream>>>(2, sentinel, nullptr, R.mmz);
     SOAP_LAUNCHED(ctx);
     k_zero_extrema<<<dim3(std::max(1, std::min(grid_for(ctx, n, 256), 4 * std::max(ctx->num_sms, 1))), R.base_b ? 2 : 1),
@@ -1378,20 +1390,19 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
     // spectra known to be zero (both flag copies given): their batches are left out of
     // the convolution and their extrema come from the bases
     const unsigned char *zs = (zero_spec && zero_host) ? zero_spec + s0 : nullptr;
+    // the non-zero spectra of the chunk (relative indices): only they are convolved, in
+    // batches of 8 without zero rows
     const int *blist = nullptr;
     int nlist = 0;
-    if (zs && blist_pre) {   // the caller uploaded the batch list with its own small inputs
+    if (zs && blist_pre) {   // the caller uploaded the list with its own small inputs
         blist = blist_pre;
         nlist = nlist_pre;
         k_zero_mm<<<(ns + 127) / 128, 128, 0, ctx->stream>>>(ns, zs, R.b_every, R.mmz, mm);
         SOAP_LAUNCHED(ctx);
     } else if (zs) {
         std::vector<int> bl;
-        for (int b = 0; b * 8 < ns; ++b) {
-            bool all0 = true;
-            for (int q = b * 8; q < std::min(ns, b * 8 + 8) && all0; ++q) all0 = zero_host[s0 + q] != 0;
-            if (!all0) bl.push_back(b);
-        }
+        for (int q = 0; q < ns; ++q)
+            if (!zero_host[s0 + q]) bl.push_back(q);
         nlist = (int)bl.size();
         if (nlist > 0)   // pageable source: staged by the driver before the call returns
             SOAP_CUDA(ctx, cudaMemcpyAsync(R.blist, bl.data(), sizeof(int) * nlist, cudaMemcpyHostToDevice, ctx->stream));

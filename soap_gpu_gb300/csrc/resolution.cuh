@@ -30,7 +30,7 @@ struct Res32 {
     unsigned long long *mm;
     float *fac, *blk;
     unsigned long long *mmz;   // exact extrema of a zero spectrum, per base: [base][min, max]
-    int *blist;                // batch list of a chunk's convolution
+    int *blist;                // the non-zero spectra of a chunk (its convolution's row list)
     char *next;   // first scratch byte after the state
 };
 int resolution32_prepare(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *d_wave, double wave0,
@@ -48,6 +48,6 @@ int resolution32_run(soapgb_ctx *ctx, const Res32 &R, const float *spec32, long 
                      const unsigned char *zero_spec = nullptr,    // [n_spec] device: 1 = spectrum known to be zero
                      const unsigned char *zero_host = nullptr,    // the same flags on the host (both or neither)
                      ZeroRows zero_rows = ZeroRows::NORM,
-                     const int *blist_pre = nullptr,   // device batch list of [s0, s1) made by the caller
+                     const int *blist_pre = nullptr,   // device list of the non-zero spectra of [s0, s1), by the caller
                      int nlist_pre = 0);
 }  // namespace soapgb
