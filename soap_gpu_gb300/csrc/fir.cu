@@ -1431,45 +1431,52 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
                 // pixels whose owner j + m lies in [0, n_eff - 2] (v == 0: [0, n_eff - 1])
                 const int jlo = max(j0, -m);
                 const int jhi = zv ? j0 + t_eff - 1 : min(j0 + t_eff - 1, n_eff - 2 - m);
+                // the group at the thread's pixels; CHECKED: some pixels of the tile fall
+                // outside [jlo, jhi], else none and no test is needed (same arithmetic)
+                auto group_at = [&](auto checked_c) {
+                    constexpr bool CHECKED = decltype(checked_c)::value;
 #pragma unroll
-                for (int q = 0; q < FIR_PIX; ++q) {
-                    const int dj = tid + q * FIR_THREADS;
-                    const int j = j0 + dj;
-                    if (j < jlo || j > jhi) continue;
-                    const int x = j + m + wo;
-                    if (zv) {   // single tap: w == 0
-                        if constexpr (MODE == MODE_QUIET) {
-                            acc[0][q].add(gr.a0 * W[0][x]);
-                        } else if (cls == CLS_SPOT) {
-                            acc[0][q].add(gr.a0 * W[0][x]);
-                            acc[1][q].add(gr.a0 * W[1][x]);
-                            acc[2][q].add(gr.a0 * W[2][x]);
-                            acc[3][q].add(gr.a0 * W[3][x]);
-                        } else {
-                            acc[0][q].add(gr.a0 * W[0][x]);
-                            acc[6][q].add(gr.a0 * W[1][x]);
-                            acc[4][q].add(gr.a0w * W[2][x]);
-                            acc[5][q].add(gr.a0w * W[3][x]);
+                    for (int q = 0; q < FIR_PIX; ++q) {
+                        const int dj = tid + q * FIR_THREADS;
+                        const int j = j0 + dj;
+                        if (CHECKED && (j < jlo || j > jhi)) continue;
+                        const int x = j + m + wo;
+                        if (zv) {   // single tap: w == 0
+                            if constexpr (MODE == MODE_QUIET) {
+                                acc[0][q].add(gr.a0 * W[0][x]);
+                            } else if (cls == CLS_SPOT) {
+                                acc[0][q].add(gr.a0 * W[0][x]);
+                                acc[1][q].add(gr.a0 * W[1][x]);
+                                acc[2][q].add(gr.a0 * W[2][x]);
+                                acc[3][q].add(gr.a0 * W[3][x]);
+                            } else {
+                                acc[0][q].add(gr.a0 * W[0][x]);
+                                acc[6][q].add(gr.a0 * W[1][x]);
+                                acc[4][q].add(gr.a0w * W[2][x]);
+                                acc[5][q].add(gr.a0w * W[3][x]);
+                            }
+                            continue;
                         }
-                        continue;
+                        const T fdj = (T)dj;
+                        const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
+                        if constexpr (MODE == MODE_QUIET) {
+                            acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                        } else if (cls == CLS_SPOT) {
+                            acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                            acc[1][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
+                            acc[2][q].add(c0 * W[2][x] + c1 * W[2][x + 1]);
+                            acc[3][q].add(c0 * W[3][x] + c1 * W[3][x + 1]);
+                        } else {
+                            const T e0 = gr.a0w - gr.bw * fdj, e1 = gr.a1w + gr.bw * fdj;
+                            acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
+                            acc[6][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
+                            acc[4][q].add(e0 * W[2][x] + e1 * W[2][x + 1]);
+                            acc[5][q].add(e0 * W[3][x] + e1 * W[3][x + 1]);
+                        }
                     }
-                    const T fdj = (T)dj;
-                    const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
-                    if constexpr (MODE == MODE_QUIET) {
-                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
-                    } else if (cls == CLS_SPOT) {
-                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
-                        acc[1][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
-                        acc[2][q].add(c0 * W[2][x] + c1 * W[2][x + 1]);
-                        acc[3][q].add(c0 * W[3][x] + c1 * W[3][x + 1]);
-                    } else {
-                        const T e0 = gr.a0w - gr.bw * fdj, e1 = gr.a1w + gr.bw * fdj;
-                        acc[0][q].add(c0 * W[0][x] + c1 * W[0][x + 1]);
-                        acc[6][q].add(c0 * W[1][x] + c1 * W[1][x + 1]);
-                        acc[4][q].add(e0 * W[2][x] + e1 * W[2][x + 1]);
-                        acc[5][q].add(e0 * W[3][x] + e1 * W[3][x + 1]);
-                    }
-                }
+                };
+                if (jlo <= j0 && jhi >= j0 + FIR_TILE - 1) group_at(std::integral_constant<bool, false>());
+                else group_at(std::integral_constant<bool, true>());
             }
             // --- wrap cells of the unit (per-cell lerp from the staged rows) ------------
             const int e_lo = st.woff[t_lo], e_hi = st.woff[t_hi];
