@@ -153,6 +153,20 @@ int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_eff, int n_s
                             double sigma_v, double window, double step_mult, double step_exp,
                             double sentinel, int mem, double *out, double *minmax_out);
 
+/* Adjoint of soapgb_lower_resolution in the PLAIN64 arithmetic (the differentiable
+ * form; the reference has no counterpart).  Same arguments as the forward plus g_out
+ * (n_spec x n_eff), the gradient of a scalar w.r.t. out.  Writes grad_spec
+ * (n_spec x n), its gradient w.r.t. spec, and -- when grad_base is not NULL, which
+ * needs a base -- grad_base (n), w.r.t. base summed over the spectra.  The
+ * normalisation's min A and max C are differentiated at the first pixel holding each
+ * (a maximum that stayed at the sentinel carries no gradient).  Deterministic: every
+ * sum runs in a fixed order, without atomics. */
+int soapgb_lower_resolution_adjoint(soapgb_ctx *ctx, int n, int n_eff, int n_spec,
+                                    const double *wave, const double *base, const double *spec,
+                                    double sigma_v, double window, double step_mult, double step_exp,
+                                    double sentinel, const double *g_out, int mem,
+                                    double *grad_spec, double *grad_base);
+
 /* ---- a9-a10: per-phase temperature and type maps -------------------------
  * Replaces spot_init_gpu / spot_phase_gpu / spot_area / spot_scan and the region
  * loop, SOAP_integration.cu:21-161,326-390,686-785.  regions: rows of

@@ -60,6 +60,8 @@ SIGNATURES = [
                                          ctypes.c_int, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp]),
     ("soapgb_lower_resolution", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
                                                _vp, _vp] + [ctypes.c_double] * 5 + [ctypes.c_int, _vp, _vp]),
+    ("soapgb_lower_resolution_adjoint", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
+     + [ctypes.c_double] * 5 + [_vp, ctypes.c_int, _vp, _vp]),
     ("soapgb_phase_maps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp,
                                          ctypes.POINTER(Activity), ctypes.c_int, _vp, _vp]),
     ("soapgb_phase_integrate", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,

@@ -199,6 +199,21 @@ class Context:
                                                    sentinel, a.mem, op, mp))
         return (out[0] if single else out), mm
 
+    def lower_resolution_adjoint(self, wave, spec, n_eff, sigma_v, g_out, base=None, window=50.0, step_mult=0.005,
+                                 step_exp=0.005, sentinel=-60000.0, want_base=True):
+        """Gradients of a scalar through lower_resolution (PLAIN64 arithmetic), given its
+        gradient g_out (n_spec x n_eff) w.r.t. the output: (grad_spec (n_spec x n),
+        grad_base (n) or None), grad_base summed over the spectra."""
+        a = self._args(wave, spec, base, g_out)
+        n = int(wave.shape[0])
+        n_spec = int(spec.shape[0])
+        gs, gsp = a.out((n_spec, n), np.float64)
+        gb, gbp = a.out((n,), np.float64) if (base is not None and want_base) else (None, None)
+        self._check(self.L.soapgb_lower_resolution_adjoint(
+            self.h, n, int(n_eff), n_spec, a.inp(wave, np.float64), a.inp(base, np.float64), a.inp(spec, np.float64),
+            sigma_v, window, step_mult, step_exp, sentinel, a.inp(g_out, np.float64), a.mem, gsp, gbp))
+        return gs, gb
+
     # -- seed preparation: bisector injection (CB_injection_faculae.py:191-244) ----------
     def bisector_inject(self, wave, flux, coeffs, coeffs_low=None, dep_cut=None, vcut=None, vshift=None,
                         scale=1.0):

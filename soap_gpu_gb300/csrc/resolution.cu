@@ -17,6 +17,7 @@
 //               (deterministic), then an FP64 normalisation pass.
 #include <algorithm>
 #include <cmath>
+#include <climits>
 #include <vector>
 
 #include "internal.cuh"
@@ -1589,4 +1590,208 @@ extern "C" int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_e
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return host ? check_status(ctx, "soapgb_lower_resolution") : SOAPGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the PLAIN64 resolution step (the differentiable form; the reference
+// has no gradient path).  Per spectrum, with f = (1 - mn) / mx and S = sum_i G_i C_i
+// (G the gradient of a scalar w.r.t. out):
+//   dL/dC_i = -f G_i + [i = i_max] S (1 - mn) / mx^2
+//   dL/dA_m = -sum_i K(i, m) dL/dC_i + [m = i_min] S / mx
+// with K(i, m) = step_mult e^{-(m-i)^2 step_exp^2 / (2 s_i^2)} / (s_i sqrt(2 pi)) on the
+// interior pixels i (m - i in [-w, w-2]), and i_min / i_max the first pixels holding
+// min A and max C (the subgradient at ties; a maximum that stayed at the sentinel has
+// no pixel and no gradient).  dL/dspec = -dL/dA with a base, dL/dA without;
+// dL/dbase = sum over the spectra of dL/dA, in spectrum order.
+// ---------------------------------------------------------------------------
+// tap constants per pixel: kq = step_mult / (s_i sqrt(2 pi)), cq = step_exp^2 / (2 s_i^2)
+// on the interior pixels, kq = 0 elsewhere
+__global__ void k_radj_taps(int n, int n_eff, const double *__restrict__ lam, double sigma_v, int wid,
+                            double step_mult, double step_exp, double *__restrict__ kq, double *__restrict__ cq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_eff) return;
+    double k = 0.0, c = 0.0;
+    if (i > wid && i + wid < n - 1) {
+        const double sig = soap_delta_lambda(sigma_v, lam[i]);
+        k = step_mult / (sig * sqrt(2.0 * SOAP_PI));
+        c = step_exp * step_exp / (2.0 * sig * sig);
+    }
+    kq[i] = k;
+    cq[i] = c;
+}
+
+constexpr int RADJ_THREADS = 512;
+
+// one block per spectrum: S in a fixed tree order, the first extremum pixels by min
+__global__ void __launch_bounds__(RADJ_THREADS) k_radj_reduce(int n, int n_eff, const double *__restrict__ spec,
+                                                               const double *__restrict__ base,
+                                                               const double *__restrict__ conv,
+                                                               const unsigned long long *__restrict__ mm,
+                                                               const double *__restrict__ g, double *par, int *idx) {
+    const int s = blockIdx.x, t = threadIdx.x;
+    const double *sp = spec + (long long)s * n;
+    const double *cp = conv + (long long)s * n_eff;
+    const double *gp = g + (long long)s * n_eff;
+    const double mn = soap_ord_dec(mm[2 * s]), mx = soap_ord_dec(mm[2 * s + 1]);
+    double acc = 0.0;
+    int im = INT_MAX, ix = INT_MAX;
+    for (int i = t; i < n; i += RADJ_THREADS) {
+        const double a = base ? __dsub_rn(base[i], sp[i]) : sp[i];
+        if (a == mn && im == INT_MAX) im = i;
+        if (i < n_eff) {
+            const double c = cp[i];
+            acc = fma(gp[i], c, acc);
+            if (c != 0.0 && c == mx && ix == INT_MAX) ix = i;
+        }
+    }
+    __shared__ double sh[RADJ_THREADS];
+    __shared__ int si[RADJ_THREADS], sx[RADJ_THREADS];
+    sh[t] = acc;
+    si[t] = im;
+    sx[t] = ix;
+    __syncthreads();
+    for (int o = RADJ_THREADS / 2; o > 0; o >>= 1) {
+        if (t < o) {
+            sh[t] += sh[t + o];
+            si[t] = min(si[t], si[t + o]);
+            sx[t] = min(sx[t], sx[t + o]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const double S = sh[0];
+        par[3 * s] = (1.0 - mn) / mx;
+        par[3 * s + 1] = S / mx;
+        par[3 * s + 2] = S * (1.0 - mn) / (mx * mx);
+        idx[2 * s] = si[0] == INT_MAX ? -1 : si[0];
+        idx[2 * s + 1] = sx[0] == INT_MAX ? -1 : sx[0];
+    }
+}
+
+// the transposed tap gather, one thread per (pixel m, spectrum)
+__global__ void __launch_bounds__(256) k_radj_spec(int n, int n_eff, int wid, const double *__restrict__ kq,
+                                                   const double *__restrict__ cq, const double *__restrict__ g,
+                                                   const double *__restrict__ par, const int *__restrict__ idx,
+                                                   int has_base, double *__restrict__ grad_spec) {
+    const int s = blockIdx.y;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    const double f = par[3 * s], dmn = par[3 * s + 1], dmx = par[3 * s + 2];
+    const int imin = idx[2 * s], imax = idx[2 * s + 1];
+    const double *gp = g + (long long)s * n_eff;
+    const int lo = max(m - wid + 2, 0), hi = min(m + wid, n_eff - 1);
+    double acc = 0.0;
+    for (int i = lo; i <= hi; ++i) {
+        const double k = kq[i];
+        if (k == 0.0) continue;
+        const double d = (double)(m - i);
+        double gc = -f * gp[i];
+        if (i == imax) gc += dmx;
+        acc = fma(k * exp(-d * d * cq[i]), gc, acc);
+    }
+    const double ga = (m == imin ? dmn : 0.0) - acc;
+    grad_spec[(long long)s * n + m] = has_base ? -ga : ga;
+}
+
+// dL/dbase[m] = sum_s dL/dA_s[m] = -sum_s grad_spec[s][m] (with a base), spectra in order
+__global__ void k_radj_base(int n, int n_spec, const double *__restrict__ grad_spec, double *__restrict__ grad_base) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    double acc = 0.0;
+    for (int s = 0; s < n_spec; ++s) acc -= grad_spec[(long long)s * n + m];
+    grad_base[m] = acc;
+}
+
+extern "C" int soapgb_lower_resolution_adjoint(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *wave,
+                                               const double *base, const double *spec, double sigma_v,
+                                               double window, double step_mult, double step_exp, double sentinel,
+                                               const double *g_out, int mem, double *grad_spec,
+                                               double *grad_base) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    if (n < 3 || n_eff < 1 || n_eff > n || n_spec < 0 || !wave || !spec || !g_out || !grad_spec ||
+        !(sigma_v > 0) || !(step_exp > 0) || (grad_base && !base))
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution_adjoint: bad arguments");
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bool host = (mem == SOAPGB_HOST);
+    if (n_spec == 0) {
+        if (grad_base) {
+            if (host) std::fill(grad_base, grad_base + n, 0.0);
+            else SOAP_CUDA(ctx, cudaMemsetAsync(grad_base, 0, sizeof(double) * n, ctx->stream));
+        }
+        return SOAPGB_OK;
+    }
+    double w01[2];
+    if (host) {
+        w01[0] = wave[0];
+        w01[1] = wave[1];
+    } else {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(w01, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    const int wid = conv_halfwidth(w01[0], w01[1], sigma_v, window);
+    if (wid < 1 || 2 * wid + 2 >= n)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution_adjoint: convolution half width %d invalid for n=%d",
+                         wid, n);
+    const size_t row_b = sizeof(double) * (size_t)n, spec_b = row_b * n_spec;
+    const size_t out_b = sizeof(double) * (size_t)n_eff * n_spec;
+    Workspace ws(ctx);
+    int s_wave = ws.add(host ? row_b : 0);
+    int s_base = ws.add(host && base ? row_b : 0);
+    int s_spec = ws.add(host ? spec_b : 0);
+    int s_g = ws.add(host ? out_b : 0);
+    int s_gs = ws.add(host ? spec_b : 0);
+    int s_gb = ws.add(host && grad_base ? row_b : 0);
+    int s_conv = ws.add(out_b);
+    int s_mm = ws.add(sizeof(unsigned long long) * 2 * n_spec);
+    int s_kq = ws.add(sizeof(double) * n_eff), s_cq = ws.add(sizeof(double) * n_eff);
+    int s_par = ws.add(sizeof(double) * 3 * n_spec), s_idx = ws.add(sizeof(int) * 2 * n_spec);
+    int rc = ws.commit();
+    if (rc) return rc;
+    const double *d_wave = (const double *)stage_in(ctx, mem, wave, row_b, ws.get<void>(s_wave), &rc);
+    if (rc) return rc;
+    const double *d_base = (const double *)stage_in(ctx, mem, base, base ? row_b : 0, ws.get<void>(s_base), &rc);
+    if (rc) return rc;
+    const double *d_spec = (const double *)stage_in(ctx, mem, spec, spec_b, ws.get<void>(s_spec), &rc);
+    if (rc) return rc;
+    const double *d_g = (const double *)stage_in(ctx, mem, g_out, out_b, ws.get<void>(s_g), &rc);
+    if (rc) return rc;
+    double *d_gs = host ? ws.get<double>(s_gs) : grad_spec;
+    double *d_gb = grad_base ? (host ? ws.get<double>(s_gb) : grad_base) : nullptr;
+    double *conv = ws.get<double>(s_conv);
+    unsigned long long *mm = ws.get<unsigned long long>(s_mm);
+    double *kq = ws.get<double>(s_kq), *cq = ws.get<double>(s_cq), *par = ws.get<double>(s_par);
+    int *idx = ws.get<int>(s_idx);
+    // the forward's C and extrema, in the reference's operation order
+    SOAP_TRACED(ctx, "conv_plain64",
+                k_conv_plain64<<<dim3(grid_for(ctx, n_eff, 256), n_spec), 256, 0, ctx->stream>>>(
+                    n, n_eff, d_wave, d_spec, n, d_base, nullptr, 0, sigma_v, wid, step_mult, step_exp, conv, n_eff));
+    SOAP_LAUNCHED(ctx);
+    k_minmax_init<<<(n_spec + 127) / 128, 128, 0, ctx->stream>>>(n_spec, sentinel, mm);
+    SOAP_LAUNCHED(ctx);
+    SOAP_TRACED(ctx, "minmax64",
+                k_minmax<<<dim3(std::max(1, std::min(64, (n + 255) / 256)), n_spec), 256, 0, ctx->stream>>>(
+                    n, n_eff, d_spec, n, d_base, nullptr, 0, conv, n_eff, nullptr, nullptr, mm));
+    SOAP_LAUNCHED(ctx);
+    k_radj_taps<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n, n_eff, d_wave, sigma_v, wid, step_mult,
+                                                                     step_exp, kq, cq);
+    SOAP_LAUNCHED(ctx);
+    SOAP_TRACED(ctx, "resolution_adjoint_reduce",
+                k_radj_reduce<<<n_spec, RADJ_THREADS, 0, ctx->stream>>>(n, n_eff, d_spec, d_base, conv, mm, d_g, par,
+                                                                        idx));
+    SOAP_LAUNCHED(ctx);
+    SOAP_TRACED(ctx, "resolution_adjoint",
+                k_radj_spec<<<dim3(grid_for(ctx, n, 256), n_spec), 256, 0, ctx->stream>>>(
+                    n, n_eff, wid, kq, cq, d_g, par, idx, d_base ? 1 : 0, d_gs));
+    SOAP_LAUNCHED(ctx);
+    if (d_gb) {
+        k_radj_base<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, n_spec, d_gs, d_gb);
+        SOAP_LAUNCHED(ctx);
+    }
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_spec, d_gs, spec_b, cudaMemcpyDeviceToHost, ctx->stream));
+        if (grad_base) SOAP_CUDA(ctx, cudaMemcpyAsync(grad_base, d_gb, row_b, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return check_status(ctx, "soapgb_lower_resolution_adjoint");
+    }
+    return SOAPGB_OK;
 }

@@ -19,6 +19,11 @@ spectra (gradients exact up to rounding) and continuous, piecewise smooth in the
 velocities; the tests check them against FP64 central differences and a dot-product
 identity.
 
+``LowerResolution`` continues the chain through the resolution step
+(SOAP_resolution.cu:216-310, PLAIN64): the Gaussian convolution and the min/max
+normalisation of base - spec, by the hand-written adjoint of
+``soapgb_lower_resolution_adjoint``.
+
 Region positions and sizes stay discrete (cell coverage), as in the reference; the
 inclination and the region contrast are not differentiated yet.
 """
@@ -115,3 +120,51 @@ def deficit_spectra(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed,
     """Differentiable (n_phase, 3, n) deficit spectra, star = (u1, u2, vsini); see
     ``DeficitSpectra``."""
     return DeficitSpectra.apply(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup)
+
+
+@dataclasses.dataclass
+class ResolutionSetup:
+    """The fixed arguments of the resolution step (SOAP_resolution.cu:216-310): the
+    wavelength grid (device, float64), n_eff and the instrument's sigma_v, the window
+    and the reference's step constants."""
+    ctx: Context
+    wave: torch.Tensor
+    n_eff: int
+    sigma_v: float
+    window: float = 50.0
+    step_mult: float = 0.005
+    step_exp: float = 0.005
+    sentinel: float = -60000.0
+
+    def kwargs(self) -> dict:
+        return dict(window=self.window, step_mult=self.step_mult, step_exp=self.step_exp, sentinel=self.sentinel)
+
+
+class LowerResolution(torch.autograd.Function):
+    """out[s] = 1 - C_s (1 - min A_s) / max C_s with A_s = base - spec[s] and C_s the
+    instrumental Gaussian convolution of 1 - A_s (``soapgb_lower_resolution``, PLAIN64).
+    The backward runs ``soapgb_lower_resolution_adjoint``: the transposed tap gather and
+    the normalisation's derivative, the extrema differentiated at their first pixel."""
+
+    @staticmethod
+    def forward(fctx, spec, base, setup: ResolutionSetup):
+        spec_d, base_d = spec.detach().contiguous(), base.detach().contiguous()
+        out, _ = setup.ctx.lower_resolution("plain64", setup.wave, spec_d, setup.n_eff, setup.sigma_v, base=base_d,
+                                            **setup.kwargs())
+        fctx.setup, fctx.spec, fctx.base = setup, spec_d, base_d
+        fctx.want_base = base.requires_grad
+        return out
+
+    @staticmethod
+    def backward(fctx, g):
+        setup = fctx.setup
+        gs, gb = setup.ctx.lower_resolution_adjoint(setup.wave, fctx.spec, setup.n_eff, setup.sigma_v,
+                                                    g.to(torch.float64).contiguous(), base=fctx.base,
+                                                    want_base=fctx.want_base, **setup.kwargs())
+        return gs, gb, None
+
+
+def lower_resolution(spec, base, setup: ResolutionSetup):
+    """Differentiable (n_spec, n_eff) normalised low-resolution spectra of
+    base - spec[s]; see ``LowerResolution``."""
+    return LowerResolution.apply(spec, base, setup)
