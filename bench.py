@@ -353,7 +353,8 @@ def adjoint_timing(ctx, dev, reps=3):
     import dataclasses
     import torch
     from soap_gpu_gb300 import synth
-    from soap_gpu_gb300.differentiable import IntegrationSetup, deficit_spectra
+    from soap_gpu_gb300.differentiable import (IntegrationSetup, ResolutionSetup, deficit_spectra,
+                                               lower_resolution)
     from soap_gpu_gb300._lib import Activity
     case = synth.small_case(seed=4, grid=200, n=100000, n_phase=5, n_mu=10)
     case = dataclasses.replace(case, regions=np.array([[20.0, 180.0, 0.1, 0.0], [-15.0, 200.0, 0.1732, 1.0],
@@ -391,10 +392,30 @@ def adjoint_timing(ctx, dev, reps=3):
         cg = [c.clone().requires_grad_(True) for c in cubes]
         (deficit_spectra(ug, *cg, setup) * W).sum().backward()
 
+    # the chain on through the resolution step: low-resolution spectra of quiet - flux deficit
+    maps = setup.maps(case.u1, case.u2, case.vsini)
+    base = ctx.quiet_disk("plain64", setup.wave, cubes[1], n_eff, maps, case.grid, case.step).reshape(-1)
+    rs = ResolutionSetup(ctx, setup.wave, n_eff, float(case.sigma_v))
+    W2 = torch.ones((case.n_phase, n_eff), dtype=torch.float64, device=dev)
+
+    def chain_fwd():
+        with torch.no_grad():
+            lower_resolution(deficit_spectra(u, *cubes, setup)[:, 0].contiguous(), base, rs)
+
+    def chain_fwd_bwd():
+        ug = u.clone().requires_grad_(True)
+        cg = [c.clone().requires_grad_(True) for c in cubes]
+        (lower_resolution(deficit_spectra(ug, *cg, setup)[:, 0].contiguous(), base, rs) * W2).sum().backward()
+
     f_ms, fb_ms = timed(fwd), timed(fwd_bwd)
+    cf_ms, cfb_ms = timed(chain_fwd), timed(chain_fwd_bwd)
     return {"case": "200x200 grid, 100,000 px, 10 mu bins, 3 regions, 5 phases over one rotation, PLAIN64; "
                     "gradients w.r.t. u1, u2, vsini, 4 seed cubes, 2 continuum rows",
-            "forward_ms": round(f_ms, 3), "forward_adjoint_ms": round(fb_ms, 3), "ratio": round(fb_ms / f_ms, 2)}
+            "forward_ms": round(f_ms, 3), "forward_adjoint_ms": round(fb_ms, 3), "ratio": round(fb_ms / f_ms, 2),
+            "with_resolution": {"case": "the same, then the resolution step (Gaussian convolution, min/max "
+                                        "normalisation) of the quiet spectrum - flux deficit of each phase",
+                                "forward_ms": round(cf_ms, 3), "forward_adjoint_ms": round(cfb_ms, 3),
+                                "ratio": round(cfb_ms / cf_ms, 2)}}
 
 
 def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, regions, act, star):
