@@ -224,6 +224,18 @@ int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel, int n_line
                double mask_step, int index_old, int n_spec, const double *spectra,
                int normalise, int mem, double *ccf_out);
 
+/* Adjoint of soapgb_ccf in FP64 (the differentiable form; the reference has no
+ * counterpart).  Same mask arguments as the forward; g_ccf (n_spec x n_v) is the
+ * gradient of a scalar w.r.t. ccf_out.  With `normalise` set, ccf_raw (n_spec x n_v)
+ * holds the forward's raw sums (soapgb_ccf with normalise = 0) and the max is
+ * differentiated at its first index.  Writes grad_spectra (n_spec x n_w).  Deterministic:
+ * one thread per pixel sums the velocities in order, without atomics. */
+int soapgb_ccf_adjoint(soapgb_ctx *ctx, int n_v, const double *vel, int n_lines,
+                       const double *line_wave, const double *line_weight, int n_w,
+                       const double *wave_trim, double step_size, double wave_extend,
+                       double mask_step, int index_old, int n_spec, const double *ccf_raw,
+                       int normalise, const double *g_ccf, int mem, double *grad_spectra);
+
 /* ---- a17-a18: Gaussian fit + bisector -------------------------------------
  * Replaces BIS_FIT2.cpp:97-317 (GSL trust-region Levenberg-Marquardt fit of
  * c + k exp(-(x-x0)^2 / 2 sigma^2), then the 91-depth bisector and its span), for
@@ -234,6 +246,18 @@ int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel, int n_line
 int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double *x, const double *y,
                      const double *err, int mem, double *model, double *par, double *depth,
                      double *bis, int *iters);
+
+/* Adjoint of the Gaussian fit of soapgb_gauss_bis (the differentiable form; the
+ * reference has no counterpart), by the implicit function theorem at the fitted
+ * optimum: H dtheta/dy = J^T W with H the full Hessian of the residual sum of squares
+ * (Gauss-Newton term plus the residual-weighted second derivatives).  x, y, err as
+ * for the fit; model and par are its outputs; g_par (n_spec x 5) holds the gradient
+ * of a scalar w.r.t. par = (c, |k|, span, v0, fwhm); the span's entry is ignored (the
+ * bisector is not differentiated).  Writes grad_y (n_spec x n).  A singular system
+ * gives a zero gradient for that spectrum and the status SOAPGB_ERR_DEVICE. */
+int soapgb_gauss_fit_adjoint(soapgb_ctx *ctx, int n_spec, int n, const double *x, const double *y,
+                             const double *err, const double *model, const double *par,
+                             const double *g_par, int mem, double *grad_y);
 
 /* ---- composite: the per-phase stages in one call --------------------------
  * Runs a9-a14 for every phase: maps, integration, convolution and normalisation of

@@ -75,6 +75,11 @@ SIGNATURES = [
     ("soapgb_ccf", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                   _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    ("soapgb_ccf_adjoint", ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int, _vp,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_int, _vp]),
+    ("soapgb_gauss_fit_adjoint", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                ctypes.c_int, _vp]),
     ("soapgb_gauss_bis", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp,
                                         _vp, _vp]),
     ("soapgb_phase_pipeline", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,

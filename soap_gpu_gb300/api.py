@@ -326,6 +326,34 @@ class Context:
                                       a.inp(spectra, np.float64), int(bool(normalise)), a.mem, op))
         return out[0] if single else out
 
+    def ccf_adjoint(self, vel, line_wave, line_weight, wave_trim, step_size, g_ccf, ccf_raw=None, normalise=True,
+                    wave_extend=100.0, mask_step=0.005, index_old=20000):
+        """Gradient (n_spec x n_w) of a scalar w.r.t. the spectra of ccf, given its
+        gradient g_ccf (n_spec x n_v) w.r.t. the CCF; ccf_raw: the raw sums (needed when
+        normalise is set)."""
+        a = self._args(g_ccf, wave_trim)
+        n_spec, n_v = int(g_ccf.shape[0]), len(vel)
+        out, op = a.out((n_spec, int(wave_trim.shape[0])), np.float64)
+        self._check(self.L.soapgb_ccf_adjoint(self.h, n_v, a.inp(vel, np.float64), len(line_wave),
+                                              a.inp(line_wave, np.float64), a.inp(line_weight, np.float64),
+                                              int(wave_trim.shape[0]), a.inp(wave_trim, np.float64), float(step_size),
+                                              float(wave_extend), float(mask_step), int(index_old), n_spec,
+                                              a.inp(ccf_raw, np.float64), int(bool(normalise)),
+                                              a.inp(g_ccf, np.float64), a.mem, op))
+        return out
+
+    def gauss_fit_adjoint(self, x, y, model, par, g_par, err=None):
+        """Gradient (n_spec x n) of a scalar w.r.t. the fitted CCFs y, given its gradient
+        g_par (n_spec x 5) w.r.t. the fit's par = (c, |k|, span, v0, fwhm); the span's
+        entry is ignored."""
+        a = self._args(y, x)
+        n_spec, n = int(y.shape[0]), int(x.shape[0])
+        out, op = a.out((n_spec, n), np.float64)
+        self._check(self.L.soapgb_gauss_fit_adjoint(self.h, n_spec, n, a.inp(x, np.float64), a.inp(y, np.float64),
+                                                    a.inp(err, np.float64), a.inp(model, np.float64),
+                                                    a.inp(par, np.float64), a.inp(g_par, np.float64), a.mem, op))
+        return out
+
     # -- a17-a18 ----------------------------------------------------------------
     def gauss_bis(self, x, y, err=None):
         a = self._args(y, x)

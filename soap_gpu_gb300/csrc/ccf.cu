@@ -218,6 +218,25 @@ __global__ void __launch_bounds__(256) k_ccf_dot(int n_w, const int *__restrict_
     }
 }
 
+// the apodisation window of run_all_SOAP.py:306-311 at velocity index i
+__device__ __forceinline__ double ccf_apod(int i, int n_v) {
+    const int nb_zeros = 5;
+    const int period = (int)((n_v - 1) / 2.);
+    const int len_app = (int)(period / 2.);
+    const int n_ones = n_v - period - 2 * nb_zeros;
+    if (i < nb_zeros) return 0.0;
+    if (i < nb_zeros + len_app) {
+        int a = i - nb_zeros;
+        return 0.5 * cos(2 * SOAP_PI / period * a - SOAP_PI) + 0.5;
+    }
+    if (i < nb_zeros + len_app + n_ones) return 1.0;
+    if (i < nb_zeros + 2 * len_app + n_ones) {
+        int a = len_app - 1 - (i - nb_zeros - len_app - n_ones);
+        return 0.5 * cos(2 * SOAP_PI / period * a - SOAP_PI) + 0.5;
+    }
+    return 0.0;
+}
+
 // normalise by the max and apodise, run_all_SOAP.py:299-314,369-370
 __global__ void k_ccf_normalise(int n_spec, int n_v, double *ccf) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,23 +244,9 @@ __global__ void k_ccf_normalise(int n_spec, int n_v, double *ccf) {
     double *c = ccf + (long long)s * n_v;
     double mx = c[0];
     for (int i = 1; i < n_v; ++i) mx = fmax(mx, c[i]);
-    int nb_zeros = 5;
-    int period = (int)((n_v - 1) / 2.);
-    int len_app = (int)(period / 2.);
-    int n_ones = n_v - period - 2 * nb_zeros;
     for (int i = 0; i < n_v; ++i) {
-        double app;
-        if (i < nb_zeros) app = 0.0;
-        else if (i < nb_zeros + len_app) {
-            int a = i - nb_zeros;
-            app = 0.5 * cos(2 * SOAP_PI / period * a - SOAP_PI) + 0.5;
-        } else if (i < nb_zeros + len_app + n_ones) app = 1.0;
-        else if (i < nb_zeros + 2 * len_app + n_ones) {
-            int a = len_app - 1 - (i - nb_zeros - len_app - n_ones);
-            app = 0.5 * cos(2 * SOAP_PI / period * a - SOAP_PI) + 0.5;
-        } else app = 0.0;
         double v = c[i] / mx;
-        c[i] = 1 - ((-v + 1) * app);
+        c[i] = 1 - ((-v + 1) * ccf_apod(i, n_v));
     }
 }
 
@@ -359,6 +364,156 @@ extern "C" int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel,
     if (rc) return set_error(ctx, rc, "soapgb_ccf: a mask hole reaches past the extended wavelength grid");
     if (host) {
         SOAP_CUDA(ctx, cudaMemcpyAsync(ccf_out, d_out, sizeof(double) * (size_t)n_v * n_spec, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return SOAPGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the CCF (the differentiable form; the reference has no gradient path).
+// The raw CCF is linear in the spectra, ccf[s, v] = sum_p M[v, p] spec[s, p], so its
+// adjoint is grad[s, p] = sum_v M[v, p] g[s, v].  Each (velocity, pixel) has one
+// owner line in the mask (the forward's owner map), so one thread per pixel walks
+// the velocities in order and recomputes its mask value: no transpose, no atomics.
+// The normalisation out_i = 1 - (1 - c_i / mx) app_i (mx the max, first index at
+// ties) contributes dL/dc_i = app_i G_i / mx - [i = i_mx] sum_j G_j app_j c_j / mx^2.
+// ---------------------------------------------------------------------------
+__global__ void k_ccf_norm_adj(int n_spec, int n_v, const double *__restrict__ raw, const double *__restrict__ g,
+                               double *__restrict__ gc) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_spec) return;
+    const double *c = raw + (long long)s * n_v;
+    const double *gs = g + (long long)s * n_v;
+    double *o = gc + (long long)s * n_v;
+    double mx = c[0];
+    int imx = 0;
+    for (int i = 1; i < n_v; ++i)
+        if (c[i] > mx) { mx = c[i]; imx = i; }
+    double S = 0.0;
+    for (int i = 0; i < n_v; ++i) {
+        const double app = ccf_apod(i, n_v);
+        S = fma(gs[i] * app, c[i], S);
+        o[i] = app * gs[i] / mx;
+    }
+    o[imx] -= S / (mx * mx);
+}
+
+template <int SB>
+__global__ void __launch_bounds__(256) k_ccf_adj(CcfGeom g, const double *__restrict__ wt,
+                                                 const double *__restrict__ vel, const double *__restrict__ lw,
+                                                 const double *__restrict__ lwt, int n_v,
+                                                 const int *__restrict__ owner, int n_spec,
+                                                 const double *__restrict__ gc, double *__restrict__ grad) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= g.n_w) return;
+    const int s0 = blockIdx.y * SB;
+    const int nsb = min(SB, n_spec - s0);
+    double acc[SB];
+#pragma unroll
+    for (int q = 0; q < SB; ++q) acc[q] = 0.0;
+    for (int iv = 0; iv < n_v; ++iv) {
+        const int sq = owner[(long long)iv * g.n_w + p];
+        if (sq < 0) continue;
+        const int l = sq / 3, kind = sq % 3;
+        const LineWin r = ccf_line(g, wt, vel[iv], lw[l], lwt[l]);
+        const double m = kind == 0 ? r.w : (kind == 1 ? __dmul_rn(r.w, r.frb) : __dmul_rn(r.w, r.fra));
+#pragma unroll
+        for (int q = 0; q < SB; ++q)
+            if (q < nsb) acc[q] = fma(m, gc[(long long)(s0 + q) * n_v + iv], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+        if (q < nsb) grad[(long long)(s0 + q) * g.n_w + p] = acc[q];
+}
+
+extern "C" int soapgb_ccf_adjoint(soapgb_ctx *ctx, int n_v, const double *vel, int n_lines,
+                                  const double *line_wave, const double *line_weight, int n_w,
+                                  const double *wave_trim, double step_size, double wave_extend, double mask_step,
+                                  int index_old, int n_spec, const double *ccf_raw, int normalise,
+                                  const double *g_ccf, int mem, double *grad_spectra) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    if (n_v < 1 || n_lines < 0 || n_w < 2 || n_spec < 0 || !vel || !wave_trim || !g_ccf || !grad_spectra ||
+        (n_lines > 0 && (!line_wave || !line_weight)) || (normalise && n_spec > 0 && !ccf_raw) ||
+        !(step_size > 0) || !(mask_step > 0))
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_ccf_adjoint: bad arguments");
+    if (n_spec == 0) return SOAPGB_OK;
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int np_ext = (int)(wave_extend / step_size);
+    const long long n_ext = (long long)n_w + 2LL * np_ext;
+    if (n_ext - 2LL * index_old != n_w)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_ccf_adjoint: mask slice does not give %d points", n_w);
+    const bool host = (mem == SOAPGB_HOST);
+    double w_first, w_last;
+    if (host) {
+        w_first = wave_trim[0];
+        w_last = wave_trim[n_w - 1];
+    } else {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(&w_first, wave_trim, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaMemcpyAsync(&w_last, wave_trim + n_w - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    if (!(w_last > w_first)) return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_ccf_adjoint: wavelengths must ascend");
+    CcfGeom g;
+    g.np_ext = np_ext;
+    g.n_ext = (int)n_ext;
+    g.n_w = n_w;
+    g.index_old = index_old;
+    g.mask_step = mask_step;
+    g.start_b = w_first - step_size * np_ext;
+    g.stop_b = w_first;
+    g.start_a = w_last;
+    g.stop_a = w_last + step_size * np_ext;
+    g.begin_wave = std::min(g.start_b, w_first);
+    const double beta = 820. / SOAP_C_LIGHT;
+    g.k_hw = sqrt((1 + beta) / (1 - beta)) - 1;
+    const long long nt = (long long)n_lines * n_v;
+    const size_t vs_b = sizeof(double) * (size_t)n_v * n_spec, ws_b = sizeof(double) * (size_t)n_w * n_spec;
+    Workspace ws(ctx);
+    int s_vel = ws.add(host ? sizeof(double) * n_v : 0);
+    int s_lw = ws.add(host ? sizeof(double) * (n_lines > 0 ? n_lines : 1) : 0);
+    int s_lwt = ws.add(host ? sizeof(double) * (n_lines > 0 ? n_lines : 1) : 0);
+    int s_wt = ws.add(host ? sizeof(double) * n_w : 0);
+    int s_raw = ws.add(host && normalise ? vs_b : 0);
+    int s_g = ws.add(host ? vs_b : 0);
+    int s_out = ws.add(host ? ws_b : 0);
+    int s_gc = ws.add(normalise ? vs_b : 0);
+    int s_owner = ws.add(sizeof(int) * (size_t)n_w * n_v);
+    int rc = ws.commit();
+    if (rc) return rc;
+#define STAGE(dst, src, bytes, slot)                                                  \
+    dst = (const double *)stage_in(ctx, mem, src, bytes, ws.get<void>(slot), &rc);   \
+    if (rc) return rc;
+    const double *d_vel, *d_lw, *d_lwt, *d_wt, *d_raw, *d_g;
+    STAGE(d_vel, vel, sizeof(double) * n_v, s_vel);
+    STAGE(d_lw, line_wave, sizeof(double) * n_lines, s_lw);
+    STAGE(d_lwt, line_weight, sizeof(double) * n_lines, s_lwt);
+    STAGE(d_wt, wave_trim, sizeof(double) * n_w, s_wt);
+    STAGE(d_raw, normalise ? ccf_raw : nullptr, normalise ? vs_b : 0, s_raw);
+    STAGE(d_g, g_ccf, vs_b, s_g);
+#undef STAGE
+    double *d_out = host ? ws.get<double>(s_out) : grad_spectra;
+    int *owner = ws.get<int>(s_owner);
+    SOAP_CUDA(ctx, cudaMemsetAsync(owner, 0xff, sizeof(int) * (size_t)n_w * n_v, ctx->stream));   // -1
+    if (nt > 0) {
+        k_ccf_owner<<<grid_for(ctx, nt, 256), 256, 0, ctx->stream>>>(g, d_wt, d_vel, d_lw, d_lwt, n_lines, n_v, owner,
+                                                                     ctx->d_status);
+        SOAP_LAUNCHED(ctx);
+    }
+    const double *gc = d_g;
+    if (normalise) {
+        double *t = ws.get<double>(s_gc);
+        k_ccf_norm_adj<<<(n_spec + 63) / 64, 64, 0, ctx->stream>>>(n_spec, n_v, d_raw, d_g, t);
+        SOAP_LAUNCHED(ctx);
+        gc = t;
+    }
+    SOAP_TRACED(ctx, "ccf_adjoint",
+                (k_ccf_adj<8><<<dim3(grid_for(ctx, n_w, 256), (n_spec + 7) / 8), 256, 0, ctx->stream>>>(
+                    g, d_wt, d_vel, d_lw, d_lwt, n_v, owner, n_spec, gc, d_out)));
+    SOAP_LAUNCHED(ctx);
+    rc = check_status(ctx, "soapgb_ccf_adjoint");
+    if (rc) return set_error(ctx, rc, "soapgb_ccf_adjoint: a mask hole reaches past the extended wavelength grid");
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_spectra, d_out, ws_b, cudaMemcpyDeviceToHost, ctx->stream));
         SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return SOAPGB_OK;

@@ -313,3 +313,160 @@ extern "C" int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double
     }
     return host ? check_status(ctx, "soapgb_gauss_bis") : SOAPGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint of the Gaussian fit (the differentiable form; the reference has no
+// gradient path).  At the fitted optimum theta = (c, k, x0, fwhm) of
+// Phi = sum_i f_i^2, f_i = (G(x_i; theta) - y_i) / err_i, the stationarity condition
+// sum_i f_i df_i/dtheta = 0 gives, by the implicit function theorem,
+//   H dtheta/dy_j = grad G_j / err_j^2,   H = sum_i (J_i J_i^T + f_i Hess f_i)
+// so dL/dy_j = (grad G_j . z) / err_j^2 with H z = dL/dtheta.  The second derivatives
+// of G = c + k e, e = exp(-d^2 / 2 s^2), d = x - x0, s = a fwhm, a = 1 / (2 sqrt(2 ln 2)):
+//   G_k,x0 = e d / s^2          G_k,fwhm = a e d^2 / s^3
+//   G_x0,x0 = k e (d^2 / s^4 - 1 / s^2)
+//   G_x0,fwhm = a k e d (d^2 / s^5 - 2 / s^3)
+//   G_fwhm,fwhm = a^2 k e d^2 (d^2 / s^6 - 3 / s^4)   (all c terms vanish).
+// The fitted outputs give c, |k|, v0 = x0 + x[0] and fwhm; the sign of k is that of
+// the model's largest excursion from c.  One warp per spectrum, fixed reduction order.
+// ---------------------------------------------------------------------------
+// 4x4 solve by Gaussian elimination with partial pivoting; false when singular
+__device__ bool solve4(double *A, double *b, double *z) {
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (fabs(A[r * 4 + c]) > fabs(A[piv * 4 + c])) piv = r;
+        if (!(fabs(A[piv * 4 + c]) > 0.0)) return false;
+        if (piv != c) {
+            for (int q = 0; q < 4; ++q) { double t = A[c * 4 + q]; A[c * 4 + q] = A[piv * 4 + q]; A[piv * 4 + q] = t; }
+            double t = b[c]; b[c] = b[piv]; b[piv] = t;
+        }
+        for (int r = c + 1; r < 4; ++r) {
+            double f = A[r * 4 + c] / A[c * 4 + c];
+            for (int q = c; q < 4; ++q) A[r * 4 + q] -= f * A[c * 4 + q];
+            b[r] -= f * b[c];
+        }
+    }
+    for (int r = 3; r >= 0; --r) {
+        double t = b[r];
+        for (int q = r + 1; q < 4; ++q) t -= A[r * 4 + q] * z[q];
+        z[r] = t / A[r * 4 + r];
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(32 * FIT_WARPS) k_gauss_fit_adj(int n_spec, int n, const double *__restrict__ x,
+                                                                  const double *__restrict__ yall,
+                                                                  const double *__restrict__ errall,
+                                                                  const double *__restrict__ model,
+                                                                  const double *__restrict__ par,
+                                                                  const double *__restrict__ gpar,
+                                                                  double *__restrict__ grad_y, int *status) {
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * FIT_WARPS + (threadIdx.x >> 5);
+    if (s >= n_spec) return;
+    const double *y = yall + (long long)s * n;
+    const double *err = errall ? errall + (long long)s * n : nullptr;
+    const double *mo = model + (long long)s * n;
+    const double *pp = par + (long long)s * 5;
+    const double *gp = gpar + (long long)s * 5;
+    double *gy = grad_y + (long long)s * n;
+    const double c = pp[0], v0 = pp[3], fwhm = pp[4];
+    // sign of k: the model's largest excursion from c (first index at ties)
+    double best = -1.0, sgn = 1.0;
+    int bi = n;
+    for (int i = lane; i < n; i += 32) {
+        const double e = fabs(mo[i] - c);
+        if (e > best) { best = e; bi = i; sgn = (mo[i] - c) >= 0.0 ? 1.0 : -1.0; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        const double os = __shfl_xor_sync(0xffffffffu, sgn, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; sgn = os; }
+    }
+    const double k = sgn * pp[1];
+    const double a = gauss_sigma(1.0);
+    const double sg = gauss_sigma(fwhm);
+    const double s2 = sg * sg, s3 = s2 * sg, s4 = s2 * s2;
+    double H[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) H[q] = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        const double inv = 1.0 / (err ? err[i] : 1.0);
+        const double d = x[i] - v0, d2 = d * d;
+        const double e = exp(-d2 / 2 / s2);
+        const double f = (c + k * e - y[i]) * inv;
+        const double G[4] = {1.0, e, k * e * d / s2, k * e * d2 * a / s3};
+        double S[10];   // second derivatives, upper triangle row-major
+        S[0] = 0.0; S[1] = 0.0; S[2] = 0.0; S[3] = 0.0;
+        S[4] = 0.0;
+        S[5] = e * d / s2;
+        S[6] = a * e * d2 / s3;
+        S[7] = k * e * (d2 / s4 - 1.0 / s2);
+        S[8] = a * k * e * d * (d2 / (s4 * sg) - 2.0 / s3);
+        S[9] = a * a * k * e * d2 * (d2 / (s4 * s2) - 3.0 / s4);
+        int t = 0;
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = p; q < 4; ++q, ++t) H[t] += inv * inv * G[p] * G[q] + f * inv * S[t];
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) H[q] = warp_sum(H[q]);
+    double A[16], b[4] = {gp[0], gp[1] * sgn, gp[3], gp[4]}, z[4] = {0, 0, 0, 0};
+    {
+        int t = 0;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p; q < 4; ++q, ++t) { A[p * 4 + q] = H[t]; A[q * 4 + p] = H[t]; }
+    }
+    if (!solve4(A, b, z)) {
+        if (lane == 0) atomicExch(status, SOAPGB_ST_FIT_SINGULAR);
+        for (int q = 0; q < 4; ++q) z[q] = 0.0;
+    }
+    for (int i = lane; i < n; i += 32) {
+        const double inv = 1.0 / (err ? err[i] : 1.0);
+        const double d = x[i] - v0, d2 = d * d;
+        const double e = exp(-d2 / 2 / s2);
+        gy[i] = inv * inv * (z[0] + e * z[1] + (k * e * d / s2) * z[2] + (k * e * d2 * a / s3) * z[3]);
+    }
+}
+
+extern "C" int soapgb_gauss_fit_adjoint(soapgb_ctx *ctx, int n_spec, int n, const double *x, const double *y,
+                                        const double *err, const double *model, const double *par,
+                                        const double *g_par, int mem, double *grad_y) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    if (n_spec < 0 || n < 8 || !x || !y || !model || !par || !g_par || !grad_y)
+        return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_gauss_fit_adjoint: bad arguments");
+    if (n_spec == 0) return SOAPGB_OK;
+    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bool host = (mem == SOAPGB_HOST);
+    const size_t sb = sizeof(double) * (size_t)n * n_spec, pb = sizeof(double) * 5 * (size_t)n_spec;
+    Workspace ws(ctx);
+    int s_x = ws.add(host ? sizeof(double) * n : 0);
+    int s_y = ws.add(host ? sb : 0), s_e = ws.add(host && err ? sb : 0), s_m = ws.add(host ? sb : 0);
+    int s_p = ws.add(host ? pb : 0), s_g = ws.add(host ? pb : 0), s_o = ws.add(host ? sb : 0);
+    int rc = ws.commit();
+    if (rc) return rc;
+#define STAGE(dst, src, bytes, slot)                                                  \
+    dst = (const double *)stage_in(ctx, mem, src, bytes, ws.get<void>(slot), &rc);   \
+    if (rc) return rc;
+    const double *d_x, *d_y, *d_e, *d_m, *d_p, *d_g;
+    STAGE(d_x, x, sizeof(double) * n, s_x);
+    STAGE(d_y, y, sb, s_y);
+    STAGE(d_e, err, err ? sb : 0, s_e);
+    STAGE(d_m, model, sb, s_m);
+    STAGE(d_p, par, pb, s_p);
+    STAGE(d_g, g_par, pb, s_g);
+#undef STAGE
+    double *d_o = host ? ws.get<double>(s_o) : grad_y;
+    SOAP_TRACED(ctx, "gauss_fit_adjoint",
+                k_gauss_fit_adj<<<(n_spec + FIT_WARPS - 1) / FIT_WARPS, 32 * FIT_WARPS, 0, ctx->stream>>>(
+                    n_spec, n, d_x, d_y, d_e, d_m, d_p, d_g, d_o, ctx->d_status));
+    SOAP_LAUNCHED(ctx);
+    if (host) {
+        SOAP_CUDA(ctx, cudaMemcpyAsync(grad_y, d_o, sb, cudaMemcpyDeviceToHost, ctx->stream));
+        SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return check_status(ctx, "soapgb_gauss_fit_adjoint");
+    }
+    return SOAPGB_OK;
+}

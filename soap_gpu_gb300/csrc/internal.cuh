@@ -103,6 +103,7 @@ const void *stage_in(soapgb_ctx *ctx, int mem, const void *p, size_t bytes, void
 int check_status(soapgb_ctx *ctx, const char *what);
 // device status word: a cached wavelength edge value no longer matches the array
 constexpr int SOAPGB_ST_EDGES = 51;
+constexpr int SOAPGB_ST_FIT_SINGULAR = 61;   // the fit adjoint met a singular 4x4 system
 // true for memory the host can read directly (pageable or page-locked host memory)
 bool host_readable(const void *p);
 // copy a small descriptor array to the host: directly from host memory, or from device

@@ -22,7 +22,10 @@ identity.
 ``LowerResolution`` continues the chain through the resolution step
 (SOAP_resolution.cu:216-310, PLAIN64): the Gaussian convolution and the min/max
 normalisation of base - spec, by the hand-written adjoint of
-``soapgb_lower_resolution_adjoint``.
+``soapgb_lower_resolution_adjoint``.  ``NormalisedCcf`` (CCF_func.py:5-91) and
+``GaussFit`` (BIS_FIT2.cpp:97-192) carry it to the RV: the mask CCF's transpose
+(``soapgb_ccf_adjoint``) and the fit's implicit derivative at its optimum
+(``soapgb_gauss_fit_adjoint``), so a loss on an RV curve reaches u1, u2 and vsini.
 
 Region positions and sizes stay discrete (cell coverage), as in the reference; the
 inclination and the region contrast are not differentiated yet.
@@ -168,3 +171,76 @@ def lower_resolution(spec, base, setup: ResolutionSetup):
     """Differentiable (n_spec, n_eff) normalised low-resolution spectra of
     base - spec[s]; see ``LowerResolution``."""
     return LowerResolution.apply(spec, base, setup)
+
+
+@dataclasses.dataclass
+class CcfSetup:
+    """The fixed arguments of the mask CCF (CCF_func.py:5-91, run_all_SOAP.py:292-314)
+    and the Gaussian fit (BIS_FIT2.cpp:97-192): velocities, mask lines, the trimmed
+    wavelengths (device, float64) and the grid step."""
+    ctx: Context
+    vel: torch.Tensor
+    line_wave: torch.Tensor
+    line_weight: torch.Tensor
+    wave_trim: torch.Tensor
+    step: float
+    wave_extend: float = 100.0
+    mask_step: float = 0.005
+    index_old: int = 20000
+
+    def kwargs(self) -> dict:
+        return dict(wave_extend=self.wave_extend, mask_step=self.mask_step, index_old=self.index_old)
+
+
+class NormalisedCcf(torch.autograd.Function):
+    """ccf[s] = the normalised, apodised mask CCF of spectra[s] (``soapgb_ccf``, FP64);
+    backward: ``soapgb_ccf_adjoint`` (the mask's transpose, the max at its first index)."""
+
+    @staticmethod
+    def forward(fctx, spectra, setup: CcfSetup):
+        sp = spectra.detach().contiguous()
+        c = setup.ctx
+        args = (setup.vel, setup.line_wave, setup.line_weight, setup.wave_trim, setup.step, sp)
+        raw = c.ccf("plain64", *args, normalise=False, **setup.kwargs())
+        out = c.ccf("plain64", *args, normalise=True, **setup.kwargs())
+        fctx.setup, fctx.raw = setup, raw
+        return out
+
+    @staticmethod
+    def backward(fctx, g):
+        s = fctx.setup
+        grad = s.ctx.ccf_adjoint(s.vel, s.line_wave, s.line_weight, s.wave_trim, s.step,
+                                 g.to(torch.float64).contiguous(), ccf_raw=fctx.raw, normalise=True, **s.kwargs())
+        return grad, None
+
+
+class GaussFit(torch.autograd.Function):
+    """(c, |k|, v0, fwhm) of the Gaussian fit of each CCF (``soapgb_gauss_bis``);
+    backward: ``soapgb_gauss_fit_adjoint`` (implicit function theorem at the optimum
+    with the full Hessian).  The bisector span is not differentiated."""
+
+    @staticmethod
+    def forward(fctx, ccf, setup: CcfSetup):
+        y = ccf.detach().contiguous()
+        res = setup.ctx.gauss_bis(setup.vel, y)
+        if bool((res["iters"] < 0).any()):
+            raise RuntimeError("Gaussian fit did not converge; its gradient is undefined")
+        fctx.setup, fctx.y, fctx.model, fctx.par = setup, y, res["model"], res["par"]
+        return res["par"][:, [0, 1, 3, 4]].clone()
+
+    @staticmethod
+    def backward(fctx, g):
+        gp = torch.zeros_like(fctx.par)
+        gp[:, [0, 1, 3, 4]] = g.to(torch.float64)
+        s = fctx.setup
+        return s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, gp), None
+
+
+def normalised_ccf(spectra, setup: CcfSetup):
+    """Differentiable (n_spec, n_v) normalised CCFs; see ``NormalisedCcf``."""
+    return NormalisedCcf.apply(spectra, setup)
+
+
+def gauss_fit(ccf, setup: CcfSetup):
+    """Differentiable (n_spec, 4) fit parameters (c, |k|, v0, fwhm); see ``GaussFit``."""
+    return GaussFit.apply(ccf, setup)
