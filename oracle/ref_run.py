@@ -5,8 +5,8 @@ executables of this repository on the same synthetic inputs, through the same ar
 contract run_all_SOAP.py uses (run_all_SOAP.py:160-250), and compares every file
 they write.  Usage (on a GPU host, after ``__graft_entry__.build()``):
 
-    python -m oracle.ref_run --case 0 --out gpurun_out/ref_case0
-    python -m oracle.ref_run --case 1 --phases 10 --rot-step 0.1 --out gpurun_out/ref_case1
+    python -m oracle.ref_run --case 0 --out ref_out/case0
+    python -m oracle.ref_run --case 1 --phases 10 --rot-step 0.1 --out ref_out/case1
 
 Writes ``summary.json`` under --out with the per-file differences and the wall time
 of every stage of every implementation.
@@ -174,7 +174,7 @@ def main():
     ap.add_argument("--case", type=int, default=0)
     ap.add_argument("--phases", type=int, default=None)
     ap.add_argument("--rot-step", type=float, default=None)
-    ap.add_argument("--out", default="gpurun_out/ref_run")
+    ap.add_argument("--out", default="ref_out/run")
     ap.add_argument("--work", default="/tmp/soap_ref_run")
     ap.add_argument("--only-time", action="store_true")
     ap.add_argument("--impls", default="patched,asis,plain64,fast32")
