@@ -16,7 +16,9 @@
  *    and n_eff = floor(n / 512) * 512 the number of pixels the reference processes
  *    and writes (it launches n/512 blocks of 512 threads).
  *  - One context = one device + one CUDA stream; a context must not be used from
- *    two host threads at once.
+ *    two host threads at once.  Each call makes the context's device current while
+ *    it runs and gives the calling thread its previous current device back before it
+ *    returns.
  *
  * Each function names the reference code it replaces (paths relative to the
  * reference's SOAP_code/ directory).  The reference exposes these steps as
@@ -311,12 +313,17 @@ int soapgb_bisector_inject(soapgb_ctx *ctx, int mode, int n, int n_mu, int n_coe
  * device-wide synchronisation of cudaMalloc / cudaFree.  Its scratch is a fixed
  * SOAPGB_NOALLOC_SCRATCH_BYTES array in the library's device image, held by every
  * GPU that loads the library until the process exits; soapgb_noalloc_capacity(n_eff)
- * gives how many spectra of n_eff pixels fit in one call, and larger requests are
- * rejected with SOAPGB_ERR_ARG.  All array arguments are device pointers.  The
- * first call on a device looks up the array's device address (a
- * cudaGetSymbolAddress call with that device current); make that first call before
- * any stream capture.  Calls share the array: two calls whose work overlaps on the
- * GPU (different streams or contexts on one device) race on it. */
+ * gives how many spectra of n_eff pixels fit in one call (a call with exactly that
+ * many is accepted), and larger requests are rejected with SOAPGB_ERR_ARG.  All
+ * array arguments are device pointers.  The first call on a device looks up the
+ * array's device address (a cudaGetSymbolAddress call with that device current), and
+ * the first call of a context with a given wavelength array reads wave[0], wave[1]
+ * and wave[n_eff - 1] back to the host, which synchronises the context's stream;
+ * later calls with the same array do not synchronise (a one-thread kernel confirms
+ * the kept values, and soapgb_synchronize reports status 51 if the array changed).
+ * Make those first calls before any stream capture.  Calls share the array: two
+ * calls whose work overlaps on the GPU (different streams or contexts on one
+ * device) race on it. */
 #define SOAPGB_NOALLOC_SCRATCH_BYTES (8 * 1024 * 1024)
 size_t soapgb_noalloc_capacity(int n_eff);
 int soapgb_lower_resolution_noalloc(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *wave,

@@ -19,9 +19,9 @@ SOAP_integration_solar.cu, SOAP_resolution.cu) for sm_103a, in two variants, int
   and the bounding box is clamped to the grid before the host scan.
   The -60000 max sentinel and the 0.005 A literals are left as written.
 
-Sources are copied from the reference checkout (``SOAP_GPU_REF`` or the default
-location) into ``oracle/_ref/src``; where the checkout is absent (the GPU host) the
-staged copies are compiled.  The binaries are the oracle's "reference" mode: only
+Sources are copied from the reference checkout (the ``SOAP_code`` directory named by
+the argument or by ``SOAP_GPU_REF``) into ``oracle/_ref/src``; where no checkout is
+given or present (the GPU host) the staged copies are compiled.  The binaries are the oracle's "reference" mode: only
 tests and the parity scripts run them.
 """
 from __future__ import annotations
@@ -36,7 +36,6 @@ REF_DIR = os.path.join(HERE, "_ref")
 SRC = os.path.join(REF_DIR, "src")
 BIN = os.path.join(REF_DIR, "bin")
 NAMES = ["SOAP_initialize", "SOAP_integration", "SOAP_integration_solar", "SOAP_resolution"]
-DEFAULT_CHECKOUT = "/root/reference/SOAP_code"
 
 # --- P4 + P2: the interval-owning interpolation (replaces fast_interp_new's body) --
 INTERP_PATCHED = r'''__global__ void fast_interp_new(double *lambda, double *lambda_shift, double *spectrum, double *spec_grad, double *spectrum_out, double delta, double limb, double step_size, int offset){
@@ -150,8 +149,8 @@ def patch(name, text):
 
 def stage(checkout=None) -> bool:
     """Copy the reference sources next to the build (asis + patched)."""
-    checkout = checkout or os.environ.get("SOAP_GPU_REF", DEFAULT_CHECKOUT)
-    if not os.path.isdir(checkout):
+    checkout = checkout or os.environ.get("SOAP_GPU_REF")
+    if not checkout or not os.path.isdir(checkout):
         return os.path.isdir(os.path.join(SRC, "asis"))
     for variant in ("asis", "patched"):
         os.makedirs(os.path.join(SRC, variant), exist_ok=True)
@@ -195,4 +194,6 @@ def build(quiet: bool = True, checkout=None) -> bool:
 
 
 if __name__ == "__main__":
-    print("built" if build(quiet=False) else "reference sources not available")
+    import sys
+    print("built" if build(quiet=False, checkout=sys.argv[1] if len(sys.argv) > 1 else None)
+          else "reference sources not available (pass the SOAP_code directory or set SOAP_GPU_REF)")

@@ -135,7 +135,7 @@ extern "C" int soapgb_bisector_inject(soapgb_ctx *ctx, int mode, int n, int n_mu
     if (mode == SOAPGB_BIS_ACTIVE && (!coeffs_low || !dep_cut || !vcut || !vshift))
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_bisector_inject: the active form needs coeffs_low, "
                                               "dep_cut, vcut and vshift");
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     const bool host = (mem == SOAPGB_HOST);
     const bool act = (mode == SOAPGB_BIS_ACTIVE);
     const size_t cube = sizeof(double) * (size_t)n * n_mu, row = sizeof(double) * (size_t)n;

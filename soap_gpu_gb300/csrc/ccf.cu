@@ -267,7 +267,7 @@ extern "C" int soapgb_ccf(soapgb_ctx *ctx, int form, int n_v, const double *vel,
                              "(n_v-1)/2 even and n_v >= 21 (n_v = %d)", n_v);
     }
     if (n_spec == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     int np_ext = (int)(wave_extend / step_size);
     long long n_ext = (long long)n_w + 2LL * np_ext;
     if (n_ext - 2LL * index_old != n_w)
@@ -436,8 +436,16 @@ extern "C" int soapgb_ccf_adjoint(soapgb_ctx *ctx, int n_v, const double *vel, i
         (n_lines > 0 && (!line_wave || !line_weight)) || (normalise && n_spec > 0 && !ccf_raw) ||
         !(step_size > 0) || !(mask_step > 0))
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_ccf_adjoint: bad arguments");
+    if (normalise) {
+        // the forward's apodisation window (run_all_SOAP.py:306-311) exists only for these n_v
+        int period = (int)((n_v - 1) / 2.), len_app = (int)(period / 2.);
+        if (n_v < 21 || 2 * len_app != period)
+            return set_error(ctx, SOAPGB_ERR_ARG,
+                             "soapgb_ccf_adjoint: the apodisation window of run_all_SOAP.py:306-311 needs "
+                             "(n_v-1)/2 even and n_v >= 21 (n_v = %d)", n_v);
+    }
     if (n_spec == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     const int np_ext = (int)(wave_extend / step_size);
     const long long n_ext = (long long)n_w + 2LL * np_ext;
     if (n_ext - 2LL * index_old != n_w)

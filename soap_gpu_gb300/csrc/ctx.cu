@@ -212,7 +212,8 @@ int soapgb_ctx_create(int device, soapgb_ctx **out) {
     *out = nullptr;
     soapgb_ctx *ctx = new soapgb_ctx();
     ctx->device = device;
-    cudaError_t e = cudaSetDevice(device);
+    soapgb::DeviceGuard guard(device);
+    cudaError_t e = guard.err;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
@@ -242,7 +243,7 @@ int soapgb_trace_enable(soapgb_ctx *ctx, int on) {
 
 int soapgb_trace_report(soapgb_ctx *ctx, char *buf, size_t len) {
     if (!ctx || !buf || len == 0) return SOAPGB_ERR_ARG;
-    cudaSetDevice(ctx->device);
+    SOAP_DEVICE(ctx);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_check(ctx, e, "soapgb_trace_report");
     // aggregate by name, in first-seen order
@@ -280,7 +281,8 @@ int soapgb_trace_report(soapgb_ctx *ctx, char *buf, size_t len) {
 
 int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     if (!ctx) return SOAPGB_OK;
-    cudaSetDevice(ctx->device);
+    {
+    soapgb::DeviceGuard guard(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto &sp : ctx->spans) {
         cudaEventDestroy(sp.a);
@@ -316,6 +318,7 @@ int soapgb_ctx_destroy(soapgb_ctx *ctx) {
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    }
     delete ctx;
     return SOAPGB_OK;
 }
@@ -331,7 +334,7 @@ int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream) {
     if (next != ctx->stream && ctx->stream) {
         // every call's work ends on the context's stream and may still be queued there,
         // using the context's scratch: the new stream starts after it
-        SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+        SOAP_DEVICE(ctx);
         if (!ctx->switch_event)
             SOAP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->switch_event, cudaEventDisableTiming));
         SOAP_CUDA(ctx, cudaEventRecord(ctx->switch_event, ctx->stream));
@@ -343,6 +346,7 @@ int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream) {
 
 int soapgb_synchronize(soapgb_ctx *ctx) {
     if (!ctx) return SOAPGB_ERR_ARG;
+    SOAP_DEVICE(ctx);
     SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return check_status(ctx, "soapgb_synchronize");
 }

@@ -204,7 +204,7 @@ extern "C" int soapgb_disk_maps(soapgb_ctx *ctx, const soapgb_star *star, int n_
     if (!ctx || !star || !maps_out) return SOAPGB_ERR_ARG;
     if (star->grid <= 0 || star->grid > 20000 || n_mu < 1 || (n_mu > 1 && !mu_boundary))
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_disk_maps: bad grid %d / n_mu %d", star->grid, n_mu);
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     int G = star->grid;
     long long gm = (long long)G * G;
     std::vector<double> ov;
@@ -262,7 +262,7 @@ extern "C" int soapgb_quiet_disk(soapgb_ctx *ctx, int form, int n, int n_eff, co
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_quiet_disk: bad arguments (n=%d n_eff=%d)", n, n_eff);
     if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_quiet_disk: unknown form %d", form);
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     long long gm = (long long)grid * grid;
     bool host = (mem == SOAPGB_HOST);
     Workspace ws(ctx);

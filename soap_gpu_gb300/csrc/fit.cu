@@ -271,7 +271,7 @@ extern "C" int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double
     if (n_spec < 0 || n < 8 || !x || !y || !model || !par || !depth || !bis)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_gauss_bis: bad arguments");
     if (n_spec == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     bool host = (mem == SOAPGB_HOST);
     Workspace ws(ctx);
     int s_x = ws.add(host ? sizeof(double) * n : 0);
@@ -438,7 +438,7 @@ extern "C" int soapgb_gauss_fit_adjoint(soapgb_ctx *ctx, int n_spec, int n, cons
     if (n_spec < 0 || n < 8 || !x || !y || !model || !par || !g_par || !grad_y)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_gauss_fit_adjoint: bad arguments");
     if (n_spec == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     const bool host = (mem == SOAPGB_HOST);
     const size_t sb = sizeof(double) * (size_t)n * n_spec, pb = sizeof(double) * 5 * (size_t)n_spec;
     Workspace ws(ctx);

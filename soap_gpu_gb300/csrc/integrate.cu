@@ -563,7 +563,7 @@ extern "C" int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_ef
     if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_integrate: unknown form %d", form);
     if (n_phase == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     long long gm = (long long)grid * grid;
     int n_mu = cubes->n_mu;
     size_t cube_b = sizeof(double) * (size_t)n * n_mu;
@@ -662,7 +662,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         !cubes->spot_sed || !cubes->fac_sed || !g_flux || !g_bconv || !g_tot || !grad_q_norm || !grad_q_sed ||
         !grad_spot_norm || !grad_fac_norm || !grad_spot_sed || !grad_fac_sed || !grad_limb || !grad_delta)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_integrate_adjoint: bad arguments");
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     const long long gm = (long long)grid * grid;
     const int n_mu = cubes->n_mu;
     const size_t cube_b = sizeof(double) * (size_t)n * n_mu, row_b = sizeof(double) * (size_t)n;

@@ -76,6 +76,34 @@ int cuda_check(soapgb_ctx *ctx, cudaError_t e, const char *what);
         if (_e != cudaSuccess) return soapgb::cuda_check(ctx, _e, "kernel launch"); \
     } while (0)
 
+// Makes a context's device current for the duration of an entry point and gives the
+// caller's current device back when the entry point returns, so no call changes the
+// calling thread's device as a side effect.
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (prev != device) {
+            err = cudaSetDevice(device);
+            changed = (err == cudaSuccess && prev >= 0);
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+#define SOAP_DEVICE(ctx)                                                              \
+    soapgb::DeviceGuard _soap_device_guard((ctx)->device);                           \
+    if (_soap_device_guard.err != cudaSuccess)                                        \
+        return soapgb::cuda_check(ctx, _soap_device_guard.err, "cudaSetDevice")
+
 // Bump allocator over the context workspace.  Usage: plan sizes with add(),
 // then commit() (grows the workspace if needed), then take pointers with get().
 struct Workspace {

@@ -43,17 +43,20 @@ int scratch_address(soapgb_ctx *ctx, unsigned char **out) {
 }  // namespace
 
 extern "C" size_t soapgb_noalloc_capacity(int n_eff) {
-    // conv rows of n_eff doubles + two 64-bit words per spectrum, each region aligned
-    // to 256 bytes (see resolution_scratch_bytes)
+    // the largest spectrum count whose scratch, by the same byte count the call checks
+    // (the PLAIN64 scratch does not depend on n), fits in the array; the count grows
+    // with the spectra, so a bisection finds it
     if (n_eff <= 0) return 0;
-    size_t n = 0;
-    for (size_t s = 1;; ++s) {
-        size_t need = ((sizeof(double) * (size_t)n_eff * s + 255) & ~size_t(255)) +
-                      ((sizeof(unsigned long long) * 2 * s + 255) & ~size_t(255));
-        if (need > SOAPGB_NOALLOC_SCRATCH_BYTES) break;
-        n = s;
+    auto fits = [n_eff](size_t s) {
+        return resolution_scratch_bytes(SOAPGB_PLAIN64, n_eff, n_eff, (int)s) <= (size_t)SOAPGB_NOALLOC_SCRATCH_BYTES;
+    };
+    if (!fits(1)) return 0;
+    size_t lo = 1, hi = (size_t)SOAPGB_NOALLOC_SCRATCH_BYTES / sizeof(double) + 1;   // fits(lo), !fits(hi)
+    while (hi - lo > 1) {
+        size_t mid = lo + (hi - lo) / 2;
+        (fits(mid) ? lo : hi) = mid;
     }
-    return n;
+    return lo;
 }
 
 extern "C" int soapgb_lower_resolution_noalloc(soapgb_ctx *ctx, int n, int n_eff, int n_spec, const double *wave,
@@ -71,15 +74,17 @@ extern "C" int soapgb_lower_resolution_noalloc(soapgb_ctx *ctx, int n, int n_eff
                          "soapgb_lower_resolution_noalloc: %d spectra of %d pixels need %zu scratch bytes, more than "
                          "the fixed %d (at most %zu spectra of this length per call)",
                          n_spec, n_eff, need, (int)SOAPGB_NOALLOC_SCRATCH_BYTES, soapgb_noalloc_capacity(n_eff));
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     unsigned char *scratch = nullptr;
     int rc = scratch_address(ctx, &scratch);
     if (rc) return rc;
-    // the half width needs the first two wavelengths on the host
+    // the half width needs wave[0] and wave[1] on the host: they are read back (one
+    // synchronisation) the first time this context sees the array and kept, and later
+    // calls with the same array confirm them on the device instead (status 51 through
+    // soapgb_synchronize when the array has changed)
     double w3[3];
-    SOAP_CUDA(ctx, cudaMemcpyAsync(w3, wave, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SOAP_CUDA(ctx, cudaMemcpyAsync(w3 + 2, wave + n_eff - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    rc = wave_edges(ctx, SOAPGB_DEVICE, wave, n, n_eff, w3);
+    if (rc) return rc;
     int wid = conv_halfwidth(w3[0], w3[1], sigma_v, window);
     if (wid < 1 || 2 * wid + 2 >= n)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution_noalloc: half width %d invalid for n=%d", wid, n);

@@ -48,7 +48,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_pipeline: unknown form %d", form);
     if (n_phase == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     bool host = (mem == SOAPGB_HOST);
     int grid = star->grid;
     long long gm = (long long)grid * grid;

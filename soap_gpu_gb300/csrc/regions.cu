@@ -207,7 +207,7 @@ extern "C" int soapgb_phase_maps(soapgb_ctx *ctx, int grid, double incl, int n_p
     if (grid < 1 || grid > 20000 || n_phase < 0 || !phases || !reg_offsets || !temp || !bi)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_maps: bad arguments");
     if (n_phase == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     // bring the (small) phase / region description to the host
     std::vector<int> h_off(n_phase + 1);
     std::vector<double> h_ph(n_phase);

@@ -1548,7 +1548,7 @@ extern "C" int soapgb_lower_resolution(soapgb_ctx *ctx, int form, int n, int n_e
     if (form != SOAPGB_PLAIN64 && form != SOAPGB_FAST64 && form != SOAPGB_FAST32)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution: unknown form %d", form);
     if (n_spec == 0) return SOAPGB_OK;
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     bool host = (mem == SOAPGB_HOST);
     double w01[3];
     if (host) {
@@ -1711,7 +1711,7 @@ extern "C" int soapgb_lower_resolution_adjoint(soapgb_ctx *ctx, int n, int n_eff
     if (n < 3 || n_eff < 1 || n_eff > n || n_spec < 0 || !wave || !spec || !g_out || !grad_spec ||
         !(sigma_v > 0) || !(step_exp > 0) || (grad_base && !base))
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_lower_resolution_adjoint: bad arguments");
-    SOAP_CUDA(ctx, cudaSetDevice(ctx->device));
+    SOAP_DEVICE(ctx);
     const bool host = (mem == SOAPGB_HOST);
     if (n_spec == 0) {
         if (grad_base) {

@@ -233,7 +233,11 @@ class GaussFit(torch.autograd.Function):
         gp = torch.zeros_like(fctx.par)
         gp[:, [0, 1, 3, 4]] = g.to(torch.float64)
         s = fctx.setup
-        return s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, gp), None
+        gy = s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, gp)
+        # a singular system gives a zero gradient and a device status: raise here, as the
+        # forward does for a fit that did not converge, rather than return that zero
+        s.ctx.synchronize()
+        return gy, None
 
 
 def normalised_ccf(spectra, setup: CcfSetup):

@@ -117,4 +117,7 @@ def main(src_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/SOAP_code")
+    checkout = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SOAP_GPU_REF")
+    if not checkout:
+        sys.exit("usage: %s <reference SOAP_code directory>  (or set SOAP_GPU_REF)" % sys.argv[0])
+    main(checkout)

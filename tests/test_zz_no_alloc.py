@@ -5,9 +5,10 @@ allocate device memory (their device memory is owned by another allocator, or a
 cudaMalloc / cudaFree pair would stall a latency-bound loop).  It keeps its scratch
 in a fixed array inside the library; these tests check that two consecutive calls
 give the same result as the allocating soapgb_lower_resolution (same PLAIN64
-arithmetic: the tolerance of the PLAIN64 parity tests), and that a request larger
-than the array is refused.  This file is collected last so that a failure here
-never hides another test's result.
+arithmetic: the tolerance of the PLAIN64 parity tests), that a request of exactly
+soapgb_noalloc_capacity(n_eff) spectra is accepted and one more is refused, and that
+the call leaves the calling thread's current device as it found it.  This file is
+collected last so that a failure here never hides another test's result.
 """
 import ctypes
 
@@ -83,3 +84,33 @@ def test_noalloc_rejects_requests_beyond_its_array():
                                                0.005, 0.005, -60000.0, _ptr(out), None)
         assert rc == _lib.ERR_ARG
         assert "scratch" in L.soapgb_last_error(ctx.h).decode()
+
+
+@pytest.mark.parametrize("n_eff", [1000, 4096, 20480])
+def test_noalloc_accepts_exactly_its_capacity(n_eff):
+    torch = pytest.importorskip("torch")
+    from soap_gpu_gb300 import _lib
+    from soap_gpu_gb300.api import Context
+
+    L = _lib.load()
+    cap = int(L.soapgb_noalloc_capacity(n_eff))
+    assert cap >= 1
+    n = n_eff + 160
+    dev = "cuda:0"
+    wave = torch.as_tensor(5000.0 + 0.005 * np.arange(n), device=dev)
+    rng = np.random.default_rng(n_eff)
+    row = np.zeros(n)
+    row[:n_eff] = rng.uniform(0.0, 0.5, n_eff)
+    spec = torch.as_tensor(np.tile(row, (cap, 1)), device=dev)
+    out = torch.full((cap, n_eff), np.nan, dtype=torch.float64, device=dev)
+    with Context(0) as ctx:
+        before = torch.cuda.current_device()
+        rc = L.soapgb_lower_resolution_noalloc(ctx.h, n, n_eff, cap, _ptr(wave), None, _ptr(spec), 1107.0, 50.0,
+                                               0.005, 0.005, -60000.0, _ptr(out), None)
+        assert rc == 0, L.soapgb_last_error(ctx.h)
+        assert L.soapgb_synchronize(ctx.h) == 0, L.soapgb_last_error(ctx.h)
+        assert torch.cuda.current_device() == before
+        o = out.cpu().numpy()
+        assert np.all(np.isfinite(o))
+        # every row is the same spectrum, so every output row is the first one
+        assert np.array_equal(o, np.tile(o[0], (cap, 1)))
