@@ -56,7 +56,11 @@ def stage_argv(rc, root, exe_dir, solar=False):
     cp = rc.cube_paths
     out = rc.output_prefix + "/" + rc.file_prefix
     phase_txt = rc.output_prefix + "/" + rc.file_prefix + "_" + "phase_locator.txt"
-    n_phase = len(rc.phases)
+    if rc.keyword == "real":
+        # run_all_SOAP.py:148-157 reuses the phase locator already in place
+        n_phase = int(np.atleast_1d(np.loadtxt(os.path.join(root, phase_txt))).size)
+    else:
+        n_phase = len(rc.phases)
     s = str
     init = lambda cube, pre: [os.path.join(exe_dir, "SOAP_initialize"), s(vector_size), s(rc.period),
                               s(rc.omega_ratio), s(rc.incl), s(rc.radius_km), s(rc.limb1), s(rc.limb2), s(rc.grid),
@@ -91,8 +95,11 @@ def write_maps(rc, root):
     np.savetxt(os.path.join(root, rc.maps_dir + "final_info.txt"), info)
 
 
-def run_impl(rc, root, exe_dir, env=None, stages=None):
-    write_maps(rc, root)
+def run_impl(rc, root, exe_dir, env=None, stages=None, write=True):
+    """Run the four stage programs in root; write=False keeps the phase locator and
+    region files already there (the keyword 'real' layout, run_all_SOAP.py:148-157)."""
+    if write:
+        write_maps(rc, root)
     times = {}
     for name, argv in stage_argv(rc, root, exe_dir):
         if stages and name not in stages:

@@ -73,3 +73,57 @@ def test_spectra_match_the_stage_executables(driven, tmp_path):
             a = np.fromfile(os.path.join(root, rc.output_prefix, rel))
             b = np.fromfile(os.path.join(r2, rc2.output_prefix, rel))
             assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+
+
+def _write_real_layout(root, rc, phases, regions):
+    """The files a 'real' run reuses (run_all_SOAP.py:148-157): the phase locator and
+    one region table per phase, written by hand here (a phase may have none)."""
+    for d in (rc.output_prefix, rc.maps_dir, rc.raw_dir, rc.final_spec_dir):
+        os.makedirs(os.path.join(root, d), exist_ok=True)
+    np.savetxt(os.path.join(root, rc.output_prefix + "/" + rc.file_prefix + "_phase_locator.txt"), phases)
+    info = np.zeros((len(phases), 2))
+    for i, reg in enumerate(regions):
+        if len(reg):
+            np.savetxt(os.path.join(root, rc.maps_dir + "maps%d_for_all.txt" % i), reg)
+        info[i] = (i, len(reg))
+    np.savetxt(os.path.join(root, rc.maps_dir + "final_info.txt"), info)
+
+
+def test_keyword_real_reuses_external_maps(tmp_path):
+    """keyword 'real': the driver takes the phases and the per-phase region tables from
+    existing files instead of the configuration.  The same files run through the stage
+    executables give the same spectra; the phase without a region has zero deficits."""
+    from soap_gpu_gb300 import build
+    case = synth.small_case(seed=13, grid=36, n=4200, n_phase=4, n_mu=5)
+    phases = np.array([0.05, 0.31, 0.5, 0.77, 0.93])
+    regions = [case.regions, case.regions[:1], np.zeros((0, 4)),
+               np.array([[10.0, 200.0, 0.15, 0.0], [-25.0, 160.0, 0.22, 1.0], [15.0, 170.0, 0.1, 0.0]]),
+               case.regions[::-1]]
+    roots = []
+    for tag in ("driver", "tools"):
+        root = str(tmp_path / tag)
+        inp = synth.generate(case)
+        cfg = synth.write_reference_layout(inp, root, keyword="real")
+        rc = config.load_config(cfg)
+        assert rc.keyword == "real"
+        _write_real_layout(root, rc, phases, regions)
+        roots.append((root, cfg, rc))
+    (r1, cfg1, rc1), (r2, cfg2, rc2) = roots
+    out = driver.run(cfg1, form="plain64", verbose=False)
+    assert out["tot"]["RV"].shape == (len(phases),)
+    assert np.array_equal(out["tot"]["time"], phases)
+    ref_run.run_impl(rc2, r2, build.BINDIR, env=dict(os.environ, SOAPGB_FORM="plain64"), write=False)
+    for p in range(len(phases)):
+        for name in ("tot", "flux", "bconv"):
+            raw = os.path.join(rc1.raw_dir, rc1.file_prefix + "_Spec_%s_%d_.bin" % (name, p))
+            a = np.fromfile(os.path.join(r1, raw))
+            b = np.fromfile(os.path.join(r2, raw))
+            if p == 2:
+                assert not np.any(a) and not np.any(b), "a phase without regions has zero deficits"
+            else:
+                assert np.max(np.abs(b)) > 0
+                assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+            low = os.path.join(rc1.final_spec_dir, rc1.file_prefix + "_lower_spec_%s_%d_.bin" % (name, p))
+            a = np.fromfile(os.path.join(r1, low))
+            b = np.fromfile(os.path.join(r2, low))
+            assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
