@@ -285,16 +285,61 @@ def run_own(args):
     if rk == 0:
         peak, peak_kind = measured_peaks()
         dom = max(ktab, key=lambda k: ktab[k][1])
-        launches_dom, ms_dom = ktab[dom]
-        ms_launch = ms_dom / max(launches_dom, 1.0)
-        alg = algorithmic_bytes(dom, case, phases_d.cpu().numpy(), regions, act, ctx, maps_d, form)
-        achieved = alg["bytes"] / (ms_launch / 1e3) / 1e9
-        traffic = profile_traffic(dom)
-        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": int(alg["bytes"]), "bytes_formula": alg["formula"],
-                "ms_per_launch": round(ms_launch, 4)}
-        err = accuracy(ctx, case, inp, form, out, wave_d, maps_d, cubes_d, phases_d, regions, act, star)
+        phases_np = phases_d.cpu().numpy()
+        roof = kernel_roofline(dom, ktab, case, phases_np, regions, act, ctx, maps_d, form, dev)
+        others = {k: kernel_roofline(k, ktab, case, phases_np, regions, act, ctx, maps_d, form, dev)
+                  for k in ("conv32", "norm32", "cube_types") if k in ktab and k != dom}
+
+        # --- the FP64 forms on the same step (the plain form is the reference's arithmetic)
+        fp64 = {}
+        outs = {}
+        for f in ("plain64", "fast64"):
+            qn = ctx.quiet_disk(f, wave_d, cubes_d["q_norm"], n_eff, maps_d, case.grid, case.step)
+            qs = ctx.quiet_disk(f, wave_d, cubes_d["q_sed"], n_eff, maps_d, case.grid, case.step)
+            o_f = torch.empty_like(out)
+
+            def step_f(f=f, qn=qn, qs=qs, o_f=o_f):
+                ctx.phase_pipeline(f, wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases, regions, qs, qn,
+                                   case.sigma_v, conv_step=case.step, out=o_f)
+
+            ms_f = timed_steps(step_f, 3, stream)
+            fp64[f] = {"value": round(len(phases) / (ms_f / 1e3), 2), "ms_per_step": round(ms_f, 3)}
+            outs[f] = (o_f, qs, qn)
+        ref_d = outs["plain64"][0]
+        fp64["fast32_over_plain64"] = round(value / fp64["plain64"]["value"], 2)
+        err = accuracy(ctx, case, inp, out, ref_d)
+
+        # --- the compensated summation variant of the FP32 integration, timed and checked once
+        comp = None
+        if form == "fast32":
+            ctx.set_compensated(True)
+            o_c = torch.empty_like(out)
+
+            def step_c():
+                ctx.phase_pipeline(form, wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases, regions,
+                                   q_sed_d, q_norm_d, case.sigma_v, conv_step=case.step, out=o_c)
+
+            ms_c = timed_steps(step_c, min(args.steps, 50), stream)
+            ctx.trace(True)
+            step_c()
+            kc = ctx.trace_report()
+            ctx.trace(False)
+            ctx.set_compensated(False)
+            comp = {"summation": "compensated (Kahan) output sums", "ms_per_step": round(ms_c, 4),
+                    "value": round(len(phases) / (ms_c / 1e3), 2),
+                    "fir_tile_phase_ms": round(kc.get("fir_tile_phase", (0, 0.0))[1], 4),
+                    "accuracy": accuracy(ctx, case, inp, o_c, ref_d)}
+
+        # --- CCF + fit stage (RV series), GPU and the reference's CPU form
+        lows = []
+        for q in (q_sed_d, q_sed_d, q_norm_d):
+            lo, _ = ctx.lower_resolution(form, wave_d, q, n_eff, case.sigma_v, step_mult=case.step,
+                                         step_exp=case.step)
+            lows.append(lo.reshape(-1))
+        quiet_low_d = torch.stack(lows)
+        ccf_stage = ccf_fit_stage(ctx, case, inp, out, quiet_low_d, stream)
+        if not args.no_cpu:
+            ccf_stage["cpu_baseline"] = ccf_fit_cpu(case, inp, ref_d[:2].cpu().numpy())
         cpu = cpu_baseline(case, inp, sample_phases=1) if not args.no_cpu else None
         result = {
             "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -303,13 +348,21 @@ def run_own(args):
             "config": {"workload": "300x300 grid, 310,000 px (3800-6900 A at 0.01 A), 20 mu bins, facula 3% + "
                                    "spot 1% overlapping, 100 phases per GPU, R=115000",
                        "form": form, "phases_per_step": len(phases), "l2": "inputs (cubes 4x49.6 MB FP64) and "
-                       "outputs (744 MB) exceed the 129 MB L2", "quiet_stage_ms": round(quiet_ms, 2)},
+                       "outputs (744 MB) exceed the 129 MB L2", "quiet_stage_ms": round(quiet_ms, 2),
+                       "summation": "FP32 per work unit, unit deficits added in plain FP32 (about 9 per pixel "
+                                    "and tile); the compensated variant is timed under 'compensated'"
+                                    if form == "fast32" else "FP64"},
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
             "roofline": roof,
+            "rooflines_other": others,
             "cpu_baseline": cpu,
             "accuracy": err,
+            "fp64_forms": fp64,
+            "compensated": comp,
+            "ref_cuda": ref_cuda_record(len(phases)),
+            "ccf_fit": ccf_stage,
             "kernels_ms_per_step": {k: round(v[1], 4) for k, v in sorted(ktab.items(), key=lambda x: -x[1][1])},
             "seed_preparation": {"bisector_injection_ms_per_cube": round(bis_ms, 4),
                                  "cube": "%d mu bins x %d px, quiet form, inputs resident" % (n_mu, n)},
@@ -323,26 +376,137 @@ def run_own(args):
     return result
 
 
-def algorithmic_bytes(kernel, case, phases, regions, act, ctx, maps_d, form):
-    """Algorithmic HBM bytes of one launch of `kernel` in one step.
+def profile_counters(kernel):
+    """ncu counters of `kernel` from the committed summary profiles/counters.txt (lines
+    "kernel metric value"): the limiter evidence printed beside the roofline."""
+    p = os.path.join(ROOT, "profiles", "counters.txt")
+    out = {}
+    if os.path.exists(p):
+        with open(p) as f:
+            for ln in f:
+                parts = ln.split()
+                if len(parts) == 3 and parts[0] == kernel:
+                    try:
+                        out[parts[1]] = float(parts[2])
+                    except ValueError:
+                        pass
+    return out
 
-    fir_tile_phase (active-region integration, all phases in one launch): per phase,
-    (distinct mu rows of its active cells x N_eff x 3 cubes + 2 continua + 3 outputs)
-    x sizeof(element); conv32 / norm32: spectra in + convolution out, convolution in +
-    FP64 spectra out."""
+
+def fp32_peak_tflops(dev):
+    """Nominal FP32 FMA rate: SMs x 128 lanes x 2 flop x the maximum SM clock
+    (MEASURED_PEAKS.json sm_max_mhz, else 2070 MHz)."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def conv32_flops(case, n_spec):
+    """FMA flops the FP32 convolution executes: per spectrum and pixel, 2 flop per tap over
+    the reach where the Gaussian weight is at least e^-30 of the centre (the reach of a
+    1024-pixel tile is that of its largest sigma, sigma growing with wavelength)."""
+    wave = np.arange(case.n_eff) * case.step + case.lambda0
+    beta = case.sigma_v / C_LIGHT
+    sig = wave * (np.sqrt((1 + beta) / (1 - beta)) - 1) / case.step   # in pixels
+    tiles = np.maximum.reduceat(sig, np.arange(0, case.n_eff, 1024))
+    reach = np.floor(np.sqrt(60.0) * tiles)
+    taps = np.repeat(2 * reach + 1, 1024)[:case.n_eff]
+    return float(2.0 * n_spec * taps.sum())
+
+
+def kernel_roofline(kernel, ktab, case, phases, regions, act, ctx, maps_d, form, dev):
+    """Roofline entry of one kernel of the step from its live CUDA-event time.
+
+    fir_tile_phase (active-region integration, all phases in one launch): algorithmic
+    bytes per phase (distinct mu rows of its active cells x N_eff x 3 cubes + 2 continua
+    + 3 outputs) x sizeof(element).  Those count each phase's read of the cube rows,
+    which the kernel serves from L2 across phases, so the DRAM traffic of the ncu capture
+    is reported beside them; the kernel is bound by instruction issue (ncu counters).
+    conv32: executed FP32 FMA flops against the nominal FP32 rate.  norm32 / cube_types:
+    bytes in + out against the measured copy bandwidth."""
+    peak, peak_kind = measured_peaks()
+    launches, ms = ktab[kernel]
+    ms_launch = ms / max(launches, 1.0)
     n_eff, n_phase = case.n_eff, len(phases)
     tsz = 4 if form == "fast32" else 8
+    traffic = profile_traffic(kernel)
+    counters = profile_counters(kernel)
     if kernel == "fir_tile_phase":
         temp, bi = ctx.phase_maps(case.grid, case.incl, phases, regions, act)
         region = maps_d["region"].cpu().numpy()
         rows = sum(len(np.unique(region[(bi[p] >= -0.5) & (bi[p] <= 1.5)])) for p in range(n_phase))
-        return {"bytes": (rows * 3 + (2 + 3) * n_phase) * n_eff * tsz,
-                "formula": "sum_p (mu rows touched x 3 cubes + 2 continua + 3 outputs) x N_eff x %d B" % tsz}
+        b = (rows * 3 + (2 + 3) * n_phase) * n_eff * tsz
+        ach = b / (ms_launch / 1e3) / 1e9
+        out = {"bound": "issue", "kernel": kernel, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+               "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+               "algorithmic_bytes_per_launch": int(b),
+               "bytes_formula": "sum_p (mu rows touched x 3 cubes + 2 continua + 3 outputs) x N_eff x %d B" % tsz,
+               "ms_per_launch": round(ms_launch, 4),
+               "bound_evidence": "instruction issue and latency: the cube rows are re-read per phase from L2, "
+                                 "DRAM moves far less than the algorithmic bytes (see dram_achieved); ncu counters "
+                                 "in counters"}
+        if traffic:
+            dr = traffic / (ms_launch / 1e3) / 1e9
+            out["dram_achieved"] = round(dr, 1)
+            out["dram_frac"] = round(dr / peak, 4)
+        if counters:
+            out["counters"] = counters
+        return out
     if kernel == "conv32":
-        return {"bytes": 3 * n_phase * (case.n + n_eff) * 4, "formula": "3 n_phase x (N + N_eff) x 4 B"}
+        # phases without a visible region have zero spectra, which the convolution skips
+        _, bi = ctx.phase_maps(case.grid, case.incl, phases, regions, act)
+        n_spec = 3 * int(np.count_nonzero(np.any(bi.reshape(n_phase, -1) >= 0, axis=1)))
+        fl = conv32_flops(case, n_spec)
+        pk = fp32_peak_tflops(dev)
+        ach = fl / (ms_launch / 1e3) / 1e12
+        out = {"bound": "fp32", "kernel": kernel, "achieved": round(ach, 2), "peak": round(pk, 1),
+               "unit": "TFLOP/s", "frac": round(ach / pk, 4), "peak_source": "nominal (SMs x 128 x 2 x max clock)",
+               "flops_per_launch": fl, "flops_formula": "2 flop x taps within e^-30 of the centre x N_eff x "
+               "convolved spectra (%d)" % n_spec, "ms_per_launch": round(ms_launch, 4), "traffic": traffic}
+        if counters:
+            out["counters"] = counters
+        return out
     if kernel == "norm32":
-        return {"bytes": 3 * n_phase * n_eff * (4 + 8), "formula": "3 n_phase x N_eff x (4 + 8) B"}
-    return {"bytes": 0, "formula": "not modelled"}
+        b = 3 * n_phase * n_eff * (4 + 8)
+        formula = "3 n_phase x N_eff x (4 B in + 8 B out)"
+    elif kernel == "cube_types":
+        b = 4 * case.n_mu * case.n * 8 + 6 * case.n_mu * case.n * 4
+        formula = "4 FP64 cubes in + 6 FP32 cubes out, n_mu x N each"
+    else:
+        return None
+    ach = b / (ms_launch / 1e3) / 1e9
+    out = {"bound": "hbm", "kernel": kernel, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+           "frac": round(ach / peak, 4), "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(b),
+           "bytes_formula": formula, "ms_per_launch": round(ms_launch, 4), "traffic": traffic}
+    if counters:
+        out["counters"] = counters
+    return out
+
+
+def ref_cuda_record(n_phase):
+    """The reference's own CUDA programs (patched for determinism) on the 300x300 /
+    310,000-px star, as run_all_SOAP.py runs them (one process per stage, float64 files
+    between stages), from the committed record of oracle/ref_run.py."""
+    p = os.path.join(ROOT, "oracle", "ref_cuda_record.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        rec = json.load(f)
+    c1 = rec.get("case1", {})
+    t = c1.get("patched", {}).get("times_s", {})
+    if not t:
+        return None
+    ph = c1.get("phases", 10)
+    per = (t.get("integration", 0.0) + t.get("resolution", 0.0)) / ph
+    return {"value": round(1.0 / per, 3) if per > 0 else None, "unit": UNIT, "phases": ph,
+            "integration_s": t.get("integration"), "resolution_s": t.get("resolution"),
+            "includes": "process start, file reads and writes of each stage, as run_all_SOAP.py runs them",
+            "source": "oracle/ref_cuda_record.json (" + rec.get("command", "python -m oracle.ref_run") + ")"}
 
 
 def adjoint_timing(ctx, dev, reps=3):
@@ -418,19 +582,15 @@ def adjoint_timing(ctx, dev, reps=3):
                                 "ratio": round(cfb_ms / cf_ms, 2)}}
 
 
-def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, regions, act, star):
-    """Error of the measured form against the plain FP64 form (the reference's
-    arithmetic): max relative flux error of the normalised spectra and the RV / BIS /
-    FWHM differences of the CCF Gaussian fits, in cm/s."""
+def accuracy(ctx, case, inp, out_d, ref_d):
+    """Error of a form's normalised spectra (out_d) against the plain FP64 form's
+    (ref_d, the reference's arithmetic) on the same step: max relative flux error and
+    the RV / BIS / FWHM differences of the CCF Gaussian fits, in cm/s."""
     import torch
     from soap_gpu_gb300 import rv
     n_eff = case.n_eff
-    q_norm64 = ctx.quiet_disk("plain64", wave_d, cubes_d["q_norm"], n_eff, maps_d, case.grid, case.step)
-    q_sed64 = ctx.quiet_disk("plain64", wave_d, cubes_d["q_sed"], n_eff, maps_d, case.grid, case.step)
-    ref = ctx.phase_pipeline("plain64", wave_d, n_eff, star, maps_d, cubes_d, case.step, act, phases_d, regions,
-                             q_sed64, q_norm64, case.sigma_v, conv_step=case.step)
     torch.cuda.synchronize()
-    o, r = out_d.cpu().numpy(), ref.cpu().numpy()
+    o, r = out_d.cpu().numpy(), ref_d.cpu().numpy()
     scale = np.max(np.abs(r), axis=2, keepdims=True)
     flux_err = float(np.max(np.abs(o - r) / scale))
     wave = inp.wave[:n_eff]
@@ -439,6 +599,79 @@ def accuracy(ctx, case, inp, form, out_d, wave_d, maps_d, cubes_d, phases_d, reg
     d = {k: float(np.max(np.abs(series_o[k] - series_r[k])) * 100.0) for k in ("rv", "span", "fwhm")}
     return {"against": "plain64", "flux_rel_max": flux_err, "rv_cms_max": d["rv"], "bis_span_cms_max": d["span"],
             "fwhm_cms_max": d["fwhm"], "rv_range_ms": float(np.ptp(series_r["rv"]))}
+
+
+def timed_steps(fn, steps, stream):
+    """ms per call of fn over `steps` calls, CUDA events on `stream` (one warm-up call)."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def ccf_fit_stage(ctx, case, inp, out_d, quiet_low_d, stream, reps=5):
+    """The CCF + fit stage of one step (run_all_SOAP.py:256-412, timed there as "RV
+    Calculation time"): the 300 phase spectra and the 3 quiet ones, trimmed, through the
+    mask CCF (normalised, apodised) and the batched Gaussian + bisector fit, inputs
+    resident.  One RV series is the n_phase + 1 spectra of one type, so a step gives 3."""
+    import torch
+    from soap_gpu_gb300 import rv
+    dev = out_d.device
+    n_eff = case.n_eff
+    wave_trim = rv.trim(inp.wave[:n_eff])
+    lw, lwt = rv.select_lines(wave_trim, inp.mask_wave, inp.mask_weight)
+    wt_d = torch.as_tensor(wave_trim, device=dev)
+    vel_d = torch.as_tensor(case.velocities, dtype=torch.float64, device=dev)
+    lw_d, lwt_d = torch.as_tensor(lw, device=dev), torch.as_tensor(lwt, device=dev)
+    n_spec = out_d.shape[0] * 3 + 3
+    no_points = int(rv.WAVE_EXTEND / case.step)
+
+    def stage():
+        spectra = torch.cat([rv.trim(out_d).reshape(-1, wave_trim.size), rv.trim(quiet_low_d)], dim=0)
+        ccf = ctx.ccf("plain64", vel_d, lw_d, lwt_d, wt_d, case.step, spectra, normalise=True,
+                      wave_extend=rv.WAVE_EXTEND, mask_step=case.step, index_old=no_points)
+        return ctx.gauss_bis(vel_d, ccf)
+
+    ms = timed_steps(stage, reps, stream)
+    res = stage()
+    torch.cuda.synchronize()
+    ok = bool((res["iters"] >= 0).all())
+    return {"value": round(3 / (ms / 1e3), 2), "unit": "RV-series/s", "ms_per_step": round(ms, 3),
+            "spectra_per_step": int(n_spec), "spectra_per_s": round(n_spec / (ms / 1e3), 1),
+            "mask_lines": int(lw.size), "velocities": int(len(case.velocities)), "fits_converged": ok,
+            "what": "trim + mask CCF (FP64 sums, normalised, apodised) + Gaussian/bisector fit of the %d spectra of "
+                    "one step (3 RV series of %d spectra), inputs resident" % (n_spec, n_spec // 3)}
+
+
+def ccf_fit_cpu(case, inp, out_np, sample=6):
+    """The reference's CPU form of the same stage on a sample of spectra: the dense mask
+    dot of CCF_func.py (oracle C) and the Gaussian + bisector fit of BIS_FIT2 (oracle C
+    restatement), one host thread per spectrum as the reference spawns them."""
+    import oracle
+    from soap_gpu_gb300 import rv
+    n_eff = case.n_eff
+    wt = rv.trim(inp.wave[:n_eff])
+    lw, lwt = rv.select_lines(wt, inp.mask_wave, inp.mask_weight)
+    t0 = time.perf_counter()
+    M = oracle.ccf_mask(case.velocities, lw, lwt, wt, case.step, mask_step=case.step,
+                        index_old=int(rv.WAVE_EXTEND / case.step))
+    t_mask = time.perf_counter() - t0
+    rows = out_np.reshape(-1, n_eff)[:sample]
+    t0 = time.perf_counter()
+    for r in rows:
+        oracle.gauss_bis(case.velocities, oracle.ccf_normalise(oracle.ccf(M, rv.trim(r))))
+    dt = (time.perf_counter() - t0) / len(rows)
+    per_series = (out_np.shape[0] + 1) * dt
+    return {"value": round(1.0 / per_series, 4), "unit": "RV-series/s", "s_per_spectrum": round(dt, 4),
+            "mask_build_s": round(t_mask, 3), "cores": 1, "kind": "port",
+            "sample": "%d spectra: dense mask dot (CCF_func.py calculate_CCF_2) + Gaussian/bisector fit "
+                      "(BIS_FIT2), oracle C; the mask is built once" % len(rows)}
 
 
 def cpu_baseline(case, inp, sample_phases=1):

@@ -51,6 +51,7 @@ SIGNATURES = [
     ("soapgb_set_stream", ctypes.c_int, [_vp, _vp]),
     ("soapgb_synchronize", ctypes.c_int, [_vp]),
     ("soapgb_launch_count", ctypes.c_longlong, [_vp]),
+    ("soapgb_set_compensated", ctypes.c_int, [_vp, ctypes.c_int]),
     ("soapgb_version", ctypes.c_char_p, []),
     ("soapgb_trace_enable", ctypes.c_int, [_vp, ctypes.c_int]),
     ("soapgb_trace_report", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),

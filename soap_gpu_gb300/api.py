@@ -136,6 +136,11 @@ class Context:
     def synchronize(self):
         self._check(self.L.soapgb_synchronize(self.h))
 
+    def set_compensated(self, on: bool = True):
+        """Compensated (Kahan) instead of plain FP32 output sums in the FP32 form's
+        per-phase integration (soapgb_set_compensated)."""
+        self._check(self.L.soapgb_set_compensated(self.h, 1 if on else 0))
+
     @property
     def launches(self) -> int:
         return int(self.L.soapgb_launch_count(self.h))

@@ -353,4 +353,10 @@ int soapgb_synchronize(soapgb_ctx *ctx) {
 
 long long soapgb_launch_count(const soapgb_ctx *ctx) { return ctx ? ctx->launches : -1; }
 
+int soapgb_set_compensated(soapgb_ctx *ctx, int on) {
+    if (!ctx) return SOAPGB_ERR_ARG;
+    ctx->fir_compensated = (on != 0);
+    return SOAPGB_OK;
+}
+
 }  // extern "C"

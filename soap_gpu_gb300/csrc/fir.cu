@@ -1682,7 +1682,6 @@ constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per c
 constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
 constexpr int FIR_PP_MINB = 2;   // resident blocks per SM the kernel is compiled for
 constexpr int FIR_PP_EXC = 64;   // directly evaluated cells per staged batch
-constexpr bool FIR_PP_COMP = false;  // compensated output sums (per tile a pixel adds about 9 unit deficits, each rounded once)
 constexpr int FIR_FOLD = 4;          // work units per fold of the partial sums
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
@@ -1709,7 +1708,9 @@ __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPS
 // buffer; the cube windows of its work units stream through two buffers, and the first
 // unit of the next tile is issued while the current tile's last unit is applied, so the
 // copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
-template <typename T>
+// COMP: the output sums (per tile a pixel adds about 9 unit deficits, each rounded once)
+// are compensated (Kahan) rather than plain FP32 sums
+template <typename T, bool COMP>
 __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTileArgs A, int ntile, int r0, int nr,
                                                         int ntot_all) {
     constexpr int NC = 4;
@@ -1770,7 +1771,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     };
 
     // compensated sums of the three outputs per pixel: flux, tot, bconv
-    Acc<T, FIR_PP_COMP> acc[3][FIR_PIX];
+    Acc<T, COMP> acc[3][FIR_PIX];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -2442,13 +2443,13 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
         if ((stage & 4) && r1 > r0) {
             const int nrun = ntile * (r1 - r0);
             size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
-            SOAP_CUDA(ctx, cudaFuncSetAttribute(k_fir_pp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+            auto kern = ctx->fir_compensated ? k_fir_pp<T, true> : k_fir_pp<T, false>;
+            SOAP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
             int per_sm = 0;
-            SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fir_pp<T>, FIR_THREADS, smem_t));
+            SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FIR_THREADS, smem_t));
             const int nblk = std::max(1, std::min(nrun, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
             SOAP_TRACED(ctx, "fir_tile_phase",
-                        k_fir_pp<T><<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, r0, r1 - r0,
-                                                                                ntile * n_lists));
+                        kern<<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, r0, r1 - r0, ntile * n_lists));
             SOAP_LAUNCHED(ctx);
         }
         return SOAPGB_OK;

@@ -54,6 +54,8 @@ struct soapgb_ctx {
     const double *edge_wave = nullptr;
     int edge_n = 0, edge_n_eff = 0;
     double edge_w3[3] = {0.0, 0.0, 0.0};
+    // FP32 per-phase integration: compensated (Kahan) output sums (soapgb_set_compensated)
+    bool fir_compensated = false;
     // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report
     bool trace = false;
     std::vector<SoapTraceSpan> spans;

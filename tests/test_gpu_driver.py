@@ -95,7 +95,7 @@ def test_keyword_real_reuses_external_maps(tmp_path):
     executables give the same spectra; the phase without a region has zero deficits."""
     from soap_gpu_gb300 import build
     case = synth.small_case(seed=13, grid=36, n=4200, n_phase=4, n_mu=5)
-    phases = np.array([0.05, 0.31, 0.5, 0.77, 0.93])
+    phases = np.array([0.42, 0.47, 0.5, 0.55, 0.61])
     regions = [case.regions, case.regions[:1], np.zeros((0, 4)),
                np.array([[10.0, 200.0, 0.15, 0.0], [-25.0, 160.0, 0.22, 1.0], [15.0, 170.0, 0.1, 0.0]]),
                case.regions[::-1]]
@@ -113,6 +113,7 @@ def test_keyword_real_reuses_external_maps(tmp_path):
     assert out["tot"]["RV"].shape == (len(phases),)
     assert np.array_equal(out["tot"]["time"], phases)
     ref_run.run_impl(rc2, r2, build.BINDIR, env=dict(os.environ, SOAPGB_FORM="plain64"), write=False)
+    visible = 0
     for p in range(len(phases)):
         for name in ("tot", "flux", "bconv"):
             raw = os.path.join(rc1.raw_dir, rc1.file_prefix + "_Spec_%s_%d_.bin" % (name, p))
@@ -121,9 +122,10 @@ def test_keyword_real_reuses_external_maps(tmp_path):
             if p == 2:
                 assert not np.any(a) and not np.any(b), "a phase without regions has zero deficits"
             else:
-                assert np.max(np.abs(b)) > 0
                 assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+                visible += bool(np.any(b))
             low = os.path.join(rc1.final_spec_dir, rc1.file_prefix + "_lower_spec_%s_%d_.bin" % (name, p))
             a = np.fromfile(os.path.join(r1, low))
             b = np.fromfile(os.path.join(r2, low))
             assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+    assert visible >= 3 * 3, "too few phases with a visible region in the test"
