@@ -367,6 +367,7 @@ def run_own(args):
             "seed_preparation": {"bisector_injection_ms_per_cube": round(bis_ms, 4),
                                  "cube": "%d mu bins x %d px, quiet form, inputs resident" % (n_mu, n)},
             "differentiable": adjoint_timing(ctx, dev),
+            "batched": batched_timing(ctx, case, inp, wave_d, cubes_d, dev, stream) if not args.no_batch else None,
             "clocks": clk,
         }
     if dist:
@@ -486,6 +487,83 @@ def kernel_roofline(kernel, ktab, case, phases, regions, act, ctx, maps_d, form,
     if counters:
         out["counters"] = counters
     return out
+
+
+def batched_timing(ctx, case, inp, wave_d, cubes_d, dev, stream, n_star=256, per_batch=64):
+    """The batched form on 256 stars of uneven sizes sharing the 310,000-px seeds (grids
+    U{100..400}, 1-12 spots and faculae of 0.1-3 % of the hemisphere at latitudes
+    U(-60, 60), U{20..200} phases over one rotation, vsini U(1, 10) km/s): every stage
+    per star (disk maps, both quiet spectra, lists, plans, integration, convolution,
+    normalisation).  The stars run in batches of `per_batch` (the outputs of all 256,
+    215 GB in FP64, do not fit the device at once); each batch's run is one persistent
+    integration launch over its (star, phase, tile) items, timed as issued and as a CUDA
+    graph replay, with the launch shape of the tuned cache.  Beside it: the same stars as
+    queued single-star calls (soapgb_disk_maps, soapgb_quiet_disk x2,
+    soapgb_phase_pipeline per star, device buffers)."""
+    import ctypes
+    import torch
+    from soap_gpu_gb300 import autotune, synth
+    from soap_gpu_gb300._lib import Activity, Star
+    from soap_gpu_gb300.api import Batch
+    stars = synth.make_batch(n_star, seed=3)
+    act = Activity(case.t_star, case.t_diff_spot, case.t_diff_fac, case.nrho, 0)
+    lb = inp.lb
+    sts = [Star(c.grid, c.period, c.w_ratio, c.incl, c.radius_km, c.u1, c.u2, (ctypes.c_double * 4)(*lb))
+           for c in stars]
+    n_eff = case.n_eff
+    total_phases = sum(c.n_phase for c in stars)
+    mu_d = torch.as_tensor(inp.mu_boundary, device=dev)
+    out_one = torch.empty((max(c.n_phase for c in stars), 3, n_eff), dtype=torch.float64, device=dev)
+
+    def per_star():
+        for c, st in zip(stars, sts):
+            maps = ctx.disk_maps(c.grid, c.period, c.w_ratio, c.incl, c.radius_km, c.u1, c.u2, mu_d, lb)
+            qn = ctx.quiet_disk("fast32", wave_d, cubes_d["q_norm"], n_eff, maps, c.grid, case.step)
+            qs = ctx.quiet_disk("fast32", wave_d, cubes_d["q_sed"], n_eff, maps, c.grid, case.step)
+            ctx.phase_pipeline("fast32", wave_d, n_eff, st, maps, cubes_d, case.step, act, c.phases,
+                               [c.regions for _ in c.phases], qs, qn, case.sigma_v, conv_step=case.step,
+                               out=out_one[:c.n_phase])
+
+    ms_single = timed_steps(per_star, 1, stream)
+    del out_one
+    torch.cuda.empty_cache()
+    ms_run = ms_graph = create_s = 0.0
+    shapes, items, dev_bytes = [], 0, 0
+    for k in range(0, n_star, per_batch):
+        sub = stars[k:k + per_batch]
+        t0 = time.perf_counter()
+        b = Batch(ctx, wave_d, n_eff, cubes_d, inp.mu_boundary, case.step, act, case.sigma_v,
+                  sts[k:k + per_batch], [c.phases for c in sub], [[c.regions for _ in c.phases] for c in sub],
+                  conv_step=case.step)
+        create_s += time.perf_counter() - t0
+        grids = [c.grid for c in sub]
+        shape = autotune.shape_for(b, grids)
+        if shape is not None:
+            b.tune(*shape)
+        shapes.append({"class": autotune.key_of(b, grids), "shape": shape})
+        items += b.items
+        dev_bytes = max(dev_bytes, b.device_bytes)
+        out = torch.empty((b.total_phases, 3, n_eff), dtype=torch.float64, device=dev)
+        ms_run += timed_steps(lambda: b.run(out), 1, stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            b.run(out)
+        ms_graph += timed_steps(g.replay, 1, stream)
+        del g
+        b.close()
+        del out
+        torch.cuda.empty_cache()
+    return {"stars": n_star, "phases": total_phases, "visible_phases": items,
+            "value": round(total_phases / (ms_graph / 1e3), 2), "unit": UNIT,
+            "ms_graph_replay": round(ms_graph, 2), "ms_run": round(ms_run, 2),
+            "value_run": round(total_phases / (ms_run / 1e3), 2),
+            "single_star_calls": {"ms": round(ms_single, 2), "value": round(total_phases / (ms_single / 1e3), 2)},
+            "speedup_vs_single_star_calls": round(ms_single / ms_graph, 3),
+            "batches": "%d batches of up to %d stars, one persistent integration launch each" %
+                       ((n_star + per_batch - 1) // per_batch, per_batch),
+            "create_s": round(create_s, 3), "device_bytes_max": int(dev_bytes), "tuned_shapes": shapes,
+            "what": "every stage per star: disk maps, 2 quiet spectra, lists, plans, integration, convolution, "
+                    "normalisation; FP32 form; inputs resident"}
 
 
 def ref_cuda_record(n_phase):
@@ -761,6 +839,7 @@ def main():
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-star batched form")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed device steps (for ncu launch lists)")
     ap.add_argument("--phases", type=int, default=100, help="phases per step (100 is the benchmarked workload)")

@@ -103,7 +103,9 @@ const char *soapgb_last_error(const soapgb_ctx *ctx);
  * context's own stream, a non-blocking stream that is not ordered with the legacy
  * default stream.  A caller whose work is on the legacy default stream (torch's
  * default stream, handle 0) passes cudaStreamLegacy.  Switching streams orders the
- * new stream after the work the context queued on the previous one. */
+ * new stream after the work the context queued on the previous one, except for a
+ * stream that is being captured into a CUDA graph (it cannot wait on work outside the
+ * capture): the caller then orders the graph's launches after that work. */
 int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream);
 int soapgb_synchronize(soapgb_ctx *ctx);
 /* Number of kernel launches issued by this context since creation. */
@@ -287,6 +289,56 @@ int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const dou
                           const double *regions, const double *quiet_sed,
                           const double *quiet_norm, double sigma_v, double conv_step,
                           double sentinel, int mem, double *lower, double *raw);
+
+/* ---- batched form: many stars in one job ---------------------------------
+ * Replaces one run_all_SOAP.py invocation per star (run_all_SOAP.py:226-250: two
+ * SOAP_initialize runs, then SOAP_integration's phase loop, SOAP_integration.cu:661-845,
+ * and SOAP_resolution) for a batch of stars of uneven grids, regions and phase counts
+ * that share the seed spectra and the wavelength grid.  FP32 form only.  Per star the
+ * run builds the disk maps (a3), the two quiet spectra (a4-a7), the region maps' lists
+ * (a9-a10) and tile plans; the active-region integration (a11-a12) of every visible
+ * phase of every star is ONE persistent launch over (star, phase, tile) items; then each
+ * star's three deficit spectra per phase are convolved and normalised against its own
+ * quiet spectra (a14).
+ * soapgb_batch_create does the host-side work once (region tables, visibility, sizes),
+ * allocates the batch's device memory (soapgb_batch_device_bytes) and uploads the
+ * descriptors; it synchronises the context's stream.  soapgb_batch_run only enqueues
+ * device work on the context's stream (and streams it joins back), reads no host memory,
+ * allocates nothing and does not synchronise, so a caller may capture it in a CUDA graph;
+ * lower (device) receives total phases x 3 x n_eff spectra (tot, flux, bconv), star s's
+ * phases at rows [phase_offsets[s], phase_offsets[s + 1]); quiet (optional, device)
+ * n_star x 2 x n (quiet with continuum, normalised quiet).  The device arrays named in the
+ * descriptor (wave, the cubes) must stay valid while the batch is used.
+ * chunk and blocks_per_sm shape the integration launch's walk: its (star, phase, tile)
+ * positions are dealt to the blocks round robin in chunks of `chunk` positions (0: one
+ * contiguous share per block), with at most blocks_per_sm blocks per SM (0: as many as
+ * fit); soapgb_batch_tune changes them for later runs. */
+typedef struct soapgb_batch soapgb_batch;
+typedef struct {
+    int form;                    /* SOAPGB_FAST32 */
+    int n, n_eff;                /* the shared wavelength grid */
+    const double *wave;          /* n, device */
+    const soapgb_cubes *cubes;   /* the shared seed cubes, device */
+    const double *mu_boundary;   /* n_mu - 1, host */
+    double step;                 /* grid step */
+    soapgb_activity act;         /* temperatures, rim points, solar variant (shared) */
+    double sigma_v, conv_step, sentinel;
+    int n_star;
+    const soapgb_star *stars;    /* n_star, host */
+    const int *phase_offsets;    /* n_star + 1, host */
+    const double *phases;        /* phase_offsets[n_star], host */
+    const int *reg_offsets;      /* phase_offsets[n_star] + 1, host: region rows of each phase */
+    const double *regions;       /* rows (lat, long, size, type), host */
+    int chunk;
+    int blocks_per_sm;
+} soapgb_batch_desc;
+int soapgb_batch_create(soapgb_ctx *ctx, const soapgb_batch_desc *desc, soapgb_batch **out);
+int soapgb_batch_run(soapgb_ctx *ctx, soapgb_batch *batch, double *lower, double *quiet);
+int soapgb_batch_tune(soapgb_batch *batch, int chunk, int blocks_per_sm);
+size_t soapgb_batch_device_bytes(const soapgb_batch *batch);
+/* number of (star, phase) items with a visible region, the integration launch's phases */
+long long soapgb_batch_items(const soapgb_batch *batch);
+int soapgb_batch_destroy(soapgb_batch *batch);
 
 /* ---- bisector injection of the seed spectra --------------------------------
  * Replaces BIS_inject_spectral_quiet / BIS_inject_spectral_active

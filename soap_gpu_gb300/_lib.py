@@ -43,6 +43,15 @@ class Activity(ctypes.Structure):
                 ("nrho", ctypes.c_int), ("solar", ctypes.c_int)]
 
 
+class BatchDesc(ctypes.Structure):
+    _fields_ = [("form", ctypes.c_int), ("n", ctypes.c_int), ("n_eff", ctypes.c_int), ("wave", _vp),
+                ("cubes", ctypes.POINTER(Cubes)), ("mu_boundary", _vp), ("step", ctypes.c_double),
+                ("act", Activity), ("sigma_v", ctypes.c_double), ("conv_step", ctypes.c_double),
+                ("sentinel", ctypes.c_double), ("n_star", ctypes.c_int), ("stars", ctypes.POINTER(Star)),
+                ("phase_offsets", _vp), ("phases", _vp), ("reg_offsets", _vp), ("regions", _vp),
+                ("chunk", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+
+
 # (name, restype, argtypes) for every entry point declared in include/soapgb.h
 SIGNATURES = [
     ("soapgb_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -90,6 +99,12 @@ SIGNATURES = [
                                              ctypes.c_int, _vp, _vp]),
     ("soapgb_bisector_inject", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
                                               _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp]),
+    ("soapgb_batch_create", ctypes.c_int, [_vp, ctypes.POINTER(BatchDesc), ctypes.POINTER(_vp)]),
+    ("soapgb_batch_run", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("soapgb_batch_tune", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    ("soapgb_batch_device_bytes", ctypes.c_size_t, [_vp]),
+    ("soapgb_batch_items", ctypes.c_longlong, [_vp]),
+    ("soapgb_batch_destroy", ctypes.c_int, [_vp]),
     ("soapgb_noalloc_capacity", ctypes.c_size_t, [ctypes.c_int]),
     ("soapgb_lower_resolution_noalloc", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
      + [ctypes.c_double] * 5 + [_vp, _vp]),

@@ -14,7 +14,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import FORMS, Activity, Cubes, Maps, SoapError, Star
+from ._lib import FORMS, Activity, BatchDesc, Cubes, Maps, SoapError, Star
 
 try:  # torch is plumbing for device buffers and streams; numpy callers do not need it
     import torch
@@ -411,6 +411,93 @@ class Context:
                                                  a.inp(quiet_sed, np.float64), a.inp(quiet_norm, np.float64),
                                                  float(sigma_v), float(conv_step), float(sentinel), a.mem, lp, rp))
         return (lower, raw) if want_raw else lower
+
+
+class Batch:
+    """Many stars through the per-phase path in one job (soapgb_batch_create / _run).
+
+    The stars share the wavelength grid ``wave`` and the seed cubes (CUDA tensors, kept
+    alive by this object); ``stars`` is a list of Star structures, ``phases`` a list of
+    per-star phase arrays and ``regions`` a list (per star) of lists (per phase) of
+    (n, 4) region tables.  ``run()`` enqueues the whole job on torch's current stream
+    without reading host memory or synchronising, so it may be captured in a CUDA graph;
+    it returns the (total phases, 3, n_eff) normalised spectra, star s at rows
+    ``offsets[s]:offsets[s + 1]``."""
+
+    def __init__(self, ctx: "Context", wave, n_eff, cubes: dict, mu_boundary, step, act: Activity, sigma_v,
+                 stars: Sequence[Star], phases: Sequence, regions: Sequence, conv_step=None, sentinel=-60000.0,
+                 chunk=0, blocks_per_sm=0, form="fast32"):
+        self.ctx = ctx
+        L = ctx.L
+        dev = "cuda:%d" % ctx.device
+        T = lambda a: (a if _is_dev(a) else torch.as_tensor(np.ascontiguousarray(a), device=dev)).to(
+            torch.float64).contiguous()
+        self.wave = T(wave)
+        self.n = int(self.wave.shape[0])
+        self.n_eff = int(n_eff)
+        self.cube_t = {k: T(cubes[k]) for k in ("q_norm", "q_sed", "spot_norm", "fac_norm")}
+        for k in ("spot_sed", "fac_sed"):
+            v = cubes[k]
+            self.cube_t[k] = T(v[0] if len(v.shape) == 2 else v)
+        n_mu = int(self.cube_t["q_norm"].shape[0])
+        self.cubes = Cubes(*[ctypes.c_void_p(self.cube_t[k].data_ptr()) for k in
+                             ("q_norm", "q_sed", "spot_norm", "fac_norm", "spot_sed", "fac_sed")], n_mu)
+        self.n_star = len(stars)
+        self.offsets = np.zeros(self.n_star + 1, dtype=np.int32)
+        for s, ph in enumerate(phases):
+            self.offsets[s + 1] = self.offsets[s] + len(ph)
+        ph_all = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.float64) for p in phases]))
+        reg_rows = [np.asarray(r, dtype=np.float64).reshape(-1, 4) for per_star in regions for r in per_star]
+        if len(reg_rows) != ph_all.size:
+            raise ValueError("one region table per phase")
+        roff = np.zeros(ph_all.size + 1, dtype=np.int32)
+        roff[1:] = np.cumsum([r.shape[0] for r in reg_rows])
+        reg = np.ascontiguousarray(np.concatenate(reg_rows) if roff[-1] > 0 else np.zeros((1, 4)))
+        mu_b = np.ascontiguousarray(np.asarray(mu_boundary, dtype=np.float64))
+        self.stars = (Star * self.n_star)(*stars)
+        self._host = (ph_all, roff, reg, mu_b)
+        desc = BatchDesc(_form(form), self.n, self.n_eff, ctypes.c_void_p(self.wave.data_ptr()),
+                         ctypes.pointer(self.cubes), ctypes.c_void_p(mu_b.ctypes.data), float(step), act,
+                         float(sigma_v), float(step if conv_step is None else conv_step), float(sentinel),
+                         self.n_star, self.stars, ctypes.c_void_p(self.offsets.ctypes.data),
+                         ctypes.c_void_p(ph_all.ctypes.data), ctypes.c_void_p(roff.ctypes.data),
+                         ctypes.c_void_p(reg.ctypes.data), int(chunk), int(blocks_per_sm))
+        h = ctypes.c_void_p()
+        ctx.L.soapgb_set_stream(ctx.h, ctypes.c_void_p(torch_stream_handle(ctx.device)))
+        ctx._check(L.soapgb_batch_create(ctx.h, ctypes.byref(desc), ctypes.byref(h)))
+        self.h = h
+        self.total_phases = int(self.offsets[-1])
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.ctx.L.soapgb_batch_device_bytes(self.h))
+
+    @property
+    def items(self) -> int:
+        return int(self.ctx.L.soapgb_batch_items(self.h))
+
+    def tune(self, chunk: int, blocks_per_sm: int):
+        self.ctx._check(self.ctx.L.soapgb_batch_tune(self.h, int(chunk), int(blocks_per_sm)))
+
+    def run(self, out=None, quiet=None):
+        dev = "cuda:%d" % self.ctx.device
+        if out is None:
+            out = torch.empty((self.total_phases, 3, self.n_eff), dtype=torch.float64, device=dev)
+        self.ctx.L.soapgb_set_stream(self.ctx.h, ctypes.c_void_p(torch_stream_handle(self.ctx.device)))
+        self.ctx._check(self.ctx.L.soapgb_batch_run(self.ctx.h, self.h, ctypes.c_void_p(out.data_ptr()),
+                                                    ctypes.c_void_p(quiet.data_ptr()) if quiet is not None else None))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.ctx.L.soapgb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def version() -> str:

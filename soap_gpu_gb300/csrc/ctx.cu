@@ -331,7 +331,14 @@ const char *soapgb_last_error(const soapgb_ctx *ctx) {
 int soapgb_set_stream(soapgb_ctx *ctx, void *cuda_stream) {
     if (!ctx) return SOAPGB_ERR_ARG;
     cudaStream_t next = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
-    if (next != ctx->stream && ctx->stream) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(next, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
+    // a stream being captured into a graph cannot wait on work outside the capture: its
+    // caller orders the graph's launch after the context's earlier work
+    if (next != ctx->stream && ctx->stream && cap == cudaStreamCaptureStatusNone) {
         // every call's work ends on the context's stream and may still be queued there,
         // using the context's scratch: the new stream starts after it
         SOAP_DEVICE(ctx);

@@ -184,6 +184,12 @@ __global__ void __launch_bounds__(256) k_quiet_plain64(int n, int n_eff, const d
 // --------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------
+namespace soapgb {
+void disk_omega_host(const soapgb_star *st, std::vector<double> &ov, double &sin_incl);
+int disk_maps_launch(soapgb_ctx *ctx, const soapgb_star *star, int n_mu, const double *d_mu, const double *d_ov,
+                     double sin_incl, double *delta, double *limb, double *mu, int *region, double *lb);
+}  // namespace soapgb
+
 static void host_omega_velo(const soapgb_star *st, std::vector<double> &ov, double &sin_incl) {
     // SOAP_initialize.cu:308-351, host libm like the reference
     double incl = st->incl * SOAP_PI / 180.;
@@ -198,6 +204,26 @@ static void host_omega_velo(const soapgb_star *st, std::vector<double> &ov, doub
     }
     sin_incl = sin(incl);
 }
+
+namespace soapgb {
+// the per-row rotation constants of a star's grid (host libm), for disk_maps_launch
+void disk_omega_host(const soapgb_star *st, std::vector<double> &ov, double &sin_incl) {
+    host_omega_velo(st, ov, sin_incl);
+}
+
+// the disk maps of one star from constants already on the device (no host memory read)
+int disk_maps_launch(soapgb_ctx *ctx, const soapgb_star *star, int n_mu, const double *d_mu, const double *d_ov,
+                     double sin_incl, double *delta, double *limb, double *mu, int *region, double *lb) {
+    const int G = star->grid;
+    const long long gm = (long long)G * G;
+    const double *c = star->lb;
+    SOAP_TRACED(ctx, "disk_maps", k_disk_maps<<<grid_for(ctx, gm, 256), 256, 0, ctx->stream>>>(
+        G, d_ov, sin_incl, 2. / G, star->u1, star->u2, n_mu, d_mu, c[0], c[1], c[2], c[3], delta, limb, mu, region,
+        lb));
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
+}
+}  // namespace soapgb
 
 extern "C" int soapgb_disk_maps(soapgb_ctx *ctx, const soapgb_star *star, int n_mu,
                                 const double *mu_boundary, int mem, soapgb_maps *maps_out) {

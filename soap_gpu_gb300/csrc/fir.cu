@@ -1709,23 +1709,26 @@ __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPS
 // unit of the next tile is issued while the current tile's last unit is applied, so the
 // copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
 // COMP: the output sums (per tile a pixel adds about 9 unit deficits, each rounded once)
-// are compensated (Kahan) rather than plain FP32 sums
-template <typename T, bool COMP>
-__global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTileArgs A, int ntile, int r0, int nr,
-                                                        int ntot_all) {
+// are compensated (Kahan) rather than plain FP32 sums.
+// MULTI: the (phase, tile) pairs of many stars in one launch.  Star s has its own lists,
+// prefix sums, plans and outputs (stars[s]); the stars share the wavelength grid and the
+// typed cubes.  items[g] = (star, phase) for the nr visible phases of all stars, and the
+// walk position v is tile v / nr of items[v % nr]; each block takes chunks of `chunk`
+// consecutive positions, chunks b, b + G, b + 2G, ... (chunk = 0: one contiguous share).
+template <typename T, bool COMP, bool MULTI>
+__global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTileArgs A0, int ntile, int r0, int nr,
+                                                        int ntot_all, const FirTileArgs *__restrict__ stars,
+                                                        const int2 *__restrict__ items, int chunk) {
     constexpr int NC = 4;
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
     extern __shared__ __align__(128) unsigned char pp_smem[];
     FirPPSmem<T> &sh = *reinterpret_cast<FirPPSmem<T> *>(pp_smem);
     FirSeg *segs = reinterpret_cast<FirSeg *>(pp_smem + fir_pp_smem_fixed<T>());
+    __shared__ FirTileArgs star_sh;   // MULTI: the arguments of the star being walked
+    const FirTileArgs &A = MULTI ? star_sh : A0;
     const int tid = threadIdx.x;
     const int G = gridDim.x;
-    const int n = A.n, n_eff = A.n_eff;
-    T *out0 = reinterpret_cast<T *>(A.out0);
-    T *out1 = reinterpret_cast<T *>(A.out1);
-    T *out2 = reinterpret_cast<T *>(A.out2);
-    const char *plans = reinterpret_cast<const char *>(A.plan);
-    const int *psize = reinterpret_cast<const int *>(plans + (size_t)ntot_all * SLOT);
+    const int n = A0.n, n_eff = A0.n_eff;   // shared by every star
     if (tid == 0) {
         for (int q = 0; q < (FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2); ++q) mbar_init(&sh.wbar[q], 1);
         mbar_init(&sh.pbar[0], 1);
@@ -1735,18 +1738,55 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     }
     __syncthreads();
 
-    // (phase, tile) index (phase * ntile + tile) of walk position v
+    // (phase, tile) index (phase * ntile + tile) of walk position v, and its star
     auto real = [&](int v) -> int {
+        if (MULTI) return items[v % nr].y * ntile + v / nr;
         const int li = r0 + v % nr;
-        return (A.run_list ? A.run_list[li] : li) * ntile + v / nr;
+        return (A0.run_list ? A0.run_list[li] : li) * ntile + v / nr;
     };
-    const int total = nr * ntile, per = (total + G - 1) / G;
-    const int vb = min(total, (int)blockIdx.x * per), ve = min(total, vb + per);
-    // (thread 0) copy the plan of tile tau (bytes long) into plan buffer b
-    auto issue_plan = [&](int tau, int b, unsigned bytes) {
+    auto star_of = [&](int v) -> int { return MULTI ? items[v % nr].x : 0; };
+    // plan record and size of walk position v (a star's plans: ntile x its lists slots, then
+    // the sizes)
+    auto plan_rec = [&](int v) -> const char * {
+        const char *base = reinterpret_cast<const char *>(MULTI ? stars[star_of(v)].plan : A0.plan);
+        return base + (size_t)real(v) * SLOT;
+    };
+    auto plan_size = [&](int v) -> unsigned {
+        if (MULTI) {
+            const FirTileArgs &S = stars[star_of(v)];
+            const char *base = reinterpret_cast<const char *>(S.plan);
+            return (unsigned)reinterpret_cast<const int *>(base + (size_t)ntile * S.n_lists_all * SLOT)[real(v)];
+        }
+        return (unsigned)reinterpret_cast<const int *>(reinterpret_cast<const char *>(A0.plan) +
+                                                       (size_t)ntot_all * SLOT)[real(v)];
+    };
+    // this block's walk: positions [vb, ve) (chunk = 0), or chunks of `chunk` positions
+    // taken round robin; step k of the walk is position pos(k), k < kend
+    const int total = nr * ntile;
+    int vb = 0, ve = 0, kend = 0;
+    if (chunk <= 0) {
+        const int per = (total + G - 1) / G;
+        vb = min(total, (int)blockIdx.x * per);
+        ve = min(total, vb + per);
+        kend = ve - vb;
+    } else {
+        const int nchunk = (total + chunk - 1) / chunk;
+        const int mine = nchunk > (int)blockIdx.x ? (nchunk - 1 - (int)blockIdx.x) / G + 1 : 0;
+        kend = mine * chunk;
+        if (mine > 0) {   // the last chunk of the walk may be short
+            const int last = (int)blockIdx.x + (mine - 1) * G;
+            kend -= (last + 1) * chunk - min(total, (last + 1) * chunk);
+        }
+    }
+    auto pos = [&](int k) -> int {
+        if (chunk <= 0) return vb + k;
+        return ((int)blockIdx.x + (k / chunk) * G) * chunk + k % chunk;
+    };
+    // (thread 0) copy the plan of walk position v into plan buffer b
+    auto issue_plan = [&](int v, int b, unsigned bytes) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(&sh.pbar[b], bytes);
-        bulk_g2s(&sh.pb[b][0], plans + (size_t)tau * SLOT, bytes, &sh.pbar[b]);
+        bulk_g2s(&sh.pb[b][0], plan_rec(v), bytes, &sh.pbar[b]);
     };
     // (thread 0) stage the rows of unit number u (buffer u % 3)
     auto issue_unit = [&](int u, const FirUnit &d) {
@@ -1764,7 +1804,8 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         if (bytes) {
 #pragma unroll
             for (int q = 0; q < NC; ++q) {
-                const char *base = reinterpret_cast<const char *>(A.cubes.c[fir_cube_index(MODE_PHASE, d.cls, q)]);
+                // the typed cubes are the same for every star
+                const char *base = reinterpret_cast<const char *>(A0.cubes.c[fir_cube_index(MODE_PHASE, d.cls, q)]);
                 bulk_g2s(&sh.win[b][q][0], base + rel, bytes, &sh.wbar[b]);
             }
         }
@@ -1953,26 +1994,43 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         return sh.fail == 0;
     };
 
-    // walk positions [vb, ve)
+    // walk steps [0, kend)
     if (tid == 0) {
-        if (vb < ve) issue_plan(real(vb), 0, (unsigned)psize[real(vb)]);
-        if (vb + 1 < ve) issue_plan(real(vb + 1), 1, (unsigned)psize[real(vb + 1)]);
+        if (kend > 0) issue_plan(pos(0), 0, plan_size(pos(0)));
+        if (kend > 1) issue_plan(pos(1), 1, plan_size(pos(1)));
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount % 3)
     bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
     int k = 0;
     int bad = 0;
-    for (int v = vb; v < ve && !bad; ++v, ++k) {
+    int cur_star = -1;     // MULTI: the star whose arguments star_sh holds
+    for (; k < kend && !bad; ++k) {
+        const int v = pos(k);
         const int pbuf = k & 1;
         // size of the plan issued at the end of this tile, read early (its latency hides
         // behind the tile's work)
-        const unsigned next_bytes = (tid == 0 && v + 2 < ve) ? (unsigned)psize[real(v + 2)] : 0u;
+        const unsigned next_bytes = (tid == 0 && k + 2 < kend) ? plan_size(pos(k + 2)) : 0u;
+        if (MULTI) {
+            const int s_v = star_of(v);   // uniform for the block
+            if (s_v != cur_star) {
+                __syncthreads();   // every thread is done with the previous star's arguments
+                constexpr int WORDS = (int)(sizeof(FirTileArgs) / sizeof(int));
+                static_assert(sizeof(FirTileArgs) % sizeof(int) == 0, "FirTileArgs copied as words");
+                const int *src = reinterpret_cast<const int *>(stars + s_v);
+                int *dst = reinterpret_cast<int *>(&star_sh);
+                for (int w = tid; w < WORDS; w += FIR_THREADS) dst[w] = src[w];
+                cur_star = s_v;
+            }
+        }
         if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1))) atomicExch(&sh.fail, 1);
         __syncthreads();
         if (sh.fail) {
             bad = 1;
             break;
         }
+        T *out0 = reinterpret_cast<T *>(A.out0);
+        T *out1 = reinterpret_cast<T *>(A.out1);
+        T *out2 = reinterpret_cast<T *>(A.out2);
         const int tr = real(v);
         const int l = tr / ntile, j0 = (tr - l * ntile) * FIR_TILE;
         const int t_eff = min(FIR_TILE, n_eff - j0);
@@ -2009,11 +2067,10 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     } else {
                         // last unit: issue the next tile's first unit, from its plan
                         pre = false;
-                        const int tn = v + 1;
-                        if (tn < ve && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
+                        if (k + 1 < kend && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
-                            const int tnr = real(tn);
+                            const int tnr = real(pos(k + 1));
                             const int ln = tnr / ntile, jn = (tnr - ln * ntile) * FIR_TILE;
                             if (hn.w && hn.x > 0 && jn < n_eff) {
                                 const FirPlanLayout<T> Ln(hn.x, hn.y, hn.z);
@@ -2166,12 +2223,12 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
             for (int a = 0; a < 3; ++a) acc[a][q].zero();
         }
         __syncthreads();   // plan buffer pbuf free
-        if (tid == 0 && v + 2 < ve) issue_plan(real(v + 2), pbuf, next_bytes);
+        if (tid == 0 && k + 2 < kend) issue_plan(pos(k + 2), pbuf, next_bytes);
     }
     if (bad && tid == 0) {
         // a copy did not land in time: record it and give the copies possibly in flight a
         // bounded wait before leaving
-        atomicExch(A.status, FIR_ST_WAIT);
+        atomicExch(A0.status, FIR_ST_WAIT);
         if (FIR_PP_STAGED) {
             mbar_wait_bounded(&sh.wbar[ucount % FIR_PP_NBUF], (unsigned)((ucount / FIR_PP_NBUF) & 1));
             mbar_wait_bounded(&sh.wbar[(ucount + 1) % FIR_PP_NBUF], (unsigned)(((ucount + 1) / FIR_PP_NBUF) & 1));
@@ -2220,14 +2277,15 @@ struct FirLayout {
     long long pre_stride = 0, pre_comp = 0;
 };
 
-FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_lists) {
+// typed_external: the typed cubes live elsewhere (shared by several stars), no slots here
+FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_lists, bool typed_external = false) {
     FirLayout L;
     size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
     size_t sz[FirLayout::NSLOT] = {0};
     sz[FirLayout::GEO] = sizeof(CellGeo) * (size_t)gm;
     sz[FirLayout::GEO32] = sizeof(CellGeo32) * (size_t)gm;
-    for (int q = 0; q < 6; ++q) sz[FirLayout::CUBE0 + q] = (q < ncube) ? tsz * (size_t)n * n_mu : 0;
-    sz[FirLayout::SED2A] = sz[FirLayout::SED2B] = sizeof(float2) * (size_t)n;
+    for (int q = 0; q < 6; ++q) sz[FirLayout::CUBE0 + q] = (q < ncube && !typed_external) ? tsz * (size_t)n * n_mu : 0;
+    sz[FirLayout::SED2A] = sz[FirLayout::SED2B] = typed_external ? 0 : sizeof(float2) * (size_t)n;
     sz[FirLayout::K1A] = sz[FirLayout::K1B] = sizeof(unsigned long long) * (size_t)gm;
     sz[FirLayout::K2A] = sz[FirLayout::K2B] = sizeof(unsigned) * (size_t)gm;
     sz[FirLayout::VA] = sz[FirLayout::VB] = sizeof(int) * (size_t)gm;
@@ -2259,11 +2317,70 @@ FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_l
 
 }  // namespace
 
-FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists) {
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists, bool typed_external) {
     FirPlanSizes p;
     if (form == SOAPGB_PLAIN64) return p;
-    p.bytes = fir_layout(form, n, n_mu, gm, phase ? 6 : 1, n_lists > 0 ? n_lists : 1).total;
+    p.bytes = fir_layout(form, n, n_mu, gm, phase ? 6 : 1, n_lists > 0 ? n_lists : 1, typed_external).total;
     return p;
+}
+
+size_t fir_typed_bytes(int form, int n, int n_mu) {
+    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    return 6 * align256(tsz * (size_t)n * n_mu) + 2 * align256(sizeof(float2) * (size_t)n);
+}
+
+// the six typed cubes of the phase integration (q_sed, q_norm, spot_norm, q_norm -
+// spot_norm, fac_norm, q_norm - fac_norm) and, in the FP32 form, the continuum rows as
+// float pairs
+static int typed_cubes_into(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, void *const dst[6],
+                            float2 *sed2a, float2 *sed2b) {
+    const int n_mu = c.n_mu;
+    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    const size_t cube_elems = (size_t)n * n_mu;
+    const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
+    const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
+    auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+    const bool fused = (tsz == 4) && (cube_elems % 2 == 0) && al16(c.q_sed) && al16(c.q_norm) &&
+                       al16(c.spot_norm) && al16(c.fac_norm);
+    if (fused) {
+        float2 *o[6];
+        for (int q = 0; q < 6; ++q) o[q] = (float2 *)dst[q];
+        const long long n2 = (long long)(cube_elems / 2);
+        // short blocks (two steps per thread): SMs free up quickly for the
+        // higher-priority geometry kernels that run beside this one
+        const int nblk = (int)std::max<long long>(1, (n2 + 511) / 512);
+        SOAP_TRACED(ctx, "cube_types",
+                    k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
+                        n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,
+                        (const double2 *)c.fac_norm, o[0], o[1], o[2], o[3], o[4], o[5]));
+        SOAP_LAUNCHED(ctx);
+    }
+    for (int q = 0; q < 6 && !fused; ++q) {
+        if (tsz == 4)
+            SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst[q]));
+        else
+            SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst[q]));
+        SOAP_LAUNCHED(ctx);
+    }
+    if (form == SOAPGB_FAST32) {
+        k_pair_rows<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, c.spot_sed, c.fac_sed, sed2a, sed2b);
+        SOAP_LAUNCHED(ctx);
+    }
+    return SOAPGB_OK;
+}
+
+int fir_typed_cubes(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, char *dst, FirTyped *out) {
+    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
+    const size_t cb = align256(tsz * (size_t)n * c.n_mu);
+    void *d[6];
+    for (int q = 0; q < 6; ++q) d[q] = dst + q * cb;
+    float2 *sa = (float2 *)(dst + 6 * cb), *sb = (float2 *)(dst + 6 * cb + align256(sizeof(float2) * (size_t)n));
+    for (int q = 0; q < 6; ++q) out->c[q] = d[q];
+    out->spot_sed = c.spot_sed;
+    out->fac_sed = c.fac_sed;
+    out->spot_sed2 = sa;
+    out->fac_sed2 = sb;
+    return typed_cubes_into(ctx, form, n, c, d, sa, sb);
 }
 
 static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
@@ -2374,13 +2491,10 @@ static int fir_lists(soapgb_ctx *ctx, const FirLayout &L, char *ws, long long gm
     return SOAPGB_OK;
 }
 
-template <typename T, int MODE, typename OutT>
-static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
-                        double los, const FirCubes &fc, long long gm, int solar,
-                        int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists,
-                        int stage = 7, int l0 = 0, int l1 = -1, const FirPhaseArgs *pa = nullptr) {
-    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
-    if (l1 < 0) l1 = n_lists;
+// the tile kernels' arguments for the lists of one workspace
+static FirTileArgs make_tile_args(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
+                                  double los, const FirCubes &fc, long long gm, int solar, int t_norm_fac, void *o0,
+                                  void *o1, void *o2, long long out_stride, int n_lists) {
     FirTileArgs A;
     A.n = n;
     A.n_eff = n_eff;
@@ -2410,6 +2524,18 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
     A.plan = nullptr;
     A.run_list = nullptr;
     A.n_lists_all = n_lists;
+    return A;
+}
+
+template <typename T, int MODE, typename OutT>
+static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, int n_eff, const double *lam,
+                        double los, const FirCubes &fc, long long gm, int solar,
+                        int t_norm_fac, void *o0, void *o1, void *o2, long long out_stride, int n_lists,
+                        int stage = 7, int l0 = 0, int l1 = -1, const FirPhaseArgs *pa = nullptr) {
+    constexpr int NC = (MODE == MODE_QUIET) ? 1 : 4;
+    if (l1 < 0) l1 = n_lists;
+    FirTileArgs A = make_tile_args(ctx, L, ws, n, n_eff, lam, los, fc, gm, solar, t_norm_fac, o0, o1, o2, out_stride,
+                                   n_lists);
     const int ntile = (n + FIR_TILE - 1) / FIR_TILE;
     if constexpr (MODE == MODE_PHASE) {
         // plans of every (phase, tile) (stage 1), then the persistent tile kernel over the
@@ -2443,13 +2569,14 @@ static int launch_tiles(soapgb_ctx *ctx, const FirLayout &L, char *ws, int n, in
         if ((stage & 4) && r1 > r0) {
             const int nrun = ntile * (r1 - r0);
             size_t smem_t = fir_pp_smem_fixed<T>() + sizeof(FirSeg) * 2 * (size_t)L.seg_cap;
-            auto kern = ctx->fir_compensated ? k_fir_pp<T, true> : k_fir_pp<T, false>;
+            auto kern = ctx->fir_compensated ? k_fir_pp<T, true, false> : k_fir_pp<T, false, false>;
             SOAP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
             int per_sm = 0;
             SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FIR_THREADS, smem_t));
             const int nblk = std::max(1, std::min(nrun, std::max(per_sm, 1) * std::max(ctx->num_sms, 1)));
             SOAP_TRACED(ctx, "fir_tile_phase",
-                        kern<<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, r0, r1 - r0, ntile * n_lists));
+                        kern<<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A, ntile, r0, r1 - r0, ntile * n_lists,
+                                                                         nullptr, nullptr, 0));
             SOAP_LAUNCHED(ctx);
         }
         return SOAPGB_OK;
@@ -2472,7 +2599,7 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     char *ws = scratch;
     CellGeo *geo = (CellGeo *)(ws + L.off[FirLayout::GEO]);
     CellGeo32 *geo32 = (CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
-    double lambda0 = 0.0;
+    double lambda0 = a.lambda0;
     int rc = fir_prepare(ctx, a.wave, a.n_eff, a.step, gm, a.delta, a.limb, nullptr, a.region, a.n_mu, geo, geo32,
                          &lambda0);
     if (rc) return rc;
@@ -2495,6 +2622,23 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
                                                     0, 0, a.out, nullptr, nullptr, 0, 1);
 }
 
+// the typed cubes a phase integration reads: its workspace slots, or the shared copies
+static FirCubes phase_cubes(const FirLayout &L, char *ws, const FirPhaseArgs &a) {
+    FirCubes fc{};
+    if (a.typed) {
+        for (int q = 0; q < 6; ++q) fc.c[q] = a.typed->c[q];
+        fc.spot_sed2 = (const float2 *)a.typed->spot_sed2;
+        fc.fac_sed2 = (const float2 *)a.typed->fac_sed2;
+    } else {
+        for (int q = 0; q < 6; ++q) fc.c[q] = ws + L.off[FirLayout::CUBE0 + q];
+        fc.spot_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2A]);
+        fc.fac_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2B]);
+    }
+    fc.spot_sed = a.cubes->spot_sed;
+    fc.fac_sed = a.cubes->fac_sed;
+    return fc;
+}
+
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan) {
     (void)plan;
     const int n_mu = a.cubes->n_mu;
@@ -2502,9 +2646,7 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         return set_error(ctx, SOAPGB_ERR_ARG, "collapsed forms support at most %d mu bins (got %d)", FIR_MAX_MU, n_mu);
     if ((form == SOAPGB_FAST32) != (a.out_f32 != 0))
         return set_error(ctx, SOAPGB_ERR_ARG, "FP32 deficits go with the FP32 form only");
-    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    const size_t cube_elems = (size_t)a.n * n_mu;
-    FirLayout L = fir_layout(form, a.n, n_mu, a.gm, 6, a.n_phase);
+    FirLayout L = fir_layout(form, a.n, n_mu, a.gm, 6, a.n_phase, a.typed != nullptr);
     char *ws = scratch;
     CellGeo *geo = (CellGeo *)(ws + L.off[FirLayout::GEO]);
     CellGeo32 *geo32 = (CellGeo32 *)(ws + L.off[FirLayout::GEO32]);
@@ -2520,45 +2662,13 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
         return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: the run stage alone needs lambda0");
     }
     const soapgb_cubes &c = *a.cubes;
-    FirCubes fc{};
-    for (int q = 0; q < 6; ++q) fc.c[q] = ws + L.off[FirLayout::CUBE0 + q];
-    fc.spot_sed = c.spot_sed;
-    fc.fac_sed = c.fac_sed;
-    fc.spot_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2A]);
-    fc.fac_sed2 = (const float2 *)(ws + L.off[FirLayout::SED2B]);
+    FirCubes fc = phase_cubes(L, ws, a);
     if (a.stage & FIR_STAGE_CUBES) {
-        // typed cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm
-        const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
-        const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
-        auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
-        const bool fused = (tsz == 4) && (cube_elems % 2 == 0) && al16(c.q_sed) && al16(c.q_norm) &&
-                           al16(c.spot_norm) && al16(c.fac_norm);
-        if (fused) {
-            float2 *o[6];
-            for (int q = 0; q < 6; ++q) o[q] = (float2 *)const_cast<void *>(fc.c[q]);
-            const long long n2 = (long long)(cube_elems / 2);
-            // short blocks (two steps per thread): SMs free up quickly for the
-            // higher-priority geometry kernels that run beside this one
-            const int nblk = (int)std::max<long long>(1, (n2 + 511) / 512);
-            SOAP_TRACED(ctx, "cube_types",
-                        k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
-                            n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,
-                            (const double2 *)c.fac_norm, o[0], o[1], o[2], o[3], o[4], o[5]));
-            SOAP_LAUNCHED(ctx);
-        }
-        for (int q = 0; q < 6 && !fused; ++q) {
-            void *dst = const_cast<void *>(fc.c[q]);
-            if (tsz == 4)
-                SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst));
-            else
-                SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst));
-            SOAP_LAUNCHED(ctx);
-        }
-        if (form == SOAPGB_FAST32) {
-            k_pair_rows<<<grid_for(ctx, a.n, 256), 256, 0, ctx->stream>>>(a.n, c.spot_sed, c.fac_sed,
-                                                                          (float2 *)fc.spot_sed2, (float2 *)fc.fac_sed2);
-            SOAP_LAUNCHED(ctx);
-        }
+        if (a.typed) return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: shared typed cubes are made by fir_typed_cubes");
+        void *d[6];
+        for (int q = 0; q < 6; ++q) d[q] = const_cast<void *>(fc.c[q]);
+        int rc = typed_cubes_into(ctx, form, a.n, c, d, (float2 *)fc.spot_sed2, (float2 *)fc.fac_sed2);
+        if (rc) return rc;
     }
     const int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
     const double los = lambda0 / a.step;
@@ -2571,4 +2681,47 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     return launch_tiles<double, MODE_PHASE, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, a.gm,
                                                     a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride,
                                                     a.n_phase, st, a.l0, l1, &a);
+}
+
+size_t fir_tile_args_bytes() { return sizeof(FirTileArgs); }
+
+int fir_phase_star_args(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, void *out) {
+    if (form != SOAPGB_FAST32) return set_error(ctx, SOAPGB_ERR_ARG, "several stars in one launch: FP32 form only");
+    if (!a.typed || !(a.lambda0 > 0.0) || !a.run_list)
+        return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase_star_args: needs shared typed cubes, lambda0 and run lists");
+    const int n_mu = a.cubes->n_mu;
+    FirLayout L = fir_layout(form, a.n, n_mu, a.gm, 6, a.n_phase, true);
+    char *ws = scratch;
+    const int t_norm_fac = (int)(a.act->t_star + a.act->t_diff_fac + 0.9 - 216.8);
+    FirTileArgs A = make_tile_args(ctx, L, ws, a.n, a.n_eff, a.wave, a.lambda0 / a.step, phase_cubes(L, ws, a), a.gm,
+                                   a.act->solar, t_norm_fac, a.flux, a.bconv, a.tot, a.out_stride, a.n_phase);
+    A.plan = ws + L.off[FirLayout::PLAN];
+    A.run_list = a.run_list;
+    memcpy(out, &A, sizeof(A));
+    return SOAPGB_OK;
+}
+
+int fir_phase_multi(soapgb_ctx *ctx, int form, const void *star0_args, const void *d_star_args, const int2 *d_items,
+                    int n_items, int chunk, int blocks_per_sm) {
+    if (form != SOAPGB_FAST32) return set_error(ctx, SOAPGB_ERR_ARG, "several stars in one launch: FP32 form only");
+    if (n_items <= 0) return SOAPGB_OK;
+    FirTileArgs A0;
+    memcpy(&A0, star0_args, sizeof(A0));
+    const int ntile = (A0.n + FIR_TILE - 1) / FIR_TILE;
+    // every star's segments fit the capacity of the cubes' mu bins (seg_cap = 2 n_mu)
+    size_t smem_t = fir_pp_smem_fixed<float>() + sizeof(FirSeg) * 2 * (size_t)A0.seg_cap;
+    auto kern = ctx->fir_compensated ? k_fir_pp<float, true, true> : k_fir_pp<float, false, true>;
+    SOAP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+    int per_sm = 0;
+    SOAP_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FIR_THREADS, smem_t));
+    per_sm = std::max(per_sm, 1);
+    if (blocks_per_sm > 0) per_sm = std::min(per_sm, blocks_per_sm);
+    const long long total = (long long)n_items * ntile;
+    if (total >= (1LL << 31)) return set_error(ctx, SOAPGB_ERR_ARG, "too many (phase, tile) pairs in one launch");
+    const int nblk = (int)std::max(1LL, std::min(total, (long long)per_sm * std::max(ctx->num_sms, 1)));
+    SOAP_TRACED(ctx, "fir_tile_phase_multi",
+                kern<<<nblk, FIR_THREADS, smem_t, ctx->stream>>>(A0, ntile, 0, n_items, 0,
+                                                                 (const FirTileArgs *)d_star_args, d_items, chunk));
+    SOAP_LAUNCHED(ctx);
+    return SOAPGB_OK;
 }

@@ -11,7 +11,20 @@ struct FirPlanSizes {
 // workspace of the FAST forms: per-cell geometry for the G*G grid, the velocity order
 // of the cells, per-list cell lists / prefix sums / segments and typed cube copies
 // (one cube for the quiet disk, six for the phase integration)
-FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists);
+// typed_external: the phase integration reads typed cubes shared with other stars
+// (fir_typed_cubes), so the workspace holds none
+FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists,
+                            bool typed_external = false);
+
+// typed copies of the seed cubes read by the phase integration, shareable by the stars of
+// a batch (they share the seed spectra)
+struct FirTyped {
+    const void *c[6];
+    const double *spot_sed, *fac_sed;
+    const void *spot_sed2, *fac_sed2;
+};
+size_t fir_typed_bytes(int form, int n, int n_mu);
+int fir_typed_cubes(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, char *dst, FirTyped *out);
 
 struct FirQuietArgs {
     int n, n_eff;
@@ -23,6 +36,7 @@ struct FirQuietArgs {
     const int *region;
     double step;
     double *out;            // n (tail set to 0)
+    double lambda0 = 0.0;   // wave[0] when known on the host (0: read from the device)
 };
 
 int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, const FirPlanSizes &plan);
@@ -61,10 +75,24 @@ struct FirPhaseArgs {
     int stage = 7;
     int l0 = 0, l1 = -1;        // l1 < 0: all phases
     double lambda0 = 0.0;       // wave[0] when known on the host (0: read from the device)
+    const FirTyped *typed = nullptr;   // shared typed cubes (the workspace then has no cube slots)
 };
 enum { FIR_STAGE_GEOMETRY = 1, FIR_STAGE_CUBES = 2, FIR_STAGE_RUN = 4 };
 
 int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, const FirPlanSizes &plan);
+
+// Several stars' phase integrations in one persistent launch (FP32 form).  Each star has
+// run its geometry stage (fir_phase with FIR_STAGE_GEOMETRY and run lists) in its own
+// workspace, with shared typed cubes; fir_phase_star_args writes its kernel arguments
+// (fir_tile_args_bytes() bytes) to out, host memory.  fir_phase_multi then integrates
+// the items (star, phase) of d_items (device, n_items) from the device copy of those
+// arguments (d_star_args, one record per star); star0_args is a host copy of the first
+// (its grid-wide fields).  chunk: positions per round-robin chunk (0: contiguous shares);
+// blocks_per_sm: 0 for as many as fit.
+size_t fir_tile_args_bytes();
+int fir_phase_star_args(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, void *out);
+int fir_phase_multi(soapgb_ctx *ctx, int form, const void *star0_args, const void *d_star_args, const int2 *d_items,
+                    int n_items, int chunk, int blocks_per_sm);
 // largest G*G whose phase lists can be built from the region boxes
 long long fir_box_lists_max_gm();
 // capacity of the per-phase sort for phases of at most max_box_cells box cells (0: too many)

@@ -12,7 +12,8 @@ standard workloads:
        a facula (3 %) then an overlapping spot (1 %), 100 phases, 4,000-line mask,
        161 CCF velocities (-20..20 km/s at 0.25 km/s).
 * 2 -- the star of 1 (computed in the FP32 compensated form by the caller).
-* 3 -- many stars of uneven sizes sharing the 310k-px seeds (batched form).
+* 3 -- many stars of uneven sizes sharing the 310k-px seeds (batched form,
+       ``make_batch``).
 * 4 -- 200x200 grid, 100,000 px, 3 regions, 50 phases (differentiable form).
 
 Spectra: continuum 1 minus Gaussian lines with centres U(range), depths U(0.05, 0.9)
@@ -126,6 +127,29 @@ def small_case(seed: int = 7, grid: int = 40, n: int = 4096, n_phase: int = 4, n
                 regions=np.array([[25.0, 185.0, 0.25, 1.0], [20.0, 175.0, 0.2, 0.0]]),
                 n_phase=n_phase, rot_step=1.0 / max(n_phase, 1), n_mask_lines=12,
                 ccf_window=20000.0, ccf_size=500.0, vsini=4.0, seed=seed)
+
+
+def make_batch(n_star: int = 256, seed: int = 3, grid=(100, 400), n_regions=(1, 12), size_pct=(0.1, 3.0),
+               lat=(-60.0, 60.0), n_phase=(20, 200), vsini=(1.0, 10.0)) -> List[Case]:
+    """The stars of the batched form: per star a grid side U{grid}, U{n_regions} spots
+    and faculae (type U{0, 1}) of size U(size_pct) % of the hemisphere (chord radius
+    sqrt(f)), latitude U(lat), longitude U(0, 360), U{n_phase} phases over one rotation
+    and vsini U(vsini) km/s; everything else as the 300x300-grid star.  The seed spectra
+    are shared (``generate(make_case(1))`` at full size)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_star):
+        g = int(rng.integers(grid[0], grid[1] + 1))
+        nr = int(rng.integers(n_regions[0], n_regions[1] + 1))
+        f = rng.uniform(size_pct[0], size_pct[1], nr) / 100.0
+        regions = np.column_stack([rng.uniform(lat[0], lat[1], nr), rng.uniform(0.0, 360.0, nr), np.sqrt(f),
+                                   rng.integers(0, 2, nr).astype(np.float64)])
+        npk = int(rng.integers(n_phase[0], n_phase[1] + 1))
+        out.append(Case("batch%d" % k, grid=g, n=310000, lambda0=3800.0, step=0.01, n_lines=6000, n_mu=20,
+                        regions=regions, n_phase=npk, rot_step=1.0 / npk, n_mask_lines=4000,
+                        ccf_window=20000.0, ccf_size=250.0, vsini=float(rng.uniform(vsini[0], vsini[1])),
+                        seed=seed))
+    return out
 
 
 @dataclasses.dataclass
