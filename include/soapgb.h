@@ -262,9 +262,11 @@ int soapgb_gauss_bis(soapgb_ctx *ctx, int n_spec, int n, const double *x, const 
  * optimum: H dtheta/dy = J^T W with H the full Hessian of the residual sum of squares
  * (Gauss-Newton term plus the residual-weighted second derivatives).  x, y, err as
  * for the fit; model and par are its outputs; g_par (n_spec x 5) holds the gradient
- * of a scalar w.r.t. par = (c, |k|, span, v0, fwhm); the span's entry is ignored (the
- * bisector is not differentiated).  Writes grad_y (n_spec x n).  A singular system
- * gives a zero gradient for that spectrum and the status SOAPGB_ERR_DEVICE. */
+ * of a scalar w.r.t. par = (c, |k|, span, v0, fwhm).  The bisector span
+ * (BIS_FIT2.cpp:214-268) is differentiated with its per-depth crossing intervals held
+ * fixed (a discrete choice, like the region coverage): through the normalised CCF
+ * directly and through the fit's parameters.  Writes grad_y (n_spec x n).  A singular
+ * system gives a zero gradient for that spectrum and the status SOAPGB_ERR_DEVICE. */
 int soapgb_gauss_fit_adjoint(soapgb_ctx *ctx, int n_spec, int n, const double *x, const double *y,
                              const double *err, const double *model, const double *par,
                              const double *g_par, int mem, double *grad_y);

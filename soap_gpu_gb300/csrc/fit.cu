@@ -414,6 +414,82 @@ __global__ void __launch_bounds__(32 * FIT_WARPS) k_gauss_fit_adj(int n_spec, in
 #pragma unroll
     for (int q = 0; q < 10; ++q) H[q] = warp_sum(H[q]);
     double A[16], b[4] = {gp[0], gp[1] * sgn, gp[3], gp[4]}, z[4] = {0, 0, 0, 0};
+    // --- the bisector span (BIS_FIT2.cpp:214-268).  Per depth the forward picks the
+    // intervals i_b, i_r where the normalised CCF a_i = (y_i - c) / k crosses it (held fixed
+    // here: a discrete choice) and evaluates on each the quadratic inverse
+    //   P_i(d) = x_i + dx_i (d - a_i) / (a_{i+1} - a_i) + q2_i (d - a_i)(d - a_{i+1}),
+    // the closed form of its p0 + p1 d + p2 d^2, with q2_i = -C''/(2 C'^3) of the fitted
+    // Gaussian at the interval's middle.  The span is the mean of the bisector over depths
+    // 0.1-0.4 minus its mean over 0.6-0.9; its gradient reaches y directly (a_i) and through
+    // the fit's parameters (c, k in a_i; v0, sigma in q2_i), the latter added to b.
+    const int wp = threadIdx.x >> 5;
+    __shared__ int sp_ib[FIT_WARPS][FIT_DEPTHS], sp_ir[FIT_WARPS][FIT_DEPTHS];
+    __shared__ double sp_d[FIT_WARPS][FIT_DEPTHS][4];
+    const double gs = gp[2];
+    if (gs != 0.0) {   // uniform for the warp
+        auto nrm = [&](int i) { return -c / k * (1. - y[i] / c); };   // the forward's expression
+        double bv = -1e308;
+        int bix = n;
+        for (int i = lane; i < n; i += 32) {
+            const double v = nrm(i);
+            if (v > bv) { bv = v; bix = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bix, o);
+            if (ov > bv || (ov == bv && oi < bix)) { bv = ov; bix = oi; }
+        }
+        const int ind_max = bix;
+        int n1 = 0, n2 = 0;
+        for (int t = 0; t < FIT_DEPTHS; ++t) {
+            const double dep = (double)(t + 5) / 100;
+            if ((dep >= 0.1) && (dep <= 0.4)) n1++;
+            if ((dep >= 0.6) && (dep <= 0.9)) n2++;
+        }
+        const double sig_b = fwhm / 2. / pow(2. * log(2.), .5), ss = sig_b * sig_b;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};   // d span / d (c, k, v0, ss)
+        for (int t = lane; t < FIT_DEPTHS; t += 32) {
+            const double dep = (double)(t + 5) / 100;
+            double w = 0.0;
+            if ((dep >= 0.1) && (dep <= 0.4)) w += 1.0 / n1;
+            if ((dep >= 0.6) && (dep <= 0.9)) w -= 1.0 / n2;
+            int i_b = ind_max, i_r = ind_max;
+            while ((nrm(i_b) > dep) && (i_b > 1)) i_b--;
+            while ((nrm(i_r + 1) > dep) && (i_r < (n - 2))) i_r++;
+            sp_ib[wp][t] = i_b;
+            sp_ir[wp][t] = i_r;
+            for (int side = 0; side < 2; ++side) {
+                const int i = side ? i_r : i_b;
+                const double a0 = nrm(i), a1 = nrm(i + 1), dx = x[i + 1] - x[i], den = a1 - a0;
+                const double dd = (x[i] + x[i + 1]) / 2. - v0;
+                const double e = exp(-(dd * dd) / 2. / ss);
+                const double dC = -dd / ss * e, d2C = ((dd * dd) / ss - 1) / ss * e;
+                const double q2 = -d2C / (2. * dC * dC * dC);
+                const double d3C = e * dd * (3. - dd * dd / ss) / (ss * ss);
+                const double dCs = dd * e / (ss * ss) * (1. - dd * dd / (2. * ss));
+                const double d2Cs = e * ((-2. * dd * dd / (ss * ss * ss) + 1. / (ss * ss)) +
+                                         (dd * dd / (ss * ss) - 1. / ss) * (dd * dd / (2. * ss * ss)));
+                const double c3 = dC * dC * dC, c4 = c3 * dC;
+                const double q2_dd = -0.5 * (d3C / c3 - 3. * d2C * d2C / c4);
+                const double q2_ss = -0.5 * (d2Cs / c3 - 3. * d2C * dCs / c4);
+                const double h = 0.5 * w;
+                const double pa0 = h * (dx * (dep - a1) / (den * den) - q2 * (dep - a1));
+                const double pa1 = h * (-dx * (dep - a0) / (den * den) - q2 * (dep - a0));
+                const double pq2 = h * (dep - a0) * (dep - a1);
+                sp_d[wp][t][2 * side] = pa0;
+                sp_d[wp][t][2 * side + 1] = pa1;
+                acc[0] += -(pa0 + pa1) / k;
+                acc[1] += -(pa0 * a0 + pa1 * a1) / k;
+                acc[2] += -pq2 * q2_dd;   // dd = vr - v0
+                acc[3] += pq2 * q2_ss;
+            }
+        }
+        b[0] += gs * warp_sum(acc[0]);
+        b[1] += gs * warp_sum(acc[1]);
+        b[2] += gs * warp_sum(acc[2]);
+        b[3] += gs * warp_sum(acc[3]) * 2. * ss / fwhm;   // ss = (fwhm / 2 sqrt(2 ln 2))^2
+    }
+    __syncwarp();
     {
         int t = 0;
         for (int p = 0; p < 4; ++p)
@@ -427,7 +503,19 @@ __global__ void __launch_bounds__(32 * FIT_WARPS) k_gauss_fit_adj(int n_spec, in
         const double inv = 1.0 / (err ? err[i] : 1.0);
         const double d = x[i] - v0, d2 = d * d;
         const double e = exp(-d2 / 2 / s2);
-        gy[i] = inv * inv * (z[0] + e * z[1] + (k * e * d / s2) * z[2] + (k * e * d2 * a / s3) * z[3]);
+        double g = inv * inv * (z[0] + e * z[1] + (k * e * d / s2) * z[2] + (k * e * d2 * a / s3) * z[3]);
+        if (gs != 0.0) {   // the span's direct dependence on y_i (through a_i), depths in order
+            double dir = 0.0;
+            for (int t = 0; t < FIT_DEPTHS; ++t) {
+                const int ib = sp_ib[wp][t], ir = sp_ir[wp][t];
+                if (ib == i) dir += sp_d[wp][t][0];
+                if (ib + 1 == i) dir += sp_d[wp][t][1];
+                if (ir == i) dir += sp_d[wp][t][2];
+                if (ir + 1 == i) dir += sp_d[wp][t][3];
+            }
+            g += gs * dir / k;
+        }
+        gy[i] = g;
     }
 }
 

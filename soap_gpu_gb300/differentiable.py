@@ -27,8 +27,26 @@ normalisation of base - spec, by the hand-written adjoint of
 (``soapgb_ccf_adjoint``) and the fit's implicit derivative at its optimum
 (``soapgb_gauss_fit_adjoint``), so a loss on an RV curve reaches u1, u2 and vsini.
 
-Region positions and sizes stay discrete (cell coverage), as in the reference; the
-inclination and the region contrast are not differentiated yet.
+``QuietSpectrum`` differentiates the quiet-star disk sum (SOAP_initialize.cu:339-395)
+in the same parameters: it is the integration of every visible cell with the quiet
+cube's row, so its adjoint is ``soapgb_phase_integrate_adjoint`` on one phase in which
+every visible cell is active (bconv = the quiet sum when the spot rows are zero).
+
+The star vector is (u1, u2, vsini[, inclination in degrees]).  The inclination enters
+the cells' velocities, v = y omega sin(i) (SOAP_initialize.cu:351), so d delta / d i =
+delta cot(i); the region maps' coverage, which also moves with the inclination (the rim
+rotation, SOAP_integration.cu:125-161), stays discrete like the regions' positions and
+sizes.  The region contrast is the level of the spot and facula continuum rows
+(SOAP_integration.cu:309-323: the Planck ratio of a spot is exactly 1, so its intensity
+is its continuum row): a caller scales those rows by contrast parameters and autograd
+carries the continuum-row gradients to them.
+
+``GaussFitBis`` adds the bisector span (BIS_FIT2.cpp:214-268) to the fitted parameters;
+``rv_series_checkpointed`` runs the chain phase chunk by phase chunk under
+``torch.utils.checkpoint``, keeping only each chunk's fitted parameters for the backward
+pass and recomputing the chunk's spectra there.
+
+Region positions and sizes stay discrete (cell coverage), as in the reference.
 """
 from __future__ import annotations
 
@@ -76,11 +94,40 @@ class IntegrationSetup:
         """Equatorial velocity [km/s] of the setup's rotation period."""
         return 2 * np.pi * self.radius_km / (self.period * 86400.0)
 
-    def maps(self, u1: float, u2: float, vsini: float) -> dict:
-        """The disk maps for limb-darkening coefficients (u1, u2) and vsini, on the device."""
+    def maps(self, u1: float, u2: float, vsini: float, incl: float = None) -> dict:
+        """The disk maps for limb-darkening coefficients (u1, u2), vsini and the
+        inclination (default: the setup's, which fixed the region maps), on the device."""
         period = 2 * np.pi * self.radius_km / (vsini * 86400.0)
-        return self.ctx.disk_maps(self.grid, period, self.omega_ratio, self.incl, self.radius_km, u1, u2,
-                                  self.mu_boundary, self.lb)
+        return self.ctx.disk_maps(self.grid, period, self.omega_ratio, self.incl if incl is None else incl,
+                                  self.radius_km, u1, u2, self.mu_boundary, self.lb)
+
+    def phases(self, p0: int, p1: int) -> "IntegrationSetup":
+        """The same setup restricted to phases [p0, p1)."""
+        return dataclasses.replace(self, temp=self.temp[p0:p1], bi=self.bi[p0:p1])
+
+    @property
+    def n_phase(self) -> int:
+        return int(self.temp.shape[0])
+
+
+def _star_maps(setup: IntegrationSetup, star):
+    incl = float(star[3]) if star.numel() > 3 else None
+    return setup.maps(float(star[0]), float(star[1]), float(star[2]), incl), incl
+
+
+def _star_grad(star, maps, gl, gd, vsini, incl):
+    """Chain rules from the limb and velocity map gradients to (u1, u2, vsini[, incl])
+    over the visible cells: L = 1 - u1 (1 - mu) - u2 (1 - mu)^2, delta proportional to
+    vsini and to sin(i)."""
+    vis = maps["limb"] > -998.0
+    zero = torch.zeros_like(maps["mu"])
+    om = torch.where(vis, 1.0 - maps["mu"], zero)
+    dl = torch.where(vis, maps["delta"], zero)
+    g = [-(gl * om).sum(), -(gl * om * om).sum(), (gd * dl).sum() / vsini]
+    if star.numel() > 3:
+        rad = np.pi / 180.0
+        g.append((gd * dl).sum() * rad * np.cos(incl * rad) / np.sin(incl * rad))
+    return torch.stack(g).to(star.dtype)
 
 
 class DeficitSpectra(torch.autograd.Function):
@@ -90,8 +137,8 @@ class DeficitSpectra(torch.autograd.Function):
     @staticmethod
     def forward(fctx, star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup: IntegrationSetup):
         vsini = float(star[2])
-        maps = setup.maps(float(star[0]), float(star[1]), vsini)
-        fctx.vsini = vsini
+        maps, incl = _star_maps(setup, star)
+        fctx.vsini, fctx.incl, fctx.star = vsini, incl, star.detach()
         cubes = dict(zip(CUBE_KEYS, (q_norm.detach(), q_sed.detach(), spot_norm.detach(), fac_norm.detach(),
                                      spot_sed.detach(), fac_sed.detach())))
         flux, bconv, tot = setup.ctx.phase_integrate("plain64", setup.wave, setup.n_eff, setup.grid, setup.temp,
@@ -108,13 +155,7 @@ class DeficitSpectra(torch.autograd.Function):
         gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, setup.temp, setup.bi, maps,
                                                fctx.cubes, setup.step, setup.act, g[:, 0].contiguous(),
                                                g[:, 1].contiguous(), g[:, 2].contiguous())
-        # chain rules over the visible cells: limb-darkening coefficients, vsini
-        vis = maps["limb"] > -998.0
-        zero = torch.zeros_like(maps["mu"])
-        om = torch.where(vis, 1.0 - maps["mu"], zero)
-        gl = gr["limb"]
-        dv = torch.where(vis, maps["delta"], zero) / fctx.vsini
-        grad_star = torch.stack((-(gl * om).sum(), -(gl * om * om).sum(), (gr["delta"] * dv).sum()))
+        grad_star = _star_grad(fctx.star, maps, gr["limb"], gr["delta"], fctx.vsini, fctx.incl)
         return (grad_star, gr["q_norm"], gr["q_sed"], gr["spot_norm"], gr["fac_norm"], gr["spot_sed"],
                 gr["fac_sed"], None)
 
@@ -123,6 +164,44 @@ def deficit_spectra(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed,
     """Differentiable (n_phase, 3, n) deficit spectra, star = (u1, u2, vsini); see
     ``DeficitSpectra``."""
     return DeficitSpectra.apply(star, q_norm, q_sed, spot_norm, fac_norm, spot_sed, fac_sed, setup)
+
+
+class QuietSpectrum(torch.autograd.Function):
+    """The quiet-star disk sum of one cube (``soapgb_quiet_disk``, PLAIN64,
+    SOAP_initialize.cu:339-395) as a function of star = (u1, u2, vsini[, incl]) and the
+    cube.  Backward: the integration adjoint on one phase in which every visible cell is
+    active with the quiet cube as its normalised row and zero active rows, so that its
+    bconv output is exactly the quiet sum."""
+
+    @staticmethod
+    def forward(fctx, star, cube, setup: IntegrationSetup):
+        maps, incl = _star_maps(setup, star)
+        c = cube.detach().contiguous()
+        out = setup.ctx.quiet_disk("plain64", setup.wave, c, setup.n_eff, maps, setup.grid, setup.step)
+        fctx.setup, fctx.maps, fctx.cube, fctx.star = setup, maps, c, star.detach()
+        fctx.vsini, fctx.incl = float(star[2]), incl
+        return out.reshape(-1)
+
+    @staticmethod
+    def backward(fctx, g):
+        setup, maps = fctx.setup, fctx.maps
+        act = setup.act
+        vis = (maps["limb"] > -998.0).reshape(1, -1)
+        # every visible cell a spot (the spot intensity ratio is 1, so its temperature is moot)
+        bi = torch.where(vis, 0.0, -9999.0).to(torch.float64)
+        temp = torch.where(vis, float(act.t_star - act.t_diff_spot), -9999.0).to(torch.float64)
+        zc = torch.zeros_like(fctx.cube)
+        zr = torch.zeros_like(setup.wave)
+        cubes = dict(q_norm=fctx.cube, q_sed=zc, spot_norm=zc, fac_norm=zc, spot_sed=zr, fac_sed=zr)
+        gz = torch.zeros((1, setup.wave.shape[0]), dtype=torch.float64, device=g.device)
+        gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, temp, bi, maps, cubes, setup.step,
+                                               act, gz, g.to(torch.float64).reshape(1, -1).contiguous(), gz)
+        return _star_grad(fctx.star, maps, gr["limb"], gr["delta"], fctx.vsini, fctx.incl), gr["q_norm"], None
+
+
+def quiet_spectrum(star, cube, setup: IntegrationSetup):
+    """Differentiable (n,) quiet-star spectrum of ``cube``; see ``QuietSpectrum``."""
+    return QuietSpectrum.apply(star, cube, setup)
 
 
 @dataclasses.dataclass
@@ -238,6 +317,70 @@ class GaussFit(torch.autograd.Function):
         # forward does for a fit that did not converge, rather than return that zero
         s.ctx.synchronize()
         return gy, None
+
+
+class GaussFitBis(torch.autograd.Function):
+    """(c, |k|, span, v0, fwhm) of the Gaussian fit and bisector of each CCF
+    (``soapgb_gauss_bis``); backward: ``soapgb_gauss_fit_adjoint`` with the span's
+    gradient (its per-depth crossing intervals held fixed)."""
+
+    @staticmethod
+    def forward(fctx, ccf, setup: CcfSetup):
+        y = ccf.detach().contiguous()
+        res = setup.ctx.gauss_bis(setup.vel, y)
+        if bool((res["iters"] < 0).any()):
+            raise RuntimeError("Gaussian fit did not converge; its gradient is undefined")
+        fctx.setup, fctx.y, fctx.model, fctx.par = setup, y, res["model"], res["par"]
+        return res["par"].clone()
+
+    @staticmethod
+    def backward(fctx, g):
+        s = fctx.setup
+        gy = s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, g.to(torch.float64).contiguous())
+        s.ctx.synchronize()
+        return gy, None
+
+
+def gauss_fit_bis(ccf, setup: CcfSetup):
+    """Differentiable (n_spec, 5) fit parameters (c, |k|, span, v0, fwhm); see ``GaussFitBis``."""
+    return GaussFitBis.apply(ccf, setup)
+
+
+def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: ResolutionSetup, csetup: CcfSetup,
+                           chunk: int = 10, kind: int = 0, quiet_cube: str = "q_sed"):
+    """RV, span and FWHM series of one spectrum type over the setup's phases, relative to
+    the quiet star, with the quiet spectrum differentiated too.  kind selects the
+    deficit (0 flux, 1 bconv, 2 tot) and quiet_cube the quiet base (q_sed for flux and
+    tot, q_norm for bconv, as run_all_SOAP.py pairs them).
+
+    The phases run in chunks of `chunk` under torch.utils.checkpoint: the forward keeps
+    each chunk's fitted parameters only, and the backward recomputes the chunk's deficit,
+    low-resolution spectra and CCFs before running their adjoints, so the memory held for
+    the backward grows with the fitted parameters, not with the spectra."""
+    from torch.utils.checkpoint import checkpoint
+    keys = CUBE_KEYS
+    cube_list = [cubes[k] for k in keys]
+    base = quiet_spectrum(star, cubes[quiet_cube], setup)
+    zero = torch.zeros((1, setup.wave.shape[0]), dtype=torch.float64, device=setup.wave.device)
+    q_par = gauss_fit_bis(normalised_ccf(_trim(lower_resolution(zero, base, rsetup)), csetup), csetup)
+
+    def chunk_par(p0, p1, star_, base_, *cl):
+        sub = setup.phases(p0, p1)
+        d = deficit_spectra(star_, *cl, sub)[:, kind].contiguous()
+        low = lower_resolution(d, base_, rsetup)
+        return gauss_fit_bis(normalised_ccf(_trim(low), csetup), csetup)
+
+    pars = []
+    for p0 in range(0, setup.n_phase, chunk):
+        p1 = min(setup.n_phase, p0 + chunk)
+        pars.append(checkpoint(chunk_par, p0, p1, star, base, *cube_list, use_reentrant=False))
+    par = torch.cat(pars)
+    return {"rv": par[:, 3] - q_par[0, 3], "span": par[:, 2], "fwhm": par[:, 4], "par": par, "quiet": q_par[0]}
+
+
+def _trim(a):
+    """The [200:-200][10:-10] trim of run_all_SOAP.py:259,266 (a view)."""
+    return a[..., 210:-210]
 
 
 def normalised_ccf(spectra, setup: CcfSetup):
