@@ -2,6 +2,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
+#include <algorithm>
 
 #include "internal.cuh"
 
@@ -226,6 +228,8 @@ int soapgb_ctx_create(int device, soapgb_ctx **out) {
         return rc;
     }
     ctx->stream = ctx->own_stream;
+    if (const char *v = getenv("SOAPGB_TEST_WAIT_LIMIT")) ctx->test_wait_limit = std::max(0LL, atoll(v));
+    if (const char *v = getenv("SOAPGB_TEST_DROP_COPY")) ctx->test_drop_copy = atoi(v);
     *out = ctx;
     return SOAPGB_OK;
 }

@@ -858,8 +858,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
         : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
-    for (long long it = 0; it < FIR_WAIT_LIMIT; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
+                                                  long long limit = FIR_WAIT_LIMIT) {
+    for (long long it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -1071,6 +1072,8 @@ struct FirTileArgs {
     const void *plan;           // FirPrePlan<T> per (list, tile), or null
     const int *run_list;        // lists to integrate (ascending), or null for all of them
     int n_lists_all;            // lists with a plan slot
+    long long wait_limit;       // polls per bounded wait of the persistent kernel
+    int drop_plan;              // failure-path test: the first plan copy is expected, not issued
 };
 
 // The list's (class, mu bin, v == 0) segments with their shift ranges at the tile
@@ -1782,11 +1785,12 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         if (chunk <= 0) return vb + k;
         return ((int)blockIdx.x + (k / chunk) * G) * chunk + k % chunk;
     };
-    // (thread 0) copy the plan of walk position v into plan buffer b
-    auto issue_plan = [&](int v, int b, unsigned bytes) {
+    // (thread 0) copy the plan of walk position v into plan buffer b; under the
+    // failure-path test the block's first plan is expected but never copied
+    auto issue_plan = [&](int v, int b, unsigned bytes, bool first = false) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(&sh.pbar[b], bytes);
-        bulk_g2s(&sh.pb[b][0], plan_rec(v), bytes, &sh.pbar[b]);
+        if (!(first && A0.drop_plan)) bulk_g2s(&sh.pb[b][0], plan_rec(v), bytes, &sh.pbar[b]);
     };
     // (thread 0) stage the rows of unit number u (buffer u % 3)
     auto issue_unit = [&](int u, const FirUnit &d) {
@@ -1989,14 +1993,14 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     };
     // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
     auto wait_unit = [&](int u) {
-        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1))) atomicExch(&sh.fail, 1);
+        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1), A0.wait_limit)) atomicExch(&sh.fail, 1);
         __syncthreads();
         return sh.fail == 0;
     };
 
     // walk steps [0, kend)
     if (tid == 0) {
-        if (kend > 0) issue_plan(pos(0), 0, plan_size(pos(0)));
+        if (kend > 0) issue_plan(pos(0), 0, plan_size(pos(0)), true);
         if (kend > 1) issue_plan(pos(1), 1, plan_size(pos(1)));
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount % 3)
@@ -2022,7 +2026,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 cur_star = s_v;
             }
         }
-        if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1))) atomicExch(&sh.fail, 1);
+        if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1), A0.wait_limit)) atomicExch(&sh.fail, 1);
         __syncthreads();
         if (sh.fail) {
             bad = 1;
@@ -2067,7 +2071,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     } else {
                         // last unit: issue the next tile's first unit, from its plan
                         pre = false;
-                        if (k + 1 < kend && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1))) {
+                        if (k + 1 < kend && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit)) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
                             const int tnr = real(pos(k + 1));
@@ -2230,11 +2234,11 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         // bounded wait before leaving
         atomicExch(A0.status, FIR_ST_WAIT);
         if (FIR_PP_STAGED) {
-            mbar_wait_bounded(&sh.wbar[ucount % FIR_PP_NBUF], (unsigned)((ucount / FIR_PP_NBUF) & 1));
-            mbar_wait_bounded(&sh.wbar[(ucount + 1) % FIR_PP_NBUF], (unsigned)(((ucount + 1) / FIR_PP_NBUF) & 1));
+            mbar_wait_bounded(&sh.wbar[ucount % FIR_PP_NBUF], (unsigned)((ucount / FIR_PP_NBUF) & 1), A0.wait_limit);
+            mbar_wait_bounded(&sh.wbar[(ucount + 1) % FIR_PP_NBUF], (unsigned)(((ucount + 1) / FIR_PP_NBUF) & 1), A0.wait_limit);
         }
-        mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1));
-        mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1));
+        mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1), A0.wait_limit);
+        mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit);
     }
 }
 
@@ -2524,6 +2528,8 @@ static FirTileArgs make_tile_args(soapgb_ctx *ctx, const FirLayout &L, char *ws,
     A.plan = nullptr;
     A.run_list = nullptr;
     A.n_lists_all = n_lists;
+    A.wait_limit = ctx->test_wait_limit > 0 ? ctx->test_wait_limit : FIR_WAIT_LIMIT;
+    A.drop_plan = (ctx->test_drop_copy == 1) ? 1 : 0;
     return A;
 }
 

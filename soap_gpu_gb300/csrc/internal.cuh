@@ -56,6 +56,13 @@ struct soapgb_ctx {
     double edge_w3[3] = {0.0, 0.0, 0.0};
     // FP32 per-phase integration: compensated (Kahan) output sums (soapgb_set_compensated)
     bool fir_compensated = false;
+    // failure-path tests only, read from the environment at context creation:
+    // SOAPGB_TEST_WAIT_LIMIT polls per bounded wait of the staged-copy kernels (0: the
+    // default 2^24) and SOAPGB_TEST_DROP_COPY, a staged copy whose bytes are expected but
+    // never issued, so that its wait runs out (1: the integration kernel's first plan
+    // copy, status 41; 2: the FP32 convolution's first window, status 42)
+    long long test_wait_limit = 0;
+    int test_drop_copy = 0;
     // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report
     bool trace = false;
     std::vector<SoapTraceSpan> spans;

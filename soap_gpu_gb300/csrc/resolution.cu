@@ -772,7 +772,8 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
                                                            float *__restrict__ conv, long long conv_stride,
                                                            unsigned *mm32, float *blk, int nbx, int *status,
                                                            const unsigned char *__restrict__ zero_spec,
-                                                           const int *__restrict__ rows, int nrows) {
+                                                           const int *__restrict__ rows, int nrows,
+                                                           long long wait_limit, int drop_first) {
     static_assert(SB <= 31, "one bit per spectrum of a batch");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned red[SB][4][FC_THREADS / 32];
@@ -820,7 +821,8 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
                      "r"(bytes * (unsigned)ncopy)
                      : "memory");
-        if (bytes) {
+        // failure-path test: the block's first window is expected but never copied
+        if (bytes && !(drop_first && it == (int)blockIdx.x)) {
             for (int q = 0; q < nsb; ++q) {
                 const int sq = row_id(bt, q);
                 if (zero_row(sq)) continue;
@@ -864,7 +866,7 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         float *xs = xbuf + (size_t)buf * SB * win;
         bool ok = false;
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
-        for (long long w = 0; w < (1LL << 24) && !ok; ++w) {
+        for (long long w = 0; w < wait_limit && !ok; ++w) {
             unsigned r;
             asm volatile(
                 "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -914,7 +916,7 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         if ((long long)blockIdx.x + (long long)(k_fail + 1) * gridDim.x < (long long)nitem) {
             const int kb = k_fail + 1;
             const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[kb & 1]);
-            for (long long w = 0; w < (1LL << 24); ++w) {
+            for (long long w = 0; w < wait_limit; ++w) {
                 unsigned r;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -1266,7 +1268,10 @@ static int conv32_run(soapgb_ctx *ctx, int n, int n_eff, int wid, int halo, cons
         SOAP_TRACED(ctx, "conv32", k_conv32t<SB><<<g, FC_THREADS, smem_t, ctx->stream>>>(n, n_eff, c2, lk, live, rblk, wid, spec, spec_stride,
                                                               n_spec, halo, b32a, b32b, c32a, c32b, b_every, conv,
                                                               n_eff, mm32, blk, nbx, ctx->d_status, zero_spec,
-                                                              rows, nrows));
+                                                              rows, nrows,
+                                                              ctx->test_wait_limit > 0 ? ctx->test_wait_limit
+                                                                                       : (1LL << 24),
+                                                              ctx->test_drop_copy == 2 ? 1 : 0));
     } else {
         const int win = (FC_TILE + 2 * halo + 4 + 3) & ~3;
         size_t smem = sizeof(float) * (size_t)SB * win;
