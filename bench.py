@@ -312,7 +312,7 @@ def run_own(args):
         # --- the compensated summation variant of the FP32 integration, timed and checked once
         comp = None
         if form == "fast32":
-            ctx.set_compensated(True)
+            ctx.set_compensated(False)
             o_c = torch.empty_like(out)
 
             def step_c():
@@ -324,8 +324,9 @@ def run_own(args):
             step_c()
             kc = ctx.trace_report()
             ctx.trace(False)
-            ctx.set_compensated(False)
-            comp = {"summation": "compensated (Kahan) output sums", "ms_per_step": round(ms_c, 4),
+            ctx.set_compensated(True)
+            comp = {"summation": "plain FP32 output sums (the timed step uses compensated ones)",
+                    "ms_per_step": round(ms_c, 4),
                     "value": round(len(phases) / (ms_c / 1e3), 2),
                     "fir_tile_phase_ms": round(kc.get("fir_tile_phase", (0, 0.0))[1], 4),
                     "accuracy": accuracy(ctx, case, inp, o_c, ref_d)}
@@ -349,9 +350,9 @@ def run_own(args):
                                    "spot 1% overlapping, 100 phases per GPU, R=115000",
                        "form": form, "phases_per_step": len(phases), "l2": "inputs (cubes 4x49.6 MB FP64) and "
                        "outputs (744 MB) exceed the 129 MB L2", "quiet_stage_ms": round(quiet_ms, 2),
-                       "summation": "FP32 per work unit, unit deficits added in plain FP32 (about 9 per pixel "
-                                    "and tile); the compensated variant is timed under 'compensated'"
-                                    if form == "fast32" else "FP64"},
+                       "summation": "FP32 per work unit, unit deficits (about 9 per pixel and tile) added in "
+                                    "compensated (Kahan) FP32 sums; the plain-sum variant is timed under "
+                                    "'summation_variant'" if form == "fast32" else "FP64"},
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -360,7 +361,7 @@ def run_own(args):
             "cpu_baseline": cpu,
             "accuracy": err,
             "fp64_forms": fp64,
-            "compensated": comp,
+            "summation_variant": comp,
             "ref_cuda": ref_cuda_record(len(phases)),
             "ccf_fit": ccf_stage,
             "kernels_ms_per_step": {k: round(v[1], 4) for k, v in sorted(ktab.items(), key=lambda x: -x[1][1])},

@@ -112,9 +112,9 @@ int soapgb_synchronize(soapgb_ctx *ctx);
 long long soapgb_launch_count(const soapgb_ctx *ctx);
 /* Summation of the FP32 form's per-phase integration (no counterpart in the reference,
  * whose sums are FP64).  Every cell's terms are summed per work unit (cells of one mu
- * bin and class in a tile) in FP32 and each unit's deficit is rounded once; on = 0 (the
- * default) adds those unit deficits, about 9 per pixel and tile, in plain FP32, on = 1
- * in compensated (Kahan) sums. */
+ * bin and class in a tile) in FP32 and each unit's deficit is rounded once; on = 1 (the
+ * default) adds those unit deficits, about 9 per pixel and tile, in compensated (Kahan)
+ * sums, on = 0 in plain FP32 sums. */
 int soapgb_set_compensated(soapgb_ctx *ctx, int on);
 /* Library version string. */
 const char *soapgb_version(void);

@@ -55,7 +55,7 @@ struct soapgb_ctx {
     int edge_n = 0, edge_n_eff = 0;
     double edge_w3[3] = {0.0, 0.0, 0.0};
     // FP32 per-phase integration: compensated (Kahan) output sums (soapgb_set_compensated)
-    bool fir_compensated = false;
+    bool fir_compensated = true;
     // failure-path tests only, read from the environment at context creation:
     // SOAPGB_TEST_WAIT_LIMIT polls per bounded wait of the staged-copy kernels (0: the
     // default 2^24) and SOAPGB_TEST_DROP_COPY, a staged copy whose bytes are expected but
