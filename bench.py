@@ -832,6 +832,64 @@ def run_reference(args):
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def profile_stage(args):
+    """One stage of the path run a few times on a small case, for ncu captures of its
+    kernels (nothing is timed or printed but a one-line note).  Stages: ccf (mask CCF +
+    Gaussian/bisector fit of 303 spectra of the 300x300 / 310,000-px step), bisector
+    (bisector injection of one 20 x 310,000 cube), adjoint (forward + adjoint of the
+    differentiable chain, 200x200 grid, 100,000 px, 5 phases), batch (the batched form on
+    16 stars sharing the 310,000-px seeds), plain64 (the plain FP64 pipeline, 2 phases)."""
+    import ctypes
+    import torch
+    from soap_gpu_gb300 import rv, synth
+    from soap_gpu_gb300._lib import Activity, Star
+    from soap_gpu_gb300.api import Batch, Context
+    torch.cuda.set_device(0)
+    dev = "cuda:0"
+    case, inp, phases = make_workload(0, args.phases, args.phase0)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    act = Activity(case.t_star, case.t_diff_spot, case.t_diff_fac, case.nrho, 0)
+    ctx = Context(0)
+    wave_d = T(inp.wave)
+    cubes_d = dict(q_norm=T(inp.q_norm), q_sed=T(inp.q_sed), spot_norm=T(inp.spot_norm), fac_norm=T(inp.fac_norm),
+                   spot_sed=T(inp.spot_sed[0]), fac_sed=T(inp.fac_sed[0]))
+    n_eff = case.n_eff
+    st = args.profile_stage
+    if st in ("ccf", "plain64"):
+        maps_d = ctx.disk_maps(case.grid, case.period, case.w_ratio, case.incl, case.radius_km, case.u1, case.u2,
+                               T(inp.mu_boundary), inp.lb)
+        form = "fast32" if st == "ccf" else "plain64"
+        qn = ctx.quiet_disk(form, wave_d, cubes_d["q_norm"], n_eff, maps_d, case.grid, case.step)
+        qs = ctx.quiet_disk(form, wave_d, cubes_d["q_sed"], n_eff, maps_d, case.grid, case.step)
+        ph = phases if st == "ccf" else phases[45:47]
+        out = ctx.phase_pipeline(form, wave_d, n_eff, star_struct(case, inp.lb), maps_d, cubes_d, case.step, act, ph,
+                                 [case.regions for _ in ph], qs, qn, case.sigma_v, conv_step=case.step)
+        if st == "ccf":
+            low = torch.stack([ctx.lower_resolution("fast32", wave_d, q, n_eff, case.sigma_v, step_mult=case.step,
+                                                    step_exp=case.step)[0].reshape(-1) for q in (qs, qs, qn)])
+            for _ in range(3):
+                ccf_fit_stage(ctx, case, inp, out, low, torch.cuda.current_stream(), reps=1)
+    elif st == "bisector":
+        rng_b = np.random.default_rng(11)
+        co = T(rng_b.uniform(-300.0, 300.0, (case.n_mu, 4)))
+        for _ in range(3):
+            ctx.bisector_inject(wave_d, T(inp.q_norm[0]), co)
+    elif st == "adjoint":
+        adjoint_timing(ctx, dev, reps=1)
+    elif st == "batch":
+        stars = synth.make_batch(16, seed=3)
+        sts = [Star(c.grid, c.period, c.w_ratio, c.incl, c.radius_km, c.u1, c.u2, (ctypes.c_double * 4)(*inp.lb))
+               for c in stars]
+        b = Batch(ctx, wave_d, n_eff, cubes_d, inp.mu_boundary, case.step, act, case.sigma_v, sts,
+                  [c.phases for c in stars], [[c.regions for _ in c.phases] for c in stars], conv_step=case.step)
+        for _ in range(2):
+            b.run()
+        b.close()
+    torch.cuda.synchronize()
+    ctx.close()
+    return {"profile_stage": st, "done": True}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -845,9 +903,14 @@ def main():
                     help="run only the warm-up and timed device steps (for ncu launch lists)")
     ap.add_argument("--phases", type=int, default=100, help="phases per step (100 is the benchmarked workload)")
     ap.add_argument("--phase0", type=int, default=0, help="index of the first phase (profiling subsets)")
+    ap.add_argument("--profile-stage", default=None, choices=["ccf", "bisector", "adjoint", "batch", "plain64"],
+                    help="run one stage a few times on a small case (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "own":
         args.warmup = 3
+    if args.profile_stage:
+        print(json.dumps(profile_stage(args)))
+        return
     res = run_reference(args) if args.impl == "reference" else run_own(args)
     if res is not None:
         print(json.dumps(res))

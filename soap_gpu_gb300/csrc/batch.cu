@@ -83,9 +83,15 @@ struct soapgb_batch {
     double *mu_b = nullptr;
     char *typed_mem = nullptr;
     FirTyped typed{};
-    char *quiet_ws = nullptr;        // the quiet-disk workspace, shared by the stars in turn
+    // worker streams: the per-star stages of star s run on worker s % n_work, so that the
+    // small launches of different stars overlap; each worker has its own quiet-disk and
+    // convolution workspaces, used by its stars in turn
+    int n_work = 1;
+    std::vector<cudaStream_t> work;
+    std::vector<cudaEvent_t> fork_ev, join_ev;   // [2]: before / after the integration; [2 n_work]
+    std::vector<char *> quiet_ws;
     FirPlanSizes quiet_fp;
-    char *res_ws = nullptr;          // the convolution workspace, shared by the stars in turn
+    std::vector<char *> res_ws;
     char *star_args = nullptr;       // the integration kernel's per-star arguments
     int2 *items = nullptr;           // (star, phase) of every visible phase
     int n_items = 0;
@@ -190,9 +196,11 @@ extern "C" int soapgb_batch_create(soapgb_ctx *ctx, const soapgb_batch_desc *d, 
     }
     b->total_phases = d->phase_offsets[d->n_star];
     // sizes
+    b->n_work = std::max(1, std::min(4, d->n_star));
     b->quiet_fp = fir_plan_sizes(b->form, n, n_mu, max_gm, false, 1);
+    const size_t res_b = resolution_scratch_bytes(b->form, n, n_eff, (int)std::max(3LL, max_spec));
     size_t total = al256(sizeof(double) * (n_mu > 1 ? n_mu - 1 : 1)) + al256(fir_typed_bytes(b->form, n, n_mu)) +
-                   al256(b->quiet_fp.bytes) + al256(resolution_scratch_bytes(b->form, n, n_eff, (int)std::max(3LL, max_spec))) +
+                   b->n_work * (al256(b->quiet_fp.bytes) + al256(res_b)) +
                    al256(fir_tile_args_bytes() * d->n_star) + al256(sizeof(int2) * (size_t)std::max(1LL, b->total_phases));
     for (auto &st : b->stars) {
         total += al256(sizeof(double) * st.star.grid) + 4 * al256(sizeof(double) * st.gm) + al256(sizeof(int) * st.gm) +
@@ -213,8 +221,10 @@ extern "C" int soapgb_batch_create(soapgb_ctx *ctx, const soapgb_batch_desc *d, 
         SOAP_CUDA(ctx, cudaMemcpyAsync(b->mu_b, d->mu_boundary, sizeof(double) * (n_mu - 1), cudaMemcpyHostToDevice,
                                        ctx->stream));
     b->typed_mem = take(b.get(), off, fir_typed_bytes(b->form, n, n_mu));
-    b->quiet_ws = take(b.get(), off, b->quiet_fp.bytes);
-    b->res_ws = take(b.get(), off, resolution_scratch_bytes(b->form, n, n_eff, (int)std::max(3LL, max_spec)));
+    for (int w = 0; w < b->n_work; ++w) {
+        b->quiet_ws.push_back(take(b.get(), off, b->quiet_fp.bytes));
+        b->res_ws.push_back(take(b.get(), off, res_b));
+    }
     b->star_args = take(b.get(), off, fir_tile_args_bytes() * d->n_star);
     b->items = (int2 *)take(b.get(), off, sizeof(int2) * (size_t)std::max(1LL, b->total_phases));
     // the typed cubes' addresses are fixed by the layout (they are written by the run)
@@ -319,6 +329,16 @@ extern "C" int soapgb_batch_create(soapgb_ctx *ctx, const soapgb_batch_desc *d, 
         }
     // the uploads read host vectors that end with this call
     SOAP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int w = 0; w < b->n_work; ++w) {
+        cudaStream_t st = nullptr;
+        SOAP_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        b->work.push_back(st);
+    }
+    for (int q = 0; q < 2 + 2 * b->n_work; ++q) {
+        cudaEvent_t e = nullptr;
+        SOAP_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        (q < 2 ? b->fork_ev : b->join_ev).push_back(e);
+    }
     *out = b.release();
     return SOAPGB_OK;
 }
@@ -346,49 +366,78 @@ extern "C" int soapgb_batch_run(soapgb_ctx *ctx, soapgb_batch *b, double *lower,
         rc = fir_typed_cubes(ctx, b->form, n, b->cubes, b->typed_mem, &t);
         if (rc) return rc;
     }
-    // per star: disk maps, quiet spectra, geometry (cell geometry, lists, prefix sums, plans)
-    for (auto &st : b->stars) {
+    // fork the workers off the context's stream
+    auto fork = [&](int f) -> int {
+        SOAP_CUDA(ctx, cudaEventRecord(b->fork_ev[f], ctx->stream));
+        for (auto w : b->work) SOAP_CUDA(ctx, cudaStreamWaitEvent(w, b->fork_ev[f], 0));
+        return SOAPGB_OK;
+    };
+    auto join = [&](int f) -> int {
+        for (int w = 0; w < b->n_work; ++w) {
+            cudaEvent_t e = b->join_ev[f * b->n_work + w];
+            SOAP_CUDA(ctx, cudaEventRecord(e, b->work[w]));
+            SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, e, 0));
+        }
+        return SOAPGB_OK;
+    };
+    rc = fork(0);
+    if (rc) return rc;
+    // per star, on its worker: disk maps, both quiet spectra (one set of lists), geometry
+    // (cell geometry, lists, prefix sums, tile plans)
+    for (size_t s = 0; s < b->stars.size(); ++s) {
+        BatchStar &st = b->stars[s];
+        const int w = (int)(s % b->n_work);
+        AuxScope on(ctx, b->work[w]);
         rc = disk_maps_launch(ctx, &st.star, n_mu, b->mu_b, st.ov, st.sin_incl, st.delta, st.limb, st.mu, st.region,
                               st.lb);
         if (rc) return rc;
-        for (int q = 0; q < 2; ++q) {
-            FirQuietArgs qa;
-            qa.n = n;
-            qa.n_eff = n_eff;
-            qa.wave = b->wave;
-            qa.cube = q == 0 ? b->cubes.q_sed : b->cubes.q_norm;
-            qa.n_mu = n_mu;
-            qa.gm = st.gm;
-            qa.delta = st.delta;
-            qa.limb = st.limb;
-            qa.region = st.region;
-            qa.step = b->step;
-            qa.out = q == 0 ? st.q_sed : st.q_norm;
-            qa.lambda0 = b->w3[0];
-            rc = fir_quiet(ctx, b->form, qa, b->quiet_ws, b->quiet_fp);
-            if (rc) return rc;
-        }
+        FirQuietArgs qa;
+        qa.n = n;
+        qa.n_eff = n_eff;
+        qa.wave = b->wave;
+        qa.cube = b->cubes.q_sed;
+        qa.cube2 = b->cubes.q_norm;
+        qa.n_mu = n_mu;
+        qa.gm = st.gm;
+        qa.delta = st.delta;
+        qa.limb = st.limb;
+        qa.region = st.region;
+        qa.step = b->step;
+        qa.out = st.q_sed;
+        qa.out2 = st.q_norm;
+        qa.lambda0 = b->w3[0];
+        rc = fir_quiet(ctx, b->form, qa, b->quiet_ws[w], b->quiet_fp);
+        if (rc) return rc;
         if (st.n_run == 0) continue;
         st.fa.stage = FIR_STAGE_GEOMETRY;
         rc = fir_phase(ctx, b->form, st.fa, st.fir, st.fp);
         if (rc) return rc;
     }
+    rc = join(0);
+    if (rc) return rc;
     // the integration of every visible phase of every star: one launch
     rc = fir_phase_multi(ctx, b->form, b->star0_args.data(), b->star_args, b->items, b->n_items, b->chunk,
                          b->blocks_per_sm);
     if (rc) return rc;
-    // per star: convolution and normalisation against its own quiet spectra
-    for (auto &st : b->stars) {
+    rc = fork(1);
+    if (rc) return rc;
+    // per star, on its worker: convolution and normalisation against its own quiet spectra
+    for (size_t s = 0; s < b->stars.size(); ++s) {
+        BatchStar &st = b->stars[s];
         if (st.n_phase == 0) continue;
+        const int w = (int)(s % b->n_work);
+        AuxScope on(ctx, b->work[w]);
         const int n_spec = 3 * st.n_phase;
         Res32 R;
         rc = resolution32_prepare(ctx, n, n_eff, n_spec, b->wave, b->w3[0], b->w3[1], b->w3[2], st.q_sed, st.q_norm, 3,
-                                  b->sigma_v, 50.0, b->conv_step, b->conv_step, b->sentinel, b->res_ws, R);
+                                  b->sigma_v, 50.0, b->conv_step, b->conv_step, b->sentinel, b->res_ws[w], R);
         if (rc) return rc;
         rc = resolution32_run(ctx, R, st.raw, n, 0, n_spec, lower + (size_t)3 * st.phase0 * n_eff, n_eff, nullptr,
                               st.zspec, st.h_zspec.data(), ZeroRows::NORM, st.blist, st.n_blist);
         if (rc) return rc;
     }
+    rc = join(1);
+    if (rc) return rc;
     if (quiet) {
         for (size_t s = 0; s < b->stars.size(); ++s) {
             SOAP_CUDA(ctx, cudaMemcpyAsync(quiet + 2 * s * n, b->stars[s].q_sed, sizeof(double) * n,
@@ -402,10 +451,16 @@ extern "C" int soapgb_batch_run(soapgb_ctx *ctx, soapgb_batch *b, double *lower,
 
 extern "C" int soapgb_batch_destroy(soapgb_batch *b) {
     if (!b) return SOAPGB_OK;
-    if (b->mem) {
+    {
         DeviceGuard g(b->device);
-        cudaDeviceSynchronize();
-        cudaFree(b->mem);
+        for (auto w : b->work) cudaStreamSynchronize(w);
+        for (auto w : b->work) cudaStreamDestroy(w);
+        for (auto e : b->fork_ev) cudaEventDestroy(e);
+        for (auto e : b->join_ev) cudaEventDestroy(e);
+        if (b->mem) {
+            cudaDeviceSynchronize();
+            cudaFree(b->mem);
+        }
     }
     delete b;
     return SOAPGB_OK;

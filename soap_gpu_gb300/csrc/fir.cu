@@ -2616,16 +2616,24 @@ int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, c
     FirCubes fc{};
     fc.c[0] = cube;
     const double los = lambda0 / a.step;
-    if (form == SOAPGB_FAST32) {
-        SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (float *)cube));
-        SOAP_LAUNCHED(ctx);
-        return launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc,
-                                                       gm, 0, 0, a.out, nullptr, nullptr, 0, 1);
+    // one cube, or two over the same lists (the typed copy is rewritten in stream order)
+    for (int q = 0; q < (a.cube2 ? 2 : 1); ++q) {
+        const double *src = q ? a.cube2 : a.cube;
+        double *out = q ? a.out2 : a.out;
+        if (form == SOAPGB_FAST32) {
+            SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src, nullptr, (float *)cube));
+            SOAP_LAUNCHED(ctx);
+            rc = launch_tiles<float, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, gm, 0, 0, out,
+                                                         nullptr, nullptr, 0, 1);
+        } else {
+            SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src, nullptr, (double *)cube));
+            SOAP_LAUNCHED(ctx);
+            rc = launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, gm, 0, 0, out,
+                                                          nullptr, nullptr, 0, 1);
+        }
+        if (rc) return rc;
     }
-    SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, a.cube, nullptr, (double *)cube));
-    SOAP_LAUNCHED(ctx);
-    return launch_tiles<double, MODE_QUIET, double>(ctx, L, ws, a.n, a.n_eff, a.wave, los, fc, gm,
-                                                    0, 0, a.out, nullptr, nullptr, 0, 1);
+    return SOAPGB_OK;
 }
 
 // the typed cubes a phase integration reads: its workspace slots, or the shared copies

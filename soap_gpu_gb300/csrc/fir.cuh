@@ -37,6 +37,9 @@ struct FirQuietArgs {
     double step;
     double *out;            // n (tail set to 0)
     double lambda0 = 0.0;   // wave[0] when known on the host (0: read from the device)
+    // optional second cube of the same disk (its cell order, lists and sums shared)
+    const double *cube2 = nullptr;
+    double *out2 = nullptr;
 };
 
 int fir_quiet(soapgb_ctx *ctx, int form, const FirQuietArgs &a, char *scratch, const FirPlanSizes &plan);
