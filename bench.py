@@ -368,6 +368,8 @@ def run_own(args):
             "seed_preparation": {"bisector_injection_ms_per_cube": round(bis_ms, 4),
                                  "cube": "%d mu bins x %d px, quiet form, inputs resident" % (n_mu, n)},
             "differentiable": adjoint_timing(ctx, dev),
+            "differentiable_shape": diff_batch_timing(ctx, dev, stream, n_star=args.diff_stars)
+            if args.diff_stars > 0 else None,
             "batched": batched_timing(ctx, case, inp, wave_d, cubes_d, dev, stream) if not args.no_batch else None,
             "clocks": clk,
         }
@@ -694,6 +696,85 @@ def timed_steps(fn, steps, stream):
     return e0.elapsed_time(e1) / steps
 
 
+def diff_batch_timing(ctx, dev, stream, n_star=8, chunk=10):
+    """The differentiable form on its own shape: stars of a 200x200 grid, 100,000 px, 10 mu
+    bins and 3 regions (random positions, 1-2 % of the hemisphere, spot or facula) over 50
+    phases of one rotation, vsini 1-4 km/s, inclination 60-90 deg.  Per star: both quiet
+    spectra, the deficit spectra of every phase, their resolution step, mask CCF and
+    Gaussian + bisector fit, for the three types; loss = a fixed combination of the RV,
+    FWHM and span series.  Forward alone (no gradient kept) against forward + every
+    adjoint (gradients w.r.t. u1, u2, vsini, inclination, the spot and facula contrasts
+    and the four seed cubes), phases checkpointed in chunks of `chunk`.  The stars are
+    independent, so the cost is the per-star cost times the stars; `n_star` of the 64 of
+    the shape are timed, and the per-star figures scale to 64."""
+    import dataclasses
+    import torch
+    from soap_gpu_gb300 import synth, rv
+    from soap_gpu_gb300._lib import Activity
+    from soap_gpu_gb300.differentiable import (CcfSetup, IntegrationSetup, ResolutionSetup, CUBE_KEYS,
+                                               rv_series_checkpointed)
+    case = synth.make_case(4)
+    inp = synth.generate(case)
+    n_eff = case.n_eff
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    cubes = {k: T(v) for k, v in zip(CUBE_KEYS, (inp.q_norm, inp.q_sed, inp.spot_norm, inp.fac_norm,
+                                                 inp.spot_sed[0], inp.fac_sed[0]))}
+    wt = rv.trim(inp.wave[:n_eff])
+    lw, lwt = rv.select_lines(wt, inp.mask_wave, inp.mask_weight)
+    cs = CcfSetup(ctx, T(case.velocities), T(lw), T(lwt), T(wt), float(case.step),
+                  mask_step=float(case.step), index_old=int(rv.WAVE_EXTEND / case.step))
+    rng = np.random.default_rng(44)
+    stars = []
+    for k in range(n_star):
+        reg = np.column_stack([rng.uniform(-50, 50, 3), rng.uniform(0, 360, 3), np.sqrt(rng.uniform(0.01, 0.02, 3)),
+                               rng.integers(0, 2, 3).astype(float)])
+        stars.append(dataclasses.replace(case, regions=reg, vsini=float(rng.uniform(1.0, 4.0)),
+                                         incl=float(rng.uniform(60.0, 90.0)), u1=float(rng.uniform(0.25, 0.35)),
+                                         u2=float(rng.uniform(0.3, 0.4))))
+    act = Activity(case.t_star, case.t_diff_spot, case.t_diff_fac, case.nrho, 0)
+    setups = [IntegrationSetup.build(ctx, inp.wave, n_eff, c.grid, c.period, c.w_ratio, c.incl, c.radius_km,
+                                     inp.mu_boundary, inp.lb, c.phases, [c.regions for _ in c.phases], act, c.step,
+                                     device=dev) for c in stars]
+    rs = ResolutionSetup(ctx, setups[0].wave, n_eff, float(case.sigma_v), step_mult=case.step, step_exp=case.step)
+
+    def one(c, setup, grad):
+        star = T([c.u1, c.u2, c.vsini, c.incl])
+        contrast = T([1.0, 1.0])
+        cb = dict(cubes)
+        if grad:
+            star.requires_grad_(True)
+            contrast.requires_grad_(True)
+            cb = {k: v.clone().requires_grad_(True) for k, v in cubes.items()}
+        cb2 = dict(cb)
+        cb2["spot_sed"] = contrast[0] * cb["spot_sed"]
+        cb2["fac_sed"] = contrast[1] * cb["fac_sed"]
+        out = rv_series_checkpointed(star, cb2, setup, rs, cs, chunk=chunk, kind=(0, 1, 2))
+        loss = sum((o["rv"] + 0.1 * o["fwhm"] + o["span"]).sum() for o in out.values())
+        if grad:
+            loss.backward()
+        return loss
+
+    def fwd():
+        with torch.no_grad():
+            for c, s in zip(stars, setups):
+                one(c, s, False)
+
+    def fwd_bwd():
+        for c, s in zip(stars, setups):
+            one(c, s, True)
+
+    f_ms = timed_steps(fwd, 1, stream)
+    fb_ms = timed_steps(fwd_bwd, 1, stream)
+    return {"case": "%d stars (of 64) x 50 phases, 200x200 grid, 100,000 px, 10 mu bins, 3 regions each, "
+                    "PLAIN64; both quiet spectra, deficits, resolution, CCF, Gaussian + bisector fit of 3 types; "
+                    "gradients w.r.t. u1, u2, vsini, inclination, 2 contrasts, 4 seed cubes; phases "
+                    "checkpointed in chunks of %d" % (n_star, chunk),
+            "stars_timed": n_star, "forward_ms": round(f_ms, 1), "forward_adjoint_ms": round(fb_ms, 1),
+            "ratio": round(fb_ms / f_ms, 2), "forward_ms_per_star": round(f_ms / n_star, 1),
+            "forward_adjoint_ms_per_star": round(fb_ms / n_star, 1),
+            "forward_adjoint_s_for_64_stars": round(fb_ms / n_star * 64 / 1e3, 1)}
+
+
 def ccf_fit_stage(ctx, case, inp, out_d, quiet_low_d, stream, reps=5):
     """The CCF + fit stage of one step (run_all_SOAP.py:256-412, timed there as "RV
     Calculation time"): the 300 phase spectra and the 3 quiet ones, trimmed, through the
@@ -899,6 +980,8 @@ def main():
     ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-star batched form")
+    ap.add_argument("--diff-stars", type=int, default=8,
+                    help="stars of the differentiable shape (64 stars x 50 phases) to time; 0 skips it")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed device steps (for ncu launch lists)")
     ap.add_argument("--phases", type=int, default=100, help="phases per step (100 is the benchmarked workload)")

@@ -347,35 +347,52 @@ def gauss_fit_bis(ccf, setup: CcfSetup):
 
 
 def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: ResolutionSetup, csetup: CcfSetup,
-                           chunk: int = 10, kind: int = 0, quiet_cube: str = "q_sed"):
-    """RV, span and FWHM series of one spectrum type over the setup's phases, relative to
-    the quiet star, with the quiet spectrum differentiated too.  kind selects the
-    deficit (0 flux, 1 bconv, 2 tot) and quiet_cube the quiet base (q_sed for flux and
-    tot, q_norm for bconv, as run_all_SOAP.py pairs them).
+                           chunk: int = 10, kind=0, quiet_cube: str = None):
+    """RV, span and FWHM series over the setup's phases, relative to the quiet star, with
+    the quiet spectra differentiated too.  kind selects the deficit (0 flux, 1 bconv,
+    2 tot) or is a tuple of them; each pairs with its quiet base as run_all_SOAP.py pairs
+    them (q_sed for flux and tot, q_norm for bconv; quiet_cube overrides it for a single
+    kind).  Returns {"rv", "span", "fwhm", "par", "quiet"} for a single kind, else a dict
+    of those per kind.
 
     The phases run in chunks of `chunk` under torch.utils.checkpoint: the forward keeps
     each chunk's fitted parameters only, and the backward recomputes the chunk's deficit,
     low-resolution spectra and CCFs before running their adjoints, so the memory held for
     the backward grows with the fitted parameters, not with the spectra."""
     from torch.utils.checkpoint import checkpoint
-    keys = CUBE_KEYS
-    cube_list = [cubes[k] for k in keys]
-    base = quiet_spectrum(star, cubes[quiet_cube], setup)
+    kinds = (kind,) if isinstance(kind, int) else tuple(kind)
+    base_key = {0: "q_sed", 1: "q_norm", 2: "q_sed"}
+    if quiet_cube is not None and len(kinds) == 1:
+        base_key = {kinds[0]: quiet_cube}
+    cube_list = [cubes[k] for k in CUBE_KEYS]
+    bases = {key: quiet_spectrum(star, cubes[key], setup) for key in sorted({base_key[k] for k in kinds})}
     zero = torch.zeros((1, setup.wave.shape[0]), dtype=torch.float64, device=setup.wave.device)
-    q_par = gauss_fit_bis(normalised_ccf(_trim(lower_resolution(zero, base, rsetup)), csetup), csetup)
+    q_par = {key: gauss_fit_bis(normalised_ccf(_trim(lower_resolution(zero, b, rsetup)), csetup), csetup)[0]
+             for key, b in bases.items()}
+    keys = sorted(bases)
 
-    def chunk_par(p0, p1, star_, base_, *cl):
-        sub = setup.phases(p0, p1)
-        d = deficit_spectra(star_, *cl, sub)[:, kind].contiguous()
-        low = lower_resolution(d, base_, rsetup)
-        return gauss_fit_bis(normalised_ccf(_trim(low), csetup), csetup)
+    def chunk_par(p0, p1, star_, *rest):
+        bl = dict(zip(keys, rest[:len(keys)]))
+        cl = rest[len(keys):]
+        d = deficit_spectra(star_, *cl, setup.phases(p0, p1))
+        out = []
+        for k in kinds:
+            low = lower_resolution(d[:, k].contiguous(), bl[base_key[k]], rsetup)
+            out.append(gauss_fit_bis(normalised_ccf(_trim(low), csetup), csetup))
+        return torch.stack(out)
 
     pars = []
     for p0 in range(0, setup.n_phase, chunk):
         p1 = min(setup.n_phase, p0 + chunk)
-        pars.append(checkpoint(chunk_par, p0, p1, star, base, *cube_list, use_reentrant=False))
-    par = torch.cat(pars)
-    return {"rv": par[:, 3] - q_par[0, 3], "span": par[:, 2], "fwhm": par[:, 4], "par": par, "quiet": q_par[0]}
+        pars.append(checkpoint(chunk_par, p0, p1, star, *[bases[k] for k in keys], *cube_list,
+                               use_reentrant=False))
+    par = torch.cat(pars, dim=1)    # (kinds, phases, 5)
+    res = {}
+    for i, k in enumerate(kinds):
+        qp = q_par[base_key[k]]
+        res[k] = {"rv": par[i, :, 3] - qp[3], "span": par[i, :, 2], "fwhm": par[i, :, 4], "par": par[i],
+                  "quiet": qp}
+    return res[kinds[0]] if isinstance(kind, int) else res
 
 
 def _trim(a):

@@ -12,7 +12,8 @@ darkening to an RV curve through the whole chain.
 * The span (BIS_FIT2.cpp:214-268) of the Gaussian fit + bisector against central
   differences of refits (1e-3 of the gradient's largest entry: the refits converge to
   xtol 1e-8 and the span's crossing intervals stay put for steps of 1e-5).
-* The checkpointed chain gives the same gradient as the chain without checkpoints.
+* The checkpointed chain gives the same gradient, to rounding (1e-12), whatever the
+  chunking of its phases.
 * 200 Adam steps fit (spot contrast, u1, u2) to a seeded RV curve of the same star.
 """
 import numpy as np
@@ -115,7 +116,7 @@ def test_span_gradient_matches_refits(ctx):
     yd = _dev(y).requires_grad_(True)
     Wp = _dev([[0.0, 0.0, 1.0, 0.2, 0.1]] * n_spec)   # loss = span + 0.2 v0 + 0.1 fwhm
     par = gauss_fit_bis(yd, cs)
-    assert float(torch.max(torch.abs(par[:, 2]))) > 1.0, "the test profiles have no span"
+    assert float(torch.max(torch.abs(par.detach()[:, 2]))) > 1.0, "the test profiles have no span"
     (par * Wp).sum().backward()
     g = yd.grad
     scale = float(torch.max(torch.abs(g)))
@@ -158,8 +159,9 @@ def test_checkpointed_chain_matches_plain_chain(ctx):
         w = _dev(np.linspace(1.0, 2.0, out["rv"].numel()))
         ((out["rv"] * w).sum() + 0.1 * (out["span"] * w).sum()).backward()
         grads.append((sg.grad.clone(), cb["q_sed"].grad.clone(), cb["spot_sed"].grad.clone()))
+    # the same adjoints, summed over the chunks in a different order: equal to rounding
     for a, b in zip(*grads):
-        assert torch.equal(a, b)
+        assert float(torch.max(torch.abs(a - b))) <= 1e-12 * float(torch.max(torch.abs(b)))
     assert float(torch.max(torch.abs(grads[0][0]))) > 0
 
 
