@@ -919,7 +919,8 @@ def profile_stage(args):
     Gaussian/bisector fit of 303 spectra of the 300x300 / 310,000-px step), bisector
     (bisector injection of one 20 x 310,000 cube), adjoint (forward + adjoint of the
     differentiable chain, 200x200 grid, 100,000 px, 5 phases), batch (the batched form on
-    16 stars sharing the 310,000-px seeds), plain64 (the plain FP64 pipeline, 2 phases)."""
+    8 stars of grids 100-160 and 20-40 phases sharing the 310,000-px seeds), plain64 (the
+    plain FP64 pipeline, 2 phases)."""
     import ctypes
     import torch
     from soap_gpu_gb300 import rv, synth
@@ -958,7 +959,8 @@ def profile_stage(args):
     elif st == "adjoint":
         adjoint_timing(ctx, dev, reps=1)
     elif st == "batch":
-        stars = synth.make_batch(16, seed=3)
+        # a small batch (8 stars, grids 100-160, 20-40 phases: about 2 GB on the device)
+        stars = synth.make_batch(8, seed=3, grid=(100, 160), n_phase=(20, 40))
         sts = [Star(c.grid, c.period, c.w_ratio, c.incl, c.radius_km, c.u1, c.u2, (ctypes.c_double * 4)(*inp.lb))
                for c in stars]
         b = Batch(ctx, wave_d, n_eff, cubes_d, inp.mu_boundary, case.step, act, case.sigma_v, sts,
