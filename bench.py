@@ -737,7 +737,7 @@ def diff_batch_timing(ctx, dev, stream, n_star=8, chunk=10):
                                      device=dev) for c in stars]
     rs = ResolutionSetup(ctx, setups[0].wave, n_eff, float(case.sigma_v), step_mult=case.step, step_exp=case.step)
 
-    def one(c, setup, grad):
+    def one(c, setup, grad, recompute=True):
         star = T([c.u1, c.u2, c.vsini, c.incl])
         contrast = T([1.0, 1.0])
         cb = dict(cubes)
@@ -748,7 +748,7 @@ def diff_batch_timing(ctx, dev, stream, n_star=8, chunk=10):
         cb2 = dict(cb)
         cb2["spot_sed"] = contrast[0] * cb["spot_sed"]
         cb2["fac_sed"] = contrast[1] * cb["fac_sed"]
-        out = rv_series_checkpointed(star, cb2, setup, rs, cs, chunk=chunk, kind=(0, 1, 2))
+        out = rv_series_checkpointed(star, cb2, setup, rs, cs, chunk=chunk, kind=(0, 1, 2), recompute=recompute)
         loss = sum((o["rv"] + 0.1 * o["fwhm"] + o["span"]).sum() for o in out.values())
         if grad:
             loss.backward()
@@ -761,16 +761,24 @@ def diff_batch_timing(ctx, dev, stream, n_star=8, chunk=10):
 
     def fwd_bwd():
         for c, s in zip(stars, setups):
+            one(c, s, True, recompute=False)
+
+    def fwd_bwd_ckpt():
+        for c, s in zip(stars, setups):
             one(c, s, True)
 
     f_ms = timed_steps(fwd, 1, stream)
     fb_ms = timed_steps(fwd_bwd, 1, stream)
+    fbc_ms = timed_steps(fwd_bwd_ckpt, 1, stream)
     return {"case": "%d stars (of 64) x 50 phases, 200x200 grid, 100,000 px, 10 mu bins, 3 regions each, "
                     "PLAIN64; both quiet spectra, deficits, resolution, CCF, Gaussian + bisector fit of 3 types; "
-                    "gradients w.r.t. u1, u2, vsini, inclination, 2 contrasts, 4 seed cubes; phases "
-                    "checkpointed in chunks of %d" % (n_star, chunk),
+                    "gradients w.r.t. u1, u2, vsini, inclination, 2 contrasts, 4 seed cubes; phases in chunks "
+                    "of %d" % (n_star, chunk),
             "stars_timed": n_star, "forward_ms": round(f_ms, 1), "forward_adjoint_ms": round(fb_ms, 1),
-            "ratio": round(fb_ms / f_ms, 2), "forward_ms_per_star": round(f_ms / n_star, 1),
+            "ratio": round(fb_ms / f_ms, 2),
+            "checkpointed": {"forward_adjoint_ms": round(fbc_ms, 1), "ratio": round(fbc_ms / f_ms, 2),
+                             "what": "the same with each chunk's forward recomputed in the backward"},
+            "forward_ms_per_star": round(f_ms / n_star, 1),
             "forward_adjoint_ms_per_star": round(fb_ms / n_star, 1),
             "forward_adjoint_s_for_64_stars": round(fb_ms / n_star * 64 / 1e3, 1)}
 

@@ -228,14 +228,7 @@ extern "C" int soapgb_batch_create(soapgb_ctx *ctx, const soapgb_batch_desc *d, 
     b->star_args = take(b.get(), off, fir_tile_args_bytes() * d->n_star);
     b->items = (int2 *)take(b.get(), off, sizeof(int2) * (size_t)std::max(1LL, b->total_phases));
     // the typed cubes' addresses are fixed by the layout (they are written by the run)
-    {
-        const size_t tsz = sizeof(float), cb = al256(tsz * (size_t)n * n_mu);
-        for (int q = 0; q < 6; ++q) b->typed.c[q] = b->typed_mem + q * cb;
-        b->typed.spot_sed = b->cubes.spot_sed;
-        b->typed.fac_sed = b->cubes.fac_sed;
-        b->typed.spot_sed2 = b->typed_mem + 6 * cb;
-        b->typed.fac_sed2 = b->typed_mem + 6 * cb + al256(sizeof(float2) * (size_t)n);
-    }
+    fir_typed_layout(b->form, n, n_mu, b->typed_mem, b->cubes, &b->typed);
     std::vector<char> args(fir_tile_args_bytes() * d->n_star, 0);
     std::vector<int2> items;
     std::vector<std::vector<double>> ovs(d->n_star);

@@ -45,6 +45,17 @@ constexpr long long FIR_WAIT_LIMIT = 1LL << 24;  // bounded mbarrier waits
 
 static_assert(FIR_MCH <= FIR_THREADS, "one shift value per thread in a unit");
 
+// four rows of one class interleaved per pixel (the rows a work unit stages): one bulk
+// copy stages a unit's window, one 16-byte (FP32) shared load fetches a pixel's 4 values
+struct __align__(32) soap_double4 {
+    double x, y, z, w;
+};
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = float4; };
+template <> struct Vec4T<double> { using type = soap_double4; };
+template <typename T> using Vec4 = typename Vec4T<T>::type;
+
+
 enum { MODE_QUIET = 0, MODE_PHASE = 1 };
 enum { CLS_SPOT = 0, CLS_FAC = 1, CLS_DIRECT = 2 };
 
@@ -134,24 +145,23 @@ __device__ __forceinline__ float soap_f64_to_f32(double v) {
     return __uint_as_float(bits | ((unsigned)(u >> 32) & 0x80000000u));
 }
 
-// The six typed cubes of the FP32 phase integration in one pass over the four FP64
-// cubes: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm.  The
-// two differences are formed in FP64 and rounded once.  Each thread keeps two steps'
-// loads (eight 16-byte loads) in flight to cover HBM latency.
-__device__ __forceinline__ void cube_types_store(long long i, double2 a, double2 b, double2 c, double2 d, float2 *o0,
-                                                 float2 *o1, float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
-    o0[i] = make_float2(soap_f64_to_f32(a.x), soap_f64_to_f32(a.y));
-    o1[i] = make_float2(soap_f64_to_f32(b.x), soap_f64_to_f32(b.y));
-    o2[i] = make_float2(soap_f64_to_f32(c.x), soap_f64_to_f32(c.y));
-    o3[i] = make_float2(soap_f64_to_f32(b.x - c.x), soap_f64_to_f32(b.y - c.y));
-    o4[i] = make_float2(soap_f64_to_f32(d.x), soap_f64_to_f32(d.y));
-    o5[i] = make_float2(soap_f64_to_f32(b.x - d.x), soap_f64_to_f32(b.y - d.y));
+// The interleaved rows of the two classes in one pass over the four FP64 cubes, pixel
+// pairs per thread: spot (q_sed, q_norm, spot_norm, q_norm - spot_norm) and facula
+// (q_sed, q_norm - fac_norm, q_norm, fac_norm), the differences formed in FP64 and
+// rounded once.  Each thread keeps two steps' loads (eight 16-byte loads) in flight.
+__device__ __forceinline__ void cube_rows_store(long long i, double2 a, double2 b, double2 c, double2 d, float4 *sp,
+                                                float4 *fa) {
+    const float qs0 = soap_f64_to_f32(a.x), qs1 = soap_f64_to_f32(a.y);
+    const float qn0 = soap_f64_to_f32(b.x), qn1 = soap_f64_to_f32(b.y);
+    sp[2 * i] = make_float4(qs0, qn0, soap_f64_to_f32(c.x), soap_f64_to_f32(b.x - c.x));
+    sp[2 * i + 1] = make_float4(qs1, qn1, soap_f64_to_f32(c.y), soap_f64_to_f32(b.y - c.y));
+    fa[2 * i] = make_float4(qs0, soap_f64_to_f32(b.x - d.x), qn0, soap_f64_to_f32(d.x));
+    fa[2 * i + 1] = make_float4(qs1, soap_f64_to_f32(b.y - d.y), qn1, soap_f64_to_f32(d.y));
 }
 
 __global__ void __launch_bounds__(256) k_cube_types32(long long n2, const double2 *__restrict__ qs,
                                                       const double2 *__restrict__ qn, const double2 *__restrict__ sn,
-                                                      const double2 *__restrict__ fn, float2 *o0, float2 *o1,
-                                                      float2 *o2, float2 *o3, float2 *o4, float2 *o5) {
+                                                      const double2 *__restrict__ fn, float4 *sp, float4 *fa) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += 2 * stride) {
         const long long j = i + stride;
@@ -163,9 +173,30 @@ __global__ void __launch_bounds__(256) k_cube_types32(long long n2, const double
             c1 = __ldcs(sn + j);
             d1 = __ldcs(fn + j);
         }
-        cube_types_store(i, a0, b0, c0, d0, o0, o1, o2, o3, o4, o5);
-        if (j < n2) cube_types_store(j, a1, b1, c1, d1, o0, o1, o2, o3, o4, o5);
+        cube_rows_store(i, a0, b0, c0, d0, sp, fa);
+        if (j < n2) cube_rows_store(j, a1, b1, c1, d1, sp, fa);
     }
+}
+
+// the same interleaved rows of any element type, one pixel per thread (the FP64 form, and
+// cubes whose layout the paired kernel cannot take)
+template <typename T>
+__global__ void k_cube_rows(long long count, const double *__restrict__ qs, const double *__restrict__ qn,
+                            const double *__restrict__ sn, const double *__restrict__ fn, Vec4<T> *sp, Vec4<T> *fa) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const double a = qs[i], b = qn[i], c = sn[i], d = fn[i];
+    Vec4<T> s, f;
+    s.x = (T)a;
+    s.y = (T)b;
+    s.z = (T)c;
+    s.w = (T)(b - c);
+    f.x = (T)a;
+    f.y = (T)(b - d);
+    f.z = (T)b;
+    f.w = (T)d;
+    sp[i] = s;
+    fa[i] = f;
 }
 
 // --- cell order ----------------------------------------------------------------
@@ -873,8 +904,10 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 }
 
 struct FirCubes {
-    // PHASE: q_sed, q_norm, spot_norm, q_norm - spot_norm, fac_norm, q_norm - fac_norm;
-    // QUIET: [0] only.  Workspace slots: 256-byte aligned, padded to 256 bytes.
+    // PHASE: c[0] the spot class's rows per pixel (q_sed, q_norm, spot_norm, q_norm -
+    // spot_norm), c[1] the facula class's (q_sed, q_norm - fac_norm, q_norm, fac_norm),
+    // each n_mu x n Vec4 -- the order in which a unit's four sums use them; QUIET: c[0],
+    // one cube of T.  Workspace slots: 256-byte aligned, padded to 256 bytes.
     const void *c[6];
     const double *spot_sed;
     const double *fac_sed;
@@ -1124,7 +1157,9 @@ __device__ int fir_segments(const FirTileArgs &A, int l, int j0, int t_eff, FirS
 }
 
 // descriptor of work unit u: its segment, shift values and source window
-template <typename T>
+// (PHASE: the staged rows are Vec4 elements, 16-byte aligned, so the window starts at
+// its first pixel; QUIET: rows of T, staged from the 16-byte boundary below w0)
+template <typename T, int MODE>
 __device__ __forceinline__ FirUnit fir_describe(int u, const FirSeg *segs, int nsg, int j0, int t_eff, int n,
                                                 int n_eff) {
     int lo = 0, hi = nsg - 1;
@@ -1144,9 +1179,9 @@ __device__ __forceinline__ FirUnit fir_describe(int u, const FirSeg *segs, int n
     d.mb = min(g.m_hi, d.ma + FIR_MCH - 1);
     d.w0 = max(0, j0 + d.ma - (d.ma > g.m_lo ? 1 : 0));
     d.w1 = min(n_eff, j0 + t_eff + d.mb + 1);
-    d.off = (d.w1 > d.w0) ? (int)(((((long long)(g.key >> 1) * n + d.w0) * (long long)sizeof(T)) & 15) /
-                                  (long long)sizeof(T))
-                          : 0;
+    d.off = (MODE == MODE_PHASE || d.w1 <= d.w0)
+                ? 0
+                : (int)(((((long long)(g.key >> 1) * n + d.w0) * (long long)sizeof(T)) & 15) / (long long)sizeof(T));
     return d;
 }
 
@@ -1177,7 +1212,7 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
     const int n = A.n, n_eff = A.n_eff;
     const double iXa = 1.0 / ((double)j0 + A.los), iXb = 1.0 / ((double)(j0 + t_eff - 1) + A.los);
     const int nbu = min(ST::NU, nunit - ub);
-    for (int t = tid; t < nbu; t += NT) st.unit[t] = fir_describe<T>(ub + t, segs, nsg, j0, t_eff, n, n_eff);
+    for (int t = tid; t < nbu; t += NT) st.unit[t] = fir_describe<T, MODE>(ub + t, segs, nsg, j0, t_eff, n, n_eff);
     __syncthreads();
     if (tid == 0) {
         int nb = 0, nt = 0;
@@ -1690,7 +1725,7 @@ constexpr int FIR_FOLD = 4;          // work units per fold of the partial sums
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
 struct FirPPSmem {
-    T win[FIR_PP_NBUF][4][FIR_PP_WIN];
+    Vec4<T> win[FIR_PP_NBUF][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
     unsigned long long wbar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2], pbar[2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
@@ -1722,7 +1757,6 @@ template <typename T, bool COMP, bool MULTI>
 __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTileArgs A0, int ntile, int r0, int nr,
                                                         int ntot_all, const FirTileArgs *__restrict__ stars,
                                                         const int2 *__restrict__ items, int chunk) {
-    constexpr int NC = 4;
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
     extern __shared__ __align__(128) unsigned char pp_smem[];
     FirPPSmem<T> &sh = *reinterpret_cast<FirPPSmem<T> *>(pp_smem);
@@ -1792,26 +1826,18 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         mbar_expect_tx(&sh.pbar[b], bytes);
         if (!(first && A0.drop_plan)) bulk_g2s(&sh.pb[b][0], plan_rec(v), bytes, &sh.pbar[b]);
     };
-    // (thread 0) stage the rows of unit number u (buffer u % 3)
+    // (thread 0) stage the interleaved rows of unit number u (buffer u % 3): pixels
+    // [w0, w1) of the class's Vec4 row, one bulk copy (Vec4 elements are 16-byte multiples)
     auto issue_unit = [&](int u, const FirUnit &d) {
         const int b = u % FIR_PP_NBUF;
-        unsigned bytes = 0;
-        uintptr_t rel = 0;
-        if (d.w1 > d.w0) {
-            const uintptr_t p0 = (uintptr_t)((long long)(d.key >> 1) * n + d.w0) * sizeof(T);
-            const uintptr_t p1 = (uintptr_t)((long long)(d.key >> 1) * n + d.w1) * sizeof(T);
-            rel = p0 & ~uintptr_t(15);
-            bytes = (unsigned)(((p1 + 15) & ~uintptr_t(15)) - rel);
-        }
+        const unsigned bytes = (d.w1 > d.w0) ? (unsigned)(d.w1 - d.w0) * (unsigned)sizeof(Vec4<T>) : 0u;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&sh.wbar[b], bytes * NC);
+        mbar_expect_tx(&sh.wbar[b], bytes);
         if (bytes) {
-#pragma unroll
-            for (int q = 0; q < NC; ++q) {
-                // the typed cubes are the same for every star
-                const char *base = reinterpret_cast<const char *>(A0.cubes.c[fir_cube_index(MODE_PHASE, d.cls, q)]);
-                bulk_g2s(&sh.win[b][q][0], base + rel, bytes, &sh.wbar[b]);
-            }
+            // the typed cubes are the same for every star
+            const Vec4<T> *row = reinterpret_cast<const Vec4<T> *>(A0.cubes.c[d.cls == CLS_SPOT ? 0 : 1]) +
+                                 (long long)(d.key >> 1) * n;
+            bulk_g2s(&sh.win[b][0], row + d.w0, bytes, &sh.wbar[b]);
         }
     };
 
@@ -1860,23 +1886,24 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
             else add_out(q, j, false, part[0][q], part[2][q], part[3][q], part[1][q]);
         }
     };
-    // source rows of a unit: staged windows (value of source pixel i at p[c][i + off]) or
-    // the cube rows in global memory (off = 0)
+    // source rows of a unit, interleaved: the staged window (source pixel i at p[i + off])
+    // or the class's row in global memory (off = 0)
     struct Src {
-        const T *p[4];
+        const Vec4<T> *p;
         int off;
         bool staged;
     };
-    auto src_of = [&](const T (*W)[FIR_PP_WIN], const FirUnit &d) {
+    auto cube_row = [&](int cls, int key) {
+        return reinterpret_cast<const Vec4<T> *>(A.cubes.c[cls == CLS_SPOT ? 0 : 1]) + (long long)(key >> 1) * n;
+    };
+    auto src_of = [&](const Vec4<T> *W, const FirUnit &d) {
         Src sr;
         if (FIR_PP_STAGED) {
-            for (int c = 0; c < 4; ++c) sr.p[c] = W[c];
+            sr.p = W;
             sr.off = d.off - d.w0;
             sr.staged = true;
         } else {
-            for (int c = 0; c < 4; ++c)
-                sr.p[c] = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE_PHASE, d.cls, c)]) +
-                          (long long)(d.key >> 1) * n;
+            sr.p = cube_row(d.cls, d.key);
             sr.off = 0;
             sr.staged = false;
         }
@@ -1887,10 +1914,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                             int t_eff) {
         const int zv = d.key & 1;
         const bool fac = (d.cls != CLS_SPOT);
-        const T *__restrict__ r0 = sr.p[0] + sr.off;
-        const T *__restrict__ r1 = sr.p[1] + sr.off;
-        const T *__restrict__ r2 = sr.p[2] + sr.off;
-        const T *__restrict__ r3 = sr.p[3] + sr.off;
+        const Vec4<T> *__restrict__ r = sr.p + sr.off;
         // one group at the thread's pixels; CHECKED: some pixels of the tile fall outside
         // [jlo, jhi] (tile edges, the grid's end), else none and no test is needed
         auto group_at = [&](auto checked_c, auto zv_c, const FirGrp<T> &gr, int jlo, int jhi, T b0, T b1, T bb) {
@@ -1903,21 +1927,23 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 const int j = j0 + dj;
                 if (CHECKED && (j < jlo || j > jhi)) continue;
                 const int x = j + m;
+                const Vec4<T> v0 = r[x];
                 if (ZV) {   // single tap: w == 0
-                    part[0][q] += gr.a0 * r0[x];
-                    part[1][q] += gr.a0 * r1[x];
-                    part[2][q] += b0 * r2[x];
-                    part[3][q] += b0 * r3[x];
+                    part[0][q] += gr.a0 * v0.x;
+                    part[1][q] += gr.a0 * v0.y;
+                    part[2][q] += b0 * v0.z;
+                    part[3][q] += b0 * v0.w;
                     continue;
                 }
+                const Vec4<T> v1 = r[x + 1];
                 const T fdj = (T)dj;
                 const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
                 const T e0 = b0 - bb * fdj, e1 = b1 + bb * fdj;
                 // two chained FMAs per row (no separate product and sum)
-                part[0][q] = fma(c1, r0[x + 1], fma(c0, r0[x], part[0][q]));
-                part[1][q] = fma(c1, r1[x + 1], fma(c0, r1[x], part[1][q]));
-                part[2][q] = fma(e1, r2[x + 1], fma(e0, r2[x], part[2][q]));
-                part[3][q] = fma(e1, r3[x + 1], fma(e0, r3[x], part[3][q]));
+                part[0][q] = fma(c1, v1.x, fma(c0, v0.x, part[0][q]));
+                part[1][q] = fma(c1, v1.y, fma(c0, v0.y, part[1][q]));
+                part[2][q] = fma(e1, v1.z, fma(e0, v0.z, part[2][q]));
+                part[3][q] = fma(e1, v1.w, fma(e0, v0.w, part[3][q]));
             }
         };
         using yes = std::integral_constant<bool, true>;
@@ -1960,23 +1986,19 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 else if (wd < (T)0) { wd += (T)1; i -= 1; }
                 if (CHECKED && (i < 0 || i > n_eff - 2)) continue;
                 const bool inwin = !CHECKED || !sr.staged || ((i >= d.w0) && (i + 1 < d.w1));
-                auto lv = [&](int c) -> T {
-                    T s0, s1;
-                    if (inwin) {
-                        s0 = sr.p[c][i + sr.off];
-                        s1 = sr.p[c][i + 1 + sr.off];
-                    } else {
-                        const T *rowp = reinterpret_cast<const T *>(A.cubes.c[fir_cube_index(MODE_PHASE, cls, c)]) +
-                                        (long long)(d.key >> 1) * n;
-                        s0 = rowp[i];
-                        s1 = rowp[i + 1];
-                    }
-                    return s0 + (s1 - s0) * wd;
-                };
-                part[0][q] += xc.L * lv(0);
-                part[1][q] += xc.L * lv(1);
-                part[2][q] += w23 * lv(2);
-                part[3][q] += w23 * lv(3);
+                Vec4<T> s0, s1;
+                if (inwin) {
+                    s0 = sr.p[i + sr.off];
+                    s1 = sr.p[i + 1 + sr.off];
+                } else {
+                    const Vec4<T> *rowp = cube_row(cls, d.key);
+                    s0 = rowp[i];
+                    s1 = rowp[i + 1];
+                }
+                part[0][q] += xc.L * (s0.x + (s1.x - s0.x) * wd);
+                part[1][q] += xc.L * (s0.y + (s1.y - s0.y) * wd);
+                part[2][q] += w23 * (s0.z + (s1.z - s0.z) * wd);
+                part[3][q] += w23 * (s0.w + (s1.w - s0.w) * wd);
             }
         };
         // the sources of a cell span [i0 - 1, i0 + FIR_TILE] over the tile
@@ -2169,7 +2191,9 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 __syncthreads();
                 for (int e = 0; e < nbd; ++e) {
                     const FirExcD<T> xc = sh.excd[e];
-                    const long long off = (long long)xc.row * n;
+                    // the class's interleaved row: spot (q_sed, q_norm, spot_norm, -),
+                    // facula (q_sed, -, q_norm, fac_norm)
+                    const Vec4<T> *rowp = cube_row(xc.kind == 0 ? CLS_SPOT : CLS_FAC, 2 * xc.row);
 #pragma unroll
                     for (int q = 0; q < FIR_PIX; ++q) {
                         const int dj = tid + q * FIR_THREADS;
@@ -2188,18 +2212,22 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                             if (i < 0 || i > n_eff - 2) continue;
                             w = wd;
                         }
-                        auto val = [&](int ci) -> T {
-                            const T *rowp = reinterpret_cast<const T *>(A.cubes.c[ci]) + off;
-                            if (xc.zero_v) return rowp[i];
-                            return rowp[i] + (rowp[i + 1] - rowp[i]) * w;
-                        };
+                        const Vec4<T> a = rowp[i];
+                        Vec4<T> v = a;
+                        if (!xc.zero_v) {
+                            const Vec4<T> b = rowp[i + 1];
+                            v.x = a.x + (b.x - a.x) * w;
+                            v.y = a.y + (b.y - a.y) * w;
+                            v.z = a.z + (b.z - a.z) * w;
+                            v.w = a.w + (b.w - a.w) * w;
+                        }
                         const T Lc = xc.L;
                         if (xc.kind == 0) {
                             T Lq = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)(int)xc.temp));
-                            add_out(q, j, true, Lc * val(0), Lq * val(1), Lq * val(2), Lc * val(3));
+                            add_out(q, j, true, Lc * v.x, Lq * v.y, Lq * v.z, Lc * v.w);
                         } else {
                             T w2 = (T)((double)Lc * fir_planck_ratio(A.lam[j], xc.temp, (double)A.t_norm_fac));
-                            add_out(q, j, false, Lc * val(0), w2 * val(1), w2 * val(4), Lc * val(5));
+                            add_out(q, j, false, Lc * v.x, w2 * v.z, w2 * v.w, Lc * v.y);
                         }
                     }
                 }
@@ -2288,7 +2316,12 @@ FirLayout fir_layout(int form, int n, int n_mu, long long gm, int ncube, int n_l
     size_t sz[FirLayout::NSLOT] = {0};
     sz[FirLayout::GEO] = sizeof(CellGeo) * (size_t)gm;
     sz[FirLayout::GEO32] = sizeof(CellGeo32) * (size_t)gm;
-    for (int q = 0; q < 6; ++q) sz[FirLayout::CUBE0 + q] = (q < ncube && !typed_external) ? tsz * (size_t)n * n_mu : 0;
+    // QUIET: one cube of T; PHASE (ncube 6): the two classes' interleaved rows (4 x T)
+    for (int q = 0; q < 6; ++q)
+        sz[FirLayout::CUBE0 + q] = typed_external ? 0
+                                   : (ncube == 1 && q == 0) ? tsz * (size_t)n * n_mu
+                                   : (ncube == 6 && q < 2)  ? 4 * tsz * (size_t)n * n_mu
+                                                            : 0;
     sz[FirLayout::SED2A] = sz[FirLayout::SED2B] = typed_external ? 0 : sizeof(float2) * (size_t)n;
     sz[FirLayout::K1A] = sz[FirLayout::K1B] = sizeof(unsigned long long) * (size_t)gm;
     sz[FirLayout::K2A] = sz[FirLayout::K2B] = sizeof(unsigned) * (size_t)gm;
@@ -2330,25 +2363,19 @@ FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase,
 
 size_t fir_typed_bytes(int form, int n, int n_mu) {
     const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    return 6 * align256(tsz * (size_t)n * n_mu) + 2 * align256(sizeof(float2) * (size_t)n);
+    return 2 * align256(4 * tsz * (size_t)n * n_mu) + 2 * align256(sizeof(float2) * (size_t)n);
 }
 
-// the six typed cubes of the phase integration (q_sed, q_norm, spot_norm, q_norm -
-// spot_norm, fac_norm, q_norm - fac_norm) and, in the FP32 form, the continuum rows as
-// float pairs
-static int typed_cubes_into(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, void *const dst[6],
+// the typed cubes of the phase integration: the two classes' interleaved rows (Vec4 of
+// T per pixel) and, in the FP32 form, the continuum rows as float pairs
+static int typed_cubes_into(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, void *const dst[2],
                             float2 *sed2a, float2 *sed2b) {
     const int n_mu = c.n_mu;
-    const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
     const size_t cube_elems = (size_t)n * n_mu;
-    const double *src_a[6] = {c.q_sed, c.q_norm, c.spot_norm, c.q_norm, c.fac_norm, c.q_norm};
-    const double *src_b[6] = {nullptr, nullptr, nullptr, c.spot_norm, nullptr, c.fac_norm};
     auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
-    const bool fused = (tsz == 4) && (cube_elems % 2 == 0) && al16(c.q_sed) && al16(c.q_norm) &&
-                       al16(c.spot_norm) && al16(c.fac_norm);
-    if (fused) {
-        float2 *o[6];
-        for (int q = 0; q < 6; ++q) o[q] = (float2 *)dst[q];
+    const bool paired = (form == SOAPGB_FAST32) && (cube_elems % 2 == 0) && al16(c.q_sed) && al16(c.q_norm) &&
+                        al16(c.spot_norm) && al16(c.fac_norm);
+    if (paired) {
         const long long n2 = (long long)(cube_elems / 2);
         // short blocks (two steps per thread): SMs free up quickly for the
         // higher-priority geometry kernels that run beside this one
@@ -2356,14 +2383,17 @@ static int typed_cubes_into(soapgb_ctx *ctx, int form, int n, const soapgb_cubes
         SOAP_TRACED(ctx, "cube_types",
                     k_cube_types32<<<nblk, 256, 0, ctx->stream>>>(
                         n2, (const double2 *)c.q_sed, (const double2 *)c.q_norm, (const double2 *)c.spot_norm,
-                        (const double2 *)c.fac_norm, o[0], o[1], o[2], o[3], o[4], o[5]));
+                        (const double2 *)c.fac_norm, (float4 *)dst[0], (float4 *)dst[1]));
         SOAP_LAUNCHED(ctx);
-    }
-    for (int q = 0; q < 6 && !fused; ++q) {
-        if (tsz == 4)
-            SOAP_TRACED(ctx, "cube_types", k_to_type<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (float *)dst[q]));
-        else
-            SOAP_TRACED(ctx, "cube_types", k_to_type<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(cube_elems, src_a[q], src_b[q], (double *)dst[q]));
+    } else if (form == SOAPGB_FAST32) {
+        SOAP_TRACED(ctx, "cube_types", k_cube_rows<float><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(
+                                           cube_elems, c.q_sed, c.q_norm, c.spot_norm, c.fac_norm,
+                                           (float4 *)dst[0], (float4 *)dst[1]));
+        SOAP_LAUNCHED(ctx);
+    } else {
+        SOAP_TRACED(ctx, "cube_types", k_cube_rows<double><<<grid_for(ctx, cube_elems, 256), 256, 0, ctx->stream>>>(
+                                           cube_elems, c.q_sed, c.q_norm, c.spot_norm, c.fac_norm,
+                                           (soap_double4 *)dst[0], (soap_double4 *)dst[1]));
         SOAP_LAUNCHED(ctx);
     }
     if (form == SOAPGB_FAST32) {
@@ -2373,18 +2403,23 @@ static int typed_cubes_into(soapgb_ctx *ctx, int form, int n, const soapgb_cubes
     return SOAPGB_OK;
 }
 
-int fir_typed_cubes(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, char *dst, FirTyped *out) {
+void fir_typed_layout(int form, int n, int n_mu, char *dst, const soapgb_cubes &c, FirTyped *out) {
     const size_t tsz = (form == SOAPGB_FAST32) ? 4 : 8;
-    const size_t cb = align256(tsz * (size_t)n * c.n_mu);
-    void *d[6];
-    for (int q = 0; q < 6; ++q) d[q] = dst + q * cb;
-    float2 *sa = (float2 *)(dst + 6 * cb), *sb = (float2 *)(dst + 6 * cb + align256(sizeof(float2) * (size_t)n));
-    for (int q = 0; q < 6; ++q) out->c[q] = d[q];
+    const size_t cb = align256(4 * tsz * (size_t)n * n_mu);
+    for (int q = 0; q < 6; ++q) out->c[q] = nullptr;
+    out->c[0] = dst;
+    out->c[1] = dst + cb;
     out->spot_sed = c.spot_sed;
     out->fac_sed = c.fac_sed;
-    out->spot_sed2 = sa;
-    out->fac_sed2 = sb;
-    return typed_cubes_into(ctx, form, n, c, d, sa, sb);
+    out->spot_sed2 = dst + 2 * cb;
+    out->fac_sed2 = dst + 2 * cb + align256(sizeof(float2) * (size_t)n);
+}
+
+int fir_typed_cubes(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, char *dst, FirTyped *out) {
+    fir_typed_layout(form, n, c.n_mu, dst, c, out);
+    void *d[2] = {const_cast<void *>(out->c[0]), const_cast<void *>(out->c[1])};
+    return typed_cubes_into(ctx, form, n, c, d, (float2 *)const_cast<void *>(out->spot_sed2),
+                            (float2 *)const_cast<void *>(out->fac_sed2));
 }
 
 static int fir_prepare(soapgb_ctx *ctx, const double *wave, int n_eff, double step, long long gm, const double *delta,
@@ -2679,8 +2714,7 @@ int fir_phase(soapgb_ctx *ctx, int form, const FirPhaseArgs &a, char *scratch, c
     FirCubes fc = phase_cubes(L, ws, a);
     if (a.stage & FIR_STAGE_CUBES) {
         if (a.typed) return set_error(ctx, SOAPGB_ERR_ARG, "fir_phase: shared typed cubes are made by fir_typed_cubes");
-        void *d[6];
-        for (int q = 0; q < 6; ++q) d[q] = const_cast<void *>(fc.c[q]);
+        void *d[2] = {const_cast<void *>(fc.c[0]), const_cast<void *>(fc.c[1])};
         int rc = typed_cubes_into(ctx, form, a.n, c, d, (float2 *)fc.spot_sed2, (float2 *)fc.fac_sed2);
         if (rc) return rc;
     }

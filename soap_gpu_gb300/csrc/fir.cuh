@@ -16,14 +16,17 @@ struct FirPlanSizes {
 FirPlanSizes fir_plan_sizes(int form, int n, int n_mu, long long gm, bool phase, int n_lists,
                             bool typed_external = false);
 
-// typed copies of the seed cubes read by the phase integration, shareable by the stars of
-// a batch (they share the seed spectra)
+// typed copies of the seed cubes read by the phase integration (c[0], c[1]: the spot and
+// facula classes' rows interleaved per pixel), shareable by the stars of a batch (they
+// share the seed spectra)
 struct FirTyped {
     const void *c[6];
     const double *spot_sed, *fac_sed;
     const void *spot_sed2, *fac_sed2;
 };
 size_t fir_typed_bytes(int form, int n, int n_mu);
+// the addresses fir_typed_cubes writes at dst (no device work)
+void fir_typed_layout(int form, int n, int n_mu, char *dst, const soapgb_cubes &c, FirTyped *out);
 int fir_typed_cubes(soapgb_ctx *ctx, int form, int n, const soapgb_cubes &c, char *dst, FirTyped *out);
 
 struct FirQuietArgs {

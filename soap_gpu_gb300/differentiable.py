@@ -347,7 +347,7 @@ def gauss_fit_bis(ccf, setup: CcfSetup):
 
 
 def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: ResolutionSetup, csetup: CcfSetup,
-                           chunk: int = 10, kind=0, quiet_cube: str = None):
+                           chunk: int = 10, kind=0, quiet_cube: str = None, recompute: bool = True):
     """RV, span and FWHM series over the setup's phases, relative to the quiet star, with
     the quiet spectra differentiated too.  kind selects the deficit (0 flux, 1 bconv,
     2 tot) or is a tuple of them; each pairs with its quiet base as run_all_SOAP.py pairs
@@ -358,7 +358,9 @@ def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: R
     The phases run in chunks of `chunk` under torch.utils.checkpoint: the forward keeps
     each chunk's fitted parameters only, and the backward recomputes the chunk's deficit,
     low-resolution spectra and CCFs before running their adjoints, so the memory held for
-    the backward grows with the fitted parameters, not with the spectra."""
+    the backward grows with the fitted parameters, not with the spectra.  recompute=False
+    keeps every chunk's intermediates instead (no second forward; memory grows with the
+    phases)."""
     from torch.utils.checkpoint import checkpoint
     kinds = (kind,) if isinstance(kind, int) else tuple(kind)
     base_key = {0: "q_sed", 1: "q_norm", 2: "q_sed"}
@@ -384,8 +386,8 @@ def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: R
     pars = []
     for p0 in range(0, setup.n_phase, chunk):
         p1 = min(setup.n_phase, p0 + chunk)
-        pars.append(checkpoint(chunk_par, p0, p1, star, *[bases[k] for k in keys], *cube_list,
-                               use_reentrant=False))
+        args = (p0, p1, star, *[bases[k] for k in keys], *cube_list)
+        pars.append(checkpoint(chunk_par, *args, use_reentrant=False) if recompute else chunk_par(*args))
     par = torch.cat(pars, dim=1)    # (kinds, phases, 5)
     res = {}
     for i, k in enumerate(kinds):
