@@ -990,7 +990,7 @@ def main():
     ap.add_argument("--form", default="fast32", choices=["fast32", "fast64", "plain64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-star batched form")
-    ap.add_argument("--diff-stars", type=int, default=8,
+    ap.add_argument("--diff-stars", type=int, default=2,
                     help="stars of the differentiable shape (64 stars x 50 phases) to time; 0 skips it")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed device steps (for ncu launch lists)")

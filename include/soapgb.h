@@ -209,6 +209,8 @@ int soapgb_phase_integrate(soapgb_ctx *ctx, int form, int n, int n_eff, const do
  * in a cell's velocity they are continuous and piecewise smooth (the derivative of the
  * interpolation weight inside each owner interval).  Chain rules: dL/du1 = -(1 - mu),
  * dL/du2 = -(1 - mu)^2 on visible cells; the velocity map is proportional to vsini.
+ * g_flux and g_tot may both be NULL, meaning zero (a scalar of bconv alone): the
+ * continuum-row gradients are then zero and cost no pass.
  * Deterministic: every sum runs in a fixed order, without atomics. */
 int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff, const double *wave,
                                    int grid, int n_phase, const double *temp, const double *bi,

@@ -659,7 +659,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     if (n < 2 || n_eff < 2 || n_eff > n || grid < 1 || n_phase < 0 || cubes->n_mu < 1 ||
         cubes->n_mu > ADJ_MAX_MU || !(step > 0) || !wave || !temp || !bi || !maps->delta || !maps->limb ||
         !maps->lb || !maps->region || !cubes->q_norm || !cubes->q_sed || !cubes->spot_norm || !cubes->fac_norm ||
-        !cubes->spot_sed || !cubes->fac_sed || !g_flux || !g_bconv || !g_tot || !grad_q_norm || !grad_q_sed ||
+        !cubes->spot_sed || !cubes->fac_sed || (!g_flux != !g_tot) || !g_bconv || !grad_q_norm || !grad_q_sed ||
         !grad_spot_norm || !grad_fac_norm || !grad_spot_sed || !grad_fac_sed || !grad_limb || !grad_delta)
         return set_error(ctx, SOAPGB_ERR_ARG, "soapgb_phase_integrate_adjoint: bad arguments");
     SOAP_DEVICE(ctx);
@@ -690,6 +690,10 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     int s_counts = ws.add(sizeof(int) * std::max(n_phase, 1));
     int s_roff = ws.add(sizeof(int) * (size_t)(n_mu + 1) * std::max(n_phase, 1));
     int s_buf = ws.add(map_b), s_bufd = ws.add(map_b);
+    // no flux or tot gradients: one zero array stands in for both, and the continuum
+    // rows, which enter only flux and tot, get no pass
+    const bool bconv_only = (g_flux == nullptr);
+    int s_zero = ws.add(bconv_only ? g_b : 0);
     int rc = ws.commit();
     if (rc) return rc;
 #define STAGE(dst, src, bytes, slot)                                                           \
@@ -715,6 +719,10 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     STAGE(d_gb, g_bconv, g_b, s_g[1]);
     STAGE(d_gt, g_tot, g_b, s_g[2]);
 #undef STAGE
+    if (bconv_only) {
+        SOAP_CUDA(ctx, cudaMemsetAsync(ws.get<void>(s_zero), 0, g_b, ctx->stream));
+        d_gf = d_gt = ws.get<double>(s_zero);
+    }
     double *o_qn = host ? ws.get<double>(s_o[0]) : grad_q_norm;
     double *o_qs = host ? ws.get<double>(s_o[1]) : grad_q_sed;
     double *o_sn = host ? ws.get<double>(s_o[2]) : grad_spot_norm;
@@ -745,12 +753,17 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
                         d_limb, d_lb, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb, d_gt, n, o_qn, o_qs,
                         o_sn, o_fn));
         SOAP_LAUNCHED(ctx);
-        SOAP_TRACED(ctx, "adjoint_continuum",
-                    k_adj_continuum<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
-                        n, n_eff, d_wave, d_qn, d_sn, d_fn, d_ss, d_fs, n_phase, gm, d_cells, d_counts, d_temp, d_bi,
-                        d_delta, d_limb, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf,
-                        d_gt, n, o_ss, o_fs));
-        SOAP_LAUNCHED(ctx);
+        if (bconv_only) {
+            SOAP_CUDA(ctx, cudaMemsetAsync(o_ss, 0, row_b, ctx->stream));
+            SOAP_CUDA(ctx, cudaMemsetAsync(o_fs, 0, row_b, ctx->stream));
+        } else {
+            SOAP_TRACED(ctx, "adjoint_continuum",
+                        k_adj_continuum<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+                            n, n_eff, d_wave, d_qn, d_sn, d_fn, d_ss, d_fs, n_phase, gm, d_cells, d_counts, d_temp,
+                            d_bi, d_delta, d_limb, d_lb, d_region, n_mu, step, act->solar, act->t_star,
+                            act->t_diff_fac, d_gf, d_gt, n, o_ss, o_fs));
+            SOAP_LAUNCHED(ctx);
+        }
         SOAP_CUDA(ctx, cudaMemsetAsync(d_buf, 0, map_b, ctx->stream));
         SOAP_CUDA(ctx, cudaMemsetAsync(d_bufd, 0, map_b, ctx->stream));
         const int gx = (int)std::min<long long>(gm, 4LL * std::max(ctx->num_sms, 1));

@@ -193,9 +193,9 @@ class QuietSpectrum(torch.autograd.Function):
         zc = torch.zeros_like(fctx.cube)
         zr = torch.zeros_like(setup.wave)
         cubes = dict(q_norm=fctx.cube, q_sed=zc, spot_norm=zc, fac_norm=zc, spot_sed=zr, fac_sed=zr)
-        gz = torch.zeros((1, setup.wave.shape[0]), dtype=torch.float64, device=g.device)
+        # only bconv carries a gradient: the adjoint skips the continuum rows' pass
         gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, temp, bi, maps, cubes, setup.step,
-                                               act, gz, g.to(torch.float64).reshape(1, -1).contiguous(), gz)
+                                               act, None, g.to(torch.float64).reshape(1, -1).contiguous(), None)
         return _star_grad(fctx.star, maps, gr["limb"], gr["delta"], fctx.vsini, fctx.incl), gr["q_norm"], None
 
 
@@ -387,7 +387,10 @@ def rv_series_checkpointed(star, cubes: dict, setup: IntegrationSetup, rsetup: R
     for p0 in range(0, setup.n_phase, chunk):
         p1 = min(setup.n_phase, p0 + chunk)
         args = (p0, p1, star, *[bases[k] for k in keys], *cube_list)
-        pars.append(checkpoint(chunk_par, *args, use_reentrant=False) if recompute else chunk_par(*args))
+        # the re-entrant form runs the chunk without a graph and reruns it under grad in the
+        # backward pass: the autograd Functions here keep their inputs on their contexts,
+        # which the non-re-entrant form's saved-tensor hooks would not release
+        pars.append(checkpoint(chunk_par, *args, use_reentrant=True) if recompute else chunk_par(*args))
     par = torch.cat(pars, dim=1)    # (kinds, phases, 5)
     res = {}
     for i, k in enumerate(kinds):
