@@ -219,21 +219,49 @@ __device__ __forceinline__ double soap_intensity(int type, double T, double lbk,
     return __dmul_rn(__dadd_rn(1.0, lbk), fsed);
 }
 
+// Per-cell constants of the adjoint weights.  In exact arithmetic the shifted grid is
+// l'_i = S l_i (S = sqrt((1+b)/(1-b))), so the interpolation weight of pixel j in the
+// owner interval o is w = (l_j - l'_o) / (S (l_{o+1} - l_o)) and
+// dw/ddelta = -l_j / (S (l_{o+1} - l_o)) * (dS/ddelta) / S, dS/ddelta = (1000/c) / (S (1-b)^2).
+// With the per-interval reciprocals inv[o] = 1 / (l_{o+1} - l_o) both take multiplications
+// only: w = (l_j - l'_o) * invS * inv[o], dw = -l_j * K * inv[o].  The forward rounds
+// ((row[o+1] - row[o]) / (l'_{o+1} - l'_o)) (l_j - l'_o); the adjoint needs the weights, not
+// that rounding (they agree to ~1e-10 of a weight).
+struct AdjCell {
+    CellShift cs;
+    double invS;   // 1 / S (1 for v == 0)
+    double K;      // (1000/c) / (S^3 (1-b)^2)
+};
+__device__ __forceinline__ AdjCell adj_cell(double d, double lambda0, double step) {
+    AdjCell a;
+    a.cs = soap_cell_shift(d, lambda0, step);
+    const double beta = d * 1000. / SOAP_C_LIGHT;
+    const double S = (d == 0.0) ? 1.0 : a.cs.sq;
+    const double omb = 1.0 - beta;
+    a.invS = 1.0 / S;
+    a.K = (1000. / SOAP_C_LIGHT) / (S * S * S * omb * omb);
+    return a;
+}
+
+// per-interval reciprocals inv[o] = 1 / (l_{o+1} - l_o), o < n_eff - 1
+__global__ void k_adj_inv(int n_eff, const double *__restrict__ lam, double *__restrict__ inv) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o < n_eff - 1) inv[o] = 1.0 / (lam[o + 1] - lam[o]);
+}
+
 // unit-limb values of a cell's three rows at output pixel j (q_norm, q_sed and the
-// spot or facula row), from one division: w = dl / dd at the owner o, then
-// row[o] + (row[o+1] - row[o]) w.  The forward forms ((row[o+1] - row[o]) / dd) dl per
-// row; the adjoint needs the values, not that rounding.
+// spot or facula row): w at the owner o, then row[o] + (row[o+1] - row[o]) w.
 struct AdjRows {
     double q, s, a;
     double dq, ds, da;   // d/ddelta of the three values (unit limb)
 };
 __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const double *__restrict__ lam,
-                                               const CellShift &cs, double d, const double *__restrict__ rq,
-                                               const double *__restrict__ rs, const double *__restrict__ ra) {
+                                               const double *__restrict__ inv, const AdjCell &ac, double d,
+                                               const double *__restrict__ rq, const double *__restrict__ rs,
+                                               const double *__restrict__ ra) {
     AdjRows v;
     // the owner interval of j; with v == 0 the forward copies pixel j (owner j, w = 0)
-    const long long o = (d == 0.0) ? ((j <= n_eff - 2) ? j : -1) : soap_owner(j, n_eff, cs);
-    const double beta = d * 1000. / SOAP_C_LIGHT;
+    const long long o = (d == 0.0) ? ((j <= n_eff - 2) ? j : -1) : soap_owner(j, n_eff, ac.cs);
     if (o < 0) {
         v.q = (d == 0.0) ? rq[j] : 0.0;
         v.s = (d == 0.0) ? rs[j] : 0.0;
@@ -241,20 +269,17 @@ __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const dou
         v.dq = v.ds = v.da = 0.0;
         return v;
     }
-    const double lo0 = lam[o], lo1 = lam[o + 1];
+    const double lo0 = lam[o], lj = lam[j], io = inv[o];
     double w = 0.0;
     if (d != 0.0) {
-        const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
-        const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
-        w = __ddiv_rn(__dsub_rn(lam[j], ls0), __dsub_rn(ls1, ls0));
+        const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, ac.cs.sq)));
+        w = (lj - ls0) * ac.invS * io;
     }
     const double eq = rq[o + 1] - rq[o], es = rs[o + 1] - rs[o], ea = ra[o + 1] - ra[o];
     v.q = fma(eq, w, rq[o]);
     v.s = fma(es, w, rs[o]);
     v.a = fma(ea, w, ra[o]);
-    const double S = (d == 0.0) ? 1.0 : cs.sq;
-    const double omb = 1.0 - beta;
-    const double dw = -lam[j] / (S * S * (lo1 - lo0)) / (S * omb * omb) * (1000. / SOAP_C_LIGHT);
+    const double dw = -lj * ac.K * io;
     v.dq = eq * dw;
     v.ds = es * dw;
     v.da = ea * dw;
@@ -263,7 +288,7 @@ __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const dou
 
 // row gradients: grid (ceil(n / 256), n_mu); thread = source pixel i of row b
 __global__ void __launch_bounds__(256) k_adj_rows(
-    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ spot_sed,
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ inv, const double *__restrict__ spot_sed,
     const double *__restrict__ fac_sed, int n_phase, long long gm, const int *__restrict__ rcells,
     const int *__restrict__ roff, int n_mu, const double *__restrict__ temp, const double *__restrict__ bi,
     const double *__restrict__ delta_m, const double *__restrict__ limb_m, const double *__restrict__ lb_m,
@@ -271,7 +296,7 @@ __global__ void __launch_bounds__(256) k_adj_rows(
     const double *__restrict__ gT, long long g_stride, double *__restrict__ d_qn, double *__restrict__ d_qs,
     double *__restrict__ d_sn, double *__restrict__ d_fn) {
     __shared__ double s_delta[PHASE_CHUNK], s_limb[PHASE_CHUNK], s_fb[PHASE_CHUNK], s_sq[PHASE_CHUNK],
-        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK];
+        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK], s_is[PHASE_CHUNK];
     __shared__ int s_type[PHASE_CHUNK];
     const int b = blockIdx.y;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -297,6 +322,7 @@ __global__ void __launch_bounds__(256) k_adj_rows(
                 s_fb[t] = cs.fbeta;
                 s_sq[t] = cs.sq;
                 s_off[t] = cs.off;
+                s_is[t] = 1.0 / cs.sq;
                 s_lb[t] = lb_m[k];
                 s_temp[t] = pt[k];
                 s_type[t] = (pb[k] == 0.0) ? 0 : 1;
@@ -326,20 +352,23 @@ __global__ void __launch_bounds__(256) k_adj_rows(
                 cs.fbeta = s_fb[t];
                 cs.sq = s_sq[t];
                 cs.off = s_off[t];
-                // owner o = i - 1 (source i is its upper neighbour) and o = i (lower)
+                const double invS = s_is[t];
+                // owner o = i - 1 (source i is its upper neighbour) and o = i (lower); the
+                // outputs of owner o are ceil(x_o) <= j < ceil(x_{o+1})
+                const long long cp[3] = {soap_ceil_pos(i - 1, cs), soap_ceil_pos(i, cs), soap_ceil_pos(i + 1, cs)};
+#pragma unroll
                 for (int side = 0; side < 2; ++side) {
                     const long long o = i - 1 + side;
                     if (o < 0 || o > n_eff - 2) continue;
-                    const long long ja = max(soap_ceil_pos(o, cs), 0LL);
-                    const long long jb = min(soap_ceil_pos(o + 1, cs), (long long)n_eff);
+                    const long long ja = max(cp[side], 0LL);
+                    const long long jb = min(cp[side + 1], (long long)n_eff);
                     if (ja >= jb) continue;
-                    const double lo0 = lam[o], lo1 = lam[o + 1];
+                    const double lo0 = lam[o];
                     const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, cs.sq)));
-                    const double ls1 = __dadd_rn(lo1, __dmul_rn(__dmul_rn(-1.0, lo1), __dsub_rn(1.0, cs.sq)));
-                    const double dd = __dsub_rn(ls1, ls0);
+                    const double sc = invS * inv[o];
                     for (long long j = ja; j < jb; ++j) {
-                        const double r = __ddiv_rn(__dsub_rn(lam[j], ls0), dd);
-                        add(j, side == 0 ? r : __dsub_rn(1.0, r));
+                        const double r = (lam[j] - ls0) * sc;
+                        add(j, side == 0 ? r : 1.0 - r);
                     }
                 }
             }
@@ -356,7 +385,7 @@ __global__ void __launch_bounds__(256) k_adj_rows(
 
 // continuum-row gradients: thread = output pixel j; all active cells of all phases
 __global__ void __launch_bounds__(256) k_adj_continuum(
-    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ q_norm,
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ inv, const double *__restrict__ q_norm,
     const double *__restrict__ spot_norm, const double *__restrict__ fac_norm, const double *__restrict__ spot_sed,
     const double *__restrict__ fac_sed, int n_phase, long long gm, const int *__restrict__ cells,
     const int *__restrict__ counts, const double *__restrict__ temp, const double *__restrict__ bi,
@@ -365,7 +394,7 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
     const double *__restrict__ gF, const double *__restrict__ gT, long long g_stride, double *__restrict__ d_ss,
     double *__restrict__ d_fs) {
     __shared__ double s_delta[PHASE_CHUNK], s_limb[PHASE_CHUNK], s_fb[PHASE_CHUNK], s_sq[PHASE_CHUNK],
-        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK];
+        s_off[PHASE_CHUNK], s_lb[PHASE_CHUNK], s_temp[PHASE_CHUNK], s_is[PHASE_CHUNK], s_k[PHASE_CHUNK];
     __shared__ int s_row[PHASE_CHUNK], s_type[PHASE_CHUNK];
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const double lambda0 = lam[0];
@@ -384,12 +413,14 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
             for (int t = threadIdx.x; t < nc; t += blockDim.x) {
                 const int k = pc[c0 + t];
                 const double d = delta_m[k];
-                const CellShift cs = soap_cell_shift(d, lambda0, step);
+                const AdjCell ac = adj_cell(d, lambda0, step);
                 s_delta[t] = d;
                 s_limb[t] = limb_m[k];
-                s_fb[t] = cs.fbeta;
-                s_sq[t] = cs.sq;
-                s_off[t] = cs.off;
+                s_fb[t] = ac.cs.fbeta;
+                s_sq[t] = ac.cs.sq;
+                s_off[t] = ac.cs.off;
+                s_is[t] = ac.invS;
+                s_k[t] = ac.K;
                 int row = region_m[k];
                 s_row[t] = ((unsigned)row < (unsigned)n_mu) ? row : 0;
                 s_lb[t] = lb_m[k];
@@ -399,14 +430,16 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
             __syncthreads();
             if (j >= n_eff) continue;
             for (int t = 0; t < nc; ++t) {
-                CellShift cs;
-                cs.fbeta = s_fb[t];
-                cs.sq = s_sq[t];
-                cs.off = s_off[t];
+                AdjCell ac;
+                ac.cs.fbeta = s_fb[t];
+                ac.cs.sq = s_sq[t];
+                ac.cs.off = s_off[t];
+                ac.invS = s_is[t];
+                ac.K = s_k[t];
                 const double d = s_delta[t], L = s_limb[t];
                 const long long off = (long long)s_row[t] * n;
                 const int type = s_type[t];
-                const AdjRows v = adj_rows_at(j, n_eff, lam, cs, d, q_norm + off, q_norm + off,
+                const AdjRows v = adj_rows_at(j, n_eff, lam, inv, ac, d, q_norm + off, q_norm + off,
                                               (type == 0 ? spot_norm : fac_norm) + off);
                 // d/dsed[j] of (-I q gF - I a gT) with I = ratio sed[j]; q, a carry L
                 const double h = __dmul_rn(L, fma(-v.q, gf, -__dmul_rn(v.a, gt)));
@@ -426,7 +459,7 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
 // ...; the dot product over the pixels is reduced in a fixed order (warp shuffles,
 // then warps in order) into buf[p][k]
 __global__ void __launch_bounds__(256) k_adj_limb(
-    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ q_norm,
+    int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ inv, const double *__restrict__ q_norm,
     const double *__restrict__ q_sed, const double *__restrict__ spot_norm, const double *__restrict__ fac_norm,
     const double *__restrict__ spot_sed, const double *__restrict__ fac_sed, long long gm,
     const int *__restrict__ cells, const int *__restrict__ counts, const double *__restrict__ temp,
@@ -445,7 +478,7 @@ __global__ void __launch_bounds__(256) k_adj_limb(
     for (int c = blockIdx.x; c < nc; c += gridDim.x) {
         const int k = pc[c];
         const double d = delta_m[k];
-        const CellShift cs = soap_cell_shift(d, lambda0, step);
+        const AdjCell ac = adj_cell(d, lambda0, step);
         int row = region_m[k];
         row = ((unsigned)row < (unsigned)n_mu) ? row : 0;
         const long long off = (long long)row * n;
@@ -454,7 +487,7 @@ __global__ void __launch_bounds__(256) k_adj_limb(
         const double *arow = (type == 0 ? spot_norm : fac_norm) + off;
         double acc = 0.0, accd = 0.0;
         for (long long j = threadIdx.x; j < n_eff; j += blockDim.x) {
-            const AdjRows v = adj_rows_at(j, n_eff, lam, cs, d, q_norm + off, q_sed + off, arow);
+            const AdjRows v = adj_rows_at(j, n_eff, lam, inv, ac, d, q_norm + off, q_sed + off, arow);
             const double I = soap_intensity(type, T, lbk, lam[j], spot_sed[j], fac_sed[j], solar, t_norm_fac);
             acc = fma(gf[j], __dsub_rn(v.s, __dmul_rn(I, v.q)), acc);
             acc = fma(gb[j], __dsub_rn(v.q, v.a), acc);
@@ -694,6 +727,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     // rows, which enter only flux and tot, get no pass
     const bool bconv_only = (g_flux == nullptr);
     int s_zero = ws.add(bconv_only ? g_b : 0);
+    int s_inv = ws.add(row_b);
     int rc = ws.commit();
     if (rc) return rc;
 #define STAGE(dst, src, bytes, slot)                                                           \
@@ -734,6 +768,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
     int *d_cells = ws.get<int>(s_cells), *d_rcells = ws.get<int>(s_rcells);
     int *d_counts = ws.get<int>(s_counts), *d_roff = ws.get<int>(s_roff);
     double *d_buf = ws.get<double>(s_buf), *d_bufd = ws.get<double>(s_bufd);
+    double *d_inv = ws.get<double>(s_inv);
     if (n_phase == 0) {
         for (double *o : {o_qn, o_qs, o_sn, o_fn})
             SOAP_CUDA(ctx, cudaMemsetAsync(o, 0, cube_b, ctx->stream));
@@ -747,9 +782,11 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         k_adj_bucket<<<n_phase, 32, 0, ctx->stream>>>(n_mu, gm, d_cells, d_counts, d_region, d_rcells, d_roff,
                                                       ctx->d_status);
         SOAP_LAUNCHED(ctx);
+        k_adj_inv<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, d_wave, d_inv);
+        SOAP_LAUNCHED(ctx);
         SOAP_TRACED(ctx, "adjoint_rows",
                     k_adj_rows<<<dim3(grid_for(ctx, n, 256), n_mu), 256, 0, ctx->stream>>>(
-                        n, n_eff, d_wave, d_ss, d_fs, n_phase, gm, d_rcells, d_roff, n_mu, d_temp, d_bi, d_delta,
+                        n, n_eff, d_wave, d_inv, d_ss, d_fs, n_phase, gm, d_rcells, d_roff, n_mu, d_temp, d_bi, d_delta,
                         d_limb, d_lb, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb, d_gt, n, o_qn, o_qs,
                         o_sn, o_fn));
         SOAP_LAUNCHED(ctx);
@@ -759,7 +796,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         } else {
             SOAP_TRACED(ctx, "adjoint_continuum",
                         k_adj_continuum<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
-                            n, n_eff, d_wave, d_qn, d_sn, d_fn, d_ss, d_fs, n_phase, gm, d_cells, d_counts, d_temp,
+                            n, n_eff, d_wave, d_inv, d_qn, d_sn, d_fn, d_ss, d_fs, n_phase, gm, d_cells, d_counts, d_temp,
                             d_bi, d_delta, d_limb, d_lb, d_region, n_mu, step, act->solar, act->t_star,
                             act->t_diff_fac, d_gf, d_gt, n, o_ss, o_fs));
             SOAP_LAUNCHED(ctx);
@@ -769,7 +806,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         const int gx = (int)std::min<long long>(gm, 4LL * std::max(ctx->num_sms, 1));
         SOAP_TRACED(ctx, "adjoint_limb",
                     k_adj_limb<<<dim3(gx, n_phase), 256, 0, ctx->stream>>>(
-                        n, n_eff, d_wave, d_qn, d_qs, d_sn, d_fn, d_ss, d_fs, gm, d_cells, d_counts, d_temp, d_bi,
+                        n, n_eff, d_wave, d_inv, d_qn, d_qs, d_sn, d_fn, d_ss, d_fs, gm, d_cells, d_counts, d_temp, d_bi,
                         d_delta, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb,
                         d_gt, n, d_limb, d_buf, d_bufd));
         SOAP_LAUNCHED(ctx);

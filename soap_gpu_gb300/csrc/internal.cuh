@@ -256,8 +256,10 @@ __device__ __forceinline__ double soap_lshift(double lam, const CellShift &c) {
 // Owner of output pixel j: the source i in [0, n_eff-2] with
 // ceil(x_i) <= j < ceil(x_{i+1}); returns -1 if none.
 __device__ __forceinline__ long long soap_owner(long long j, int n_eff, const CellShift &c) {
-    double r = 1 + c.fbeta;
-    long long i = (long long)floor(((double)j - c.off) / r);
+    // seed: x = (j - off) / (1 + f) to second order in f; the two loops below then pin
+    // the owner exactly, so the seed's rounding never reaches the result
+    const double x = (double)j - c.off;
+    long long i = (long long)floor(x * (1.0 - c.fbeta + c.fbeta * c.fbeta));
     if (i < -1) i = -1;
     if (i > n_eff - 1) i = n_eff - 1;
     // advance while the next source still starts at or before j
