@@ -1928,22 +1928,44 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 if (CHECKED && (j < jlo || j > jhi)) continue;
                 const int x = j + m;
                 const Vec4<T> v0 = r[x];
-                if (ZV) {   // single tap: w == 0
-                    part[0][q] += gr.a0 * v0.x;
-                    part[1][q] += gr.a0 * v0.y;
-                    part[2][q] += b0 * v0.z;
-                    part[3][q] += b0 * v0.w;
-                    continue;
+                if constexpr (sizeof(T) == 4) {
+                    // FP32: the four rows as two packed pairs (x, y) and (z, w), each lane
+                    // rounded as the scalar FMA would be
+                    if (ZV) {   // single tap: w == 0
+                        soap_fma2(part[0][q], part[1][q], gr.a0, gr.a0, v0.x, v0.y);
+                        soap_fma2(part[2][q], part[3][q], b0, b0, v0.z, v0.w);
+                        continue;
+                    }
+                    const Vec4<T> v1 = r[x + 1];
+                    const float fdj = (float)dj;
+                    float c0 = gr.a0, c0b = gr.a0, c1 = gr.a1, c1b = gr.a1;
+                    float e0 = b0, e0b = b0, e1 = b1, e1b = b1;
+                    soap_fma2(c0, c0b, -gr.b, -gr.b, fdj, fdj);
+                    soap_fma2(c1, c1b, gr.b, gr.b, fdj, fdj);
+                    soap_fma2(e0, e0b, -bb, -bb, fdj, fdj);
+                    soap_fma2(e1, e1b, bb, bb, fdj, fdj);
+                    soap_fma2(part[0][q], part[1][q], c0, c0b, v0.x, v0.y);
+                    soap_fma2(part[0][q], part[1][q], c1, c1b, v1.x, v1.y);
+                    soap_fma2(part[2][q], part[3][q], e0, e0b, v0.z, v0.w);
+                    soap_fma2(part[2][q], part[3][q], e1, e1b, v1.z, v1.w);
+                } else {
+                    if (ZV) {   // single tap: w == 0
+                        part[0][q] = fma(gr.a0, v0.x, part[0][q]);
+                        part[1][q] = fma(gr.a0, v0.y, part[1][q]);
+                        part[2][q] = fma(b0, v0.z, part[2][q]);
+                        part[3][q] = fma(b0, v0.w, part[3][q]);
+                        continue;
+                    }
+                    const Vec4<T> v1 = r[x + 1];
+                    const T fdj = (T)dj;
+                    const T c0 = fma(-gr.b, fdj, gr.a0), c1 = fma(gr.b, fdj, gr.a1);
+                    const T e0 = fma(-bb, fdj, b0), e1 = fma(bb, fdj, b1);
+                    // two chained FMAs per row (no separate product and sum)
+                    part[0][q] = fma(c1, v1.x, fma(c0, v0.x, part[0][q]));
+                    part[1][q] = fma(c1, v1.y, fma(c0, v0.y, part[1][q]));
+                    part[2][q] = fma(e1, v1.z, fma(e0, v0.z, part[2][q]));
+                    part[3][q] = fma(e1, v1.w, fma(e0, v0.w, part[3][q]));
                 }
-                const Vec4<T> v1 = r[x + 1];
-                const T fdj = (T)dj;
-                const T c0 = gr.a0 - gr.b * fdj, c1 = gr.a1 + gr.b * fdj;
-                const T e0 = b0 - bb * fdj, e1 = b1 + bb * fdj;
-                // two chained FMAs per row (no separate product and sum)
-                part[0][q] = fma(c1, v1.x, fma(c0, v0.x, part[0][q]));
-                part[1][q] = fma(c1, v1.y, fma(c0, v0.y, part[1][q]));
-                part[2][q] = fma(e1, v1.z, fma(e0, v0.z, part[2][q]));
-                part[3][q] = fma(e1, v1.w, fma(e0, v0.w, part[3][q]));
             }
         };
         using yes = std::integral_constant<bool, true>;
@@ -1995,10 +2017,21 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     s0 = rowp[i];
                     s1 = rowp[i + 1];
                 }
-                part[0][q] += xc.L * (s0.x + (s1.x - s0.x) * wd);
-                part[1][q] += xc.L * (s0.y + (s1.y - s0.y) * wd);
-                part[2][q] += w23 * (s0.z + (s1.z - s0.z) * wd);
-                part[3][q] += w23 * (s0.w + (s1.w - s0.w) * wd);
+                if constexpr (sizeof(T) == 4) {   // packed pairs (x, y) and (z, w)
+                    float gx = s1.x, gy = s1.y, gz = s1.z, gw = s1.w;
+                    soap_sub2(gx, gy, s0.x, s0.y);
+                    soap_sub2(gz, gw, s0.z, s0.w);
+                    float ux = s0.x, uy = s0.y, uz = s0.z, uw = s0.w;
+                    soap_fma2(ux, uy, gx, gy, wd, wd);
+                    soap_fma2(uz, uw, gz, gw, wd, wd);
+                    soap_fma2(part[0][q], part[1][q], xc.L, xc.L, ux, uy);
+                    soap_fma2(part[2][q], part[3][q], w23, w23, uz, uw);
+                } else {
+                    part[0][q] = fma(xc.L, fma(s1.x - s0.x, wd, s0.x), part[0][q]);
+                    part[1][q] = fma(xc.L, fma(s1.y - s0.y, wd, s0.y), part[1][q]);
+                    part[2][q] = fma(w23, fma(s1.z - s0.z, wd, s0.z), part[2][q]);
+                    part[3][q] = fma(w23, fma(s1.w - s0.w, wd, s0.w), part[3][q]);
+                }
             }
         };
         // the sources of a cell span [i0 - 1, i0 + FIR_TILE] over the tile

@@ -219,6 +219,34 @@ __device__ __forceinline__ unsigned long long soap_ord64(double v) {
     return (u & 0x8000000000000000ULL) ? ~u : (u | 0x8000000000000000ULL);
 }
 
+// Packed FP32 pairs (the f32x2 instructions of the sm_100 family): one instruction
+// does two FP32 operations with the rounding of each done separately.
+__device__ __forceinline__ void soap_add2(float &x, float &y, float a, float b) {   // (x, y) += (a, b)
+    asm("{\n\t.reg .b64 p, q;\n\tmov.b64 p, {%0, %1};\n\tmov.b64 q, {%2, %3};\n\t"
+        "add.rn.f32x2 p, p, q;\n\tmov.b64 {%0, %1}, p;\n\t}"
+        : "+f"(x), "+f"(y)
+        : "f"(a), "f"(b));
+}
+__device__ __forceinline__ void soap_sub2(float &x, float &y, float a, float b) {   // (x, y) -= (a, b)
+    asm("{\n\t.reg .b64 p, q;\n\tmov.b64 p, {%0, %1};\n\tmov.b64 q, {%2, %3};\n\t"
+        "sub.rn.f32x2 p, p, q;\n\tmov.b64 {%0, %1}, p;\n\t}"
+        : "+f"(x), "+f"(y)
+        : "f"(a), "f"(b));
+}
+__device__ __forceinline__ void soap_mul2(float &x, float &y, float a, float b, float c, float d) {   // (a c, b d)
+    asm("{\n\t.reg .b64 p, q, r;\n\tmov.b64 p, {%2, %3};\n\tmov.b64 q, {%4, %5};\n\t"
+        "mul.rn.f32x2 r, p, q;\n\tmov.b64 {%0, %1}, r;\n\t}"
+        : "=f"(x), "=f"(y)
+        : "f"(a), "f"(b), "f"(c), "f"(d));
+}
+// (x, y) = (a, b) * (c, d) + (x, y)
+__device__ __forceinline__ void soap_fma2(float &x, float &y, float a, float b, float c, float d) {
+    asm("{\n\t.reg .b64 p, q, r;\n\tmov.b64 p, {%2, %3};\n\tmov.b64 q, {%4, %5};\n\tmov.b64 r, {%0, %1};\n\t"
+        "fma.rn.f32x2 r, p, q, r;\n\tmov.b64 {%0, %1}, r;\n\t}"
+        : "+f"(x), "+f"(y)
+        : "f"(a), "f"(b), "f"(c), "f"(d));
+}
+
 // Delta_lambda, SOAP_initialize.cu:55-66
 __device__ __forceinline__ double soap_delta_lambda(double line_width, double lambda_line0) {
     double beta = line_width / SOAP_C_LIGHT;

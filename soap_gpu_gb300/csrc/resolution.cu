@@ -541,7 +541,10 @@ __device__ __forceinline__ float soap_ex2(float x) {
 // --- FAST32 convolution, shared pieces -------------------------------------------------
 // taps of 4 consecutive pixels ib .. ib+3 over SB staged spectra: xrow(q) + x0 is the
 // staged value of source pixel ib - R - sh (x0 + 4 k is 16-byte aligned), R the block's
-// reach, sh in [0, 3] the alignment shift; every weight one FFMA + one ex2
+// reach, sh in [0, 3] the alignment shift; every weight one ex2.  The arithmetic runs on
+// packed pairs: the weights of taps (k, k+1) of a pixel, and the sums of a pixel's even
+// and odd taps (added once at the end), so a float4 of staged values feeds two packed
+// FMAs per pixel.
 template <int SB>
 __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, int R, int sh, int wid,
                                             const float (&c2)[FC_PIX], const float (&lk)[FC_PIX],
@@ -549,37 +552,58 @@ __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, in
     // |d| <= R + 6 over the thread's taps: mask only if that can leave [-wid, wid - 2]
     const bool mask = (R + 8 > wid);
     const int nch = (3 + 2 * R + sh) / 4 + 1;
-    float dd[FC_PIX];
+    // tap offsets of the chunk: (d0, d1) = taps 0, 1 and (d2, d3) = taps 2, 3 of pixel p
+    float d0[FC_PIX], d1[FC_PIX], d2[FC_PIX], d3[FC_PIX];
 #pragma unroll
-    for (int p = 0; p < FC_PIX; ++p) dd[p] = (float)(-R - sh - p);
+    for (int p = 0; p < FC_PIX; ++p) {
+        d0[p] = (float)(-R - sh - p);
+        d1[p] = d0[p] + 1.f;
+        d2[p] = d0[p] + 2.f;
+        d3[p] = d0[p] + 3.f;
+    }
+    float ao[SB][FC_PIX];   // odd-tap sums; acc takes the even taps
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) ao[q][p] = 0.f;
     for (int ch = 0; ch < nch; ++ch) {
-        float w[4][FC_PIX];
+        float w0[FC_PIX], w1[FC_PIX], w2[FC_PIX], w3[FC_PIX];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-#pragma unroll
-            for (int p = 0; p < FC_PIX; ++p) {
-                const float d = dd[p] + (float)k;
-                float wv = soap_ex2(fmaf(d * d, c2[p], lk[p]));
-                if (mask && (d < (float)-wid || d > (float)(wid - 2))) wv = 0.f;
-                w[k][p] = wv;
+        for (int p = 0; p < FC_PIX; ++p) {
+            float y0 = lk[p], y1 = lk[p], y2 = lk[p], y3 = lk[p], s0, s1, s2, s3;
+            soap_mul2(s0, s1, d0[p], d1[p], d0[p], d1[p]);
+            soap_mul2(s2, s3, d2[p], d3[p], d2[p], d3[p]);
+            soap_fma2(y0, y1, s0, s1, c2[p], c2[p]);
+            soap_fma2(y2, y3, s2, s3, c2[p], c2[p]);
+            w0[p] = soap_ex2(y0);
+            w1[p] = soap_ex2(y1);
+            w2[p] = soap_ex2(y2);
+            w3[p] = soap_ex2(y3);
+            if (mask) {
+                const float lo = (float)-wid, hi = (float)(wid - 2);
+                if (d0[p] < lo || d0[p] > hi) w0[p] = 0.f;
+                if (d1[p] < lo || d1[p] > hi) w1[p] = 0.f;
+                if (d2[p] < lo || d2[p] > hi) w2[p] = 0.f;
+                if (d3[p] < lo || d3[p] > hi) w3[p] = 0.f;
             }
-#pragma unroll
-        for (int p = 0; p < FC_PIX; ++p) dd[p] += 4.f;
+            soap_add2(d0[p], d1[p], 4.f, 4.f);
+            soap_add2(d2[p], d3[p], 4.f, 4.f);
+        }
         const int li = x0 + 4 * ch;
 #pragma unroll
         for (int q = 0; q < SB; ++q) {
             const float4 x4 = *reinterpret_cast<const float4 *>(&xs[q * win + li]);
 #pragma unroll
             for (int p = 0; p < FC_PIX; ++p) {
-                float a = acc[q][p];
-                a = fmaf(w[0][p], x4.x, a);
-                a = fmaf(w[1][p], x4.y, a);
-                a = fmaf(w[2][p], x4.z, a);
-                a = fmaf(w[3][p], x4.w, a);
-                acc[q][p] = a;
+                soap_fma2(acc[q][p], ao[q][p], w0[p], w1[p], x4.x, x4.y);
+                soap_fma2(acc[q][p], ao[q][p], w2[p], w3[p], x4.z, x4.w);
             }
         }
     }
+#pragma unroll
+    for (int q = 0; q < SB; ++q)
+#pragma unroll
+        for (int p = 0; p < FC_PIX; ++p) acc[q][p] += ao[q][p];
 }
 
 // conv outputs of the SB spectra and their extrema: per block of 1024 pixels and
@@ -760,7 +784,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const 
 // source pixel mb = floor4(i0 - halo); pixels outside [0, n) are zeroed by the threads
 // once the copy has landed.
 template <int SB>
-__global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
+__global__ void __launch_bounds__(FC_THREADS, 2) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
                                                            const float *__restrict__ lka,
                                                            const int *__restrict__ livea, const int *__restrict__ rblk,
                                                            int wid, const float *__restrict__ spec,
