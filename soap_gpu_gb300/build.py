@@ -80,7 +80,7 @@ def build(verbose: bool = False, force: bool = False, jobs: int = 0) -> str:
         objs = list(ex.map(compile_one, srcs))
     if force or _stale(LIB, objs):
         tmp = LIB + ".tmp.%d" % os.getpid()
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
 
     def link_tool(name):

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -33,6 +34,32 @@ __global__ void k_widen_rows(long long n_rows, int n, int n_eff, const float *__
     if (t >= n_rows * n_eff) return;
     long long r = t / n_eff, i = t % n_eff;
     out[t] = soap_f32_to_f64(in[r * n + i]);
+}
+
+// Copies the `bytes` at src to every dst[k] (host memory), on up to eight host threads
+// (one per 4 MiB of copies), each a contiguous share of the concatenated destinations.
+static void host_replicate(const char *src, const std::vector<char *> &dst, size_t bytes) {
+    const size_t total = bytes * dst.size();
+    if (total == 0) return;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = (int)std::max<size_t>(1, std::min<size_t>({(size_t)8, (size_t)std::max(1u, hw / 2), total >> 22}));
+    auto work = [&](int t) {
+        const size_t a = total * t / nt, b = total * (t + 1) / nt;
+        for (size_t o = a; o < b;) {
+            const size_t d = o / bytes, off = o % bytes, len = std::min(bytes - off, b - o);
+            memcpy(dst[d] + off, src + off, len);
+            o += len;
+        }
+    };
+    std::vector<std::thread> pool;
+    int started = 1;
+    try {
+        for (int t = 1; t < nt; ++t, ++started) pool.emplace_back(work, t);
+    } catch (...) {   // no thread to be had: the remaining shares on this one
+    }
+    for (int t = started; t < nt; ++t) work(t);
+    work(0);
+    for (auto &th : pool) th.join();
 }
 
 extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff, const double *wave,
@@ -127,7 +154,7 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
     // last operation
     std::unique_ptr<TraceScope> span_main, span_copy, span_d2h;
     if (overlap) {
-        rc = copy_resources(ctx, n_chunk + 3);
+        rc = copy_resources(ctx, n_chunk + 4);
         if (rc) return rc;
         span_main.reset(new TraceScope(ctx, "call_main"));
         span_copy.reset(new TraceScope(ctx, "call_copy", ctx->copy_stream));
@@ -323,15 +350,16 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
             if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->aux_events[1], ctx->aux_stream), "aux join");
         }
         if (rc) return rc;
+        // the zero phases' rows are all the same: one crosses the host link, and the host
+        // copies it into the others while the visible phases are computed
+        cudaEvent_t zero_ev = overlap ? ctx->sync_events[3 + n_chunk] : nullptr;
         if (early_zero) {
             SOAP_CUDA(ctx, cudaStreamWaitEvent(ctx->d2h_stream, ctx->sync_events[2], 0));
             TraceScope ts(ctx, "d2h_zero", ctx->d2h_stream);
             const double *tmpl = ws.get<double>(s_ztmpl);
-            for (int q = 0; q < n_zero; ++q) {
-                const int p = h_lists[n_run + q];
-                SOAP_CUDA(ctx, cudaMemcpyAsync(lower + (size_t)3 * p * n_eff, tmpl, sizeof(double) * 3 * n_eff,
-                                               cudaMemcpyDeviceToHost, ctx->d2h_stream));
-            }
+            SOAP_CUDA(ctx, cudaMemcpyAsync(lower + (size_t)3 * h_lists[n_run] * n_eff, tmpl,
+                                           sizeof(double) * 3 * n_eff, cudaMemcpyDeviceToHost, ctx->d2h_stream));
+            SOAP_CUDA(ctx, cudaEventRecord(zero_ev, ctx->d2h_stream));
         }
         {
             // the geometry (lists, prefix sums, tile plans) is latency-bound and on the
@@ -359,10 +387,15 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
             }
             const int span = c_hi - c_lo;
             const int nc = chunked ? std::max(1, std::min(n_chunk, span)) : 1;
-            const int per = span > 0 ? (span + nc - 1) / nc : 0;
-            for (int c = 0; c < nc && span > 0; ++c) {
-                const int p0 = c_lo + c * per, p1 = std::min(c_hi, p0 + per);
-                if (p0 >= p1) break;
+            std::vector<int> cb;   // chunk c: phases [cb[c], cb[c + 1])
+            if (span > 0) {
+                const int per = (span + nc - 1) / nc;
+                for (int c = 0; c < nc; ++c) cb.push_back(std::min(c_hi, c_lo + c * per));
+                cb.push_back(c_hi);
+            }
+            for (int c = 0; c + 1 < (int)cb.size(); ++c) {
+                const int p0 = cb[c], p1 = cb[c + 1];
+                if (p0 >= p1) continue;
                 fa.stage = FIR_STAGE_RUN;
                 fa.l0 = p0;
                 fa.l1 = p1;
@@ -427,6 +460,13 @@ extern "C" int soapgb_phase_pipeline(soapgb_ctx *ctx, int form, int n, int n_eff
             }
         }
         if (!host) return SOAPGB_OK;
+        if (early_zero && n_zero > 1) {
+            SOAP_CUDA(ctx, cudaEventSynchronize(zero_ev));
+            std::vector<char *> dst;
+            for (int q = 1; q < n_zero; ++q) dst.push_back((char *)(lower + (size_t)3 * h_lists[n_run + q] * n_eff));
+            host_replicate((const char *)(lower + (size_t)3 * h_lists[n_run] * n_eff), dst,
+                           sizeof(double) * 3 * (size_t)n_eff);
+        }
         span_main.reset();
         span_copy.reset();
         span_d2h.reset();
