@@ -878,6 +878,9 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned
                  "r"(bytes)
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -1728,6 +1731,10 @@ struct FirPPSmem {
     Vec4<T> win[FIR_PP_NBUF][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
     unsigned long long wbar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2], pbar[2];
+    // released window buffers: every warp arrives once it has read a unit's window for
+    // the last time, and thread 0 waits for all of them before it copies a later unit
+    // into that buffer, so the warps need no block-wide barrier per unit
+    unsigned long long ebar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
     FirExcD<T> excd[FIR_PP_EXC];
     int wsum[FIR_THREADS / 32];
@@ -1767,7 +1774,10 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     const int G = gridDim.x;
     const int n = A0.n, n_eff = A0.n_eff;   // shared by every star
     if (tid == 0) {
-        for (int q = 0; q < (FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2); ++q) mbar_init(&sh.wbar[q], 1);
+        for (int q = 0; q < (FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2); ++q) {
+            mbar_init(&sh.wbar[q], 1);
+            mbar_init(&sh.ebar[q], FIR_THREADS / 32);
+        }
         mbar_init(&sh.pbar[0], 1);
         mbar_init(&sh.pbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1831,6 +1841,12 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     auto issue_unit = [&](int u, const FirUnit &d) {
         const int b = u % FIR_PP_NBUF;
         const unsigned bytes = (d.w1 > d.w0) ? (unsigned)(d.w1 - d.w0) * (unsigned)sizeof(Vec4<T>) : 0u;
+        // buffer b last held unit u - NBUF: every warp must have released it
+        if (u >= FIR_PP_NBUF &&
+            !mbar_wait_bounded(&sh.ebar[b], (unsigned)((u / FIR_PP_NBUF - 1) & 1), A0.wait_limit)) {
+            atomicExch(&sh.fail, 1);   // the unit is never copied: its readers' waits run out
+            return;
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(&sh.wbar[b], bytes);
         if (bytes) {
@@ -2047,10 +2063,24 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         }
     };
     // wait for unit u's rows (every thread; a timeout sets the block's fail flag)
+    // wait for unit u's rows.  Planned tiles: every thread for itself, with no barrier;
+    // a timeout sets the block's fail flag, the thread goes on with the buffer as it is
+    // (its reads stay inside the window) and the block leaves together at the next tile's
+    // barrier.  Tiles that plan themselves (block-wide steps with barriers): the barrier
+    // here, and the block leaves together at once.
     auto wait_unit = [&](int u) {
-        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1), A0.wait_limit)) atomicExch(&sh.fail, 1);
+        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1), A0.wait_limit))
+            atomicExch(&sh.fail, 1);
+    };
+    auto wait_unit_sync = [&](int u) {
+        wait_unit(u);
         __syncthreads();
         return sh.fail == 0;
+    };
+    // (every thread) done with unit u's window: one arrival per warp
+    auto release_unit = [&](int u) {
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&sh.ebar[u % FIR_PP_NBUF]);
     };
 
     // walk steps [0, kend)
@@ -2063,6 +2093,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     int k = 0;
     int bad = 0;
     int cur_star = -1;     // MULTI: the star whose arguments star_sh holds
+    unsigned next_plan_bytes = 0;   // (thread 0) size of the plan of step k + 1, read during step k - 1
     for (; k < kend && !bad; ++k) {
         const int v = pos(k);
         const int pbuf = k & 1;
@@ -2082,11 +2113,13 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
             }
         }
         if (!mbar_wait_bounded(&sh.pbar[pbuf], (unsigned)((k >> 1) & 1), A0.wait_limit)) atomicExch(&sh.fail, 1);
-        __syncthreads();
+        __syncthreads();   // the one barrier of a planned tile: the block leaves together on a failure
         if (sh.fail) {
             bad = 1;
             break;
         }
+        // every thread is done with step k - 1, so its plan buffer takes the plan of step k + 1
+        if (tid == 0 && k >= 1 && k + 1 < kend) issue_plan(pos(k + 1), pbuf ^ 1, next_plan_bytes);
         T *out0 = reinterpret_cast<T *>(A.out0);
         T *out1 = reinterpret_cast<T *>(A.out1);
         T *out2 = reinterpret_cast<T *>(A.out2);
@@ -2139,10 +2172,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                         }
                     }
                 }
-                if (!wait_unit(u)) {
-                    bad = 1;
-                    break;
-                }
+                wait_unit(u);
                 const FirUnit d = units[ui];
                 const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
                 if (nfold == 0) part_zero();
@@ -2154,7 +2184,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     part_fold(d.cls, j0);
                     nfold = 0;
                 }
-                if (FIR_PP_NBUF == 2) __syncthreads();   // buffer u % 2 free for unit u + 2
+                release_unit(u);
                 ++ucount;
             }
         } else if (t_eff > 0) {
@@ -2174,7 +2204,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                             if (ui == 0) issue_unit(u, st.unit[0]);
                             if (ui + 1 < nb) issue_unit(u + 1, st.unit[ui + 1]);
                         }
-                        if (!wait_unit(u)) {
+                        if (!wait_unit_sync(u)) {
                             bad = 1;
                             break;
                         }
@@ -2197,6 +2227,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     }
                     part_fold(d.cls, j0);
                     __syncthreads();
+                    if (FIR_PP_STAGED) release_unit(u);
                     ++ucount;
                 }
                 ub += nb;
@@ -2287,9 +2318,11 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
 #pragma unroll
             for (int a = 0; a < 3; ++a) acc[a][q].zero();
         }
-        __syncthreads();   // plan buffer pbuf free
-        if (tid == 0 && k + 2 < kend) issue_plan(pos(k + 2), pbuf, next_bytes);
+        next_plan_bytes = next_bytes;
     }
+    // a wait that ran out in the last step (no tile barrier after it)
+    __syncthreads();
+    if (sh.fail) bad = 1;
     if (bad && tid == 0) {
         // a copy did not land in time: record it and give the copies possibly in flight a
         // bounded wait before leaving
