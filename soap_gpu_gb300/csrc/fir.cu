@@ -145,6 +145,23 @@ __device__ __forceinline__ float soap_f64_to_f32(double v) {
     return __uint_as_float(bits | ((unsigned)(u >> 32) & 0x80000000u));
 }
 
+// int -> FP64, exact, on the integer pipes (the conversion instruction runs on GB300's
+// FP64 pipe, at 1/64 of the FP32 rate)
+__device__ __forceinline__ double soap_i2d(int m) {
+    if (m == 0) return 0.0;
+    const unsigned long long s = m < 0 ? 1ull : 0ull;
+    const unsigned a = m < 0 ? 0u - (unsigned)m : (unsigned)m;
+    const int e = 31 - __clz((int)a);   // a in [2^e, 2^(e+1))
+    const unsigned long long frac = ((unsigned long long)a << (52 - e)) & 0xfffffffffffffULL;
+    return __longlong_as_double((long long)((s << 63) | ((unsigned long long)(1023 + e) << 52) | frac));
+}
+// FP64 -> T rounded to nearest (FP32: on the integer pipes)
+template <typename T>
+__device__ __forceinline__ T soap_to(double v) {
+    if constexpr (sizeof(T) == 4) return soap_f64_to_f32(v);
+    else return v;
+}
+
 // The interleaved rows of the two classes in one pass over the four FP64 cubes, pixel
 // pairs per thread: spot (q_sed, q_norm, spot_norm, q_norm - spot_norm) and facula
 // (q_sed, q_norm - fac_norm, q_norm, fac_norm), the differences formed in FP64 and
@@ -240,6 +257,17 @@ __device__ __forceinline__ int fir_class_tb(const CellGeo &g, double t, double b
     if (!(g.L > -998.0)) return -1;
     if (!(b >= -0.5 && b <= 1.5)) return -1;
     if (bits_is_zero(b)) return bits_is_integral(t) ? CLS_SPOT : CLS_DIRECT;
+    return solar ? CLS_DIRECT : CLS_FAC;
+}
+
+// fir_class_tb for a box cell of a region of type `type` (b = 0 or 1; a spot's
+// temperature t_star - t_diff_spot is integral), with no FP64 instruction: the limb
+// test !(L > -998) on the order-preserving integer images (a NaN is not visible)
+__device__ __forceinline__ int fir_class_box(const CellGeo &g, int type, int solar) {
+    const unsigned long long lb = (unsigned long long)__double_as_longlong(g.L);
+    if ((lb & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL) return -1;   // NaN
+    if (!(soap_ord64(g.L) > soap_ord64(-998.0))) return -1;
+    if (type == 0) return CLS_SPOT;
     return solar ? CLS_DIRECT : CLS_FAC;
 }
 
@@ -438,9 +466,8 @@ __global__ void __launch_bounds__(FIR_BLIST_THREADS)
             if (owner != r) continue;
             // the class needs the type alone: a spot's temperature t_star - t_diff_spot is
             // integral, a facula's class does not depend on its temperature
-            const double t = (double)(t_star - t_diff_spot), b = (rp.type == 0) ? 0.0 : 1.0;
             const int k = iy * grid + iz;
-            const int c = fir_class_tb(geo[k], t, b, solar);
+            const int c = fir_class_box(geo[k], rp.type, solar);
             if (c < 0) continue;
             const int rk = rank[k];
             atomicOr(&bm[c * W + (rk >> 5)], 1u << (rk & 31));
@@ -539,10 +566,9 @@ __global__ void __launch_bounds__(FIR_SLIST_THREADS)
                 owner = region_cell_value(table, r0, r1, iy, iz, delta_grid, t_star, t_diff_spot, t_diff_fac, t, b);
             }
             if (owner != r) continue;
-            const double t = (double)(t_star - t_diff_spot), b = (rp.type == 0) ? 0.0 : 1.0;
             const int k = iy * grid + iz;
             const CellGeo &g = geo[k];
-            const int c = fir_class_tb(g, t, b, solar);
+            const int c = fir_class_box(g, rp.type, solar);
             if (c < 0) continue;
             atomicAdd(&ccnt[c], 1);
             const int pos = atomicAdd(&cnt, 1);
@@ -1213,7 +1239,8 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
                                int nunit, const double *sl, ST &st, int ub, int *wsum) {
     const int tid = threadIdx.x;
     const int n = A.n, n_eff = A.n_eff;
-    const double iXa = 1.0 / ((double)j0 + A.los), iXb = 1.0 / ((double)(j0 + t_eff - 1) + A.los);
+    const double dj0 = soap_i2d(j0);
+    const double iXa = 1.0 / (dj0 + A.los), iXb = 1.0 / (soap_i2d(j0 + t_eff - 1) + A.los);
     const int nbu = min(ST::NU, nunit - ub);
     for (int t = tid; t < nbu; t += NT) st.unit[t] = fir_describe<T, MODE>(ub + t, segs, nsg, j0, t_eff, n, n_eff);
     __syncthreads();
@@ -1239,10 +1266,11 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
         }
         const FirUnit d = st.unit[ui];
         const int m = d.ma + (k - st.ut[ui]);
+        const double dm = soap_i2d(m), dm1 = soap_i2d(m + 1);
         // the four boundaries in lock-step (those at the unit's first and last shift are
         // the range's ends)
-        const unsigned long long th[4] = {soap_ord64((double)m * iXa), soap_ord64((double)m * iXb),
-                                          soap_ord64((double)(m + 1) * iXa), soap_ord64((double)(m + 1) * iXb)};
+        const unsigned long long th[4] = {soap_ord64(dm * iXa), soap_ord64(dm * iXb), soap_ord64(dm1 * iXa),
+                                          soap_ord64(dm1 * iXb)};
         int bnd[4];
         fir_lower_bound4(sl, d.start, d.end, th, bnd);
         const int lowA = (m == d.m_lo) ? d.start : bnd[0], lowB = (m == d.m_lo) ? d.start : bnd[1];
@@ -1258,18 +1286,18 @@ __device__ void fir_plan_batch(const FirTileArgs &A, int l, int j0, int t_eff, c
             const double SL = P[rhi] - P[rlo];
             const double SLd = P[pc + rhi] - P[pc + rlo];
             const double SLo = P[2 * pc + rhi] - P[2 * pc + rlo];
-            const double A1 = (double)j0 * SLd - SLo - (double)m * SL;
-            gr.a1 = (T)A1;
-            gr.a0 = (T)(SL - A1);
-            gr.b = (T)SLd;
+            const double A1 = dj0 * SLd - SLo - dm * SL;
+            gr.a1 = soap_to<T>(A1);
+            gr.a0 = soap_to<T>(SL - A1);
+            gr.b = soap_to<T>(SLd);
             if (MODE == MODE_PHASE && d.cls == CLS_FAC) {
                 const double Wt = P[3 * pc + rhi] - P[3 * pc + rlo];
                 const double Wd = P[4 * pc + rhi] - P[4 * pc + rlo];
                 const double Wo = P[5 * pc + rhi] - P[5 * pc + rlo];
-                const double W1 = (double)j0 * Wd - Wo - (double)m * Wt;
-                gr.a1w = (T)W1;
-                gr.a0w = (T)(Wt - W1);
-                gr.bw = (T)Wd;
+                const double W1 = dj0 * Wd - Wo - dm * Wt;
+                gr.a1w = soap_to<T>(W1);
+                gr.a0w = soap_to<T>(Wt - W1);
+                gr.bw = soap_to<T>(Wd);
             }
         }
         st.grp[k] = gr;

@@ -125,6 +125,11 @@ static int build_region_table(soapgb_ctx *ctx, int grid, double incl, int n_phas
             rp.r0 = r3[0];
             rp.r1 = r3[1];
             rp.r2 = r3[2];
+            // the FP32 owner test's constants (its margins absorb their rounding)
+            rp.f0 = (float)rp.r0;
+            rp.f1 = (float)rp.r1;
+            rp.f2 = (float)rp.r2;
+            rp.fcap = (float)(1.0 - s * s);
         }
     }
     return SOAPGB_OK;

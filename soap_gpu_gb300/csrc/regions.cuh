@@ -12,6 +12,7 @@ struct RegionPhase {
     int type;                // 0 spot, 1 facula
     double s;                // cap chord radius
     double r0, r1, r2;       // first row of the inverse rotation
+    float f0, f1, f2, fcap;  // FP32 copies of r0, r1, r2 and of 1 - s^2 (the FP32 owner test)
 };
 
 // Temperature t and type b of cell (iy, iz) after the regions [r0, r1) of one phase,
@@ -79,8 +80,8 @@ __device__ __forceinline__ int region_owner_fp32(const RegionPhase *__restrict__
         const float rest = 1.f - q;
         if (rest < 1e-2f) return -2;
         const float xa = sqrtf(rest);
-        const float xi = fmaf((float)rp.r0, xa, fmaf((float)rp.r1, y, (float)rp.r2 * z));
-        const float d = fmaf(xi, xi, -(float)(1.0 - rp.s * rp.s));
+        const float xi = fmaf(rp.f0, xa, fmaf(rp.f1, y, rp.f2 * z));
+        const float d = fmaf(xi, xi, -rp.fcap);
         if (fabsf(d) <= 2e-4f) return -2;
         if (d > 0.f) owner = r;
     }
