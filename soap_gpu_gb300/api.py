@@ -349,8 +349,8 @@ class Context:
 
     def gauss_fit_adjoint(self, x, y, model, par, g_par, err=None):
         """Gradient (n_spec x n) of a scalar w.r.t. the fitted CCFs y, given its gradient
-        g_par (n_spec x 5) w.r.t. the fit's par = (c, |k|, span, v0, fwhm); the span's
-        entry is ignored."""
+        g_par (n_spec x 5) w.r.t. the fit's par = (c, |k|, span, v0, fwhm), the bisector
+        span's with its per-depth crossing intervals held fixed."""
         a = self._args(y, x)
         n_spec, n = int(y.shape[0]), int(x.shape[0])
         out, op = a.out((n_spec, n), np.float64)

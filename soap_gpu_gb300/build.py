@@ -97,7 +97,32 @@ def build(verbose: bool = False, force: bool = False, jobs: int = 0) -> str:
     if os.path.isdir(TOOLS):
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
             list(ex.map(link_tool, TOOL_NAMES))
+    build_torch_ops(verbose=verbose)
     return LIB
+
+
+TORCH_SRC = os.path.join(CSRC, "torch", "soapgb_torch.cpp")
+TORCH_OPS = os.path.join(LIBDIR, "soapgb_torch.so")
+
+
+def build_torch_ops(verbose: bool = False) -> str:
+    """The torch operators over libsoapgb (csrc/torch/soapgb_torch.cpp: torch.ops.soapgb.*)
+    as lib/soapgb_torch.so, through torch.utils.cpp_extension (a C++ source linked
+    against libsoapgb and the CUDA runtime; no device code)."""
+    deps = [TORCH_SRC, LIB, os.path.join(ROOT, "include", "soapgb.h")]
+    if not _stale(TORCH_OPS, deps):
+        return TORCH_OPS
+    import torch.utils.cpp_extension as ce
+    bdir = os.path.join(OBJ, "torch_ops")
+    os.makedirs(bdir, exist_ok=True)
+    ce.load(name="soapgb_torch", sources=[TORCH_SRC], extra_include_paths=[os.path.join(ROOT, "include")],
+            extra_cflags=["-O2"], extra_ldflags=["-L" + LIBDIR, "-lsoapgb", "-Wl,-rpath," + LIBDIR],
+            with_cuda=True, build_directory=bdir, is_python_module=False, verbose=verbose)
+    built = os.path.join(bdir, "soapgb_torch.so")
+    tmp = TORCH_OPS + ".tmp.%d" % os.getpid()
+    shutil.copyfile(built, tmp)
+    os.replace(tmp, TORCH_OPS)
+    return TORCH_OPS
 
 
 if __name__ == "__main__":

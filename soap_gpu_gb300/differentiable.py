@@ -47,6 +47,10 @@ carries the continuum-row gradients to them.
 pass and recomputing the chunk's spectra there.
 
 Region positions and sizes stay discrete (cell coverage), as in the reference.
+
+Every call into the library here goes through the torch operators of
+``torch_ops`` (``torch.ops.soapgb.*``, the C++ extension over the C ABI): CUDA tensors
+in and out, on torch's current stream.
 """
 from __future__ import annotations
 
@@ -55,8 +59,9 @@ import dataclasses
 import numpy as np
 import torch
 
-from .api import Context
 from ._lib import Activity
+from .api import Context
+from .torch_ops import ops
 
 CUBE_KEYS = ("q_norm", "q_sed", "spot_norm", "fac_norm", "spot_sed", "fac_sed")
 
@@ -98,7 +103,7 @@ class IntegrationSetup:
         """The disk maps for limb-darkening coefficients (u1, u2), vsini and the
         inclination (default: the setup's, which fixed the region maps), on the device."""
         period = 2 * np.pi * self.radius_km / (vsini * 86400.0)
-        return self.ctx.disk_maps(self.grid, period, self.omega_ratio, self.incl if incl is None else incl,
+        return ops(self.ctx).disk_maps(self.grid, period, self.omega_ratio, self.incl if incl is None else incl,
                                   self.radius_km, u1, u2, self.mu_boundary, self.lb)
 
     def phases(self, p0: int, p1: int) -> "IntegrationSetup":
@@ -141,8 +146,8 @@ class DeficitSpectra(torch.autograd.Function):
         fctx.vsini, fctx.incl, fctx.star = vsini, incl, star.detach()
         cubes = dict(zip(CUBE_KEYS, (q_norm.detach(), q_sed.detach(), spot_norm.detach(), fac_norm.detach(),
                                      spot_sed.detach(), fac_sed.detach())))
-        flux, bconv, tot = setup.ctx.phase_integrate("plain64", setup.wave, setup.n_eff, setup.grid, setup.temp,
-                                                     setup.bi, maps, cubes, setup.step, setup.act)
+        flux, bconv, tot = ops(setup.ctx).phase_integrate("plain64", setup.wave, setup.n_eff, setup.grid,
+                                                          setup.temp, setup.bi, maps, cubes, setup.step, setup.act)
         fctx.setup = setup
         fctx.maps = maps
         fctx.cubes = cubes
@@ -152,9 +157,9 @@ class DeficitSpectra(torch.autograd.Function):
     def backward(fctx, g):
         setup, maps = fctx.setup, fctx.maps
         g = g.to(torch.float64)
-        gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, setup.temp, setup.bi, maps,
-                                               fctx.cubes, setup.step, setup.act, g[:, 0].contiguous(),
-                                               g[:, 1].contiguous(), g[:, 2].contiguous())
+        gr = ops(setup.ctx).phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, setup.temp, setup.bi,
+                                                    maps, fctx.cubes, setup.step, setup.act, g[:, 0].contiguous(),
+                                                    g[:, 1].contiguous(), g[:, 2].contiguous())
         grad_star = _star_grad(fctx.star, maps, gr["limb"], gr["delta"], fctx.vsini, fctx.incl)
         return (grad_star, gr["q_norm"], gr["q_sed"], gr["spot_norm"], gr["fac_norm"], gr["spot_sed"],
                 gr["fac_sed"], None)
@@ -177,7 +182,7 @@ class QuietSpectrum(torch.autograd.Function):
     def forward(fctx, star, cube, setup: IntegrationSetup):
         maps, incl = _star_maps(setup, star)
         c = cube.detach().contiguous()
-        out = setup.ctx.quiet_disk("plain64", setup.wave, c, setup.n_eff, maps, setup.grid, setup.step)
+        out = ops(setup.ctx).quiet_disk("plain64", setup.wave, c, setup.n_eff, maps, setup.grid, setup.step)
         fctx.setup, fctx.maps, fctx.cube, fctx.star = setup, maps, c, star.detach()
         fctx.vsini, fctx.incl = float(star[2]), incl
         return out.reshape(-1)
@@ -194,8 +199,9 @@ class QuietSpectrum(torch.autograd.Function):
         zr = torch.zeros_like(setup.wave)
         cubes = dict(q_norm=fctx.cube, q_sed=zc, spot_norm=zc, fac_norm=zc, spot_sed=zr, fac_sed=zr)
         # only bconv carries a gradient: the adjoint skips the continuum rows' pass
-        gr = setup.ctx.phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, temp, bi, maps, cubes, setup.step,
-                                               act, None, g.to(torch.float64).reshape(1, -1).contiguous(), None)
+        gr = ops(setup.ctx).phase_integrate_adjoint(setup.wave, setup.n_eff, setup.grid, temp, bi, maps, cubes,
+                                                    setup.step, act, None,
+                                                    g.to(torch.float64).reshape(1, -1).contiguous(), None)
         return _star_grad(fctx.star, maps, gr["limb"], gr["delta"], fctx.vsini, fctx.incl), gr["q_norm"], None
 
 
@@ -231,8 +237,8 @@ class LowerResolution(torch.autograd.Function):
     @staticmethod
     def forward(fctx, spec, base, setup: ResolutionSetup):
         spec_d, base_d = spec.detach().contiguous(), base.detach().contiguous()
-        out, _ = setup.ctx.lower_resolution("plain64", setup.wave, spec_d, setup.n_eff, setup.sigma_v, base=base_d,
-                                            **setup.kwargs())
+        out, _ = ops(setup.ctx).lower_resolution("plain64", setup.wave, spec_d, setup.n_eff, setup.sigma_v,
+                                                 base=base_d, **setup.kwargs())
         fctx.setup, fctx.spec, fctx.base = setup, spec_d, base_d
         fctx.want_base = base.requires_grad
         return out
@@ -240,9 +246,9 @@ class LowerResolution(torch.autograd.Function):
     @staticmethod
     def backward(fctx, g):
         setup = fctx.setup
-        gs, gb = setup.ctx.lower_resolution_adjoint(setup.wave, fctx.spec, setup.n_eff, setup.sigma_v,
-                                                    g.to(torch.float64).contiguous(), base=fctx.base,
-                                                    want_base=fctx.want_base, **setup.kwargs())
+        gs, gb = ops(setup.ctx).lower_resolution_adjoint(setup.wave, fctx.spec, setup.n_eff, setup.sigma_v,
+                                                         g.to(torch.float64).contiguous(), base=fctx.base,
+                                                         want_base=fctx.want_base, **setup.kwargs())
         return gs, gb, None
 
 
@@ -278,7 +284,7 @@ class NormalisedCcf(torch.autograd.Function):
     @staticmethod
     def forward(fctx, spectra, setup: CcfSetup):
         sp = spectra.detach().contiguous()
-        c = setup.ctx
+        c = ops(setup.ctx)
         args = (setup.vel, setup.line_wave, setup.line_weight, setup.wave_trim, setup.step, sp)
         raw = c.ccf("plain64", *args, normalise=False, **setup.kwargs())
         out = c.ccf("plain64", *args, normalise=True, **setup.kwargs())
@@ -288,7 +294,7 @@ class NormalisedCcf(torch.autograd.Function):
     @staticmethod
     def backward(fctx, g):
         s = fctx.setup
-        grad = s.ctx.ccf_adjoint(s.vel, s.line_wave, s.line_weight, s.wave_trim, s.step,
+        grad = ops(s.ctx).ccf_adjoint(s.vel, s.line_wave, s.line_weight, s.wave_trim, s.step,
                                  g.to(torch.float64).contiguous(), ccf_raw=fctx.raw, normalise=True, **s.kwargs())
         return grad, None
 
@@ -301,7 +307,7 @@ class GaussFit(torch.autograd.Function):
     @staticmethod
     def forward(fctx, ccf, setup: CcfSetup):
         y = ccf.detach().contiguous()
-        res = setup.ctx.gauss_bis(setup.vel, y)
+        res = ops(setup.ctx).gauss_bis(setup.vel, y)
         if bool((res["iters"] < 0).any()):
             raise RuntimeError("Gaussian fit did not converge; its gradient is undefined")
         fctx.setup, fctx.y, fctx.model, fctx.par = setup, y, res["model"], res["par"]
@@ -312,10 +318,10 @@ class GaussFit(torch.autograd.Function):
         gp = torch.zeros_like(fctx.par)
         gp[:, [0, 1, 3, 4]] = g.to(torch.float64)
         s = fctx.setup
-        gy = s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, gp)
+        gy = ops(s.ctx).gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, gp)
         # a singular system gives a zero gradient and a device status: raise here, as the
         # forward does for a fit that did not converge, rather than return that zero
-        s.ctx.synchronize()
+        ops(s.ctx).synchronize()
         return gy, None
 
 
@@ -327,7 +333,7 @@ class GaussFitBis(torch.autograd.Function):
     @staticmethod
     def forward(fctx, ccf, setup: CcfSetup):
         y = ccf.detach().contiguous()
-        res = setup.ctx.gauss_bis(setup.vel, y)
+        res = ops(setup.ctx).gauss_bis(setup.vel, y)
         if bool((res["iters"] < 0).any()):
             raise RuntimeError("Gaussian fit did not converge; its gradient is undefined")
         fctx.setup, fctx.y, fctx.model, fctx.par = setup, y, res["model"], res["par"]
@@ -336,8 +342,8 @@ class GaussFitBis(torch.autograd.Function):
     @staticmethod
     def backward(fctx, g):
         s = fctx.setup
-        gy = s.ctx.gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, g.to(torch.float64).contiguous())
-        s.ctx.synchronize()
+        gy = ops(s.ctx).gauss_fit_adjoint(s.vel, fctx.y, fctx.model, fctx.par, g.to(torch.float64).contiguous())
+        ops(s.ctx).synchronize()
         return gy, None
 
 

@@ -61,3 +61,15 @@ def test_dropin_executables_check_argv():
         p = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
         assert p.returncode == 1
         assert "expected" in p.stderr
+
+
+def test_torch_operators_registered(lib):
+    """The torch extension over the C ABI (torch.ops.soapgb.*) builds, loads and registers
+    every operator (no compute calls)."""
+    pytest.importorskip("torch")
+    from soap_gpu_gb300 import build, torch_ops
+    if not os.path.exists(torch_ops.PATH):
+        build.build_torch_ops()
+    o = torch_ops.load()
+    for name in torch_ops.OPS:
+        assert hasattr(o, name), name
