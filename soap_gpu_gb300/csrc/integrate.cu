@@ -255,6 +255,7 @@ struct AdjRows {
     double q, s, a;
     double dq, ds, da;   // d/ddelta of the three values (unit limb)
 };
+template <bool WITH_S = true>
 __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const double *__restrict__ lam,
                                                const double *__restrict__ inv, const AdjCell &ac, double d,
                                                const double *__restrict__ rq, const double *__restrict__ rs,
@@ -275,9 +276,9 @@ __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const dou
         const double ls0 = __dadd_rn(lo0, __dmul_rn(__dmul_rn(-1.0, lo0), __dsub_rn(1.0, ac.cs.sq)));
         w = (lj - ls0) * ac.invS * io;
     }
-    const double eq = rq[o + 1] - rq[o], es = rs[o + 1] - rs[o], ea = ra[o + 1] - ra[o];
+    const double eq = rq[o + 1] - rq[o], es = WITH_S ? rs[o + 1] - rs[o] : 0.0, ea = ra[o + 1] - ra[o];
     v.q = fma(eq, w, rq[o]);
-    v.s = fma(es, w, rs[o]);
+    v.s = WITH_S ? fma(es, w, rs[o]) : 0.0;
     v.a = fma(ea, w, ra[o]);
     const double dw = -lj * ac.K * io;
     v.dq = eq * dw;
@@ -287,6 +288,8 @@ __device__ __forceinline__ AdjRows adj_rows_at(long long j, int n_eff, const dou
 }
 
 // row gradients: grid (ceil(n / 256), n_mu); thread = source pixel i of row b
+// BC: the bconv gradient alone (gF = gT = 0): no intensity, no q_sed or continuum terms
+template <bool BC>
 __global__ void __launch_bounds__(256) k_adj_rows(
     int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ inv, const double *__restrict__ spot_sed,
     const double *__restrict__ fac_sed, int n_phase, long long gm, const int *__restrict__ rcells,
@@ -334,10 +337,17 @@ __global__ void __launch_bounds__(256) k_adj_rows(
                 const int type = s_type[t];
                 // contributions of output pixel j with weight w on source i
                 auto add = [&](long long j, double w) {
+                    const double lw = __dmul_rn(L, w);
+                    if constexpr (BC) {
+                        const double g = gb[j];
+                        aqn = fma(lw, g, aqn);
+                        if (type == 0) asn = fma(lw, -g, asn);
+                        else afn = fma(lw, -g, afn);
+                        return;
+                    }
                     const double lj = lam[j];
                     const double I = soap_intensity(type, s_temp[t], s_lb[t], lj, spot_sed[j], fac_sed[j], solar,
                                                     t_norm_fac);
-                    const double lw = __dmul_rn(L, w);
                     aqs = fma(lw, __dadd_rn(gf[j], gt[j]), aqs);
                     aqn = fma(lw, __dsub_rn(gb[j], __dmul_rn(I, gf[j])), aqn);
                     const double ha = __dsub_rn(-gb[j], __dmul_rn(I, gt[j]));
@@ -458,6 +468,7 @@ __global__ void __launch_bounds__(256) k_adj_continuum(
 // limb gradients per (phase, cell): block (x, p) takes the phase's cells x, x + gridDim.x,
 // ...; the dot product over the pixels is reduced in a fixed order (warp shuffles,
 // then warps in order) into buf[p][k]
+template <bool BC>
 __global__ void __launch_bounds__(256) k_adj_limb(
     int n, int n_eff, const double *__restrict__ lam, const double *__restrict__ inv, const double *__restrict__ q_norm,
     const double *__restrict__ q_sed, const double *__restrict__ spot_norm, const double *__restrict__ fac_norm,
@@ -487,6 +498,13 @@ __global__ void __launch_bounds__(256) k_adj_limb(
         const double *arow = (type == 0 ? spot_norm : fac_norm) + off;
         double acc = 0.0, accd = 0.0;
         for (long long j = threadIdx.x; j < n_eff; j += blockDim.x) {
+            if constexpr (BC) {   // bconv alone: (q - a) against gB
+                const AdjRows v = adj_rows_at<false>(j, n_eff, lam, inv, ac, d, q_norm + off, q_norm + off, arow);
+                const double g = gb[j];
+                acc = fma(g, __dsub_rn(v.q, v.a), acc);
+                accd = fma(g, v.dq - v.da, accd);
+                continue;
+            }
             const AdjRows v = adj_rows_at(j, n_eff, lam, inv, ac, d, q_norm + off, q_sed + off, arow);
             const double I = soap_intensity(type, T, lbk, lam[j], spot_sed[j], fac_sed[j], solar, t_norm_fac);
             acc = fma(gf[j], __dsub_rn(v.s, __dmul_rn(I, v.q)), acc);
@@ -785,7 +803,8 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         k_adj_inv<<<grid_for(ctx, n_eff, 256), 256, 0, ctx->stream>>>(n_eff, d_wave, d_inv);
         SOAP_LAUNCHED(ctx);
         SOAP_TRACED(ctx, "adjoint_rows",
-                    k_adj_rows<<<dim3(grid_for(ctx, n, 256), n_mu), 256, 0, ctx->stream>>>(
+                    (bconv_only ? k_adj_rows<true> : k_adj_rows<false>)<<<dim3(grid_for(ctx, n, 256), n_mu), 256, 0,
+                                                                              ctx->stream>>>(
                         n, n_eff, d_wave, d_inv, d_ss, d_fs, n_phase, gm, d_rcells, d_roff, n_mu, d_temp, d_bi, d_delta,
                         d_limb, d_lb, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb, d_gt, n, o_qn, o_qs,
                         o_sn, o_fn));
@@ -805,7 +824,7 @@ extern "C" int soapgb_phase_integrate_adjoint(soapgb_ctx *ctx, int n, int n_eff,
         SOAP_CUDA(ctx, cudaMemsetAsync(d_bufd, 0, map_b, ctx->stream));
         const int gx = (int)std::min<long long>(gm, 4LL * std::max(ctx->num_sms, 1));
         SOAP_TRACED(ctx, "adjoint_limb",
-                    k_adj_limb<<<dim3(gx, n_phase), 256, 0, ctx->stream>>>(
+                    (bconv_only ? k_adj_limb<true> : k_adj_limb<false>)<<<dim3(gx, n_phase), 256, 0, ctx->stream>>>(
                         n, n_eff, d_wave, d_inv, d_qn, d_qs, d_sn, d_fn, d_ss, d_fs, gm, d_cells, d_counts, d_temp, d_bi,
                         d_delta, d_lb, d_region, n_mu, step, act->solar, act->t_star, act->t_diff_fac, d_gf, d_gb,
                         d_gt, n, d_limb, d_buf, d_bufd));
