@@ -480,13 +480,9 @@ class Batch:
         self.ctx._check(self.ctx.L.soapgb_batch_tune(self.h, int(chunk), int(blocks_per_sm)))
 
     def run(self, out=None, quiet=None):
-        dev = "cuda:%d" % self.ctx.device
-        if out is None:
-            out = torch.empty((self.total_phases, 3, self.n_eff), dtype=torch.float64, device=dev)
-        self.ctx.L.soapgb_set_stream(self.ctx.h, ctypes.c_void_p(torch_stream_handle(self.ctx.device)))
-        self.ctx._check(self.ctx.L.soapgb_batch_run(self.ctx.h, self.h, ctypes.c_void_p(out.data_ptr()),
-                                                    ctypes.c_void_p(quiet.data_ptr()) if quiet is not None else None))
-        return out
+        """Enqueues the batch on torch's current stream (torch.ops.soapgb.batch_run)."""
+        from .torch_ops import ops
+        return ops(self.ctx).batch_run(self, out, quiet)
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

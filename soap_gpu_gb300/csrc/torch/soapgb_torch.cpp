@@ -1,4 +1,4 @@
-// soapgb_torch: the differentiable form's calls into libsoapgb as torch operators.
+// soapgb_torch: libsoapgb's calls for the differentiable and batched forms as torch operators.
 //
 // torch.ops.soapgb.* take the context handle (the soapgb_ctx pointer as an int, from
 // soap_gpu_gb300.api.Context), CUDA tensors (float64 / int32, contiguous) and scalars,
@@ -291,6 +291,26 @@ Tensor gauss_fit_adjoint(int64_t h, const Tensor &x, const Tensor &y, const Tens
     return out;
 }
 
+// ---- batched form: one run of a batch made by soapgb_batch_create -----------------------
+// out: (total phases, 3, n_eff), allocated here when None; quiet: the stars' quiet
+// spectra (optional output, as soapgb_batch_run takes it)
+Tensor batch_run(int64_t h, int64_t batch, int64_t total_phases, int64_t n_eff, int64_t device,
+                 const std::optional<Tensor> &out, const std::optional<Tensor> &quiet) {
+    TORCH_CHECK(batch != 0, "soapgb: null batch");
+    Tensor o = (out.has_value() && out->defined())
+                   ? *out
+                   : at::empty({total_phases, 3, n_eff},
+                               at::TensorOptions().dtype(at::kDouble).device(at::kCUDA, (c10::DeviceIndex)device));
+    TORCH_CHECK(o.numel() == total_phases * 3 * n_eff, "soapgb: out is (total phases, 3, n_eff)");
+    c10::cuda::CUDAGuard guard(o.device());
+    soapgb_ctx *ctx = on_stream(h, o);
+    check(ctx, soapgb_batch_run(ctx, reinterpret_cast<soapgb_batch *>(static_cast<uintptr_t>(batch)),
+                                const_cast<double *>(f64(o, "out")),
+                                const_cast<double *>(f64_opt(quiet, "quiet"))),
+          "soapgb_batch_run");
+    return o;
+}
+
 // waits for the context's stream and raises a device status (a singular fit system)
 void synchronize(int64_t h) {
     soapgb_ctx *ctx = as_ctx(h);
@@ -335,5 +355,8 @@ TORCH_LIBRARY(soapgb, m) {
     m.def("gauss_fit_adjoint(int ctx, Tensor x, Tensor y, Tensor model, Tensor par, Tensor g_par, Tensor? err) "
           "-> Tensor",
           gauss_fit_adjoint);
+    m.def("batch_run(int ctx, int batch, int total_phases, int n_eff, int device, Tensor? out, Tensor? quiet) "
+          "-> Tensor",
+          batch_run);
     m.def("synchronize(int ctx) -> ()", synchronize);
 }

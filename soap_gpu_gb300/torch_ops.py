@@ -1,7 +1,7 @@
 """torch operators over libsoapgb: ``torch.ops.soapgb.*`` (csrc/torch/soapgb_torch.cpp).
 
-The differentiable form's autograd Functions (``differentiable.py``) call the library
-through these operators: CUDA tensors in, CUDA tensors out (allocated by torch on the
+The differentiable form's autograd Functions (``differentiable.py``) and the batched
+form's runs (``api.Batch.run``) call the library through these operators: CUDA tensors in, CUDA tensors out (allocated by torch on the
 inputs' device), on torch's current stream, an error status raised with the library's
 message.  ``Ops(ctx)`` binds them to an ``api.Context`` with the argument conventions
 of the context's own methods.  The operators are built by ``build.build()`` into
@@ -18,7 +18,7 @@ from ._lib import FORMS, Activity
 
 PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "soapgb_torch.so")
 OPS = ("disk_maps", "quiet_disk", "phase_integrate", "phase_integrate_adjoint", "lower_resolution",
-       "lower_resolution_adjoint", "ccf", "ccf_adjoint", "gauss_bis", "gauss_fit_adjoint", "synchronize")
+       "lower_resolution_adjoint", "ccf", "ccf_adjoint", "gauss_bis", "gauss_fit_adjoint", "batch_run", "synchronize")
 _loaded = False
 
 
@@ -133,6 +133,11 @@ class Ops:
 
     def gauss_fit_adjoint(self, x, y, model, par, g_par, err=None):
         return self.o.gauss_fit_adjoint(self.h, _t(x), _t(y), _t(model), _t(par), _t(g_par), _t(err))
+
+    def batch_run(self, batch, out=None, quiet=None):
+        """One run of an ``api.Batch`` into ``out`` (allocated when None)."""
+        return self.o.batch_run(self.h, int(batch.h.value), int(batch.total_phases), int(batch.n_eff),
+                                int(self.ctx.device), out, quiet)
 
     def synchronize(self):
         self.o.synchronize(self.h)
