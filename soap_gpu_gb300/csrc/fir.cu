@@ -1751,7 +1751,7 @@ constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per c
 constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
 constexpr int FIR_PP_MINB = 2;   // resident blocks per SM the kernel is compiled for
 constexpr int FIR_PP_EXC = 64;   // directly evaluated cells per staged batch
-constexpr int FIR_FOLD = 4;          // work units per fold of the partial sums
+constexpr int FIR_FOLD = 8;          // work units per fold of the partial sums
 // Shared memory of k_fir_pp: staged cube windows, two plan buffers, storage for the
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
