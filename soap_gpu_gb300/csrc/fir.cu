@@ -1136,6 +1136,7 @@ struct FirTileArgs {
     int n_lists_all;            // lists with a plan slot
     long long wait_limit;       // polls per bounded wait of the persistent kernel
     int drop_plan;              // failure-path test: the first plan copy is expected, not issued
+    int drop_unit;              // failure-path test: each block's first window copy is expected, not issued
 };
 
 // The list's (class, mu bin, v == 0) segments with their shift ranges at the tile
@@ -1867,6 +1868,9 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     // (thread 0) stage the interleaved rows of unit number u (buffer u % 3): pixels
     // [w0, w1) of the class's Vec4 row, one bulk copy (Vec4 elements are 16-byte multiples)
     auto issue_unit = [&](int u, const FirUnit &d) {
+        // after a failed wait the block stops feeding the pipeline (no new expected bytes
+        // on a buffer whose copy may never have landed) and leaves at the next barrier
+        if (*reinterpret_cast<volatile int *>(&sh.fail)) return;
         const int b = u % FIR_PP_NBUF;
         const unsigned bytes = (d.w1 > d.w0) ? (unsigned)(d.w1 - d.w0) * (unsigned)sizeof(Vec4<T>) : 0u;
         // buffer b last held unit u - NBUF: every warp must have released it
@@ -1877,7 +1881,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_expect_tx(&sh.wbar[b], bytes);
-        if (bytes) {
+        if (bytes && !(A0.drop_unit && u == 0)) {
             // the typed cubes are the same for every star
             const Vec4<T> *row = reinterpret_cast<const Vec4<T> *>(A0.cubes.c[d.cls == CLS_SPOT ? 0 : 1]) +
                                  (long long)(d.key >> 1) * n;
@@ -2659,6 +2663,7 @@ static FirTileArgs make_tile_args(soapgb_ctx *ctx, const FirLayout &L, char *ws,
     A.n_lists_all = n_lists;
     A.wait_limit = ctx->test_wait_limit > 0 ? ctx->test_wait_limit : FIR_WAIT_LIMIT;
     A.drop_plan = (ctx->test_drop_copy == 1) ? 1 : 0;
+    A.drop_unit = (ctx->test_drop_copy == 3) ? 1 : 0;
     return A;
 }
 

@@ -60,7 +60,8 @@ struct soapgb_ctx {
     // SOAPGB_TEST_WAIT_LIMIT polls per bounded wait of the staged-copy kernels (0: the
     // default 2^24) and SOAPGB_TEST_DROP_COPY, a staged copy whose bytes are expected but
     // never issued, so that its wait runs out (1: the integration kernel's first plan
-    // copy, status 41; 2: the FP32 convolution's first window, status 42)
+    // copy, status 41; 2: the FP32 convolution's first window, status 42; 3: the
+    // integration kernel's first window copy of each block, status 41)
     long long test_wait_limit = 0;
     int test_drop_copy = 0;
     // per-kernel tracing (soapgb_trace_enable): spans recorded since the last report

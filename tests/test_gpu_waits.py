@@ -2,8 +2,10 @@
 (the persistent integration kernel and the FP32 convolution) run out cleanly.
 
 A context created with SOAPGB_TEST_WAIT_LIMIT (polls per wait) and SOAPGB_TEST_DROP_COPY
-in the environment expects the bytes of one staged copy per block but never issues it,
-so that wait runs out: the kernel records its status word (41 integration, 42
+in the environment expects the bytes of one staged copy per block but never issues it
+(1: the integration kernel's first plan; 2: the convolution's first window; 3: the
+integration kernel's first work-unit window, whose wait each thread takes without a
+block barrier), so that wait runs out: the kernel records its status word (41 integration, 42
 convolution), gives the copies it did issue a bounded wait and returns.  The call
 reports the status (soapgb_synchronize: SOAPGB_ERR_DEVICE with the status in the
 message), and the GPU stays usable: a fresh context then runs the same call to the
@@ -37,7 +39,7 @@ def _pipeline(ctx):
                               [case.regions for _ in case.phases], qs, qn, case.sigma_v, conv_step=case.step)
 
 
-@pytest.mark.parametrize("drop,status", [(1, 41), (2, 42)])
+@pytest.mark.parametrize("drop,status", [(1, 41), (2, 42), (3, 41)])
 def test_staged_copy_wait_runs_out_and_reports(monkeypatch, drop, status):
     from soap_gpu_gb300.api import Context
     with Context(0) as good:
