@@ -542,9 +542,9 @@ __device__ __forceinline__ float soap_ex2(float x) {
 // taps of 4 consecutive pixels ib .. ib+3 over SB staged spectra: xrow(q) + x0 is the
 // staged value of source pixel ib - R - sh (x0 + 4 k is 16-byte aligned), R the block's
 // reach, sh in [0, 3] the alignment shift; every weight one ex2.  The arithmetic runs on
-// packed pairs: the weights of taps (k, k+1) of a pixel, and the sums of a pixel's even
-// and odd taps (added once at the end), so a float4 of staged values feeds two packed
-// FMAs per pixel.
+// packed pairs over the pixel pairs (0, 1) and (2, 3): their exponents, and their sums,
+// each staged value feeding two packed FMAs (one per pixel pair) in the scalar form's
+// order, so the sums are the scalar FMA chain's bit for bit.
 template <int SB>
 __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, int R, int sh, int wid,
                                             const float (&c2)[FC_PIX], const float (&lk)[FC_PIX],
@@ -552,58 +552,46 @@ __device__ __forceinline__ void conv32_taps(const float *xs, int win, int x0, in
     // |d| <= R + 6 over the thread's taps: mask only if that can leave [-wid, wid - 2]
     const bool mask = (R + 8 > wid);
     const int nch = (3 + 2 * R + sh) / 4 + 1;
-    // tap offsets of the chunk: (d0, d1) = taps 0, 1 and (d2, d3) = taps 2, 3 of pixel p
-    float d0[FC_PIX], d1[FC_PIX], d2[FC_PIX], d3[FC_PIX];
-#pragma unroll
-    for (int p = 0; p < FC_PIX; ++p) {
-        d0[p] = (float)(-R - sh - p);
-        d1[p] = d0[p] + 1.f;
-        d2[p] = d0[p] + 2.f;
-        d3[p] = d0[p] + 3.f;
-    }
-    float ao[SB][FC_PIX];   // odd-tap sums; acc takes the even taps
-#pragma unroll
-    for (int q = 0; q < SB; ++q)
-#pragma unroll
-        for (int p = 0; p < FC_PIX; ++p) ao[q][p] = 0.f;
+    // tap offset of tap 0 of the chunk at pixels (0, 1) and (2, 3), as pairs
+    float e0 = (float)(-R - sh), e1 = e0 - 1.f, e2 = e0 - 2.f, e3 = e0 - 3.f;
     for (int ch = 0; ch < nch; ++ch) {
-        float w0[FC_PIX], w1[FC_PIX], w2[FC_PIX], w3[FC_PIX];
+        float w[4][FC_PIX];   // w[k][p]: tap k of pixel p
 #pragma unroll
-        for (int p = 0; p < FC_PIX; ++p) {
-            float y0 = lk[p], y1 = lk[p], y2 = lk[p], y3 = lk[p], s0, s1, s2, s3;
-            soap_mul2(s0, s1, d0[p], d1[p], d0[p], d1[p]);
-            soap_mul2(s2, s3, d2[p], d3[p], d2[p], d3[p]);
-            soap_fma2(y0, y1, s0, s1, c2[p], c2[p]);
-            soap_fma2(y2, y3, s2, s3, c2[p], c2[p]);
-            w0[p] = soap_ex2(y0);
-            w1[p] = soap_ex2(y1);
-            w2[p] = soap_ex2(y2);
-            w3[p] = soap_ex2(y3);
+        for (int k = 0; k < 4; ++k) {
+            float da = e0, db = e1, dc = e2, dd = e3;
+            soap_add2(da, db, (float)k, (float)k);
+            soap_add2(dc, dd, (float)k, (float)k);
+            float ya = lk[0], yb = lk[1], yc = lk[2], yd = lk[3], sa, sb, sc, sd;
+            soap_mul2(sa, sb, da, db, da, db);
+            soap_mul2(sc, sd, dc, dd, dc, dd);
+            soap_fma2(ya, yb, sa, sb, c2[0], c2[1]);
+            soap_fma2(yc, yd, sc, sd, c2[2], c2[3]);
+            w[k][0] = soap_ex2(ya);
+            w[k][1] = soap_ex2(yb);
+            w[k][2] = soap_ex2(yc);
+            w[k][3] = soap_ex2(yd);
             if (mask) {
                 const float lo = (float)-wid, hi = (float)(wid - 2);
-                if (d0[p] < lo || d0[p] > hi) w0[p] = 0.f;
-                if (d1[p] < lo || d1[p] > hi) w1[p] = 0.f;
-                if (d2[p] < lo || d2[p] > hi) w2[p] = 0.f;
-                if (d3[p] < lo || d3[p] > hi) w3[p] = 0.f;
+                if (da < lo || da > hi) w[k][0] = 0.f;
+                if (db < lo || db > hi) w[k][1] = 0.f;
+                if (dc < lo || dc > hi) w[k][2] = 0.f;
+                if (dd < lo || dd > hi) w[k][3] = 0.f;
             }
-            soap_add2(d0[p], d1[p], 4.f, 4.f);
-            soap_add2(d2[p], d3[p], 4.f, 4.f);
         }
+        soap_add2(e0, e1, 4.f, 4.f);
+        soap_add2(e2, e3, 4.f, 4.f);
         const int li = x0 + 4 * ch;
 #pragma unroll
         for (int q = 0; q < SB; ++q) {
             const float4 x4 = *reinterpret_cast<const float4 *>(&xs[q * win + li]);
+            const float xv[4] = {x4.x, x4.y, x4.z, x4.w};
 #pragma unroll
-            for (int p = 0; p < FC_PIX; ++p) {
-                soap_fma2(acc[q][p], ao[q][p], w0[p], w1[p], x4.x, x4.y);
-                soap_fma2(acc[q][p], ao[q][p], w2[p], w3[p], x4.z, x4.w);
+            for (int k = 0; k < 4; ++k) {
+                soap_fma2(acc[q][0], acc[q][1], w[k][0], w[k][1], xv[k], xv[k]);
+                soap_fma2(acc[q][2], acc[q][3], w[k][2], w[k][3], xv[k], xv[k]);
             }
         }
     }
-#pragma unroll
-    for (int q = 0; q < SB; ++q)
-#pragma unroll
-        for (int p = 0; p < FC_PIX; ++p) acc[q][p] += ao[q][p];
 }
 
 // conv outputs of the SB spectra and their extrema: per block of 1024 pixels and
@@ -784,7 +772,7 @@ __global__ void __launch_bounds__(FC_THREADS) k_conv32x(int n, int n_eff, const 
 // source pixel mb = floor4(i0 - halo); pixels outside [0, n) are zeroed by the threads
 // once the copy has landed.
 template <int SB>
-__global__ void __launch_bounds__(FC_THREADS, 2) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
+__global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, const float *__restrict__ c2a,
                                                            const float *__restrict__ lka,
                                                            const int *__restrict__ livea, const int *__restrict__ rblk,
                                                            int wid, const float *__restrict__ spec,
