@@ -35,6 +35,7 @@
 using namespace soapgb;
 
 constexpr int FIR_THREADS = 256;
+constexpr int FIR_WARPS = FIR_THREADS / 32;
 constexpr int FIR_PIX = 4;
 constexpr int FIR_TILE = FIR_THREADS * FIR_PIX;
 constexpr int FIR_WIN = 1152;                    // staged values per cube row (window capacity)
@@ -1761,8 +1762,8 @@ struct FirPPSmem {
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
     unsigned long long wbar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2], pbar[2];
     // released window buffers: every warp arrives once it has read a unit's window for
-    // the last time, and thread 0 waits for all of them before it copies a later unit
-    // into that buffer, so the warps need no block-wide barrier per unit
+    // the last time, and the thread that copies a later unit into that buffer waits for
+    // all of them first, so the warps need no block-wide barrier per unit
     unsigned long long ebar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
     FirExcD<T> excd[FIR_PP_EXC];
@@ -1865,7 +1866,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         mbar_expect_tx(&sh.pbar[b], bytes);
         if (!(first && A0.drop_plan)) bulk_g2s(&sh.pb[b][0], plan_rec(v), bytes, &sh.pbar[b]);
     };
-    // (thread 0) stage the interleaved rows of unit number u (buffer u % 3): pixels
+    // (one thread) stage the interleaved rows of unit number u (buffer u % 3): pixels
     // [w0, w1) of the class's Vec4 row, one bulk copy (Vec4 elements are 16-byte multiples)
     auto issue_unit = [&](int u, const FirUnit &d) {
         // after a failed wait the block stops feeding the pipeline (no new expected bytes
@@ -2121,7 +2122,9 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         if (kend > 1) issue_plan(pos(1), 1, plan_size(pos(1)));
     }
     int ucount = 0;        // units staged and applied so far (window buffer ucount % 3)
-    bool pre = false;      // (thread 0) the current tile's first unit was issued ahead
+    // the previous tile was planned and its last unit issued this tile's first unit ahead
+    // when this tile's plan has units (the issuing thread's test, repeated by every thread)
+    bool prev_ahead = false;
     int k = 0;
     int bad = 0;
     int cur_star = -1;     // MULTI: the star whose arguments star_sh holds
@@ -2162,6 +2165,8 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         const int *cn = A.counts + 4 * l;
         const unsigned char *rec = sh.pb[pbuf];
         const int4 hdr = *reinterpret_cast<const int4 *>(rec);
+        const bool pre = prev_ahead && t_eff > 0 && hdr.w && hdr.x > 0;
+        prev_ahead = false;
         if (t_eff > 0 && hdr.w) {
             // --- planned tile ------------------------------------------------------------
             const int nb = hdr.x;
@@ -2184,14 +2189,15 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     part_fold(d.cls, j0);
                     continue;
                 }
-                if (tid == 0) {
-                    if (ui == 0 && !pre) issue_unit(u, units[0]);
+                // unit u is copied by lane 0 of warp u % 8: the copies' mbarrier latencies
+                // are spread over the warps instead of holding back one of them
+                if (ui == 0 && !pre && tid == (u % FIR_WARPS) * 32) issue_unit(u, units[0]);
+                if (tid == ((u + 1) % FIR_WARPS) * 32) {
                     if (ui + 1 < nb) {
                         issue_unit(u + 1, units[1 + ui]);
-                    } else {
+                    } else if (k + 1 < kend) {
                         // last unit: issue the next tile's first unit, from its plan
-                        pre = false;
-                        if (k + 1 < kend && mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit)) {
+                        if (mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit)) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
                             const int tnr = real(pos(k + 1));
@@ -2199,8 +2205,9 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                             if (hn.w && hn.x > 0 && jn < n_eff) {
                                 const FirPlanLayout<T> Ln(hn.x, hn.y, hn.z);
                                 issue_unit(u + 1, *reinterpret_cast<const FirUnit *>(rn + Ln.o_unit));
-                                pre = true;
                             }
+                        } else {
+                            atomicExch(&sh.fail, 1);   // the block leaves at the next tile's barrier
                         }
                     }
                 }
@@ -2219,9 +2226,9 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 release_unit(u);
                 ++ucount;
             }
+            prev_ahead = nb > 0 && k + 1 < kend;
         } else if (t_eff > 0) {
             // --- tile that plans itself, batch by batch ----------------------------------
-            if (tid == 0) pre = false;
             const int nsg = A.nseg[2 * l] + A.nseg[2 * l + 1];
             const int nunit = fir_segments<MODE_PHASE, FIR_THREADS>(A, l, j0, t_eff, segs, nsg, &sh.nunit_sh);
             auto &st = sh.st;
