@@ -1746,11 +1746,17 @@ __global__ void __launch_bounds__(FIR_THREADS) k_fir(const FirTileArgs A) {
 // false: the apply loops read them from global memory (L1-cached), with no per-unit barrier
 constexpr bool FIR_PP_STAGED = true;
 constexpr int FIR_PP_WIN = FIR_PP_STAGED ? FIR_WIN : 4;   // staged values per cube row
-// window buffers: unit u is staged in buffer u % NBUF.  With three, the copy of unit
-// u + 1 (issued before unit u is applied) lands in the buffer of unit u - 2, which every
-// thread left before the barrier of unit u - 1: one barrier per unit.  With two, a
-// second barrier after each unit frees its buffer.
-constexpr int FIR_PP_NBUF = FIR_PP_STAGED ? 3 : 1;
+// window buffers: unit u is staged in buffer u % NBUF, copied LEAD units ahead (when unit
+// u - LEAD starts) into the buffer of unit u - NBUF, which every warp has released unless it
+// lags NBUF - LEAD - 1 units behind the copying warp.  FP32 windows (18 KB): four buffers,
+// copies two units ahead, so a copy's mbarrier and TMA latencies stay off the next unit's
+// path; FP64 windows (37 KB, two blocks per SM): three buffers, one unit ahead.
+template <typename T>
+struct FirPPBuf {
+    static constexpr int NBUF = FIR_PP_STAGED ? (sizeof(T) == 4 ? 4 : 3) : 2;
+    static constexpr int LEAD = sizeof(T) == 4 ? 2 : 1;
+    static_assert(!FIR_PP_STAGED || NBUF >= LEAD + 2, "a copy must not wait for the unit before it");
+};
 constexpr int FIR_PP_MINB = 2;   // resident blocks per SM the kernel is compiled for
 constexpr int FIR_PP_EXC = 64;   // directly evaluated cells per staged batch
 constexpr int FIR_FOLD = 8;          // work units per fold of the partial sums
@@ -1758,13 +1764,13 @@ constexpr int FIR_FOLD = 8;          // work units per fold of the partial sums
 // tiles that plan themselves, the direct cells' batch.
 template <typename T>
 struct FirPPSmem {
-    Vec4<T> win[FIR_PP_NBUF][FIR_PP_WIN];
+    Vec4<T> win[FirPPBuf<T>::NBUF][FIR_PP_WIN];
     __align__(16) unsigned char pb[2][FirPlanSlot<T>::BYTES];
-    unsigned long long wbar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2], pbar[2];
+    unsigned long long wbar[FirPPBuf<T>::NBUF], pbar[2];
     // released window buffers: every warp arrives once it has read a unit's window for
     // the last time, and the thread that copies a later unit into that buffer waits for
     // all of them first, so the warps need no block-wide barrier per unit
-    unsigned long long ebar[FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2];
+    unsigned long long ebar[FirPPBuf<T>::NBUF];
     FirPlanSt<T, 32, FIR_THREADS, FIR_THREADS> st;
     FirExcD<T> excd[FIR_PP_EXC];
     int wsum[FIR_THREADS / 32];
@@ -1795,6 +1801,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                                                         int ntot_all, const FirTileArgs *__restrict__ stars,
                                                         const int2 *__restrict__ items, int chunk) {
     constexpr int SLOT = FirPlanSlot<T>::BYTES;
+    constexpr int NBUF = FirPPBuf<T>::NBUF, LEAD = FirPPBuf<T>::LEAD;
     extern __shared__ __align__(128) unsigned char pp_smem[];
     FirPPSmem<T> &sh = *reinterpret_cast<FirPPSmem<T> *>(pp_smem);
     FirSeg *segs = reinterpret_cast<FirSeg *>(pp_smem + fir_pp_smem_fixed<T>());
@@ -1804,7 +1811,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     const int G = gridDim.x;
     const int n = A0.n, n_eff = A0.n_eff;   // shared by every star
     if (tid == 0) {
-        for (int q = 0; q < (FIR_PP_NBUF > 1 ? FIR_PP_NBUF : 2); ++q) {
+        for (int q = 0; q < NBUF; ++q) {
             mbar_init(&sh.wbar[q], 1);
             mbar_init(&sh.ebar[q], FIR_THREADS / 32);
         }
@@ -1872,11 +1879,11 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         // after a failed wait the block stops feeding the pipeline (no new expected bytes
         // on a buffer whose copy may never have landed) and leaves at the next barrier
         if (*reinterpret_cast<volatile int *>(&sh.fail)) return;
-        const int b = u % FIR_PP_NBUF;
+        const int b = u % NBUF;
         const unsigned bytes = (d.w1 > d.w0) ? (unsigned)(d.w1 - d.w0) * (unsigned)sizeof(Vec4<T>) : 0u;
         // buffer b last held unit u - NBUF: every warp must have released it
-        if (u >= FIR_PP_NBUF &&
-            !mbar_wait_bounded(&sh.ebar[b], (unsigned)((u / FIR_PP_NBUF - 1) & 1), A0.wait_limit)) {
+        if (u >= NBUF &&
+            !mbar_wait_bounded(&sh.ebar[b], (unsigned)((u / NBUF - 1) & 1), A0.wait_limit)) {
             atomicExch(&sh.fail, 1);   // the unit is never copied: its readers' waits run out
             return;
         }
@@ -2102,7 +2109,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     // barrier.  Tiles that plan themselves (block-wide steps with barriers): the barrier
     // here, and the block leaves together at once.
     auto wait_unit = [&](int u) {
-        if (!mbar_wait_bounded(&sh.wbar[u % FIR_PP_NBUF], (unsigned)((u / FIR_PP_NBUF) & 1), A0.wait_limit))
+        if (!mbar_wait_bounded(&sh.wbar[u % NBUF], (unsigned)((u / NBUF) & 1), A0.wait_limit))
             atomicExch(&sh.fail, 1);
     };
     auto wait_unit_sync = [&](int u) {
@@ -2113,7 +2120,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
     // (every thread) done with unit u's window: one arrival per warp
     auto release_unit = [&](int u) {
         __syncwarp();
-        if ((tid & 31) == 0) mbar_arrive(&sh.ebar[u % FIR_PP_NBUF]);
+        if ((tid & 31) == 0) mbar_arrive(&sh.ebar[u % NBUF]);
     };
 
     // walk steps [0, kend)
@@ -2121,10 +2128,10 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         if (kend > 0) issue_plan(pos(0), 0, plan_size(pos(0)), true);
         if (kend > 1) issue_plan(pos(1), 1, plan_size(pos(1)));
     }
-    int ucount = 0;        // units staged and applied so far (window buffer ucount % 3)
-    // the previous tile was planned and its last unit issued this tile's first unit ahead
-    // when this tile's plan has units (the issuing thread's test, repeated by every thread)
-    bool prev_ahead = false;
+    int ucount = 0;        // units staged and applied so far (window buffer ucount % NBUF)
+    // a planned tile's units [ahead_lo, LEAD) were copied during the previous tile (the
+    // copying thread's test, repeated by every thread); the others are copied at its start
+    int ahead_lo = LEAD;
     int k = 0;
     int bad = 0;
     int cur_star = -1;     // MULTI: the star whose arguments star_sh holds
@@ -2165,8 +2172,8 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         const int *cn = A.counts + 4 * l;
         const unsigned char *rec = sh.pb[pbuf];
         const int4 hdr = *reinterpret_cast<const int4 *>(rec);
-        const bool pre = prev_ahead && t_eff > 0 && hdr.w && hdr.x > 0;
-        prev_ahead = false;
+        const int lo = ahead_lo;
+        ahead_lo = LEAD;
         if (t_eff > 0 && hdr.w) {
             // --- planned tile ------------------------------------------------------------
             const int nb = hdr.x;
@@ -2177,6 +2184,11 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
             const FirGrp<T> *grp = reinterpret_cast<const FirGrp<T> *>(rec + L.o_grp);
             const FirExcW<T> *exc = reinterpret_cast<const FirExcW<T> *>(rec + L.o_exc);
             int nfold = 0;   // units summed in part[] since the last fold
+            // unit u is copied by lane 0 of warp u % 8: the copies' mbarrier latencies are
+            // spread over the warps instead of holding back one of them
+            if (FIR_PP_STAGED)
+                for (int i = 0; i < min(lo, nb); ++i)
+                    if (tid == ((ucount + i) % FIR_WARPS) * 32) issue_unit(ucount + i, units[i]);
             for (int ui = 0; ui < nb; ++ui) {
                 const int u = ucount;
                 if (!FIR_PP_STAGED) {   // rows read from global memory: no staging, no barrier
@@ -2189,22 +2201,21 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                     part_fold(d.cls, j0);
                     continue;
                 }
-                // unit u is copied by lane 0 of warp u % 8: the copies' mbarrier latencies
-                // are spread over the warps instead of holding back one of them
-                if (ui == 0 && !pre && tid == (u % FIR_WARPS) * 32) issue_unit(u, units[0]);
-                if (tid == ((u + 1) % FIR_WARPS) * 32) {
-                    if (ui + 1 < nb) {
-                        issue_unit(u + 1, units[1 + ui]);
+                // unit u + LEAD: this tile's unit ui + LEAD, else the next tile's unit
+                // ui + LEAD - nb, from its plan
+                if (tid == ((u + LEAD) % FIR_WARPS) * 32) {
+                    const int i2 = ui + LEAD;
+                    if (i2 < nb) {
+                        issue_unit(u + LEAD, units[i2]);
                     } else if (k + 1 < kend) {
-                        // last unit: issue the next tile's first unit, from its plan
                         if (mbar_wait_bounded(&sh.pbar[pbuf ^ 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit)) {
                             const unsigned char *rn = sh.pb[pbuf ^ 1];
                             const int4 hn = *reinterpret_cast<const int4 *>(rn);
                             const int tnr = real(pos(k + 1));
                             const int ln = tnr / ntile, jn = (tnr - ln * ntile) * FIR_TILE;
-                            if (hn.w && hn.x > 0 && jn < n_eff) {
+                            if (hn.w && i2 - nb < hn.x && jn < n_eff) {
                                 const FirPlanLayout<T> Ln(hn.x, hn.y, hn.z);
-                                issue_unit(u + 1, *reinterpret_cast<const FirUnit *>(rn + Ln.o_unit));
+                                issue_unit(u + LEAD, reinterpret_cast<const FirUnit *>(rn + Ln.o_unit)[i2 - nb]);
                             }
                         } else {
                             atomicExch(&sh.fail, 1);   // the block leaves at the next tile's barrier
@@ -2213,7 +2224,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 }
                 wait_unit(u);
                 const FirUnit d = units[ui];
-                const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
+                const Src sr = src_of(sh.win[u % NBUF], d);
                 if (nfold == 0) part_zero();
                 apply_groups(sr, d, grp, ut[ui], ut[ui + 1], j0, t_eff);
                 const int e_lo = woff[ut[ui]], e_hi = woff[ut[ui + 1]];
@@ -2226,7 +2237,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                 release_unit(u);
                 ++ucount;
             }
-            prev_ahead = nb > 0 && k + 1 < kend;
+            if (k + 1 < kend) ahead_lo = max(0, LEAD - nb);
         } else if (t_eff > 0) {
             // --- tile that plans itself, batch by batch ----------------------------------
             const int nsg = A.nseg[2 * l] + A.nseg[2 * l + 1];
@@ -2249,7 +2260,7 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
                         }
                     }
                     const FirUnit d = st.unit[ui];
-                    const Src sr = src_of(sh.win[u % FIR_PP_NBUF], d);
+                    const Src sr = src_of(sh.win[u % NBUF], d);
                     part_zero();
                     apply_groups(sr, d, st.grp, st.ut[ui], st.ut[ui + 1], j0, t_eff);
                     const int e_lo = st.woff[st.ut[ui]], e_hi = st.woff[st.ut[ui + 1]];
@@ -2367,8 +2378,8 @@ __global__ void __launch_bounds__(FIR_THREADS, FIR_PP_MINB) k_fir_pp(const FirTi
         // bounded wait before leaving
         atomicExch(A0.status, FIR_ST_WAIT);
         if (FIR_PP_STAGED) {
-            mbar_wait_bounded(&sh.wbar[ucount % FIR_PP_NBUF], (unsigned)((ucount / FIR_PP_NBUF) & 1), A0.wait_limit);
-            mbar_wait_bounded(&sh.wbar[(ucount + 1) % FIR_PP_NBUF], (unsigned)(((ucount + 1) / FIR_PP_NBUF) & 1), A0.wait_limit);
+            for (int i = 0; i < LEAD; ++i)
+                mbar_wait_bounded(&sh.wbar[(ucount + i) % NBUF], (unsigned)(((ucount + i) / NBUF) & 1), A0.wait_limit);
         }
         mbar_wait_bounded(&sh.pbar[k & 1], (unsigned)((k >> 1) & 1), A0.wait_limit);
         mbar_wait_bounded(&sh.pbar[(k + 1) & 1], (unsigned)(((k + 1) >> 1) & 1), A0.wait_limit);
