@@ -820,40 +820,42 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
         fail = 0;
     }
     __syncthreads();
-    auto issue = [&](int it, int buf) {   // thread 0
+    // (warp 0) copy item it's rows into buffer buf: lane q looks up and copies row q, so
+    // the lookups' latencies overlap instead of adding up
+    auto issue = [&](int it, int buf) {
+        const int lane = threadIdx.x & 31;
         const int bt = batch_of(it), x = it % nbx;
         const int nsb = min(SB, nlisted - bt * SB);
         int mb, ca, cb;
         window(x, mb, ca, cb);
         const unsigned bytes = (cb > ca) ? (unsigned)(cb - ca) * 4u : 0u;
         const unsigned bar_a = (unsigned)__cvta_generic_to_shared(&bar[buf]);
-        int ncopy = 0;
-        for (int q = 0; q < nsb; ++q) ncopy += zero_row(row_id(bt, q)) ? 0 : 1;
+        const int sq = (lane < nsb) ? row_id(bt, lane) : 0;
+        const bool cp = (lane < nsb) && !zero_row(sq);
+        const unsigned ncopy = (unsigned)__popc(__ballot_sync(0xffffffffu, cp));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
-                     "r"(bytes * (unsigned)ncopy)
-                     : "memory");
+        if (lane == 0)
+            asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
+                         "r"(bytes * ncopy)
+                         : "memory");
+        __syncwarp();
         // failure-path test: the block's first window is expected but never copied
-        if (bytes && !(drop_first && it == (int)blockIdx.x)) {
-            for (int q = 0; q < nsb; ++q) {
-                const int sq = row_id(bt, q);
-                if (zero_row(sq)) continue;
-                const float *src = spec + (long long)sq * spec_stride + ca;
-                float *dst = xbuf + ((size_t)buf * SB + q) * win + (ca - mb);
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        (unsigned)__cvta_generic_to_shared(dst)),
-                    "l"(src), "r"(bytes), "r"(bar_a)
-                    : "memory");
-            }
+        if (cp && bytes && !(drop_first && it == (int)blockIdx.x)) {
+            const float *src = spec + (long long)sq * spec_stride + ca;
+            float *dst = xbuf + ((size_t)buf * SB + lane) * win + (ca - mb);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    (unsigned)__cvta_generic_to_shared(dst)),
+                "l"(src), "r"(bytes), "r"(bar_a)
+                : "memory");
         }
     };
     int k = 0, k_fail = -1;
-    if (threadIdx.x == 0 && (int)blockIdx.x < nitem) issue(blockIdx.x, 0);
+    if (threadIdx.x < 32 && (int)blockIdx.x < nitem) issue(blockIdx.x, 0);
     for (int it = blockIdx.x; it < nitem; it += gridDim.x, ++k) {
         const int bt = batch_of(it), x = it % nbx;
         const int buf = k & 1;
-        if (threadIdx.x == 0 && it + (int)gridDim.x < nitem) issue(it + gridDim.x, buf ^ 1);
+        if (threadIdx.x < 32 && it + (int)gridDim.x < nitem) issue(it + gridDim.x, buf ^ 1);
         const int nsb = min(SB, nlisted - bt * SB);
         // the item's spectra (shared: the epilogue's last step indexes them by thread);
         // written before the barrier below, read after it, rewritten after the epilogue's
@@ -889,8 +891,9 @@ __global__ void __launch_bounds__(FC_THREADS, 3) k_conv32t(int n, int n_eff, con
             ok = (r != 0);
         }
         if (!ok) atomicExch(&fail, 1);
-        unsigned zmask = 0;   // rows of zero spectra in this batch
-        for (int q = 0; q < nsb; ++q) zmask |= zero_row(row_id(bt, q)) ? (1u << q) : 0u;
+        // rows of zero spectra in this batch (lane q looks up row q)
+        const unsigned zmask = __ballot_sync(
+            0xffffffffu, (int)(threadIdx.x & 31) < nsb && zero_row(row_id(bt, (int)(threadIdx.x & 31))));
         // zero the staged pixels outside [0, n), and the rows of absent and zero spectra
         if (ca > mb || cb < mb + win || nsb < SB || zmask) {
             for (int q = 0; q < SB; ++q)
