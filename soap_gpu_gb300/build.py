@@ -101,6 +101,18 @@ def build(verbose: bool = False, force: bool = False, jobs: int = 0) -> str:
     return LIB
 
 
+def _torch_ops_registered() -> bool:
+    """torch.ops.soapgb is registered in this process (torch imported and the operator
+    library loaded)."""
+    if "torch" not in sys.modules:
+        return False
+    try:
+        sys.modules["torch"].ops.soapgb.synchronize
+        return True
+    except (AttributeError, RuntimeError):
+        return False
+
+
 TORCH_SRC = os.path.join(CSRC, "torch", "soapgb_torch.cpp")
 TORCH_OPS = os.path.join(LIBDIR, "soapgb_torch.so")
 
@@ -111,6 +123,13 @@ def build_torch_ops(verbose: bool = False) -> str:
     against libsoapgb and the CUDA runtime; no device code)."""
     deps = [TORCH_SRC, LIB, os.path.join(ROOT, "include", "soapgb.h")]
     if not _stale(TORCH_OPS, deps):
+        return TORCH_OPS
+    if _torch_ops_registered():
+        # cpp_extension.load also loads what it builds, and torch takes an operator
+        # namespace once per process: a process that holds the operators already builds
+        # the new copy in a child process
+        _run([sys.executable, "-c", "import sys; sys.path.insert(0, %r); "
+              "from soap_gpu_gb300.build import build_torch_ops; build_torch_ops()" % ROOT])
         return TORCH_OPS
     import torch.utils.cpp_extension as ce
     bdir = os.path.join(OBJ, "torch_ops")

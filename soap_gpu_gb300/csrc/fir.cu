@@ -1011,7 +1011,9 @@ template <typename T>
 using FirTileSt = FirPlanSt<T, 128, (sizeof(T) == 4) ? 512 : 256, (sizeof(T) == 4) ? 512 : 256>;
 template <typename T>
 using FirPrePlan = FirPlanSt<T, 32, 128, 128>;
-constexpr int FIR_PLAN_THREADS = 64;
+// one warp per (list, tile): the plan's block barriers are then a single warp's
+// (0.106 ms per 100-phase step against 0.112 with 64 threads and 0.152 with 128)
+constexpr int FIR_PLAN_THREADS = 32;
 
 // Compact plan record of one (list, tile) as the plan kernel writes it: int4 header
 // (units, tasks, wrap cells, ok) at 0, then units, ut[nb + 1], woff[ntask + 1], groups and
