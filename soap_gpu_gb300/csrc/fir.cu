@@ -1788,9 +1788,10 @@ __host__ __device__ constexpr size_t fir_pp_smem_fixed() { return (sizeof(FirPPS
 // block b takes the consecutive positions [b per, (b + 1) per): one block works through
 // the phases of one tile, so consecutive phases read the same cube rows (L1 / L2).
 // A tile's compact plan (k_fir_plan) is copied by TMA one tile ahead into the other plan
-// buffer; the cube windows of its work units stream through two buffers, and the first
-// unit of the next tile is issued while the current tile's last unit is applied, so the
-// copies' latencies overlap the arithmetic.  Tiles whose plan did not fit plan themselves.
+// buffer; the cube windows of its work units stream through NBUF buffers, LEAD units
+// ahead (across the tile boundary, from the next tile's plan), each copy issued by lane 0
+// of a rotating warp, so the copies' latencies overlap the arithmetic.  Tiles whose plan
+// did not fit plan themselves.
 // COMP: the output sums (per tile a pixel adds about 9 unit deficits, each rounded once)
 // are compensated (Kahan) rather than plain FP32 sums.
 // MULTI: the (phase, tile) pairs of many stars in one launch.  Star s has its own lists,
